@@ -1,0 +1,203 @@
+// Ghost and reconstruction-layer fill before every residual evaluation, in the reference's order
+// (source/BoundaryCondition.cpp:9-63): total-condition inlet (source/BndCondInlet.cpp:7-127),
+// axial outlet with radial equilibrium (source/BndCondOutlet.cpp:13-113), no-slip wall
+// (source/BndCondWall.cpp:20-285) and rotational periodicity as a precomputed gather list
+// equivalent to the shadow copies of source/ShadowOutIn.cpp and
+// source/BndCondInteriorPeriodic.cpp:36-69.
+#include "gbt_common.cuh"
+#include "kernels.hpp"
+#include "flux.cuh"
+
+namespace gbt {
+
+template <typename T>
+__device__ __forceinline__ void st_state(Flow<T> &W, long long g, const double c[5], const T q[6])
+{
+#pragma unroll
+    for (int n = 0; n < 5; n++) W.cv[n][g] = c[n];
+#pragma unroll
+    for (int n = 0; n < 6; n++) W.pv[n][g] = q[n];
+}
+
+// inlet: Riemann invariant from the interior, total pressure/temperature and flow direction
+template <typename T>
+__global__ void k_bc_inlet(Batch B, Phys P, Geo G, Flow<T> W, const DevInOut *pat)
+{
+    const DevInOut pt = pat[blockIdx.y];
+    const Lvl L = B.lv[pt.solve];
+    const int ni = pt.ie - pt.is + 1, nj = pt.je - pt.js + 1;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ni * nj) return;
+    const int i = pt.is + t / nj, j = pt.js + t % nj;
+    const bool low = (pt.ks == 1);
+    const int k = low ? 1 : L.KM - 1, kv = low ? 0 : L.KM;
+    const long long fp = ix(L, i, j, low ? 1 : L.KM);
+    const double Sx = G.S[2][0][fp], Sy = G.S[2][1][fp], Sz = G.S[2][2][fp];
+    const double n_m = sqrt(Sx * Sx + Sy * Sy + Sz * Sz);
+    const long long p = ix(L, i, j, k), g = ix(L, i, j, kv);
+    const double u = W.pv[PU][p], v = W.pv[PV][p], w = W.pv[PW][p];
+    double vdn = (u * Sx / n_m + v * Sy / n_m + w * Sz / n_m);
+    if (low) vdn = -1.0 * vdn;
+    const double gam = P.gamma, g1 = gam - 1.0, R = P.rgas, Ttin = P.ttin, Ptin = P.ptin;
+    const double c_d = sqrt(gam * R * (double)W.pv[PT][p]);
+    const double V2 = u * u + v * v + w * w;
+    const double costh = -1.0 * vdn / sqrt(V2);
+    const double c02 = c_d * c_d + g1 * V2 / 2.0;
+    const double Rm = vdn - 2.0 * c_d / g1;
+    const double mA = (-Rm * g1) / (g1 * costh * costh + 2.0);
+    const double mB = sqrt(c02 * (g1 * costh * costh + 2.0) / g1 / (Rm * Rm) - g1 / 2.0);
+    const double cb = mA * (1.0 + costh * mB);
+    double Tb = Ttin * (cb * cb / c02);
+    if (Tb > Ttin) Tb = (double)0.99f * Ttin;
+    const double pb = Ptin * pow(Tb / Ttin, gam / g1);
+    const double db = pb / R / Tb;
+    const double Vb = sqrt(2.0 * gam / g1 * R * (Ttin - Tb));
+    const double gu = Vb * P.inlet_dir[0] / P.inlet_vnm, gv = Vb * P.inlet_dir[1] / P.inlet_vnm,
+                 gw = Vb * P.inlet_dir[2] / P.inlet_vnm;
+    const double e = pb / db / g1 + (gu * gu + gv * gv + gw * gw) / 2.0;
+    const double c[5] = {db, db * gu, db * gv, db * gw, db * e};
+    const T q[6] = {(T)db, (T)gu, (T)gv, (T)gw, (T)pb, (T)Tb};
+    st_state(W, g, c, q);
+    for (int nd = 1; nd <= P.ndummy; nd++) st_state(W, ix(L, i, j, low ? -nd : L.KM + nd), c, q);
+}
+
+// axial outlet, one block per outlet patch: mass-weighted swirl per radial row, radial
+// equilibrium marched from p_out at i = IM/2 using the previous ghost density, then ghosts
+// extrapolated from the last interior layer
+template <typename T>
+__global__ void k_bc_outlet(Batch B, Phys P, Geo G, Flow<T> W, const DevInOut *pat)
+{
+    extern __shared__ double cu[];
+    const DevInOut pt = pat[blockIdx.x];
+    const Lvl L = B.lv[pt.solve];
+    const int IM = L.IM, JM = L.JM, KM = L.KM;
+    for (int i = 1 + threadIdx.x; i <= IM - 1; i += blockDim.x) {
+        double acc = 0.0, sa = 0.0;
+        for (int j = 1; j <= JM - 1; j++) {
+            const long long p = ix(L, i, j, KM - 1), f = ix(L, i, j, KM);
+            const double th = G.th[2][f];
+            const double ct = -1.0 * (double)W.pv[PU][p] * sin(th) + (double)W.pv[PV][p] * cos(th);
+            acc = acc + ct * G.s[2][f];
+            sa = sa + G.s[2][f];
+        }
+        cu[i] = acc / sa;
+    }
+    __syncthreads();
+    const int iref = (int)(0.5 * IM);
+    const double pout = B.sc[pt.solve].pout;
+    for (int j = 1 + threadIdx.x; j <= JM - 1; j += blockDim.x) {
+        double pr = pout;
+        W.pv[PP][ix(L, iref, j, KM)] = (T)pr;
+        for (int i = iref - 1; i >= 1; i--) {
+            const double rn = G.r[2][ix(L, i, j, KM)], rn1 = G.r[2][ix(L, i + 1, j, KM)];
+            const double dpdr = W.cv[0][ix(L, i, j, KM)] * cu[i] * cu[i] / rn;
+            pr = pr - dpdr * (rn1 - rn);
+            W.pv[PP][ix(L, i, j, KM)] = (T)pr;
+        }
+        pr = pout;
+        for (int i = iref + 1; i <= IM - 1; i++) {
+            // radii of the k = KM-1 face row here, as the reference takes them
+            const double rn1 = G.r[2][ix(L, i, j, KM - 1)], rn = G.r[2][ix(L, i - 1, j, KM - 1)];
+            const double dpdr = W.cv[0][ix(L, i, j, KM)] * cu[i] * cu[i] / rn;
+            pr = pr + dpdr * (rn1 - rn);
+            W.pv[PP][ix(L, i, j, KM)] = (T)pr;
+        }
+    }
+    __syncthreads();
+    const int n = (IM - 1) * (JM - 1);
+    const double g1 = P.gamma - 1.0;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int i = 1 + t / (JM - 1), j = 1 + t % (JM - 1);
+        const long long g = ix(L, i, j, KM), p = ix(L, i, j, KM - 1);
+        const double d = W.cv[0][p];
+        const double pr = (double)W.pv[PP][g];
+        const double u = W.pv[PU][p], v = W.pv[PV][p], w = W.pv[PW][p];
+        const double c[5] = {d, W.cv[1][p], W.cv[2][p], W.cv[3][p], pr / g1 + d * (u * u + v * v + w * w) / 2.0};
+        const T q[6] = {(T)d, (T)u, (T)v, (T)w, (T)pr, (T)(pr / P.rgas / d)};
+        st_state(W, g, c, q);
+        for (int nd = 1; nd <= P.ndummy; nd++) st_state(W, ix(L, i, j, KM + nd), c, q);
+    }
+}
+
+// no-slip wall: ghost keeps p, T, rho, rho*E of the first cell, relative velocity reflected;
+// reconstruction layers = mean of ghost and first cell
+template <typename T>
+__global__ void k_bc_wall(Batch B, Phys P, Geo G, Flow<T> W, const DevWall *walls)
+{
+    const DevWall wl = walls[blockIdx.y];
+    const Lvl L = B.lv[wl.solve];
+    const int ni = wl.ie - wl.is + 1, nj = wl.je - wl.js + 1, nk = wl.ke - wl.ks + 1;
+    int i, j, k;
+    if (!box_index(ni, nj, nk, i, j, k)) return;
+    i += wl.is - 1; j += wl.js - 1; k += wl.ks - 1;
+    const int f = (wl.face - 1) / 2;
+    const bool lo = wl.face % 2 == 1;
+    const long long sn = f == 0 ? (long long)L.NJ * L.NK : (f == 1 ? (long long)L.NK : 1LL);
+    // (i,j,k) is the wall face; interior cell next to it and the ghost on the other side
+    const long long fp = ix(L, i, j, k);
+    const long long pin = lo ? fp : fp - sn, g = lo ? fp - sn : fp;
+    const long long step = lo ? -sn : sn;           // from the ghost outwards
+    const double rot = wl.rotate ? B.sc[wl.solve].w_rot : 0.0;
+    const double x = G.c[f][0][fp], y = G.c[f][1][fp];
+    const double vwx = -rot * y, vwy = rot * x;
+    const double u = W.pv[PU][pin], v = W.pv[PV][pin], w = W.pv[PW][pin];
+    const double gu = (0.0 - (u - vwx)) + vwx, gv = (0.0 - (v - vwy)) + vwy, gw = (0.0 - (w - 0.0)) + 0.0;
+    const double d = W.cv[0][pin];
+    const double c[5] = {d, gu * d, gv * d, gw * d, W.cv[4][pin]};
+    const T q[6] = {W.pv[PD][pin], (T)gu, (T)gv, (T)gw, W.pv[PP][pin], W.pv[PT][pin]};
+    st_state(W, g, c, q);
+    double cm[5];
+    T qm[6];
+#pragma unroll
+    for (int n = 0; n < 5; n++) cm[n] = 0.5 * (c[n] + W.cv[n][pin]);
+#pragma unroll
+    for (int n = 0; n < 6; n++) qm[n] = (T)0.5 * (q[n] + W.pv[n][pin]);
+    for (int nd = 1; nd <= P.ndummy; nd++) st_state(W, g + nd * step, cm, qm);
+}
+
+// periodic exchange: ghost/dummy <- interior cell of the partner face, velocity and momentum
+// rotated about z by +-delta_th
+template <typename T>
+__global__ void k_bc_periodic(Batch B, Flow<T> W, const long long *dst, const long long *src, const int *meta,
+                              long long n)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int mt = meta[t];
+    const int s = mt >> 2, sg = (mt & 3) - 1;
+    const long long a = src[t], b = dst[t];
+    const double dr = sg * B.sc[s].delta_th;
+    double c[5];
+    T q[6];
+#pragma unroll
+    for (int m = 0; m < 5; m++) c[m] = W.cv[m][a];
+#pragma unroll
+    for (int m = 0; m < 6; m++) q[m] = W.pv[m][a];
+    if (dr != 0.0) {
+        const double cs = cos(dr), sn = sin(dr);
+        const double mx = c[1], my = c[2];
+        c[1] = mx * cs - my * sn;
+        c[2] = my * cs + mx * sn;
+        const double u = q[PU], v = q[PV];
+        q[PU] = (T)(u * cs - v * sn);
+        q[PV] = (T)(v * cs + u * sn);
+    }
+    st_state(W, b, c, q);
+}
+
+template <typename T>
+void launch_boundary(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const BcTables &bc)
+{
+    const Batch &B = ctx.batch;
+    if (bc.n_inlet) k_bc_inlet<T><<<dim3((bc.max_inlet + 127) / 128, bc.n_inlet), 128, 0, ctx.stream>>>(B, P, G, W, bc.inlet);
+    if (bc.n_outlet)
+        k_bc_outlet<T><<<bc.n_outlet, 256, (size_t)(bc.max_outlet_im + 1) * sizeof(double), ctx.stream>>>(B, P, G, W, bc.outlet);
+    if (bc.n_wall) k_bc_wall<T><<<dim3((bc.max_wall + 127) / 128, bc.n_wall), 128, 0, ctx.stream>>>(B, P, G, W, bc.wall);
+    if (bc.n_per)
+        k_bc_periodic<T><<<(unsigned)((bc.n_per + 255) / 256), 256, 0, ctx.stream>>>(B, W, bc.per_dst, bc.per_src, bc.per_meta, bc.n_per);
+}
+
+template void launch_boundary<double>(const LaunchCtx &, const Phys &, const Geo &, Flow<double>, const BcTables &);
+template void launch_boundary<float>(const LaunchCtx &, const Phys &, const Geo &, Flow<float>, const BcTables &);
+
+}  // namespace gbt

@@ -1,0 +1,177 @@
+// extern "C" boundary: forwards to gbt::SolverBase and turns exceptions into error codes.
+#include "../../include/gbturbo.h"
+#include "solver.hpp"
+#include <cstring>
+#include <string>
+
+struct gb_solver {
+    std::unique_ptr<gbt::SolverBase> s;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+};
+
+static thread_local std::string g_err;
+
+template <class F>
+static int guard(F &&f)
+{
+    try {
+        f();
+        return GB_OK;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        std::string m = e.what();
+        if (m.find("cuda") != std::string::npos || m.find("CUDA") != std::string::npos) return GB_ERR_CUDA;
+        return GB_ERR_CASE;
+    } catch (...) {
+        g_err = "unknown error";
+        return GB_ERR_CASE;
+    }
+}
+#define NEED(h) do { if (!(h) || !(h)->s) { g_err = "null handle"; return GB_ERR_ARG; } } while (0)
+#define LEVEL(h, l) do { if ((l) < 1 || (l) > (h)->s->ng) { g_err = "level out of range"; return GB_ERR_ARG; } } while (0)
+
+extern "C" {
+
+const char *gb_last_error(void) { return g_err.c_str(); }
+
+int gb_solver_create(const char *const *case_dirs, int n_solves, int precision, gb_solver **out)
+{
+    if (!case_dirs || n_solves < 1 || !out) { g_err = "bad arguments"; return GB_ERR_ARG; }
+    *out = nullptr;
+    return guard([&] {
+        std::vector<std::string> d;
+        for (int i = 0; i < n_solves; i++) d.push_back(case_dirs[i] ? case_dirs[i] : "");
+        auto h = new gb_solver;
+        try {
+            h->s = gbt::make_solver(d, precision);
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+int gb_solver_destroy(gb_solver *h)
+{
+    if (!h) return GB_OK;
+    if (h->t0) cudaEventDestroy(h->t0);
+    if (h->t1) cudaEventDestroy(h->t1);
+    delete h;
+    return GB_OK;
+}
+
+int gb_dims(gb_solver *h, int solve, int level, int out[4])
+{
+    NEED(h); LEVEL(h, level);
+    if (solve < 0 || solve >= h->s->nsolve) { g_err = "solve out of range"; return GB_ERR_ARG; }
+    return guard([&] { h->s->dims(solve, level, out); });
+}
+
+int gb_init_uniform(gb_solver *h) { NEED(h); return guard([&] { h->s->init_uniform(); }); }
+int gb_resflux(gb_solver *h, int level) { NEED(h); LEVEL(h, level); return guard([&] { h->s->resflux(level); }); }
+int gb_time_marching(gb_solver *h, int level) { NEED(h); LEVEL(h, level); return guard([&] { h->s->time_marching(level); }); }
+int gb_primitive_vars(gb_solver *h, int level) { NEED(h); LEVEL(h, level); return guard([&] { h->s->primitive_vars(level); }); }
+int gb_limit_vars(gb_solver *h, int level) { NEED(h); LEVEL(h, level); return guard([&] { h->s->limit_vars(level); }); }
+int gb_corner_treatment(gb_solver *h, int level) { NEED(h); LEVEL(h, level); return guard([&] { h->s->corner_treatment(level); }); }
+int gb_restrict(gb_solver *h) { NEED(h); return guard([&] { h->s->restrict_to_coarse(); }); }
+int gb_interpolate(gb_solver *h, int init) { NEED(h); return guard([&] { h->s->interpolate(init); }); }
+int gb_delta_cons(gb_solver *h) { NEED(h); return guard([&] { h->s->delta_cons(); }); }
+int gb_set_use_force(gb_solver *h, int level, int on) { NEED(h); LEVEL(h, level); return guard([&] { h->s->set_use_force(level, on != 0); }); }
+int gb_solver_step(gb_solver *h) { NEED(h); return guard([&] { h->s->solver_step(); }); }
+
+int gb_res_calculate(gb_solver *h, int level, double *out)
+{
+    NEED(h); LEVEL(h, level);
+    return guard([&] {
+        h->s->res_calculate(level);
+        if (out) {
+            std::vector<gbt::SolveState> st(h->s->nsolve);
+            h->s->states(st.data());
+            for (int s = 0; s < h->s->nsolve; s++)
+                for (int c = 0; c < 5; c++) out[s * 5 + c] = st[s].res[c];
+        }
+    });
+}
+
+int gb_integrals(gb_solver *h, int level, double *out)
+{
+    NEED(h); LEVEL(h, level);
+    return guard([&] {
+        h->s->integrals(level);
+        if (out) {
+            std::vector<gbt::SolveState> st(h->s->nsolve);
+            h->s->states(st.data());
+            for (int s = 0; s < h->s->nsolve; s++) {
+                out[s * 5 + 0] = st[s].m_in; out[s * 5 + 1] = st[s].m_out; out[s * 5 + 2] = st[s].pr;
+                out[s * 5 + 3] = st[s].eff; out[s * 5 + 4] = st[s].m_ratio;
+            }
+        }
+    });
+}
+
+int gb_iterate(gb_solver *h, int n, double *hist)
+{
+    NEED(h);
+    if (n < 0) { g_err = "negative iteration count"; return GB_ERR_ARG; }
+    return guard([&] { h->s->iterate(n, hist); });
+}
+
+int gb_get_status(gb_solver *h, int *out)
+{
+    NEED(h);
+    if (!out) { g_err = "null buffer"; return GB_ERR_ARG; }
+    return guard([&] {
+        std::vector<gbt::SolveState> st(h->s->nsolve);
+        h->s->states(st.data());
+        for (int s = 0; s < h->s->nsolve; s++) out[s] = st[s].status;
+    });
+}
+
+long gb_get_field(gb_solver *h, int solve, int level, const char *name, double *out, long cap)
+{
+    NEED(h);
+    if (!name || !out) { g_err = "null argument"; return GB_ERR_ARG; }
+    long r = -1;
+    int rc = guard([&] { r = h->s->get_field(solve, level, name, out, cap); });
+    if (rc) return rc;
+    if (r < 0) { g_err = std::string("unknown field, level, solve or short buffer: ") + name; return GB_ERR_ARG; }
+    return r;
+}
+
+int gb_set_cv(gb_solver *h, int solve, int level, const double *cv, long n)
+{
+    NEED(h);
+    if (!cv) { g_err = "null buffer"; return GB_ERR_ARG; }
+    return guard([&] { h->s->set_cv(solve, level, cv, n); });
+}
+
+int gb_sync(gb_solver *h)
+{
+    NEED(h);
+    return guard([&] { gbt::check_cuda(cudaStreamSynchronize(h->s->stream), "cudaStreamSynchronize"); });
+}
+
+int gb_set_graphs(gb_solver *h, int enable) { NEED(h); h->s->use_graphs = enable != 0; return GB_OK; }
+
+int gb_timer_start(gb_solver *h)
+{
+    NEED(h);
+    return guard([&] {
+        if (!h->t0) { gbt::check_cuda(cudaEventCreate(&h->t0), "cudaEventCreate"); gbt::check_cuda(cudaEventCreate(&h->t1), "cudaEventCreate"); }
+        gbt::check_cuda(cudaEventRecord(h->t0, h->s->stream), "cudaEventRecord");
+    });
+}
+
+int gb_timer_stop(gb_solver *h, float *ms)
+{
+    NEED(h);
+    if (!h->t0) { g_err = "timer not started"; return GB_ERR_ARG; }
+    return guard([&] {
+        gbt::check_cuda(cudaEventRecord(h->t1, h->s->stream), "cudaEventRecord");
+        gbt::check_cuda(cudaEventSynchronize(h->t1), "cudaEventSynchronize");
+        gbt::check_cuda(cudaEventElapsedTime(ms, h->t0, h->t1), "cudaEventElapsedTime");
+    });
+}
+
+}  // extern "C"

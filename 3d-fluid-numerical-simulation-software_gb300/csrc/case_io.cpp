@@ -1,0 +1,298 @@
+// Case-file reader. Follows the reference's positional parsing (source/UserInput.cpp:17-239,
+// 241-334, 336-446, 799-1068; include/fstringIO.h:15-42) so the same files drive both solvers.
+#include "case_io.hpp"
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <sstream>
+#include <algorithm>
+
+namespace gbt {
+
+std::string ref_read_line(std::FILE *f, bool *ok)
+{
+    std::string s;
+    int ch;
+    bool any = false;
+    while ((ch = std::fgetc(f)) != EOF) {
+        any = true;
+        if (ch == '\n') break;
+        s.push_back((char)ch);
+    }
+    if (ok) *ok = any;
+    if (!s.empty() && s.back() == '\r') s.pop_back();
+    size_t h = s.find('#');
+    if (h != std::string::npos) s.erase(h);
+    size_t a = s.find_first_not_of(' ');
+    if (a == std::string::npos) return std::string();
+    s.erase(0, a);
+    size_t b = s.find_last_not_of(' ');
+    s.erase(b + 1);
+    return s;
+}
+
+namespace {
+
+struct LineReader {
+    std::FILE *f = nullptr;
+    std::string name;
+    int lineno = 0;
+    LineReader(const std::string &path, const std::string &nm) : name(nm)
+    {
+        f = std::fopen(path.c_str(), "r");
+        if (!f) throw std::runtime_error("cannot open " + path);
+    }
+    ~LineReader() { if (f) std::fclose(f); }
+    std::string next()
+    {
+        bool ok;
+        std::string s = ref_read_line(f, &ok);
+        lineno++;
+        if (!ok) throw std::runtime_error(name + ": file ended at line " + std::to_string(lineno));
+        return s;
+    }
+    void skip(int n) { for (int i = 0; i < n; i++) next(); }
+};
+
+// std::stof, then widened: the reference's REAL is double but its options pass through float
+double as_float(const std::string &s, const std::string &what)
+{
+    char *e = nullptr;
+    float v = std::strtof(s.c_str(), &e);
+    if (e == s.c_str()) throw std::runtime_error("config.dat: cannot read " + what + " from '" + s + "'");
+    return (double)v;
+}
+int as_int(const std::string &s, const std::string &what)
+{
+    char *e = nullptr;
+    long v = std::strtol(s.c_str(), &e, 10);
+    if (e == s.c_str()) throw std::runtime_error("cannot read " + what + " from '" + s + "'");
+    return (int)v;
+}
+bool is_yes(const std::string &s) { return s == "y" || s == "Y"; }
+
+std::vector<int> ints(const std::string &s)
+{
+    std::vector<int> v;
+    const char *p = s.c_str();
+    char *e;
+    for (;;) {
+        long x = std::strtol(p, &e, 10);
+        if (e == p) break;
+        v.push_back((int)x);
+        p = e;
+    }
+    return v;
+}
+
+void read_config(CaseSpec &c)
+{
+    LineReader r(c.dir + "/config.dat", "config.dat");
+    r.next(); c.grid_file = r.next();
+    r.skip(2); c.bc_file = r.next();
+    r.skip(3);
+    std::string s = r.next(); c.turbo_axial = (s == "a" || s == "A");
+    s = r.next(); c.equation_ns = !(s == "e" || s == "E");
+    s = r.next(); c.uniform_init = (s == "u" || s == "U");
+    c.Rgas = as_float(r.next(), "gas constant");
+    c.Gamma = as_float(r.next(), "specific heat ratio");
+    c.Pr_lam = as_float(r.next(), "laminar Prandtl number");
+    c.Pr_tur = as_float(r.next(), "turbulent Prandtl number");
+    r.skip(3);
+    c.Ptin = as_float(r.next(), "inlet total pressure");
+    c.Ttin = as_float(r.next(), "inlet total temperature");
+    c.Pout = as_float(r.next(), "outlet static pressure");
+    c.P21 = as_float(r.next(), "pressure ratio guess");
+    c.Ma0 = as_float(r.next(), "initial Mach number");
+    c.Len_ref = as_float(r.next(), "reference length");
+    c.ev_ratio = as_float(r.next(), "eddy viscosity ratio");
+    {
+        std::istringstream is(r.next());
+        is >> c.inlet_dir[0] >> c.inlet_dir[1] >> c.inlet_dir[2];
+    }
+    r.next();
+    c.mass_imposed = is_yes(r.next());
+    r.next();
+    r.skip(3);
+    c.maxiter = as_int(r.next(), "max iterations");
+    c.coarse_iter = as_int(r.next(), "coarse iterations");
+    c.outstep = as_int(r.next(), "output step");
+    c.convtol = as_float(r.next(), "convergence tolerance");
+    c.nt = as_int(r.next(), "thread count");
+    c.use_mg = is_yes(r.next());
+    c.restart = is_yes(r.next());
+    r.next();
+    r.skip(3);
+    c.CFL = as_float(r.next(), "CFL");
+    c.C_timestep = as_float(r.next(), "time step coefficient");
+    c.relax = as_float(r.next(), "LU-SGS relaxation");
+    c.epsEntr = as_float(r.next(), "entropy correction");
+    c.k2 = as_float(r.next(), "k2");
+    c.k4 = as_float(r.next(), "k4");
+    c.k4 = (double)(1.0f / c.k4);
+    c.irs = is_yes(r.next());
+    c.limiter = is_yes(r.next());
+    s = r.next(); c.global_dt = !(s == "l" || s == "L");
+    c.recon_var = as_int(r.next(), "reconstruction variables");
+    c.recon = as_int(r.next(), "reconstruction scheme");
+    c.scheme = as_int(r.next(), "space scheme");
+    c.time_scheme = as_int(r.next(), "time scheme");
+    c.turb = as_int(r.next(), "turbulence model");
+}
+
+void ng_check(int is, int ie, int js, int je, int ks, int ke, int &NG)
+{
+    if (is != ie) ie = ie + 1;
+    if (js != je) je = je + 1;
+    if (ks != ke) ke = ke + 1;
+    int num = 1;
+    if ((is - 1) % 2 == 0 && (ie - 1) % 2 == 0 && (js - 1) % 2 == 0 && (je - 1) % 2 == 0 &&
+        (ks - 1) % 2 == 0 && (ke - 1) % 2 == 0)
+        num = 2;
+    NG = std::min(num, NG);
+}
+
+void read_bc(CaseSpec &c)
+{
+    LineReader r(c.dir + "/" + c.bc_file, c.bc_file);
+    int NG = 4;
+    auto count = [&](const char *what) { return as_int(r.next(), what); };
+    r.skip(4);
+    int n = count("inlet count");
+    r.next();
+    for (int q = 0; q < n; q++) {
+        auto v = ints(r.next());
+        if (v.size() < 9) throw std::runtime_error(c.bc_file + ": bad inlet line");
+        if (v[1] != 1) throw std::runtime_error("multi-block cases are not supported");
+        c.inlets.push_back({v[2], v[3], v[4], v[5], v[6], v[7], v[8]});
+        ng_check(v[3], v[4], v[5], v[6], v[7], v[8], NG);
+    }
+    r.skip(3);
+    n = count("outlet count");
+    r.next();
+    for (int q = 0; q < n; q++) {
+        auto v = ints(r.next());
+        if (v.size() < 9) throw std::runtime_error(c.bc_file + ": bad outlet line");
+        if (v[1] != 1) throw std::runtime_error("multi-block cases are not supported");
+        c.outlets.push_back({v[2], v[3], v[4], v[5], v[6], v[7], v[8]});
+        ng_check(v[3], v[4], v[5], v[6], v[7], v[8], NG);
+    }
+    r.skip(3);
+    n = count("wall count");
+    r.next();
+    for (int q = 0; q < n; q++) {
+        auto v = ints(r.next());
+        if (v.size() < 10) throw std::runtime_error(c.bc_file + ": bad wall line");
+        if (v[1] != 1) throw std::runtime_error("multi-block cases are not supported");
+        c.walls.push_back({v[2], v[3] != 0, v[4], v[5], v[6], v[7], v[8], v[9]});
+        ng_check(v[4], v[5], v[6], v[7], v[8], v[9], NG);
+    }
+    r.skip(3);
+    n = count("periodic count");
+    r.next();
+    for (int q = 0; q < n; q++) {
+        auto v = ints(r.next());
+        if (v.size() < 18) throw std::runtime_error(c.bc_file + ": bad periodic line");
+        if (v[2] != 1 || v[10] != 1) throw std::runtime_error("multi-block cases are not supported");
+        PeriodicIO p;
+        p.orient = v[1]; p.f1 = v[3]; p.f2 = v[11];
+        for (int d = 0; d < 6; d++) { p.r1[d] = v[4 + d]; p.r2[d] = v[12 + d]; }
+        c.periodics.push_back(p);
+        ng_check(v[4], v[5], v[6], v[7], v[8], v[9], NG);
+    }
+    r.skip(3);
+    if (count("interior count") != 0) throw std::runtime_error("block interfaces are not supported (single-block cases only)");
+    r.next();
+    r.skip(3);
+    if (count("mixing-plane count") != 0) throw std::runtime_error("mixing planes are not supported");
+    r.next();
+    r.skip(3);
+    if (count("block count") != 1) throw std::runtime_error("only single-block cases are supported");
+    r.next();
+    {
+        // BID IM JM KM NBlade rpm (rpm read by a stream into a REAL: exact decimal parse)
+        std::string s = r.next();
+        const char *p = s.c_str();
+        char *e;
+        int v[5];
+        for (int q = 0; q < 5; q++) { v[q] = (int)std::strtol(p, &e, 10); p = e; }
+        c.rpm = std::strtod(p, &e);
+        c.IM = v[1]; c.JM = v[2]; c.KM = v[3]; c.nblade = v[4];
+        int IM = c.IM, JM = c.JM, KM = c.KM;
+        for (int j = 1; j <= std::min(std::min(IM, JM), KM); j++) {
+            int nn = 2 * j;
+            if ((IM - 1) % nn == 0 && (JM - 1) % nn == 0 && (KM - 1) % nn == 0 && (IM - 1) / nn > 2 &&
+                (JM - 1) / nn > 2 && (KM - 1) / nn > 2)
+                NG = std::min(j + 1, NG);
+            else
+                break;
+        }
+    }
+    c.ng = c.use_mg ? std::min(NG, 2) : 1;
+}
+
+void read_grid(CaseSpec &c)
+{
+    std::string path = c.dir + "/" + c.grid_file;
+    LineReader r(path, c.grid_file);
+    if (as_int(r.next(), "block count") != 1) throw std::runtime_error("only single-block grids are supported");
+    r.next();
+    int IM, JM, KM;
+    {
+        std::istringstream is(r.next());
+        if (!(is >> IM >> JM >> KM)) throw std::runtime_error(c.grid_file + ": bad block size line");
+    }
+    if (IM != c.IM || JM != c.JM || KM != c.KM)
+        throw std::runtime_error("grid and boundary file disagree on the block size");
+    size_t n = (size_t)IM * JM * KM;
+    c.x.resize(n); c.y.resize(n); c.z.resize(n);
+    for (size_t q = 0; q < n; q++) {
+        std::string s = r.next();
+        const char *p = s.c_str();
+        char *e;
+        c.x[q] = std::strtod(p, &e); if (e == p) throw std::runtime_error(c.grid_file + ": bad node line"); p = e;
+        c.y[q] = std::strtod(p, &e); if (e == p) throw std::runtime_error(c.grid_file + ": bad node line"); p = e;
+        c.z[q] = std::strtod(p, &e); if (e == p) throw std::runtime_error(c.grid_file + ": bad node line");
+    }
+}
+
+void validate(const CaseSpec &c)
+{
+    if (c.IM < 4 || c.JM < 4 || c.KM < 4) throw std::runtime_error("each direction needs at least 4 nodes");
+    if (c.scheme != 200 && c.scheme != 300)
+        throw std::runtime_error("space scheme " + std::to_string(c.scheme) + " is not on this path (Steger-Warming 200, Roe 300)");
+    if (c.recon_var != 100 && c.recon_var != 200)
+        throw std::runtime_error("reconstruction variables " + std::to_string(c.recon_var) + " are not supported (100, 200)");
+    if (c.time_scheme >= 100 && c.time_scheme <= 400)
+        throw std::runtime_error("Runge-Kutta marching is not on this path (LU-SGS only)");
+    if (c.turb != 0 && c.turb != 100)
+        throw std::runtime_error("turbulence model " + std::to_string(c.turb) + " is not on this path (none 0, Baldwin-Lomax 100)");
+    if (c.irs) throw std::runtime_error("implicit residual smoothing is not on this path");
+    if (c.restart) throw std::runtime_error("restart from RestartSolution.dat is not supported by this reader");
+    if (!c.turbo_axial) throw std::runtime_error("only the axial outlet is on this path");
+    if (c.use_mg && c.coarse_iter < 1)
+        throw std::runtime_error("multigrid needs at least one coarse-grid iteration (the fine level is initialised from it)");
+    if (c.inlets.empty() || c.outlets.empty()) throw std::runtime_error("the case needs an inlet and an outlet");
+    for (auto &p : c.inlets)
+        if (p.ks != p.ke || (p.ks != 1 && p.ks != c.KM)) throw std::runtime_error("inlets must be k-faces (k = 1 or KM)");
+    for (auto &p : c.outlets)
+        if (p.ks != p.ke || p.ke != c.KM) throw std::runtime_error("the axial outlet must be the k = KM face");
+    for (auto &w : c.walls)
+        if (c.turb == 100 && (w.face == 5 || w.face == 6))
+            throw std::runtime_error("Baldwin-Lomax with k-face walls is not supported");
+}
+
+}  // namespace
+
+CaseSpec read_case(const std::string &dir)
+{
+    CaseSpec c;
+    c.dir = dir;
+    read_config(c);
+    read_bc(c);
+    read_grid(c);
+    validate(c);
+    return c;
+}
+
+}  // namespace gbt

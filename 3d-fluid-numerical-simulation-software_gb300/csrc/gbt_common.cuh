@@ -1,0 +1,146 @@
+// Shared device-side definitions of the GB300 residual-and-update path.
+//
+// Data layout: every array of one mesh level of one operating point ("solve") lives on a padded
+// box i in [-3, IM+3] x j in [-3, JM+3] x k in [-3, KM+3] with k contiguous (the axial index is
+// the longest one on turbomachinery passages, so warps read along it). Cell (i,j,k) spans nodes
+// i..i+1; index 0 and IM hold the first ghost layer of the reference solver and the two
+// reconstruction layers ("dummies") sit at -1,-2 and IM+1, IM+2. Face family f (0=I, 1=J, 2=K)
+// at (i,j,k) is the reference's FaceI/J/K[i][j][k]. All solves of a batch share one pool per
+// field; a solve's box starts at Lvl::base.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gbt {
+
+constexpr int PAD = 3;
+constexpr int NQ = 5;
+constexpr int NPV = 6;                 // dens u v w press temp
+enum { PD = 0, PU, PV, PW, PP, PT };
+
+struct Lvl {
+    int IM, JM, KM;                    // node counts
+    int NJ, NK;                        // padded extents (strides)
+    long long base;                    // offset of this solve's box in every pool of the level
+};
+
+__host__ __device__ inline long long ix(const Lvl &L, int i, int j, int k)
+{
+    return L.base + ((long long)(i + PAD) * L.NJ + (j + PAD)) * (long long)L.NK + (k + PAD);
+}
+__host__ __device__ inline long long box_size(int IM, int JM, int KM)
+{
+    return (long long)(IM + 1 + 2 * PAD) * (JM + 1 + 2 * PAD) * (KM + 1 + 2 * PAD);
+}
+
+// Geometry of a level (FP64 in both precision forms).
+struct Geo {
+    double *x, *y, *z;                        // nodes
+    double *S[3][3], *s[3], *c[3][3];          // face area vector, |S|, face centre
+    double *r[3], *th[3];                      // face polar radius / angle
+    double *m[3][9];                           // face metric coefficients
+    double *nrm[3][3], *t1[3][3], *t2[3][3];   // face frame: unit normal, tau1, tau2
+    double *qe[3];                             // normal entrainment speed of the face
+    double *vol, *cc[3], *cm[9];               // cell volume, centre, metrics
+    double *sb[3][3];                          // per cell, per direction: mean area vector
+    double *cn[3][3];                          // per cell, per direction: mean unit normal
+    double *cs[3];                             // per cell, per direction: mean |S|
+    double *cve[3];                            // per cell, per direction: entrainment speed
+};
+
+// Flow arrays of a level. T is the working type (double, or float in the mixed form).
+template <typename T>
+struct Flow {
+    double *cv[NQ];                                  // conserved variables (FP64 in both forms)
+    double *cvold[NQ];
+    T *pv[NPV];
+    T *mut, *omega, *dt;
+    T *lamc[3], *lamv[3];
+    T *Ff[3][NQ], *Vf[3][NQ];                        // face convective / viscous fluxes
+    T *res[NQ], *dq[NQ];
+    double *cv2h[NQ];                                // multigrid (coarse level only)
+    T *res2h[NQ], *dq2h[NQ];
+    int *flag;                                       // Baldwin-Lomax first-touch marks
+    const int *wallf[3];                             // per face: wall patch (1-based) or 0
+};
+
+// Per-solve scalars that evolve on the device (one record per solve).
+struct SolveState {
+    double cfl, cfl_res;
+    double res[NQ];
+    double m_in, m_out, pr, eff, m_ratio;
+    int flag_low_dt[4];                              // per level (index = level)
+    int iter;
+    int status;                                      // bit flags, see GBT_STATUS_*
+    int limiter_hits;
+    int pad_;
+};
+
+// Per-solve constants (copied once).
+struct SolveConst {
+    double w_rot;                                    // nondimensional rotation speed
+    double delta_th;                                 // periodic pitch angle (sign as used)
+    double pout;                                     // nondimensional back pressure
+    double nblade;
+};
+
+// Global (per handle) physical constants, in the reference's nondimensional units.
+struct Phys {
+    double gamma, rgas, pr_lam, pr_tur, re_ref;
+    double ptin, ttin;
+    double dens_ref, vel_ref, temp_ref;
+    double inlet_dir[3], inlet_vnm;
+    double c_timestep, relax;
+    double suth_c1, suth_c2;                         // (1 + 110.4/288.15) and 110.4/288.15 (float-rounded)
+    int equation_ns, turb_bl, recon_var, recon, scheme, limiter, global_dt, ndummy;
+};
+
+// Status bits reported per solve.
+enum {
+    GBT_STATUS_NAN = 1,          // a residual norm or an integral is not finite
+    GBT_STATUS_LIMITER = 2,      // the positivity limiter replaced cells in the last step
+    GBT_STATUS_LIMITER_OVF = 4,  // more limited cells than the list holds (processed by a full scan)
+};
+
+template <typename T> __device__ __forceinline__ T tsqrt(T x);
+template <> __device__ __forceinline__ double tsqrt<double>(double x) { return sqrt(x); }
+template <> __device__ __forceinline__ float tsqrt<float>(float x) { return sqrtf(x); }
+
+// Sutherland law of the reference (include/FluidProps.h:107-112); T^1.5 as T*sqrt(T).
+template <typename T>
+__device__ __forceinline__ T sutherland(const Phys &P, T temp)
+{
+    return (T)(1.0 / P.re_ref) * (temp * tsqrt(temp)) * (T)P.suth_c1 / (temp + (T)P.suth_c2);
+}
+
+// block -> (solve, local block) mapping: grid.y enumerates solves, grid.x covers the largest one
+struct Batch {
+    const Lvl *lv;               // per-solve level descriptors (device)
+    const SolveConst *sc;        // per-solve constants (device)
+    SolveState *st;              // per-solve state (device)
+    int nsolve;
+};
+
+// Thread -> (i,j,k) over the box [1, 1+ni) x [1, 1+nj) x [1, 1+nk), k fastest. Returns false for
+// threads past the end of the box of this solve.
+__device__ __forceinline__ bool box_index(int ni, int nj, int nk, int &i, int &j, int &k)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long n = (long long)ni * nj * nk;
+    if (t >= n) return false;
+    k = (int)(t % nk) + 1;
+    long long q = t / nk;
+    j = (int)(q % nj) + 1;
+    i = (int)(q / nj) + 1;
+    return true;
+}
+
+// number of faces of family f / of cells in each direction
+__host__ __device__ inline void face_extent(const Lvl &L, int f, int &ni, int &nj, int &nk)
+{
+    ni = L.IM - 1 + (f == 0);
+    nj = L.JM - 1 + (f == 1);
+    nk = L.KM - 1 + (f == 2);
+}
+
+}  // namespace gbt

@@ -1,0 +1,88 @@
+// Host-side declarations of the kernel launchers (one translation unit per stage).
+#pragma once
+#include "gbt_common.cuh"
+
+namespace gbt {
+
+// launch geometry of one level of a batch: grid.y enumerates solves, grid.x covers the largest
+// solve's box (blocks past a smaller solve's end return at once)
+struct LaunchCtx {
+    Batch batch;
+    cudaStream_t stream;
+    int maxIM = 0, maxJM = 0, maxKM = 0;     // maxima over the solves of this level
+    long long pool_n = 0;                     // elements of one field pool of this level
+    dim3 grid_n(long long n, int bs) const { return dim3((unsigned)((n + bs - 1) / bs), batch.nsolve); }
+    dim3 grid_cells(int bs) const { return grid_n((long long)(maxIM - 1) * (maxJM - 1) * (maxKM - 1), bs); }
+    dim3 grid_faces(int f, int bs) const
+    {
+        return grid_n((long long)(maxIM - 1 + (f == 0)) * (maxJM - 1 + (f == 1)) * (maxKM - 1 + (f == 2)), bs);
+    }
+    dim3 grid_plane(int bs) const { return grid_n((long long)(maxIM - 1) * (maxJM - 1), bs); }
+};
+
+// boundary patches in device form; every record names its solve
+struct DevInOut { int solve, face, is, ie, js, je, ks, ke; };
+struct DevWall { int solve, face, rotate, is, ie, js, je, ks, ke; };
+struct BcTables {
+    const DevInOut *inlet = nullptr; int n_inlet = 0, max_inlet = 0;     // max cells of a patch
+    const DevInOut *outlet = nullptr; int n_outlet = 0;
+    const DevWall *wall = nullptr; int n_wall = 0, max_wall = 0;
+    // walls grouped by their position in each solve's list (the reference applies them in order)
+    int n_wall_slot = 0;
+    int wall_slot_off[65] = {0};                  // first record of slot q; slot q has off[q+1]-off[q]
+    int wall_slot_lines[64] = {0};                // most wall-normal lines of a patch in slot q
+    // periodic exchange as a gather list: dst <- rotate(src, sign * delta_th of the solve)
+    const long long *per_dst = nullptr, *per_src = nullptr;
+    const int *per_meta = nullptr;                // solve * 4 + (sign + 1)
+    long long n_per = 0;
+    int max_outlet_im = 0;
+    const DevInOut *inlet_first = nullptr, *outlet_first = nullptr;   // per solve: Inlet[1], Outlet[1]
+};
+
+void launch_geometry(const LaunchCtx &ctx, const Geo &G, double *totalvol);
+
+template <typename T>
+void launch_boundary(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> F, const BcTables &bc);
+
+// residual stages; level = 1 for the fine mesh (turbulence model only there)
+template <typename T>
+void launch_resflux(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> F, const BcTables &bc,
+                    int level, T *scratch_dtmin);
+
+template <typename T>
+void launch_lusgs_sweeps(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> F, int max_plane);
+
+template <typename T>
+void launch_update(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> F, int level,
+                   int *bad_list, int bad_cap, int *bad_count);
+
+template <typename T>
+void launch_res_norm(const LaunchCtx &ctx, const Geo &G, Flow<T> F, const double *totalvol, double *partials,
+                     int nblk);
+
+template <typename T>
+void launch_integrals(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> F, const BcTables &bc);
+
+template <typename T>
+void launch_primitive(const LaunchCtx &ctx, const Phys &P, Flow<T> F);
+
+template <typename T>
+void launch_limiter(const LaunchCtx &ctx, const Phys &P, Flow<T> F, int level, int *bad_list, int bad_cap,
+                    int *bad_count);
+
+// multigrid transfer between fine (f) and coarse (c) levels
+template <typename T>
+void launch_restrict(const LaunchCtx &cf, const LaunchCtx &cc, const Geo &Gf, const Geo &Gc, Flow<T> Ff, Flow<T> Fc);
+template <typename T>
+void launch_forcing(const LaunchCtx &cc, Flow<T> Fc);
+template <typename T>
+void launch_delta(const LaunchCtx &cc, Flow<T> Fc);
+template <typename T>
+void launch_corner(const LaunchCtx &cc, Flow<T> Fc);
+template <typename T>
+void launch_interpolate(const LaunchCtx &cf, const LaunchCtx &cc, Flow<T> Ff, Flow<T> Fc, int init_from_coarse);
+
+// per-solve scalar stages
+void launch_cfl_ramp(const LaunchCtx &ctx, int iter);
+
+}  // namespace gbt

@@ -1,0 +1,430 @@
+// LU-SGS on i+j+k hyperplanes (source/LU_SGS_Marching.cpp:10-419): the forward sweep visits
+// planes 3 .. IM+JM+KM-3, the backward sweep the same planes in reverse; the cells of a plane
+// are independent, so a plane is one launch over all cells of all solves of the batch. The
+// off-diagonal terms use the matrix-free flux difference of the neighbour in the rotating
+// frame. Followed by the update Q += dQ (FP64 accumulation in both precision forms), the
+// primitive variables (source/PrimitiveVars.cpp:7-28), detection of out-of-range cells for the
+// limiter (source/Limit_FlowVars.cpp:8-118), and the residual norm (source/ComputeAllBlockVars.cpp:318-372).
+#include "gbt_common.cuh"
+#include "kernels.hpp"
+#include "flux.cuh"
+
+namespace gbt {
+
+// flux difference F_n(Q+dQ) - F_n(Q) of neighbour cell nb across its mean normal in direction d
+template <typename T>
+__device__ __forceinline__ void delt_fn(const Phys &P, const Geo &G, const Flow<T> &W, int d, long long nb, T out[5])
+{
+    const T nx = (T)G.cn[d][0][nb], ny = (T)G.cn[d][1][nb], nz = (T)G.cn[d][2][nb];
+    const T ve = (T)G.cve[d][nb];
+    const T od = (T)W.cv[0][nb], omx = (T)W.cv[1][nb], omy = (T)W.cv[2][nb], omz = (T)W.cv[3][nb], oe = (T)W.cv[4][nb];
+    const T nd = od + W.dq[0][nb], nmx = omx + W.dq[1][nb], nmy = omy + W.dq[2][nb], nmz = omz + W.dq[3][nb],
+            ne = oe + W.dq[4][nb];
+    const T inv = (T)1 / nd;
+    const T u = nmx * inv, v = nmy * inv, w = nmz * inv, E = ne * inv;
+    const T pn = ((T)P.gamma - (T)1) * nd * (E - (T)0.5 * (u * u + v * v + w * w));
+    const T po = W.pv[PP][nb];
+    const T oinv = (T)1 / od;
+    const T Vo = omx * oinv * nx + omy * oinv * ny + omz * oinv * nz;
+    const T Vn = u * nx + v * ny + w * nz;
+    const T dn = Vn - ve, dov = Vo - ve;
+    out[0] = nd * dn - od * dov;
+    out[1] = (nmx * dn + pn * nx) - (omx * dov + po * nx);
+    out[2] = (nmy * dn + pn * ny) - (omy * dov + po * ny);
+    out[3] = (nmz * dn + pn * nz) - (omz * dov + po * nz);
+    out[4] = ((ne + pn) * dn + pn * ve) - ((oe + po) * dov + po * ve);
+}
+
+template <typename T, int DIR>      // DIR = +1 forward (lower neighbours), -1 backward
+__global__ void __launch_bounds__(128) k_sweep(Batch B, Phys P, Geo G, Flow<T> W, int plane)
+{
+    const int s = blockIdx.y;
+    const Lvl L = B.lv[s];
+    const int nI = L.IM - 1, nJ = L.JM - 1, nK = L.KM - 1;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    // cells of the plane: i in [max(1, plane-nJ-nK), min(nI, plane-2)], j then k = plane-i-j
+    const int ilo = max(1, plane - nJ - nK), ihi = min(nI, plane - 2);
+    if (ilo > ihi) return;
+    const int i = ilo + t / nJ, j = 1 + t % nJ;
+    if (i > ihi) return;
+    const int k = plane - i - j;
+    if (k < 1 || k > nK) return;
+    const long long p = ix(L, i, j, k);
+    const long long stv[3] = {(long long)L.NJ * L.NK, (long long)L.NK, 1LL};
+    const int idx[3] = {i, j, k}, top[3] = {nI, nJ, nK};
+    const T relax = (T)P.relax;
+    const T alpha = (T)G.vol[p] / W.dt[p] + relax * (W.lamc[0][p] + W.lamc[1][p] + W.lamc[2][p]) +
+                    (T)2 * (W.lamv[0][p] + W.lamv[1][p] + W.lamv[2][p]);
+    T aw[3][5], vw[3][5];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const bool has = DIR > 0 ? (idx[d] != 1) : (idx[d] != top[d]);
+        if (has) {
+            const long long nb = DIR > 0 ? p - stv[d] : p + stv[d];
+            T dF[5];
+            delt_fn(P, G, W, d, nb, dF);
+            const T sd = (T)G.cs[d][nb];
+            const T rl = relax * W.lamc[d][nb], lv = W.lamv[d][nb];
+#pragma unroll
+            for (int c = 0; c < 5; c++) {
+                const T dqn = W.dq[c][nb];
+                aw[d][c] = DIR > 0 ? (T)0.5 * (dF[c] * sd + rl * dqn) : (T)0.5 * (dF[c] * sd - rl * dqn);
+                vw[d][c] = lv * dqn;
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < 5; c++) { aw[d][c] = (T)0; vw[d][c] = (T)0; }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 5; c++) {
+        T r;
+        if (DIR > 0) r = -W.res[c][p] + aw[0][c] + aw[1][c] + aw[2][c] + vw[0][c] + vw[1][c] + vw[2][c];
+        else r = alpha * W.dq[c][p] - aw[0][c] - aw[1][c] - aw[2][c] + vw[0][c] + vw[1][c] + vw[2][c];
+        W.dq[c][p] = r / alpha;
+    }
+}
+
+template <typename T>
+void launch_lusgs_sweeps(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, int max_plane)
+{
+    const Batch &B = ctx.batch;
+    // widest plane: at most min(nI, ...) rows of nJ cells; launch nI*nJ threads (rows outside the
+    // plane's i range exit at once)
+    dim3 g = ctx.grid_plane(128);
+    for (int pl = 3; pl <= max_plane; pl++) k_sweep<T, 1><<<g, 128, 0, ctx.stream>>>(B, P, G, W, pl);
+    for (int pl = max_plane; pl >= 3; pl--) k_sweep<T, -1><<<g, 128, 0, ctx.stream>>>(B, P, G, W, pl);
+}
+
+// primitive variables from the conserved ones
+template <typename T>
+__device__ __forceinline__ void prim_from_cons(const Phys &P, const double c[5], T q[6])
+{
+    const double d = c[0], u = c[1] / d, v = c[2] / d, w = c[3] / d;
+    const double V2 = u * u + v * v + w * w;
+    const double pr = (P.gamma - 1.0) * (c[4] - d * V2 / 2.0);
+    q[PD] = (T)d; q[PU] = (T)u; q[PV] = (T)v; q[PW] = (T)w; q[PP] = (T)pr; q[PT] = (T)(pr / d / P.rgas);
+}
+
+template <typename T>
+__device__ __forceinline__ bool out_of_range(const T q[6])
+{
+    const T dmin = (T)(double)1.0E-6f, dmax = (T)1000, pmin = (T)(double)1.0E-6f, pmax = (T)1000, vmax = (T)1000;
+    return q[PD] < dmin || q[PD] > dmax || q[PP] < pmin || q[PP] > pmax || q[PU] > vmax || q[PV] > vmax || q[PW] > vmax;
+}
+
+// Q_old = Q; Q += dQ; primitive variables; out-of-range cells appended to the solve's list
+template <typename T>
+__global__ void __launch_bounds__(256) k_update(Batch B, Phys P, Flow<T> W, int *bad_list, int bad_cap, int *bad_count)
+{
+    const int s = blockIdx.y;
+    const Lvl L = B.lv[s];
+    int i, j, k;
+    if (!box_index(L.IM - 1, L.JM - 1, L.KM - 1, i, j, k)) return;
+    const long long p = ix(L, i, j, k);
+    double c[5];
+#pragma unroll
+    for (int n = 0; n < 5; n++) {
+        const double o = W.cv[n][p];
+        W.cvold[n][p] = o;
+        c[n] = o + (double)W.dq[n][p];
+        W.cv[n][p] = c[n];
+    }
+    T q[6];
+    prim_from_cons<T>(P, c, q);
+#pragma unroll
+    for (int n = 0; n < 6; n++) W.pv[n][p] = q[n];
+    if (P.limiter && out_of_range(q)) {
+        int slot = atomicAdd(&bad_count[s], 1);
+        if (slot < bad_cap) bad_list[(long long)s * bad_cap + slot] = (int)(((long long)(i - 1) * (L.JM - 1) + (j - 1)) * (L.KM - 1) + (k - 1));
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_primitive(Batch B, Phys P, Flow<T> W)
+{
+    const Lvl L = B.lv[blockIdx.y];
+    int i, j, k;
+    if (!box_index(L.IM - 1, L.JM - 1, L.KM - 1, i, j, k)) return;
+    const long long p = ix(L, i, j, k);
+    double c[5];
+#pragma unroll
+    for (int n = 0; n < 5; n++) c[n] = W.cv[n][p];
+    T q[6];
+    prim_from_cons<T>(P, c, q);
+#pragma unroll
+    for (int n = 0; n < 6; n++) W.pv[n][p] = q[n];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_detect(Batch B, Phys P, Flow<T> W, int *bad_list, int bad_cap, int *bad_count)
+{
+    const int s = blockIdx.y;
+    const Lvl L = B.lv[s];
+    int i, j, k;
+    if (!box_index(L.IM - 1, L.JM - 1, L.KM - 1, i, j, k)) return;
+    const long long p = ix(L, i, j, k);
+    T q[6];
+#pragma unroll
+    for (int n = 0; n < 6; n++) q[n] = W.pv[n][p];
+    if (out_of_range(q)) {
+        int slot = atomicAdd(&bad_count[s], 1);
+        if (slot < bad_cap) bad_list[(long long)s * bad_cap + slot] = (int)(((long long)(i - 1) * (L.JM - 1) + (j - 1)) * (L.KM - 1) + (k - 1));
+    }
+}
+
+// The reference repairs limited cells one after another in i, j, k order, each from the mean of
+// its in-range neighbours as they are at that moment, so a repaired cell can feed a later one.
+// Rare; one thread per solve replays that order over the (sorted) list of flagged cells. When
+// the list overflowed, the thread scans every cell instead.
+template <typename T>
+__global__ void k_limiter(Batch B, Phys P, Flow<T> W, int level, int *bad_list, int bad_cap, int *bad_count)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= B.nsolve) return;
+    const int n = bad_count[s];
+    if (n == 0) { B.st[s].status &= ~GBT_STATUS_LIMITER; return; }
+    const Lvl L = B.lv[s];
+    const int nI = L.IM - 1, nJ = L.JM - 1, nK = L.KM - 1;
+    int *lst = bad_list + (long long)s * bad_cap;
+    const bool full = n > bad_cap;
+    if (!full) {
+        for (int a = 1; a < n; a++) {                 // insertion sort: lists are short
+            int v = lst[a], b = a - 1;
+            while (b >= 0 && lst[b] > v) { lst[b + 1] = lst[b]; b--; }
+            lst[b + 1] = v;
+        }
+    }
+    const long long total = (long long)nI * nJ * nK;
+    const long long m = full ? total : n;
+    for (long long e = 0; e < m; e++) {
+        const long long lin = full ? e : lst[e];
+        const int i = 1 + (int)(lin / ((long long)nJ * nK)), j = 1 + (int)((lin / nK) % nJ), k = 1 + (int)(lin % nK);
+        const long long p = ix(L, i, j, k);
+        T q[6];
+        for (int c = 0; c < 6; c++) q[c] = W.pv[c][p];
+        if (!out_of_range(q)) continue;
+        double d = 0, u = 0, v = 0, w = 0, pr = 0;
+        int kn = 0, i1 = 0, j1 = 0, k1 = 0;
+        for (int ia = -1; ia <= 1; ia++)
+            for (int ja = -1; ja <= 1; ja++)
+                for (int ka = -1; ka <= 1; ka++) {
+                    k1 = k + ka; j1 = j + ja; i1 = i + ia;
+                    if (i1 > 0 && i1 < L.IM && j1 > 0 && j1 < L.JM && k1 > 0 && k1 < L.KM) {
+                        const long long r = ix(L, i1, j1, k1);
+                        T qq[6];
+                        for (int c = 0; c < 6; c++) qq[c] = W.pv[c][r];
+                        if (!out_of_range(qq)) {
+                            d += qq[PD]; u += qq[PU]; v += qq[PV]; w += qq[PW]; pr += qq[PP]; kn++;
+                        }
+                    }
+                }
+        if (kn == 0) {
+            // last visited neighbour (i+1, j+1, k+1), clipped to the admissible range
+            const long long r = ix(L, i1, j1, k1);
+            d = W.pv[PD][r]; u = W.pv[PU][r]; v = W.pv[PV][r]; w = W.pv[PW][r]; pr = W.pv[PP][r];
+            const double lo = (double)1.0E-6f;
+            if (d < lo) d = lo;
+            if (d > 1000.0) d = 1000.0;
+            if (pr < lo) pr = lo;
+            if (pr > 1000.0) pr = 1000.0;
+            if (fabs(u) > 1000.0) u = u < 0 ? -1000.0 : 1000.0;
+            if (fabs(v) > 1000.0) v = v < 0 ? -1000.0 : 1000.0;
+            if (fabs(w) > 1000.0) w = w < 0 ? -1000.0 : 1000.0;
+        } else {
+            const double sn1 = (double)(1.0f / (float)kn);
+            d *= sn1; u *= sn1; v *= sn1; w *= sn1; pr *= sn1;
+        }
+        W.pv[PD][p] = (T)d; W.pv[PU][p] = (T)u; W.pv[PV][p] = (T)v; W.pv[PW][p] = (T)w; W.pv[PP][p] = (T)pr;
+        W.pv[PT][p] = (T)(pr / d / P.rgas);
+        W.cv[0][p] = d; W.cv[1][p] = d * u; W.cv[2][p] = d * v; W.cv[3][p] = d * w;
+        W.cv[4][p] = pr / (P.gamma - 1.0) + d * (u * u + v * v + w * w) / 2.0;
+    }
+    B.st[s].flag_low_dt[level] = 10;
+    B.st[s].status |= GBT_STATUS_LIMITER | (full ? GBT_STATUS_LIMITER_OVF : 0);
+    B.st[s].limiter_hits += n;
+}
+
+template <typename T>
+void launch_update(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, int level, int *bad_list,
+                   int bad_cap, int *bad_count)
+{
+    (void)G;
+    const Batch &B = ctx.batch;
+    cudaMemsetAsync(bad_count, 0, sizeof(int) * B.nsolve, ctx.stream);
+    k_update<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, W, bad_list, bad_cap, bad_count);
+    if (P.limiter) k_limiter<T><<<(B.nsolve + 31) / 32, 32, 0, ctx.stream>>>(B, P, W, level, bad_list, bad_cap, bad_count);
+}
+
+template <typename T>
+void launch_primitive(const LaunchCtx &ctx, const Phys &P, Flow<T> W)
+{
+    k_primitive<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(ctx.batch, P, W);
+}
+
+template <typename T>
+void launch_limiter(const LaunchCtx &ctx, const Phys &P, Flow<T> W, int level, int *bad_list, int bad_cap,
+                    int *bad_count)
+{
+    if (!P.limiter) return;
+    const Batch &B = ctx.batch;
+    cudaMemsetAsync(bad_count, 0, sizeof(int) * B.nsolve, ctx.stream);
+    k_detect<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, W, bad_list, bad_cap, bad_count);
+    k_limiter<T><<<(B.nsolve + 31) / 32, 32, 0, ctx.stream>>>(B, P, W, level, bad_list, bad_cap, bad_count);
+}
+
+// ---- residual norm: sum |(Q_old - Q)/Q_old| * Vol / V_total, FP64, fixed-order two-stage sum ----
+template <typename T>
+__global__ void __launch_bounds__(256) k_norm_partial(Batch B, Geo G, Flow<T> W, double *partials, int nblk)
+{
+    const int s = blockIdx.y;
+    const Lvl L = B.lv[s];
+    const int nI = L.IM - 1, nJ = L.JM - 1, nK = L.KM - 1;
+    const long long n = (long long)nI * nJ * nK;
+    double acc[5] = {0, 0, 0, 0, 0};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)nblk * blockDim.x) {
+        const int k = (int)(t % nK) + 1;
+        const long long q = t / nK;
+        const int j = (int)(q % nJ) + 1, i = (int)(q / nJ) + 1;
+        const long long p = ix(L, i, j, k);
+        const double vol = G.vol[p];
+#pragma unroll
+        for (int c = 0; c < 5; c++) {
+            const double o = W.cvold[c][p];
+            acc[c] += fabs((o - W.cv[c][p]) / o) * vol;
+        }
+    }
+    __shared__ double sh[8][5];
+#pragma unroll
+    for (int c = 0; c < 5; c++) {
+        double v = acc[c];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5][c] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
+        double v = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += sh[w][threadIdx.x];
+        partials[((long long)s * nblk + blockIdx.x) * 5 + threadIdx.x] = v;
+    }
+}
+
+__global__ void k_norm_final(Batch B, const double *partials, int nblk, const double *totalvol)
+{
+    const int s = blockIdx.x;
+    if (threadIdx.x >= 5) return;
+    double v = 0;
+    for (int b = 0; b < nblk; b++) v += partials[((long long)s * nblk + b) * 5 + threadIdx.x];
+    v = v / totalvol[s];
+    B.st[s].res[threadIdx.x] = v;
+    if (threadIdx.x == 0 && !isfinite(v)) B.st[s].status |= GBT_STATUS_NAN;
+}
+
+template <typename T>
+void launch_res_norm(const LaunchCtx &ctx, const Geo &G, Flow<T> W, const double *totalvol, double *partials, int nblk)
+{
+    const Batch &B = ctx.batch;
+    k_norm_partial<T><<<dim3(nblk, B.nsolve), 256, 0, ctx.stream>>>(B, G, W, partials, nblk);
+    k_norm_final<<<B.nsolve, 32, 0, ctx.stream>>>(B, partials, nblk, totalvol);
+}
+
+// ---- inlet/outlet integrals (source/Ouput.cpp:9-107,282-300), one block per solve ----
+template <typename T>
+__device__ void section_sums(const Phys &P, const Geo &G, const Flow<T> &W, const Lvl &L, int K, double out[3])
+{
+    // out: mass flow, sum Pt^((g-1)/g) * m, sum Tt * m (all over the same faces)
+    const int nI = L.IM - 1, nJ = L.JM - 1;
+    const double g = P.gamma, g1 = g - 1.0, R = P.rgas;
+    double m = 0, pm = 0, tm = 0;
+    for (int t = threadIdx.x; t < nI * nJ; t += blockDim.x) {
+        const int i = 1 + t / nJ, j = 1 + t % nJ;
+        const long long p = ix(L, i, j, K), q = ix(L, i, j, K - 1);
+        const double d = 0.5 * ((double)W.pv[PD][p] + (double)W.pv[PD][q]);
+        const double u = 0.5 * ((double)W.pv[PU][p] + (double)W.pv[PU][q]);
+        const double v = 0.5 * ((double)W.pv[PV][p] + (double)W.pv[PV][q]);
+        const double w = 0.5 * ((double)W.pv[PW][p] + (double)W.pv[PW][q]);
+        const double mc = d * (u * G.S[2][0][p] + v * G.S[2][1][p] + w * G.S[2][2][p]);
+        const double tf = 0.5 * ((double)W.pv[PT][p] + (double)W.pv[PT][q]);
+        const double Ma = sqrt(u * u + v * v + w * w) / sqrt(g * R * tf);
+        const double fac = 1.0 + g1 / 2.0 * Ma * Ma;
+        const double Pt = (double)W.pv[PP][p] * pow(fac, g / g1);
+        m += mc;
+        pm += pow(Pt, g1 / g) * mc;
+        tm += (double)W.pv[PT][p] * fac * mc;
+    }
+    __shared__ double sh[3][32];
+    double v3[3] = {m, pm, tm};
+    for (int c = 0; c < 3; c++) {
+        double v = v3[c];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) sh[c][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    for (int c = 0; c < 3; c++) {
+        double v = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += sh[c][w];
+        out[c] = v;
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__global__ void k_integrals(Batch B, Phys P, Geo G, Flow<T> W, const DevInOut *inl, const DevInOut *outl)
+{
+    const int s = blockIdx.x;
+    const Lvl L = B.lv[s];
+    double a[3], b[3];
+    section_sums(P, G, W, L, inl[s].ks, a);
+    section_sums(P, G, W, L, outl[s].ks, b);
+    if (threadIdx.x != 0) return;
+    const double g = P.gamma, g1 = g - 1.0, R = P.rgas;
+    const double nbl = B.sc[s].nblade;
+    const double mi = a[0] * P.dens_ref * P.vel_ref * nbl, mo = b[0] * P.dens_ref * P.vel_ref * nbl;
+    const double pti = pow(a[1] / a[0], g / g1) * P.dens_ref * P.vel_ref * P.vel_ref;
+    const double pto = pow(b[1] / b[0], g / g1) * P.dens_ref * P.vel_ref * P.vel_ref;
+    const double tti = a[2] / a[0] * P.temp_ref, tto = b[2] / b[0] * P.temp_ref;
+    const double PR = pto / pti;
+    const double Ladk = g / g1 * R * tti * (pow(PR, g1 / g) - 1.0);
+    const double Lk = g / g1 * R * tti * (tto / tti - 1.0);
+    SolveState &st = B.st[s];
+    st.m_in = mi; st.m_out = mo; st.pr = PR; st.eff = Ladk / Lk;
+    st.m_ratio = fabs((mi - mo) / mi);
+    if (!isfinite(mi) || !isfinite(mo)) st.status |= GBT_STATUS_NAN;
+}
+
+template <typename T>
+void launch_integrals(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const BcTables &bc)
+{
+    // first inlet and first outlet patch of every solve (the reference reports Inlet[1], Outlet[1])
+    k_integrals<T><<<ctx.batch.nsolve, 256, 0, ctx.stream>>>(ctx.batch, P, G, W, bc.inlet_first, bc.outlet_first);
+}
+
+// CFL ramp of the driver (source/Solver.cpp:49-60): x1.2 whenever the density residual falls
+// below a threshold that then drops tenfold; capped at 10
+__global__ void k_cfl_ramp(Batch B, int iter)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= B.nsolve || iter <= 1) return;
+    SolveState &st = B.st[s];
+    if (st.res[0] <= st.cfl_res) {
+        st.cfl = st.cfl * (double)1.2f;
+        st.cfl_res = st.cfl_res / 10.0;
+    }
+    if (st.cfl > 10.0) st.cfl = 10.0;
+}
+void launch_cfl_ramp(const LaunchCtx &ctx, int iter)
+{
+    k_cfl_ramp<<<(ctx.batch.nsolve + 127) / 128, 128, 0, ctx.stream>>>(ctx.batch, iter);
+}
+
+#define GBT_INST(T)                                                                                                   \
+    template void launch_lusgs_sweeps<T>(const LaunchCtx &, const Phys &, const Geo &, Flow<T>, int);                 \
+    template void launch_update<T>(const LaunchCtx &, const Phys &, const Geo &, Flow<T>, int, int *, int, int *);     \
+    template void launch_primitive<T>(const LaunchCtx &, const Phys &, Flow<T>);                                       \
+    template void launch_limiter<T>(const LaunchCtx &, const Phys &, Flow<T>, int, int *, int, int *);                 \
+    template void launch_res_norm<T>(const LaunchCtx &, const Geo &, Flow<T>, const double *, double *, int);          \
+    template void launch_integrals<T>(const LaunchCtx &, const Phys &, const Geo &, Flow<T>, const BcTables &);
+GBT_INST(double)
+GBT_INST(float)
+
+}  // namespace gbt

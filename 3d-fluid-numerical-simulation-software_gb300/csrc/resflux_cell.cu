@@ -1,0 +1,238 @@
+// Cell-centred stages of the residual: spectral radii and vorticity magnitude
+// (source/Spectral_curl_grad.cpp:9-83), Baldwin-Lomax eddy viscosity along wall-normal grid
+// lines (source/BL_Model.cpp:8-329), local time step and viscous spectral radii
+// (source/TimeStep.cpp:7-93), and the wall ghost of mu_t (source/WallFlux.cpp:106-109).
+#include "gbt_common.cuh"
+#include "kernels.hpp"
+#include "flux.cuh"
+
+namespace gbt {
+
+// lambda_c per direction and |curl V| (needs ghosts of the velocity)
+template <typename T>
+__global__ void __launch_bounds__(256) k_cell_a(Batch B, Phys P, Geo G, Flow<T> W)
+{
+    const int s = blockIdx.y;
+    const Lvl L = B.lv[s];
+    int i, j, k;
+    if (!box_index(L.IM - 1, L.JM - 1, L.KM - 1, i, j, k)) return;
+    const long long p = ix(L, i, j, k);
+    const T w_rot = (T)B.sc[s].w_rot;
+    const T u = W.pv[PU][p], v = W.pv[PV][p], w = W.pv[PW][p];
+    const T ur = u + w_rot * (T)G.cc[1][p];
+    const T vr = v - w_rot * (T)G.cc[0][p];
+    const T cs = tsqrt((T)P.gamma * (T)P.rgas * W.pv[PT][p]);
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        T sx = (T)G.sb[d][0][p], sy = (T)G.sb[d][1][p], sz = (T)G.sb[d][2][p];
+        W.lamc[d][p] = tabs(ur * sx + vr * sy + w * sz) + cs * tsqrt(sx * sx + sy * sy + sz * sz);
+    }
+    if (!P.equation_ns) return;
+    const long long sI = (long long)L.NJ * L.NK, sJ = L.NK;
+    const T h = (T)0.5;
+    T uk = h * (W.pv[PU][p + sI] - W.pv[PU][p - sI]), vk = h * (W.pv[PV][p + sI] - W.pv[PV][p - sI]), wk = h * (W.pv[PW][p + sI] - W.pv[PW][p - sI]);
+    T ue = h * (W.pv[PU][p + sJ] - W.pv[PU][p - sJ]), ve = h * (W.pv[PV][p + sJ] - W.pv[PV][p - sJ]), we = h * (W.pv[PW][p + sJ] - W.pv[PW][p - sJ]);
+    T uz = h * (W.pv[PU][p + 1] - W.pv[PU][p - 1]), vz = h * (W.pv[PV][p + 1] - W.pv[PV][p - 1]), wz = h * (W.pv[PW][p + 1] - W.pv[PW][p - 1]);
+    T m0 = (T)G.cm[0][p], m1 = (T)G.cm[1][p], m2 = (T)G.cm[2][p], m3 = (T)G.cm[3][p], m4 = (T)G.cm[4][p],
+      m5 = (T)G.cm[5][p], m6 = (T)G.cm[6][p], m7 = (T)G.cm[7][p], m8 = (T)G.cm[8][p];
+    T v_x = vk * m0 + ve * m3 + vz * m6, w_x = wk * m0 + we * m3 + wz * m6;
+    T u_y = uk * m1 + ue * m4 + uz * m7, w_y = wk * m1 + we * m4 + wz * m7;
+    T u_z = uk * m2 + ue * m5 + uz * m8, v_z = vk * m2 + ve * m5 + vz * m8;
+    W.omega[p] = tsqrt(h * ((w_y - v_z) * (w_y - v_z) + (u_z - w_x) * (u_z - w_x) + (v_x - u_y) * (v_x - u_y)));
+}
+
+// One thread per wall-normal line of one wall patch. The line runs across the whole block from
+// the wall face; Baldwin-Lomax inner/outer viscosity (source/BL_Model.cpp:283-329), merged into
+// mu_t as the minimum over all walls whose lines cross the cell, wall-adjacent cell and its ghost
+// set to zero (source/BL_Model.cpp:101-119).
+template <typename T>
+__global__ void __launch_bounds__(128) k_bl(Batch B, Phys P, Geo G, Flow<T> W, const DevWall *walls, int off)
+{
+    const DevWall wl = walls[off + blockIdx.y];
+    const int s = wl.solve;
+    const Lvl L = B.lv[s];
+    const int dirn = (wl.face - 1) / 2, lo = wl.face % 2 == 1;
+    int a0, a1, b0, b1;                  // a: fast (coalesced) tangential index, b: the other one
+    if (dirn == 0) { a0 = wl.ks; a1 = wl.ke; b0 = wl.js; b1 = wl.je; }
+    else if (dirn == 1) { a0 = wl.ks; a1 = wl.ke; b0 = wl.is; b1 = wl.ie; }
+    else { a0 = wl.js; a1 = wl.je; b0 = wl.is; b1 = wl.ie; }
+    const int na = a1 - a0 + 1, nb = b1 - b0 + 1;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)na * nb) return;
+    const int a = a0 + (int)(t % na), b = b0 + (int)(t / na);
+    const int N = dirn == 0 ? L.IM : (dirn == 1 ? L.JM : L.KM);
+    const long long sn = dirn == 0 ? (long long)L.NJ * L.NK : (dirn == 1 ? (long long)L.NK : 1LL);
+    long long p0;                        // cell n = 0 of the line; cell n is p0 + n*sn
+    long long fw;                        // wall face
+    if (dirn == 0) { p0 = ix(L, 0, b, a); fw = ix(L, lo ? 1 : L.IM, b, a); }
+    else if (dirn == 1) { p0 = ix(L, b, 0, a); fw = ix(L, b, lo ? 1 : L.JM, a); }
+    else { p0 = ix(L, b, a, 0); fw = ix(L, b, a, lo ? 1 : L.KM); }
+    const double fx = G.c[dirn][0][fw], fy = G.c[dirn][1][fw], fz = G.c[dirn][2][fw];
+    // walk in the reference's line order n0 = 1..N-1 (n0 = 1 next to the wall)
+#define CELL(n0) (p0 + (long long)(lo ? (n0) : N - (n0)) * sn)
+    T Tw = (T)0, dens1 = (T)0, mul1 = (T)1;
+    for (int n0 = 1; n0 < N; n0++) {
+        long long p = CELL(n0);
+        T ml = sutherland(P, W.pv[PT][p]);
+        T tw = tabs(W.omega[p] * ml);
+        if (n0 == 1) { Tw = tw; dens1 = W.pv[PD][p]; mul1 = ml; }
+        else if (tw > Tw) Tw = tw;
+    }
+    const T Ret = tsqrt(dens1 * Tw) / mul1;
+    const T Aplus = (T)26.0, kap = (T)(double)0.4f, Ckleb = (T)(double)0.3f;
+    const T aCcp = (T)((double)0.0168f * (double)1.6f);
+    T Fmax = (T)0, ymax = (T)0, Udif = (T)0;
+    for (int n0 = 1; n0 < N; n0++) {
+        long long p = CELL(n0);
+        T dx = (T)(G.cc[0][p] - fx), dy = (T)(G.cc[1][p] - fy), dz = (T)(G.cc[2][p] - fz);
+        T dis = tsqrt(dx * dx + dy * dy + dz * dz);
+        T u = W.pv[PU][p], v = W.pv[PV][p], w = W.pv[PW][p];
+        T V = tsqrt(u * u + v * v + w * w);
+        if (V > Udif) Udif = V;
+        T F = dis * tabs(W.omega[p]) * ((T)1 - exp(-(dis * Ret) / Aplus));
+        if (F > Fmax) { Fmax = F; ymax = dis; }
+    }
+    T q = ymax * Udif * Udif / Fmax;
+    T Fwake = (ymax * Fmax < q) ? ymax * Fmax : q;
+    for (int n0 = 1; n0 < N; n0++) {
+        long long p = CELL(n0);
+        T dx = (T)(G.cc[0][p] - fx), dy = (T)(G.cc[1][p] - fy), dz = (T)(G.cc[2][p] - fz);
+        T dis = tsqrt(dx * dx + dy * dy + dz * dz);
+        T bL = kap * dis * ((T)1 - exp(-(Ret * dis) / Aplus));
+        T om = W.omega[p], rho = W.pv[PD][p];
+        T m_in = rho * bL * bL * om;
+        T r = Ckleb * dis / ymax;
+        T r2 = r * r;
+        T Fk = (T)1 / ((T)1 + (T)5.5 * (r2 * r2 * r2));
+        T m_out = aCcp * rho * Fwake * Fk;
+        T mt = (tabs(m_in) > tabs(m_out)) ? m_out : m_in;
+        if (W.flag[p] == 0) { W.flag[p] = 1; W.mut[p] = mt; }
+        else { T old = W.mut[p]; W.mut[p] = (old < mt) ? old : mt; }
+    }
+    W.mut[CELL(1)] = (T)0;
+    W.mut[p0 + (long long)(lo ? 0 : N) * sn] = (T)0;
+#undef CELL
+}
+
+// ghost mu_t mirrored across every wall face (source/WallFlux.cpp:106-109,137-140,168-171)
+template <typename T>
+__global__ void k_wall_mut(Batch B, Flow<T> W, const DevWall *walls)
+{
+    const DevWall wl = walls[blockIdx.y];
+    const Lvl L = B.lv[wl.solve];
+    const int ni = wl.ie - wl.is + 1, nj = wl.je - wl.js + 1, nk = wl.ke - wl.ks + 1;
+    int i, j, k;
+    if (!box_index(ni, nj, nk, i, j, k)) return;
+    i += wl.is - 1; j += wl.js - 1; k += wl.ks - 1;
+    const int f = (wl.face - 1) / 2;
+    const long long p = ix(L, i, j, k);
+    const long long m = f == 0 ? ix(L, i - 1, j, k) : (f == 1 ? ix(L, i, j - 1, k) : ix(L, i, j, k - 1));
+    if (wl.face % 2 == 1) W.mut[m] = -W.mut[p];
+    else W.mut[p] = -W.mut[m];
+}
+
+// viscous spectral radii and the local time step
+template <typename T>
+__global__ void __launch_bounds__(256) k_cell_b(Batch B, Phys P, Geo G, Flow<T> W, int level)
+{
+    const int s = blockIdx.y;
+    const Lvl L = B.lv[s];
+    int i, j, k;
+    if (!box_index(L.IM - 1, L.JM - 1, L.KM - 1, i, j, k)) return;
+    const long long p = ix(L, i, j, k);
+    const int fl = B.st[s].flag_low_dt[level];
+    const double dtf = fl == 0 ? 1.0 : (double)(1.0f / (1.0f + (float)fl));
+    const T vol = (T)G.vol[p];
+    T lc = W.lamc[0][p] + W.lamc[1][p] + W.lamc[2][p];
+    T lv = (T)0;
+    if (P.equation_ns) {
+        const T ml = sutherland(P, W.pv[PT][p]);
+        const T mt = W.mut[p];
+        const T rho = W.pv[PD][p];
+        const T a = (T)(double)(4.0f / 3.0f) / rho, b = (T)P.gamma / rho;
+        const T coef = (a > b ? a : b) * (ml / (T)P.pr_lam + mt / (T)P.pr_tur);
+        T l[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            T sx = (T)G.sb[d][0][p], sy = (T)G.sb[d][1][p], sz = (T)G.sb[d][2][p];
+            l[d] = coef * (sx * sx + sy * sy + sz * sz) / vol;
+            W.lamv[d][p] = l[d];
+        }
+        lv = l[0] + l[1] + l[2];
+    }
+    W.dt[p] = (T)(dtf * B.st[s].cfl) * vol / (lc + (T)P.c_timestep * lv);
+}
+
+// global time stepping: minimum over the solve, then broadcast (source/TimeStep.cpp:64-87)
+template <typename T>
+__global__ void k_dt_min(Batch B, Flow<T> W, T *out)
+{
+    const Lvl L = B.lv[blockIdx.y];
+    const int nI = L.IM - 1, nJ = L.JM - 1, nK = L.KM - 1;
+    const long long n = (long long)nI * nJ * nK;
+    T m = (T)1E10;
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+        int k = (int)(t % nK) + 1;
+        long long q = t / nK;
+        int j = (int)(q % nJ) + 1, i = (int)(q / nJ) + 1;
+        T v = W.dt[ix(L, i, j, k)];
+        m = (m < v) ? m : v;
+    }
+    __shared__ T sh[1024];
+    sh[threadIdx.x] = m;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) { T v = sh[threadIdx.x + o]; sh[threadIdx.x] = sh[threadIdx.x] < v ? sh[threadIdx.x] : v; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.y] = sh[0];
+}
+template <typename T>
+__global__ void k_dt_set(Batch B, Flow<T> W, const T *mn)
+{
+    const Lvl L = B.lv[blockIdx.y];
+    int i, j, k;
+    if (!box_index(L.IM - 1, L.JM - 1, L.KM - 1, i, j, k)) return;
+    W.dt[ix(L, i, j, k)] = mn[blockIdx.y];
+}
+
+// decrement of the low-time-step counter after the time step used it
+__global__ void k_after_timestep(Batch B, int level)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= B.nsolve) return;
+    if (B.st[s].flag_low_dt[level] > 0) B.st[s].flag_low_dt[level] -= 1;
+}
+
+template <typename T>
+void launch_cell_stages(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const BcTables &bc,
+                        int level, T *scratch)
+{
+    const Batch &B = ctx.batch;
+    k_cell_a<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, G, W);
+    if (level == 1 && P.turb_bl && bc.n_wall > 0) {
+        // first-touch marks of the minimum merge, reset every evaluation
+        cudaMemsetAsync(W.flag, 0, (size_t)ctx.pool_n * sizeof(int), ctx.stream);
+        for (int q = 0; q < bc.n_wall_slot; q++) {
+            int n = bc.wall_slot_off[q + 1] - bc.wall_slot_off[q];
+            if (n <= 0) continue;
+            dim3 g((unsigned)((bc.wall_slot_lines[q] + 127) / 128), n);
+            k_bl<T><<<g, 128, 0, ctx.stream>>>(B, P, G, W, bc.wall, bc.wall_slot_off[q]);
+        }
+    }
+    if (bc.n_wall > 0) {
+        dim3 g((unsigned)((bc.max_wall + 127) / 128), bc.n_wall);
+        k_wall_mut<T><<<g, 128, 0, ctx.stream>>>(B, W, bc.wall);
+    }
+    k_cell_b<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, G, W, level);
+    if (P.global_dt) {
+        k_dt_min<T><<<dim3(1, B.nsolve), 1024, 0, ctx.stream>>>(B, W, scratch);
+        k_dt_set<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, W, scratch);
+    }
+    k_after_timestep<<<(B.nsolve + 127) / 128, 128, 0, ctx.stream>>>(B, level);
+}
+
+template void launch_cell_stages<double>(const LaunchCtx &, const Phys &, const Geo &, Flow<double>, const BcTables &, int, double *);
+template void launch_cell_stages<float>(const LaunchCtx &, const Phys &, const Geo &, Flow<float>, const BcTables &, int, float *);
+
+}  // namespace gbt

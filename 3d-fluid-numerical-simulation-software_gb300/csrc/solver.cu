@@ -1,0 +1,765 @@
+// Solver orchestration: memory layout of a batch, boundary tables, geometry set-up and the
+// reference's iteration sequence (source/Solver.cpp:47-140, source/LU_SGS_Marching.cpp:10-291,
+// source/ComputeAllBlockVars.cpp:223-255) as kernel launches on one stream, replayed through
+// CUDA graphs.
+#include "solver.hpp"
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <stdexcept>
+#include <algorithm>
+
+namespace gbt {
+
+void check_cuda(cudaError_t e, const char *what)
+{
+    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(x) check_cuda((x), #x)
+
+NonDim nondimensionalise(const CaseSpec &c)
+{
+    NonDim n;
+    const float PIf = 3.1415926535897932f;
+    n.temp_ref = c.Ttin;
+    n.vel_ref = std::sqrt(c.Gamma * c.Rgas * n.temp_ref);
+    n.mue_ref = 1.716e-5f * std::pow(n.temp_ref / 288.15f, 3.0f / 2.0f) * (288.15f + 110.4f) / (n.temp_ref + 110.4f);
+    n.dens_ref = c.Ptin / c.Rgas / n.temp_ref;
+    n.re_ref = n.dens_ref * n.vel_ref * c.Len_ref / n.mue_ref;
+    double ma_ref = 1.0f;
+    n.pout = c.Pout / (n.dens_ref * n.vel_ref * n.vel_ref);
+    n.ttin = 1.0f;
+    n.ptin = 1.0f / c.Gamma;
+    n.rgas = 1.0f / (ma_ref * ma_ref * c.Gamma);
+    n.w_rot = (2.0f * PIf * c.rpm / 60.0f) / (n.vel_ref / c.Len_ref);
+    n.delta_th = (double)(2.0f * PIf / (float)c.nblade);
+    return n;
+}
+
+// ----------------------------------------------------------------------------------------
+// one mesh level of the whole batch
+// ----------------------------------------------------------------------------------------
+template <typename T>
+struct Level {
+    int id = 1;
+    std::vector<Lvl> lv;                  // per solve
+    std::vector<SolveConst> sc;
+    Lvl *lv_d = nullptr;
+    SolveConst *sc_d = nullptr;
+    long long pool_n = 0;
+    int maxIM = 0, maxJM = 0, maxKM = 0, max_plane = 0;
+    DevBuf geo_mem, flow_d_mem, flow_t_mem, int_mem, tab_mem, meta_mem;
+    Geo G{};
+    Flow<T> W{};
+    double *totalvol = nullptr;
+    BcTables bc;
+    std::vector<DevWall> walls_h;
+    bool use_force = false;
+    LaunchCtx ctx(const Batch &B, cudaStream_t s) const
+    {
+        LaunchCtx c;
+        c.batch = B;
+        c.batch.lv = lv_d;
+        c.batch.sc = sc_d;
+        c.stream = s;
+        c.maxIM = maxIM; c.maxJM = maxJM; c.maxKM = maxKM;
+        c.pool_n = pool_n;
+        return c;
+    }
+};
+
+// level boxes of one case: level 2 re-indexes the patches of level 1 (source/UserInput.cpp:449-796)
+static int ci(int s0, int e0, bool first) { return first ? (s0 + 1) / 2 : (s0 == e0 ? (e0 + 1) / 2 : e0 / 2); }
+static void coarse_patch(int &s, int &e) { int a = s, b = e; s = ci(a, b, true); e = ci(a, b, false); }
+
+struct LevelCase {
+    int IM, JM, KM;
+    std::vector<PatchIO> in, out;
+    std::vector<WallIO> walls;
+    std::vector<PeriodicIO> per;
+    std::vector<double> x, y, z;          // nodes, ((k-1)*JM + (j-1))*IM + (i-1)
+};
+
+static LevelCase level_case(const CaseSpec &c, int level)
+{
+    LevelCase L;
+    if (level == 1) {
+        L.IM = c.IM; L.JM = c.JM; L.KM = c.KM;
+        L.in = c.inlets; L.out = c.outlets; L.walls = c.walls; L.per = c.periodics;
+        L.x = c.x; L.y = c.y; L.z = c.z;
+        return L;
+    }
+    L.IM = (c.IM + 1) / 2; L.JM = (c.JM + 1) / 2; L.KM = (c.KM + 1) / 2;
+    size_t n = (size_t)L.IM * L.JM * L.KM;
+    L.x.resize(n); L.y.resize(n); L.z.resize(n);
+    for (int k = 1; k <= L.KM; k++)
+        for (int j = 1; j <= L.JM; j++)
+            for (int i = 1; i <= L.IM; i++) {
+                size_t q = ((size_t)(k - 1) * L.JM + (j - 1)) * L.IM + (i - 1);
+                size_t f = ((size_t)(2 * k - 2) * c.JM + (2 * j - 2)) * c.IM + (2 * i - 2);
+                L.x[q] = c.x[f]; L.y[q] = c.y[f]; L.z[q] = c.z[f];
+            }
+    for (auto p : c.inlets) { coarse_patch(p.is, p.ie); coarse_patch(p.js, p.je); coarse_patch(p.ks, p.ke); L.in.push_back(p); }
+    for (auto p : c.outlets) { coarse_patch(p.is, p.ie); coarse_patch(p.js, p.je); coarse_patch(p.ks, p.ke); L.out.push_back(p); }
+    for (auto w : c.walls) { coarse_patch(w.is, w.ie); coarse_patch(w.js, w.je); coarse_patch(w.ks, w.ke); L.walls.push_back(w); }
+    for (auto p : c.periodics) {
+        for (int d = 0; d < 3; d++) { coarse_patch(p.r1[2 * d], p.r1[2 * d + 1]); coarse_patch(p.r2[2 * d], p.r2[2 * d + 1]); }
+        L.per.push_back(p);
+    }
+    return L;
+}
+
+// Face-local traversal of a periodic patch in the order of the reference's shadow buffers
+// (source/ShadowOutIn.cpp:15-164, 324-497): returns, for every (l, m), the interior cell read at
+// layer nd and the ghost / reconstruction cell written at layer nd.
+struct PatchCell { int l, m; int ri, rj, rk; int gi, gj, gk; };
+static std::vector<PatchCell> patch_walk(int fc, int nd, const int *r, int IM, int JM, int KM, int &lmax, int &mmax)
+{
+    std::vector<PatchCell> v;
+    int is = r[0], ie = r[1], js = r[2], je = r[3], ks = r[4], ke = r[5];
+    auto rng = [](int s, int e) { std::vector<int> a; int x = s; do { a.push_back(x); x++; } while (x <= e); return a; };
+    switch (fc) {
+    case 1: lmax = std::abs(ke - ks) + 1; mmax = std::abs(je - js) + 1;
+        { int l = 1; for (int k : rng(ks, ke)) { int m = 1; for (int j : rng(js, je)) { v.push_back({l, m, nd, j, k, -nd, j, k}); m++; } l++; } } break;
+    case 2: lmax = std::abs(je - js) + 1; mmax = std::abs(ke - ks) + 1;
+        { int l = 1; for (int j : rng(js, je)) { int m = 1; for (int k : rng(ks, ke)) { v.push_back({l, m, IM - nd, j, k, IM + nd, j, k}); m++; } l++; } } break;
+    case 3: lmax = std::abs(ie - is) + 1; mmax = std::abs(ke - ks) + 1;
+        { int l = 1; for (int i : rng(is, ie)) { int m = 1; for (int k : rng(ks, ke)) { v.push_back({l, m, i, nd, k, i, -nd, k}); m++; } l++; } } break;
+    case 4: lmax = std::abs(ke - ks) + 1; mmax = std::abs(ie - is) + 1;
+        { int l = 1; for (int k : rng(ks, ke)) { int m = 1; for (int i : rng(is, ie)) { v.push_back({l, m, i, JM - nd, k, i, JM + nd, k}); m++; } l++; } } break;
+    case 5: lmax = std::abs(je - js) + 1; mmax = std::abs(ie - is) + 1;
+        { int l = 1; for (int j : rng(js, je)) { int m = 1; for (int i : rng(is, ie)) { v.push_back({l, m, i, j, nd, i, j, -nd}); m++; } l++; } } break;
+    case 6: lmax = std::abs(ie - is) + 1; mmax = std::abs(je - js) + 1;
+        { int l = 1; for (int i : rng(is, ie)) { int m = 1; for (int j : rng(js, je)) { v.push_back({l, m, i, j, KM - nd, i, j, KM + nd}); m++; } l++; } } break;
+    default: throw std::runtime_error("bad periodic face type");
+    }
+    return v;
+}
+// (l1, m1) of the sending face -> (l2, m2) of the receiving face (source/ShadowOutIn.cpp:167-321)
+static void trans(int ori, int l1, int m1, int L1, int M1, int &l2, int &m2)
+{
+    switch (ori) {
+    case 1: l2 = l1; m2 = M1 + 1 - m1; break;
+    case 2: l2 = m1; m2 = l1; break;
+    case 3: l2 = L1 + 1 - l1; m2 = m1; break;
+    case 4: l2 = M1 + 1 - m1; m2 = L1 + 1 - l1; break;
+    default: throw std::runtime_error("bad periodic orientation");
+    }
+}
+
+// interior cells of a level set to the uniform start (source/Initialization.cpp:17-76)
+__global__ void k_fill_uniform(Batch B, double *cv0, double *cv1, double *cv2, double *cv3, double *cv4, double c0,
+                               double c1, double c2, double c3, double c4)
+{
+    const Lvl L = B.lv[blockIdx.y];
+    int i, j, k;
+    if (!box_index(L.IM - 1, L.JM - 1, L.KM - 1, i, j, k)) return;
+    const long long p = ix(L, i, j, k);
+    cv0[p] = c0; cv1[p] = c1; cv2[p] = c2; cv3[p] = c3; cv4[p] = c4;
+}
+
+// start of a driver iteration: iteration counter and CFL ramp (source/Solver.cpp:49-60)
+__global__ void k_iter_begin(Batch B)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= B.nsolve) return;
+    SolveState &st = B.st[s];
+    st.iter += 1;
+    if (st.iter > 1) {
+        if (st.res[0] <= st.cfl_res) {
+            st.cfl = st.cfl * (double)1.2f;
+            st.cfl_res = st.cfl_res / (double)10.0f;
+        }
+        if (st.cfl > (double)10.0f) st.cfl = (double)10.0f;
+    }
+}
+
+template <typename T>
+class SolverT : public SolverBase {
+public:
+    Level<T> lev[3];
+    DevBuf st_mem, scratch_mem;
+    SolveState *st_d = nullptr;
+    int *bad_list = nullptr, *bad_count = nullptr;
+    const int bad_cap = 4096;
+    double *norm_part = nullptr;
+    const int norm_blk = 64;
+    T *dtmin = nullptr;
+    cudaGraphExec_t graphs[3] = {nullptr, nullptr, nullptr};
+
+    Batch batch(int l) const
+    {
+        Batch B;
+        B.lv = lev[l].lv_d; B.sc = lev[l].sc_d; B.st = st_d; B.nsolve = nsolve;
+        return B;
+    }
+    LaunchCtx ctx(int l) const { return lev[l].ctx(batch(l), stream); }
+
+    explicit SolverT(const std::vector<std::string> &dirs, int prec)
+    {
+        precision = prec;
+        nsolve = (int)dirs.size();
+        if (nsolve < 1) throw std::runtime_error("no case directories given");
+        for (auto &d : dirs) cases.push_back(read_case(d));
+        const CaseSpec &c0 = cases[0];
+        for (auto &c : cases) {
+            if (c.ng != c0.ng || c.coarse_iter != c0.coarse_iter || c.scheme != c0.scheme || c.recon != c0.recon ||
+                c.recon_var != c0.recon_var || c.turb != c0.turb || c.equation_ns != c0.equation_ns ||
+                c.limiter != c0.limiter || c.global_dt != c0.global_dt || c.Gamma != c0.Gamma || c.Rgas != c0.Rgas ||
+                c.Pr_lam != c0.Pr_lam || c.Pr_tur != c0.Pr_tur || c.Ptin != c0.Ptin || c.Ttin != c0.Ttin ||
+                c.Len_ref != c0.Len_ref || c.relax != c0.relax || c.C_timestep != c0.C_timestep ||
+                std::memcmp(c.inlet_dir, c0.inlet_dir, sizeof c.inlet_dir) != 0)
+                throw std::runtime_error("the cases of one batch must share numerics, gas and inlet options (only grid, back pressure, speed and blade count may differ)");
+        }
+        ng = c0.ng;
+        coarse_iter = c0.coarse_iter;
+        NonDim nd0 = nondimensionalise(c0);
+        P.gamma = c0.Gamma; P.rgas = nd0.rgas; P.pr_lam = c0.Pr_lam; P.pr_tur = c0.Pr_tur; P.re_ref = nd0.re_ref;
+        P.ptin = nd0.ptin; P.ttin = nd0.ttin; P.dens_ref = nd0.dens_ref; P.vel_ref = nd0.vel_ref; P.temp_ref = nd0.temp_ref;
+        for (int d = 0; d < 3; d++) P.inlet_dir[d] = c0.inlet_dir[d];
+        P.inlet_vnm = std::sqrt(c0.inlet_dir[0] * c0.inlet_dir[0] + c0.inlet_dir[1] * c0.inlet_dir[1] + c0.inlet_dir[2] * c0.inlet_dir[2]);
+        P.c_timestep = c0.C_timestep; P.relax = c0.relax;
+        P.suth_c1 = (double)(1.0f + 110.4f / 288.15f);
+        P.suth_c2 = (double)(110.4f / 288.15f);
+        P.equation_ns = c0.equation_ns; P.turb_bl = c0.turb == 100; P.recon_var = c0.recon_var; P.recon = c0.recon;
+        P.scheme = c0.scheme; P.limiter = c0.limiter; P.global_dt = c0.global_dt;
+        P.ndummy = c0.recon == 0 ? 3 : 2;
+
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        // per-solve state
+        st_mem.bytes = sizeof(SolveState) * nsolve;
+        CK(cudaMalloc(&st_mem.p, st_mem.bytes));
+        st_d = (SolveState *)st_mem.p;
+        std::vector<SolveState> st(nsolve);
+        for (int s = 0; s < nsolve; s++) {
+            std::memset(&st[s], 0, sizeof(SolveState));
+            st[s].cfl = cases[s].CFL;
+            st[s].cfl_res = (double)1.0E-3f;
+        }
+        CK(cudaMemcpy(st_d, st.data(), st_mem.bytes, cudaMemcpyHostToDevice));
+        // scratch: limiter lists, norm partials, global-dt minima
+        size_t sb = sizeof(int) * (size_t)nsolve * (bad_cap + 1) + sizeof(double) * (size_t)nsolve * norm_blk * 5 + sizeof(T) * nsolve + 256;
+        scratch_mem.bytes = sb;
+        CK(cudaMalloc(&scratch_mem.p, sb));
+        char *q = (char *)scratch_mem.p;
+        norm_part = (double *)q; q += sizeof(double) * (size_t)nsolve * norm_blk * 5;
+        bad_list = (int *)q; q += sizeof(int) * (size_t)nsolve * bad_cap;
+        bad_count = (int *)q; q += sizeof(int) * nsolve;
+        dtmin = (T *)(((uintptr_t)q + 15) & ~(uintptr_t)15);
+        for (int l = 1; l <= ng; l++) build_level(l);
+    }
+
+    ~SolverT() override
+    {
+        for (auto &g : graphs) if (g) cudaGraphExecDestroy(g);
+        if (stream) { cudaStreamSynchronize(stream); cudaStreamDestroy(stream); }
+    }
+
+    void build_level(int l)
+    {
+        Level<T> &Lv = lev[l];
+        Lv.id = l;
+        std::vector<LevelCase> lc;
+        long long base = 0;
+        for (int s = 0; s < nsolve; s++) {
+            lc.push_back(level_case(cases[s], l));
+            const LevelCase &c = lc.back();
+            Lvl v;
+            v.IM = c.IM; v.JM = c.JM; v.KM = c.KM;
+            v.NJ = c.JM + 1 + 2 * PAD; v.NK = c.KM + 1 + 2 * PAD;
+            v.base = base;
+            base += box_size(c.IM, c.JM, c.KM);
+            Lv.lv.push_back(v);
+            NonDim nd = nondimensionalise(cases[s]);
+            SolveConst sc;
+            sc.w_rot = nd.w_rot; sc.delta_th = nd.delta_th; sc.pout = nd.pout; sc.nblade = cases[s].nblade;
+            Lv.sc.push_back(sc);
+            Lv.maxIM = std::max(Lv.maxIM, c.IM); Lv.maxJM = std::max(Lv.maxJM, c.JM); Lv.maxKM = std::max(Lv.maxKM, c.KM);
+            Lv.max_plane = std::max(Lv.max_plane, c.IM + c.JM + c.KM - 3);
+        }
+        Lv.pool_n = base;
+        const size_t N = (size_t)base;
+        // device descriptors
+        CK(cudaMalloc(&Lv.meta_mem.p, sizeof(Lvl) * nsolve + sizeof(SolveConst) * nsolve + 16));
+        Lv.lv_d = (Lvl *)Lv.meta_mem.p;
+        Lv.sc_d = (SolveConst *)((char *)Lv.meta_mem.p + ((sizeof(Lvl) * nsolve + 15) & ~(size_t)15));
+        CK(cudaMemcpy(Lv.lv_d, Lv.lv.data(), sizeof(Lvl) * nsolve, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(Lv.sc_d, Lv.sc.data(), sizeof(SolveConst) * nsolve, cudaMemcpyHostToDevice));
+        // geometry pools (FP64)
+        const int NGEO = 124;
+        Lv.geo_mem.bytes = sizeof(double) * N * NGEO + sizeof(double) * nsolve;
+        CK(cudaMalloc(&Lv.geo_mem.p, Lv.geo_mem.bytes));
+        CK(cudaMemset(Lv.geo_mem.p, 0, Lv.geo_mem.bytes));
+        double *g = (double *)Lv.geo_mem.p;
+        auto take = [&]() { double *r = g; g += N; return r; };
+        Geo &G = Lv.G;
+        G.x = take(); G.y = take(); G.z = take();
+        for (int f = 0; f < 3; f++) {
+            for (int c = 0; c < 3; c++) { G.S[f][c] = take(); G.c[f][c] = take(); G.nrm[f][c] = take(); G.t1[f][c] = take(); G.t2[f][c] = take(); }
+            G.s[f] = take(); G.r[f] = take(); G.th[f] = take(); G.qe[f] = take();
+            for (int c = 0; c < 9; c++) G.m[f][c] = take();
+            for (int c = 0; c < 3; c++) { G.sb[f][c] = take(); G.cn[f][c] = take(); }
+            G.cs[f] = take(); G.cve[f] = take();
+        }
+        G.vol = take();
+        for (int c = 0; c < 3; c++) G.cc[c] = take();
+        for (int c = 0; c < 9; c++) G.cm[c] = take();
+        Lv.totalvol = g;
+        // flow pools
+        Lv.flow_d_mem.bytes = sizeof(double) * N * 15;
+        CK(cudaMalloc(&Lv.flow_d_mem.p, Lv.flow_d_mem.bytes));
+        CK(cudaMemset(Lv.flow_d_mem.p, 0, Lv.flow_d_mem.bytes));
+        double *d = (double *)Lv.flow_d_mem.p;
+        Flow<T> &W = Lv.W;
+        for (int c = 0; c < NQ; c++) { W.cv[c] = d; d += N; W.cvold[c] = d; d += N; W.cv2h[c] = d; d += N; }
+        Lv.flow_t_mem.bytes = sizeof(T) * N * 66;
+        CK(cudaMalloc(&Lv.flow_t_mem.p, Lv.flow_t_mem.bytes));
+        CK(cudaMemset(Lv.flow_t_mem.p, 0, Lv.flow_t_mem.bytes));
+        T *t = (T *)Lv.flow_t_mem.p;
+        auto tk = [&]() { T *r = t; t += N; return r; };
+        for (int c = 0; c < NPV; c++) W.pv[c] = tk();
+        W.mut = tk(); W.omega = tk(); W.dt = tk();
+        for (int f = 0; f < 3; f++) { W.lamc[f] = tk(); W.lamv[f] = tk(); for (int c = 0; c < NQ; c++) { W.Ff[f][c] = tk(); W.Vf[f][c] = tk(); } }
+        for (int c = 0; c < NQ; c++) { W.res[c] = tk(); W.dq[c] = tk(); W.res2h[c] = tk(); W.dq2h[c] = tk(); }
+        Lv.int_mem.bytes = sizeof(int) * N * 4;
+        CK(cudaMalloc(&Lv.int_mem.p, Lv.int_mem.bytes));
+        CK(cudaMemset(Lv.int_mem.p, 0, Lv.int_mem.bytes));
+        int *ip = (int *)Lv.int_mem.p;
+        W.flag = ip;
+        int *wallf[3] = {ip + N, ip + 2 * N, ip + 3 * N};
+        for (int f = 0; f < 3; f++) W.wallf[f] = wallf[f];
+        // nodes
+        {
+            std::vector<double> hx(N, 0.0), hy(N, 0.0), hz(N, 0.0);
+            for (int s = 0; s < nsolve; s++) {
+                const LevelCase &c = lc[s];
+                const Lvl &v = Lv.lv[s];
+                for (int k = 1; k <= c.KM; k++)
+                    for (int j = 1; j <= c.JM; j++)
+                        for (int i = 1; i <= c.IM; i++) {
+                            size_t q = ((size_t)(k - 1) * c.JM + (j - 1)) * c.IM + (i - 1);
+                            long long p = ix(v, i, j, k);
+                            hx[p] = c.x[q]; hy[p] = c.y[q]; hz[p] = c.z[q];
+                        }
+            }
+            CK(cudaMemcpy(G.x, hx.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(G.y, hy.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(G.z, hz.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+            build_tables(l, lc, hx, hy);
+        }
+        launch_geometry(ctx(l), G, Lv.totalvol);
+        CK(cudaStreamSynchronize(stream));
+        CK(cudaGetLastError());
+    }
+
+    void build_tables(int l, const std::vector<LevelCase> &lc, const std::vector<double> &hx, const std::vector<double> &hy)
+    {
+        Level<T> &Lv = lev[l];
+        BcTables &bc = Lv.bc;
+        std::vector<DevInOut> inl, outl, inl1, outl1;
+        std::vector<DevWall> walls;
+        std::vector<long long> pdst, psrc;
+        std::vector<int> pmeta;
+        std::vector<int> wallf[3];
+        for (int f = 0; f < 3; f++) wallf[f].assign((size_t)Lv.pool_n, 0);
+        size_t max_walls = 0;
+        for (auto &c : lc) max_walls = std::max(max_walls, c.walls.size());
+        if (max_walls > 64) throw std::runtime_error("at most 64 wall patches per case");
+        for (int s = 0; s < nsolve; s++) {
+            const LevelCase &c = lc[s];
+            for (auto &p : c.in) {
+                inl.push_back({s, p.face, p.is, p.ie, p.js, p.je, p.ks, p.ke});
+                bc.max_inlet = std::max(bc.max_inlet, (p.ie - p.is + 1) * (p.je - p.js + 1));
+            }
+            for (auto &p : c.out) outl.push_back({s, p.face, p.is, p.ie, p.js, p.je, p.ks, p.ke});
+            if (c.out.size() != 1) throw std::runtime_error("exactly one axial outlet per case is supported");
+            inl1.push_back(inl[inl.size() - c.in.size()]);
+            outl1.push_back(outl.back());
+            bc.max_outlet_im = std::max(bc.max_outlet_im, c.IM);
+        }
+        // walls ordered by their position in each case's list, then by solve
+        bc.n_wall_slot = (int)max_walls;
+        for (size_t q = 0; q < max_walls; q++) {
+            bc.wall_slot_off[q] = (int)walls.size();
+            int lines = 0;
+            for (int s = 0; s < nsolve; s++) {
+                if (q >= lc[s].walls.size()) continue;
+                const WallIO &w = lc[s].walls[q];
+                walls.push_back({s, w.face, w.rotate, w.is, w.ie, w.js, w.je, w.ks, w.ke});
+                int nf = (w.ie - w.is + 1) * (w.je - w.js + 1) * (w.ke - w.ks + 1);
+                bc.max_wall = std::max(bc.max_wall, nf);
+                lines = std::max(lines, nf);
+            }
+            bc.wall_slot_lines[q] = lines;
+        }
+        bc.wall_slot_off[max_walls] = (int)walls.size();
+        // per-face wall marks in patch order (a later patch overwrites an earlier one's face)
+        for (int s = 0; s < nsolve; s++) {
+            for (size_t q = 0; q < lc[s].walls.size(); q++) {
+                int rec = -1;
+                for (int r = bc.wall_slot_off[q]; r < bc.wall_slot_off[q + 1]; r++)
+                    if (walls[r].solve == s) rec = r;
+                const WallIO &w = lc[s].walls[q];
+                int f = (w.face - 1) / 2;
+                for (int i = w.is; i <= w.ie; i++)
+                    for (int j = w.js; j <= w.je; j++)
+                        for (int k = w.ks; k <= w.ke; k++) wallf[f][ix(Lv.lv[s], i, j, k)] = rec + 1;
+            }
+        }
+        // periodic gather list, last writer wins as in the reference's sequential copies
+        for (int s = 0; s < nsolve; s++) {
+            const LevelCase &c = lc[s];
+            const Lvl &v = Lv.lv[s];
+            std::map<long long, size_t> last;
+            for (auto &pr : c.per) {
+                long long pa = ix(v, pr.r1[0], pr.r1[2], pr.r1[4]), pb = ix(v, pr.r2[0], pr.r2[2], pr.r2[4]);
+                double th1 = std::atan(hy[pa] / hx[pa]), th2 = std::atan(hy[pb] / hx[pb]);
+                if ((th2 - th1) < 0.0)
+                    throw std::runtime_error("periodic pair listed against the pitch direction (the reference flips the pitch sign on every call then); list the lower-theta face first");
+                for (int nd = 1; nd <= P.ndummy; nd++) {
+                    for (int dir = 0; dir < 2; dir++) {
+                        const int *ra = dir == 0 ? pr.r1 : pr.r2, *rb = dir == 0 ? pr.r2 : pr.r1;
+                        int fa = dir == 0 ? pr.f1 : pr.f2, fb = dir == 0 ? pr.f2 : pr.f1;
+                        int La, Ma, Lb, Mb;
+                        auto A = patch_walk(fa, nd, ra, c.IM, c.JM, c.KM, La, Ma);
+                        auto Bw = patch_walk(fb, nd, rb, c.IM, c.JM, c.KM, Lb, Mb);
+                        std::map<std::pair<int, int>, long long> src;
+                        for (auto &e : A) {
+                            int l2, m2;
+                            trans(pr.orient, e.l, e.m, La, Ma, l2, m2);
+                            src[{l2, m2}] = ix(v, e.ri, e.rj, e.rk);
+                        }
+                        for (auto &e : Bw) {
+                            auto it = src.find({e.l, e.m});
+                            if (it == src.end()) throw std::runtime_error("periodic patches of different size");
+                            int sign = dir == 0 ? 1 : -1;
+                            long long dsts[2] = {ix(v, e.gi, e.gj, e.gk), -1};
+                            if (nd == 1) {
+                                // the first layer also fills the ghost cell next to the face
+                                int gi = e.gi, gj = e.gj, gk = e.gk;
+                                if (gi < 0) gi = 0; else if (gi > c.IM) gi = c.IM;
+                                if (gj < 0) gj = 0; else if (gj > c.JM) gj = c.JM;
+                                if (gk < 0) gk = 0; else if (gk > c.KM) gk = c.KM;
+                                if (gi == c.IM + 1) gi = c.IM;
+                                dsts[1] = ix(v, gi, gj, gk);
+                            }
+                            for (long long dd : dsts) {
+                                if (dd < 0) continue;
+                                auto f = last.find(dd);
+                                if (f != last.end()) { psrc[f->second] = it->second; pmeta[f->second] = s * 4 + sign + 1; }
+                                else { last[dd] = pdst.size(); pdst.push_back(dd); psrc.push_back(it->second); pmeta.push_back(s * 4 + sign + 1); }
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        // upload everything into one table buffer
+        auto bytes = [](size_t n, size_t sz) { return (n * sz + 255) & ~(size_t)255; };
+        size_t tot = bytes(inl.size(), sizeof(DevInOut)) + bytes(outl.size(), sizeof(DevInOut)) + bytes(inl1.size(), sizeof(DevInOut)) +
+                     bytes(outl1.size(), sizeof(DevInOut)) + bytes(walls.size(), sizeof(DevWall)) + bytes(pdst.size(), 8) * 2 +
+                     bytes(pmeta.size(), 4) + 256;
+        CK(cudaMalloc(&Lv.tab_mem.p, tot));
+        char *q = (char *)Lv.tab_mem.p;
+        auto up = [&](const void *h, size_t n, size_t sz) {
+            void *dptr = q;
+            if (n) CK(cudaMemcpy(dptr, h, n * sz, cudaMemcpyHostToDevice));
+            q += bytes(n, sz);
+            return dptr;
+        };
+        bc.inlet = (const DevInOut *)up(inl.data(), inl.size(), sizeof(DevInOut)); bc.n_inlet = (int)inl.size();
+        bc.outlet = (const DevInOut *)up(outl.data(), outl.size(), sizeof(DevInOut)); bc.n_outlet = (int)outl.size();
+        bc.inlet_first = (const DevInOut *)up(inl1.data(), inl1.size(), sizeof(DevInOut));
+        bc.outlet_first = (const DevInOut *)up(outl1.data(), outl1.size(), sizeof(DevInOut));
+        bc.wall = (const DevWall *)up(walls.data(), walls.size(), sizeof(DevWall)); bc.n_wall = (int)walls.size();
+        bc.per_dst = (const long long *)up(pdst.data(), pdst.size(), 8);
+        bc.per_src = (const long long *)up(psrc.data(), psrc.size(), 8);
+        bc.per_meta = (const int *)up(pmeta.data(), pmeta.size(), 4);
+        bc.n_per = (long long)pdst.size();
+        for (int f = 0; f < 3; f++)
+            CK(cudaMemcpy((void *)Lv.W.wallf[f], wallf[f].data(), sizeof(int) * (size_t)Lv.pool_n, cudaMemcpyHostToDevice));
+        Lv.walls_h = walls;
+    }
+
+    // ---------------------------------------------------------------- reference call surface
+    void init_uniform() override
+    {
+        // source/Initialization.cpp:34-68 (nondimensional inlet totals; FP64 like the reference)
+        const CaseSpec &c = cases[0];
+        const double Gamma = P.gamma, Rgas = P.rgas, Ma0 = c.Ma0;
+        const double press = P.ptin * std::pow(1.0f + (Gamma - 1.0f) / 2.0f * Ma0 * Ma0, 0.0f - Gamma / (Gamma - 1.0f));
+        const double temp = P.ttin * std::pow(1.0f + (Gamma - 1.0f) / 2.0f * Ma0 * Ma0, 0.0f - 1.0f);
+        const double dens = press / (Rgas * temp);
+        const double Vel = std::pow(Gamma * Rgas * temp, 0.5f) * Ma0;
+        const double *a = c.inlet_dir;
+        const double n_m = std::pow(a[0] * a[0] + a[1] * a[1] + a[2] * a[2], 0.5);
+        const double u = Vel * a[0] / n_m, v = Vel * a[1] / n_m, w = Vel * a[2] / n_m;
+        const double V2 = u * u + v * v + w * w;
+        const double ener = press / (dens * (Gamma - 1.0f)) + V2 / 2.0f;
+        int l = ng == 1 ? 1 : 2;
+        LaunchCtx cx = ctx(l);
+        Flow<T> &W = lev[l].W;
+        k_fill_uniform<<<cx.grid_cells(256), 256, 0, stream>>>(cx.batch, W.cv[0], W.cv[1], W.cv[2], W.cv[3], W.cv[4], dens,
+                                                               dens * u, dens * v, dens * w, dens * ener);
+        launch_primitive<T>(cx, P, W);
+        CK(cudaGetLastError());
+    }
+    void resflux(int l) override
+    {
+        launch_resflux<T>(ctx(l), P, lev[l].G, lev[l].W, lev[l].bc, l, dtmin);
+    }
+    void time_marching(int l) override
+    {
+        LaunchCtx cx = ctx(l);
+        Level<T> &Lv = lev[l];
+        if (!Lv.use_force) resflux(l);
+        else launch_forcing<T>(cx, Lv.W);
+        launch_lusgs_sweeps<T>(cx, P, Lv.G, Lv.W, Lv.max_plane);
+        launch_update<T>(cx, P, Lv.G, Lv.W, l, bad_list, bad_cap, bad_count);
+    }
+    void res_calculate(int l) override { launch_res_norm<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, norm_part, norm_blk); }
+    void primitive_vars(int l) override { launch_primitive<T>(ctx(l), P, lev[l].W); }
+    void limit_vars(int l) override { launch_limiter<T>(ctx(l), P, lev[l].W, l, bad_list, bad_cap, bad_count); }
+    void corner_treatment(int l) override { launch_corner<T>(ctx(l), lev[l].W); }
+    void restrict_to_coarse() override
+    {
+        need_mg();
+        launch_restrict<T>(ctx(1), ctx(2), lev[1].G, lev[2].G, lev[1].W, lev[2].W);
+    }
+    void interpolate(int init) override
+    {
+        need_mg();
+        launch_interpolate<T>(ctx(1), ctx(2), lev[1].W, lev[2].W, init);
+    }
+    void delta_cons() override { need_mg(); launch_delta<T>(ctx(2), lev[2].W); }
+    void integrals(int l) override { launch_integrals<T>(ctx(l), P, lev[l].G, lev[l].W, lev[l].bc); }
+    void set_use_force(int l, bool on) override { lev[l].use_force = on; }
+    void need_mg() const { if (ng < 2) throw std::runtime_error("the case runs on a single grid level"); }
+
+    void begin_iteration() { k_iter_begin<<<(nsolve + 127) / 128, 128, 0, stream>>>(batch(1)); }
+
+    // CSolver::Solver (source/Solver.cpp:47-140) for the current iteration number
+    void step_body()
+    {
+        if (ng == 1) { time_marching(1); res_calculate(1); return; }
+        if (iter < coarse_iter) { time_marching(2); res_calculate(2); }
+        else if (iter == coarse_iter) {
+            time_marching(2); res_calculate(2); corner_treatment(2);
+            interpolate(1); primitive_vars(1); limit_vars(1);
+        } else {
+            lev[2].use_force = true;
+            time_marching(1); res_calculate(1);
+            resflux(1);
+            restrict_to_coarse();
+            primitive_vars(2); limit_vars(2);
+            time_marching(2);
+            delta_cons();
+            corner_treatment(2);
+            interpolate(0);
+            primitive_vars(1); limit_vars(1);
+        }
+    }
+    int report_level() const { return (ng != 1 && iter <= coarse_iter) ? 2 : 1; }
+    int phase() const { return ng == 1 ? 0 : (iter < coarse_iter ? 1 : (iter == coarse_iter ? -1 : 2)); }
+
+    void solver_step() override
+    {
+        iter++;
+        begin_iteration();
+        step_body();
+    }
+
+    // the driver loop (source/Structured_FV3D.cpp:142-219): step + integrals, one graph per phase
+    void iterate(int n, double *hist) override
+    {
+        std::vector<SolveState> st(nsolve);
+        for (int q = 0; q < n; q++) {
+            iter++;
+            int ph = phase();
+            if (use_graphs && ph >= 0) {
+                if (!graphs[ph]) {
+                    cudaGraph_t g;
+                    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                    begin_iteration();
+                    step_body();
+                    integrals(report_level());
+                    CK(cudaStreamEndCapture(stream, &g));
+                    CK(cudaGraphInstantiate(&graphs[ph], g, 0));
+                    cudaGraphDestroy(g);
+                }
+                CK(cudaGraphLaunch(graphs[ph], stream));
+            } else {
+                begin_iteration();
+                step_body();
+                integrals(report_level());
+            }
+            if (hist) {
+                CK(cudaMemcpyAsync(st.data(), st_d, sizeof(SolveState) * nsolve, cudaMemcpyDeviceToHost, stream));
+                CK(cudaStreamSynchronize(stream));
+                for (int s = 0; s < nsolve; s++) {
+                    double *r = hist + ((size_t)q * nsolve + s) * 12;
+                    r[0] = st[s].iter;
+                    for (int c = 0; c < 5; c++) r[1 + c] = st[s].res[c];
+                    r[6] = st[s].m_in; r[7] = st[s].m_out; r[8] = st[s].pr; r[9] = st[s].eff; r[10] = st[s].m_ratio;
+                    r[11] = st[s].cfl;
+                }
+            }
+        }
+        CK(cudaGetLastError());
+    }
+
+    void states(SolveState *out) override
+    {
+        CK(cudaMemcpyAsync(out, st_d, sizeof(SolveState) * nsolve, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+    }
+
+    void dims(int solve, int l, int out[4]) const override
+    {
+        const Lvl &v = lev[l].lv[solve];
+        out[0] = v.IM; out[1] = v.JM; out[2] = v.KM; out[3] = ng;
+    }
+
+    // ---------------------------------------------------------------- field access (tests, I/O)
+    template <typename U>
+    void fetch(const U *dptr, const Lvl &v, std::vector<double> &out)
+    {
+        long long n = box_size(v.IM, v.JM, v.KM);
+        std::vector<U> tmp((size_t)n);
+        CK(cudaMemcpyAsync(tmp.data(), dptr + v.base, sizeof(U) * n, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        out.assign(tmp.begin(), tmp.end());
+    }
+
+    // a box [i0,i1]x[j0,j1]x[k0,k1] of several component arrays, components fastest
+    struct Comp { const double *d; const T *t; };
+    long box(const Lvl &v, const std::vector<Comp> &cs, int i0, int i1, int j0, int j1, int k0, int k1, double *out, long cap)
+    {
+        long n = (long)(i1 - i0 + 1) * (j1 - j0 + 1) * (k1 - k0 + 1) * (long)cs.size();
+        if (n > cap) return -1;
+        std::vector<std::vector<double>> h(cs.size());
+        for (size_t c = 0; c < cs.size(); c++) {
+            if (cs[c].d) fetch(cs[c].d, v, h[c]);
+            else fetch(cs[c].t, v, h[c]);
+        }
+        long q = 0;
+        Lvl z = v;
+        z.base = 0;
+        for (int i = i0; i <= i1; i++)
+            for (int j = j0; j <= j1; j++)
+                for (int k = k0; k <= k1; k++) {
+                    long long p = ix(z, i, j, k);
+                    for (size_t c = 0; c < cs.size(); c++) out[q++] = h[c][(size_t)p];
+                }
+        return n;
+    }
+
+    long get_field(int solve, int l, const std::string &name, double *out, long cap) override
+    {
+        if (solve < 0 || solve >= nsolve || l < 1 || l > ng) return -1;
+        CK(cudaStreamSynchronize(stream));
+        const Lvl &v = lev[l].lv[solve];
+        const Flow<T> &W = lev[l].W;
+        const Geo &G = lev[l].G;
+        const int IM = v.IM, JM = v.JM, KM = v.KM;
+        auto D = [](const double *p) { return Comp{p, nullptr}; };
+        auto Tt = [](const T *p) { return Comp{nullptr, p}; };
+        std::vector<Comp> cs;
+        if (name == "cv") { for (int c = 0; c < 5; c++) cs.push_back(D(W.cv[c])); return box(v, cs, 0, IM, 0, JM, 0, KM, out, cap); }
+        if (name == "pv") { for (int c = 0; c < 6; c++) cs.push_back(Tt(W.pv[c])); return box(v, cs, 0, IM, 0, JM, 0, KM, out, cap); }
+        if (name == "mut") return box(v, {Tt(W.mut)}, 0, IM, 0, JM, 0, KM, out, cap);
+        if (name == "res") { for (int c = 0; c < 5; c++) cs.push_back(Tt(W.res[c])); return box(v, cs, 1, IM - 1, 1, JM - 1, 1, KM - 1, out, cap); }
+        if (name == "dq") { for (int c = 0; c < 5; c++) cs.push_back(Tt(W.dq[c])); return box(v, cs, 1, IM - 1, 1, JM - 1, 1, KM - 1, out, cap); }
+        if (name == "dt") return box(v, {Tt(W.dt)}, 1, IM - 1, 1, JM - 1, 1, KM - 1, out, cap);
+        if (name == "omega") return box(v, {Tt(W.omega)}, 1, IM - 1, 1, JM - 1, 1, KM - 1, out, cap);
+        const char *lam[6] = {"lamcI", "lamcJ", "lamcK", "lamvI", "lamvJ", "lamvK"};
+        for (int q = 0; q < 6; q++)
+            if (name == lam[q]) return box(v, {Tt(q < 3 ? W.lamc[q] : W.lamv[q - 3])}, 1, IM - 1, 1, JM - 1, 1, KM - 1, out, cap);
+        const char *fcn[3] = {"FcI", "FcJ", "FcK"}, *fvn[3] = {"FvI", "FvJ", "FvK"}, *gn[3] = {"faceI", "faceJ", "faceK"};
+        for (int f = 0; f < 3; f++) {
+            int i1 = f == 0 ? IM : IM - 1, j1 = f == 1 ? JM : JM - 1, k1 = f == 2 ? KM : KM - 1;
+            if (name == fcn[f]) { for (int c = 0; c < 5; c++) cs.push_back(Tt(W.Ff[f][c])); return box(v, cs, 1, i1, 1, j1, 1, k1, out, cap); }
+            if (name == fvn[f]) { for (int c = 0; c < 5; c++) cs.push_back(Tt(W.Vf[f][c])); return box(v, cs, 1, i1, 1, j1, 1, k1, out, cap); }
+            if (name == gn[f]) {
+                for (int c = 0; c < 3; c++) cs.push_back(D(G.S[f][c]));
+                cs.push_back(D(G.s[f]));
+                for (int c = 0; c < 3; c++) cs.push_back(D(G.c[f][c]));
+                cs.push_back(D(G.r[f])); cs.push_back(D(G.th[f]));
+                for (int c = 0; c < 9; c++) cs.push_back(D(G.m[f][c]));
+                return box(v, cs, 1, i1, 1, j1, 1, k1, out, cap);
+            }
+        }
+        if (name == "cell") {
+            cs.push_back(D(G.vol));
+            for (int c = 0; c < 3; c++) cs.push_back(D(G.cc[c]));
+            for (int c = 0; c < 9; c++) cs.push_back(D(G.cm[c]));
+            return box(v, cs, 1, IM - 1, 1, JM - 1, 1, KM - 1, out, cap);
+        }
+        if (name == "totalvol") {
+            if (cap < 1) return -1;
+            CK(cudaMemcpy(out, lev[l].totalvol + solve, sizeof(double), cudaMemcpyDeviceToHost));
+            return 1;
+        }
+        // reconstruction layers, [layer 1..2] along the face normal
+        const char *dn[6] = {"dIS", "dIP", "dJS", "dJP", "dKS", "dKP"};
+        for (int q = 0; q < 6; q++) {
+            bool is_cv = name == std::string(dn[q]) + "_cv", is_pv = name == std::string(dn[q]) + "_pv";
+            if (!is_cv && !is_pv) continue;
+            int dir = q / 2, hi = q % 2;
+            if (is_cv) for (int c = 0; c < 5; c++) cs.push_back(D(W.cv[c]));
+            else for (int c = 0; c < 6; c++) cs.push_back(Tt(W.pv[c]));
+            int r0[3] = {1, 1, 1}, r1[3] = {IM - 1, JM - 1, KM - 1};
+            int N = dir == 0 ? IM : (dir == 1 ? JM : KM);
+            long cnt = 2L * (long)cs.size();
+            for (int d = 0; d < 3; d++) if (d != dir) cnt *= (r1[d] - r0[d] + 1);
+            if (cnt > cap) return -1;
+            std::vector<std::vector<double>> h(cs.size());
+            for (size_t c = 0; c < cs.size(); c++) { if (cs[c].d) fetch(cs[c].d, v, h[c]); else fetch(cs[c].t, v, h[c]); }
+            r0[dir] = 1; r1[dir] = 2;
+            Lvl z = v; z.base = 0;
+            long o = 0;
+            for (int a = r0[0]; a <= r1[0]; a++)
+                for (int b = r0[1]; b <= r1[1]; b++)
+                    for (int e = r0[2]; e <= r1[2]; e++) {
+                        int ii[3] = {a, b, e};
+                        int nd = ii[dir];
+                        ii[dir] = hi ? N + nd : -nd;
+                        long long p = ix(z, ii[0], ii[1], ii[2]);
+                        for (size_t c = 0; c < cs.size(); c++) out[o++] = h[c][(size_t)p];
+                    }
+            return cnt;
+        }
+        return -1;
+    }
+
+    void set_cv(int solve, int l, const double *in, long n) override
+    {
+        if (solve < 0 || solve >= nsolve || l < 1 || l > ng) throw std::runtime_error("bad solve or level");
+        const Lvl &v = lev[l].lv[solve];
+        long need = (long)(v.IM - 1) * (v.JM - 1) * (v.KM - 1) * 5;
+        if (n != need) throw std::runtime_error("state size does not match the level");
+        CK(cudaStreamSynchronize(stream));
+        long long bn = box_size(v.IM, v.JM, v.KM);
+        Lvl z = v; z.base = 0;
+        for (int c = 0; c < 5; c++) {
+            std::vector<double> h((size_t)bn);
+            CK(cudaMemcpy(h.data(), lev[l].W.cv[c] + v.base, sizeof(double) * bn, cudaMemcpyDeviceToHost));
+            long q = c;
+            for (int i = 1; i <= v.IM - 1; i++)
+                for (int j = 1; j <= v.JM - 1; j++)
+                    for (int k = 1; k <= v.KM - 1; k++, q += 5) h[(size_t)ix(z, i, j, k)] = in[q];
+            CK(cudaMemcpy(lev[l].W.cv[c] + v.base, h.data(), sizeof(double) * bn, cudaMemcpyHostToDevice));
+        }
+        launch_primitive<T>(ctx(l), P, lev[l].W);
+        CK(cudaStreamSynchronize(stream));
+    }
+};
+
+std::unique_ptr<SolverBase> make_solver(const std::vector<std::string> &dirs, int precision)
+{
+    if (precision == 0) return std::unique_ptr<SolverBase>(new SolverT<double>(dirs, 0));
+    if (precision == 1) return std::unique_ptr<SolverBase>(new SolverT<float>(dirs, 1));
+    throw std::runtime_error("precision must be 0 (FP64) or 1 (mixed FP32/FP64)");
+}
+
+}  // namespace gbt

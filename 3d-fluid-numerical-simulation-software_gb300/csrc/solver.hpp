@@ -1,0 +1,62 @@
+// Host orchestration of a batch of operating points ("solves") on one GPU. The class keeps the
+// reference's call surface (CSolver::Solver, CMesh::ResFlux / Time_Marching / Res_Calculate /
+// PrimitiveVars / Limit_Vars / CornerTreatment, CSolver::Prolong / Interpolate /
+// ComputeDeltConsVars, COutput::OutputGeneralParameters) as methods that enqueue kernels on the
+// handle's stream; the C-ABI in capi.cu forwards to them.
+#pragma once
+#include <memory>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+#include "case_io.hpp"
+#include "kernels.hpp"
+
+namespace gbt {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    ~DevBuf() { if (p) cudaFree(p); }
+};
+
+class SolverBase {
+public:
+    virtual ~SolverBase() = default;
+    int nsolve = 0, ng = 1, coarse_iter = 0, iter = 0, precision = 0;
+    std::vector<CaseSpec> cases;
+    Phys P{};
+    cudaStream_t stream = nullptr;
+    bool use_graphs = true;
+
+    virtual void init_uniform() = 0;
+    virtual void resflux(int level) = 0;
+    virtual void time_marching(int level) = 0;
+    virtual void res_calculate(int level) = 0;
+    virtual void primitive_vars(int level) = 0;
+    virtual void limit_vars(int level) = 0;
+    virtual void corner_treatment(int level) = 0;
+    virtual void restrict_to_coarse() = 0;
+    virtual void interpolate(int init) = 0;
+    virtual void delta_cons() = 0;
+    virtual void integrals(int level) = 0;
+    virtual void solver_step() = 0;
+    // n driver iterations; hist (if not null) receives n * nsolve rows of 12 values
+    virtual void iterate(int n, double *hist) = 0;
+    virtual void dims(int solve, int level, int out[4]) const = 0;
+    virtual long get_field(int solve, int level, const std::string &name, double *out, long cap) = 0;
+    virtual void set_cv(int solve, int level, const double *in, long n) = 0;
+    virtual void states(SolveState *out) = 0;
+    virtual void set_use_force(int level, bool on) = 0;
+};
+
+std::unique_ptr<SolverBase> make_solver(const std::vector<std::string> &dirs, int precision);
+
+// nondimensional constants exactly as the reference derives them (source/UserInput.cpp:1070-1092)
+struct NonDim {
+    double vel_ref, dens_ref, temp_ref, mue_ref, re_ref, pout, ptin, ttin, rgas, w_rot, delta_th;
+};
+NonDim nondimensionalise(const CaseSpec &c);
+
+void check_cuda(cudaError_t e, const char *what);
+
+}  // namespace gbt

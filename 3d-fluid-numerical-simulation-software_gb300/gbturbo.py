@@ -1,0 +1,234 @@
+"""Python host of the GB300 residual-and-update path: a thin ctypes layer over the C-ABI in
+include/gbturbo.h (libgbturbo.so, built in-tree by build.py).
+
+The method names follow the reference solver's call surface (CSolver::Solver, CMesh::ResFlux,
+CMesh::Time_Marching, CMesh::Res_Calculate, COutput::OutputGeneralParameters, ...). There is no
+CPU fallback: if the library is missing, importing the solver raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import List, Optional, Sequence, Union
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgbturbo.so")
+
+FP64 = 0
+MIXED = 1
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def load() -> ctypes.CDLL:
+    """Loads libgbturbo.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run build.py (the GPU path has no CPU fallback)")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, ip, dp = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)
+    sig = {
+        "gb_solver_create": ([ctypes.POINTER(ctypes.c_char_p), ip, ip, ctypes.POINTER(vp)], ip),
+        "gb_solver_destroy": ([vp], ip),
+        "gb_last_error": ([], ctypes.c_char_p),
+        "gb_dims": ([vp, ip, ip, ctypes.POINTER(ip)], ip),
+        "gb_init_uniform": ([vp], ip),
+        "gb_resflux": ([vp, ip], ip),
+        "gb_time_marching": ([vp, ip], ip),
+        "gb_res_calculate": ([vp, ip, dp], ip),
+        "gb_primitive_vars": ([vp, ip], ip),
+        "gb_limit_vars": ([vp, ip], ip),
+        "gb_corner_treatment": ([vp, ip], ip),
+        "gb_restrict": ([vp], ip),
+        "gb_interpolate": ([vp, ip], ip),
+        "gb_delta_cons": ([vp], ip),
+        "gb_set_use_force": ([vp, ip, ip], ip),
+        "gb_solver_step": ([vp], ip),
+        "gb_integrals": ([vp, ip, dp], ip),
+        "gb_iterate": ([vp, ip, dp], ip),
+        "gb_get_status": ([vp, ctypes.POINTER(ip)], ip),
+        "gb_get_field": ([vp, ip, ip, ctypes.c_char_p, dp, ctypes.c_long], ctypes.c_long),
+        "gb_set_cv": ([vp, ip, ip, dp, ctypes.c_long], ip),
+        "gb_sync": ([vp], ip),
+        "gb_set_graphs": ([vp, ip], ip),
+        "gb_timer_start": ([vp], ip),
+        "gb_timer_stop": ([vp, ctypes.POINTER(ctypes.c_float)], ip),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+EXPORTED = ["gb_solver_create", "gb_solver_destroy", "gb_last_error", "gb_dims", "gb_init_uniform",
+            "gb_resflux", "gb_time_marching", "gb_res_calculate", "gb_primitive_vars", "gb_limit_vars",
+            "gb_corner_treatment", "gb_restrict", "gb_interpolate", "gb_delta_cons", "gb_set_use_force",
+            "gb_solver_step", "gb_integrals", "gb_iterate", "gb_get_status", "gb_get_field", "gb_set_cv",
+            "gb_sync", "gb_set_graphs", "gb_timer_start", "gb_timer_stop"]
+
+
+class GBError(RuntimeError):
+    pass
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+FIELD_SHAPES = {
+    "cv": lambda I, J, K: (I + 1, J + 1, K + 1, 5), "pv": lambda I, J, K: (I + 1, J + 1, K + 1, 6),
+    "mut": lambda I, J, K: (I + 1, J + 1, K + 1, 1),
+    "res": lambda I, J, K: (I - 1, J - 1, K - 1, 5), "dq": lambda I, J, K: (I - 1, J - 1, K - 1, 5),
+    "FcI": lambda I, J, K: (I, J - 1, K - 1, 5), "FcJ": lambda I, J, K: (I - 1, J, K - 1, 5),
+    "FcK": lambda I, J, K: (I - 1, J - 1, K, 5), "FvI": lambda I, J, K: (I, J - 1, K - 1, 5),
+    "FvJ": lambda I, J, K: (I - 1, J, K - 1, 5), "FvK": lambda I, J, K: (I - 1, J - 1, K, 5),
+    "faceI": lambda I, J, K: (I, J - 1, K - 1, 18), "faceJ": lambda I, J, K: (I - 1, J, K - 1, 18),
+    "faceK": lambda I, J, K: (I - 1, J - 1, K, 18), "cell": lambda I, J, K: (I - 1, J - 1, K - 1, 13),
+    "totalvol": lambda I, J, K: (1,),
+}
+for _n in ("dt", "omega", "lamcI", "lamcJ", "lamcK", "lamvI", "lamvJ", "lamvK"):
+    FIELD_SHAPES[_n] = lambda I, J, K: (I - 1, J - 1, K - 1, 1)
+for _d, _f in (("I", lambda I, J, K: (2, J - 1, K - 1)), ("J", lambda I, J, K: (I - 1, 2, K - 1)),
+               ("K", lambda I, J, K: (I - 1, J - 1, 2))):
+    for _s in ("S", "P"):
+        FIELD_SHAPES[f"d{_d}{_s}_cv"] = (lambda f: lambda I, J, K: f(I, J, K) + (5,))(_f)
+        FIELD_SHAPES[f"d{_d}{_s}_pv"] = (lambda f: lambda I, J, K: f(I, J, K) + (6,))(_f)
+
+HIST_COLUMNS = ["iter", "res_dens", "res_xmom", "res_ymom", "res_zmom", "res_ener", "m_in", "m_out", "PR",
+                "eta", "m_ratio", "CFL"]
+
+
+class Solver:
+    """A batch of operating points, each read from a reference case directory."""
+
+    def __init__(self, case_dirs: Union[str, Sequence[str]], precision: int = FP64):
+        self._L = load()
+        if isinstance(case_dirs, str):
+            case_dirs = [case_dirs]
+        self.case_dirs = [os.path.abspath(d) for d in case_dirs]
+        arr = (ctypes.c_char_p * len(self.case_dirs))(*[d.encode() for d in self.case_dirs])
+        h = ctypes.c_void_p()
+        rc = self._L.gb_solver_create(arr, len(self.case_dirs), precision, ctypes.byref(h))
+        if rc != 0:
+            raise GBError(self._L.gb_last_error().decode())
+        self.h = h
+        self.n = len(self.case_dirs)
+        self.precision = precision
+        self.ng = self.dims(0, 1)[3]
+
+    def _ck(self, rc: int) -> None:
+        if rc != 0:
+            raise GBError(self._L.gb_last_error().decode())
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self._L.gb_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- reference call surface
+    def dims(self, solve: int = 0, level: int = 1):
+        d = (ctypes.c_int * 4)()
+        self._ck(self._L.gb_dims(self.h, solve, level, d))
+        return tuple(d)
+
+    def init_uniform(self) -> None:
+        self._ck(self._L.gb_init_uniform(self.h))
+
+    def resflux(self, level: int = 1) -> None:
+        self._ck(self._L.gb_resflux(self.h, level))
+
+    def time_marching(self, level: int = 1) -> None:
+        self._ck(self._L.gb_time_marching(self.h, level))
+
+    def res_calculate(self, level: int = 1) -> np.ndarray:
+        out = np.zeros(5 * self.n)
+        self._ck(self._L.gb_res_calculate(self.h, level, _dp(out)))
+        return out.reshape(self.n, 5)
+
+    def primitive_vars(self, level: int = 1) -> None:
+        self._ck(self._L.gb_primitive_vars(self.h, level))
+
+    def limit_vars(self, level: int = 1) -> None:
+        self._ck(self._L.gb_limit_vars(self.h, level))
+
+    def corner_treatment(self, level: int = 2) -> None:
+        self._ck(self._L.gb_corner_treatment(self.h, level))
+
+    def restrict(self) -> None:
+        self._ck(self._L.gb_restrict(self.h))
+
+    def interpolate(self, init: bool = False) -> None:
+        self._ck(self._L.gb_interpolate(self.h, int(init)))
+
+    def delta_cons(self) -> None:
+        self._ck(self._L.gb_delta_cons(self.h))
+
+    def set_use_force(self, level: int, on: bool) -> None:
+        self._ck(self._L.gb_set_use_force(self.h, level, int(on)))
+
+    def solver_step(self) -> None:
+        self._ck(self._L.gb_solver_step(self.h))
+
+    def integrals(self, level: int = 1) -> np.ndarray:
+        out = np.zeros(5 * self.n)
+        self._ck(self._L.gb_integrals(self.h, level, _dp(out)))
+        return out.reshape(self.n, 5)
+
+    def iterate(self, n: int, history: bool = True) -> Optional[np.ndarray]:
+        """n driver iterations; with history, returns an array (n, n_solves, 12) of HIST_COLUMNS."""
+        if history:
+            out = np.zeros((n, self.n, 12))
+            self._ck(self._L.gb_iterate(self.h, n, _dp(out)))
+            return out
+        self._ck(self._L.gb_iterate(self.h, n, None))
+        return None
+
+    def status(self) -> np.ndarray:
+        out = (ctypes.c_int * self.n)()
+        self._ck(self._L.gb_get_status(self.h, out))
+        return np.array(out[:])
+
+    def get(self, name: str, solve: int = 0, level: int = 1) -> np.ndarray:
+        I, J, K, _ = self.dims(solve, level)
+        shape = FIELD_SHAPES[name](I, J, K)
+        out = np.zeros(int(np.prod(shape)))
+        n = self._L.gb_get_field(self.h, solve, level, name.encode(), _dp(out), out.size)
+        if n < 0:
+            raise GBError(self._L.gb_last_error().decode())
+        return out.reshape(shape)
+
+    def set_cv(self, cv: np.ndarray, solve: int = 0, level: int = 1) -> None:
+        a = np.ascontiguousarray(cv, dtype=np.float64).ravel()
+        self._ck(self._L.gb_set_cv(self.h, solve, level, _dp(a), a.size))
+
+    def sync(self) -> None:
+        self._ck(self._L.gb_sync(self.h))
+
+    def set_graphs(self, on: bool) -> None:
+        self._ck(self._L.gb_set_graphs(self.h, int(on)))
+
+    def timer_start(self) -> None:
+        self._ck(self._L.gb_timer_start(self.h))
+
+    def timer_stop(self) -> float:
+        ms = ctypes.c_float()
+        self._ck(self._L.gb_timer_stop(self.h, ctypes.byref(ms)))
+        return float(ms.value)

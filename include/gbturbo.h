@@ -1,0 +1,98 @@
+/* gbturbo: C-ABI of the GB300 residual-and-update path of the structured-grid turbomachinery
+ * RANS solver (wuchuankang/3D-fluid-numerical-simulation-software).
+ *
+ * A handle owns one batch of operating points ("solves") on the current CUDA device; each solve
+ * is configured from the reference's own case files (config.dat, BoundaryDefinition.dat and the
+ * grid file named in config.dat) and all solves of a batch share the numerical options. The
+ * entry points replace the reference's C++ member-function surface one for one (file:line of the
+ * reference in each comment). All calls are asynchronous on the handle's stream unless they
+ * return data to host buffers; all return 0 on success and a negative code on failure, with
+ * the message available from gb_last_error(). The device owns all state; the caller passes
+ * host buffers only.
+ */
+#ifndef GBTURBO_H
+#define GBTURBO_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gb_solver gb_solver;
+
+#define GB_PRECISION_FP64 0   /* every field FP64: parity with the reference's FP64 build */
+#define GB_PRECISION_MIXED 1  /* fluxes, residuals, sweeps, transfers FP32; Q, geometry, norms, integrals FP64 */
+
+#define GB_OK 0
+#define GB_ERR_ARG -1
+#define GB_ERR_CASE -2
+#define GB_ERR_CUDA -3
+
+/* Reads n case directories and builds the batch: input reading of source/Structured_FV3D.cpp:36-56
+ * (CUserInput::ReadConfig, NumberOfMultigrid, ReadGrids, ReadBndGrid, NonDimensionalization),
+ * memory and geometry of :59-69 (CMesh::AllocateMemory, CMesh::Geometry). */
+int gb_solver_create(const char *const *case_dirs, int n_solves, int precision, gb_solver **out);
+int gb_solver_destroy(gb_solver *h);
+/* message of the last failure on the calling thread */
+const char *gb_last_error(void);
+
+/* out[0..3] = IM, JM, KM (node counts) of a level of one solve, and the number of levels */
+int gb_dims(gb_solver *h, int solve, int level, int out[4]);
+
+/* CMesh::Initial, uniform start (source/Initialization.cpp:17-76) on the coarsest used level */
+int gb_init_uniform(gb_solver *h);
+/* CMesh::ResFlux (source/ComputeAllBlockVars.cpp:223-255): boundary fill, spectral radii, curl,
+ * Baldwin-Lomax (fine level), time step, convective + wall + viscous flux, residual */
+int gb_resflux(gb_solver *h, int level);
+/* CMesh::Time_Marching -> LU_SGS_Marching (source/LU_SGS_Marching.cpp:10-291) */
+int gb_time_marching(gb_solver *h, int level);
+/* CMesh::Res_Calculate (source/ComputeAllBlockVars.cpp:318-372); out[5*n_solves] may be NULL */
+int gb_res_calculate(gb_solver *h, int level, double *out);
+/* CMesh::PrimitiveVars (source/PrimitiveVars.cpp:7-28) */
+int gb_primitive_vars(gb_solver *h, int level);
+/* CMesh::Limit_Vars (source/Limit_FlowVars.cpp:8-118) */
+int gb_limit_vars(gb_solver *h, int level);
+/* CMesh::CornerTreatment (source/ComputeAllBlockVars.cpp:374-438) */
+int gb_corner_treatment(gb_solver *h, int level);
+/* CSolver::Prolong: restriction fine -> coarse (source/Prolong_Interpolate.cpp:7-50) */
+int gb_restrict(gb_solver *h);
+/* CSolver::Interpolate: prolongation coarse -> fine (source/Prolong_Interpolate.cpp:52-156);
+ * init = 1 interpolates Q itself (first fine-level iteration), 0 adds the coarse correction */
+int gb_interpolate(gb_solver *h, int init);
+/* CSolver::ComputeDeltConsVars (source/Prolong_Interpolate.cpp:159-176) */
+int gb_delta_cons(gb_solver *h);
+/* CMesh::UseForceFunction of a level (source/Solver.cpp:98) */
+int gb_set_use_force(gb_solver *h, int level, int on);
+/* CSolver::Solver (source/Solver.cpp:47-140): one iteration of the driver, CFL ramp included */
+int gb_solver_step(gb_solver *h);
+/* COutput::OutputGeneralParameters (source/Ouput.cpp:282-300) on a level; out[5*n_solves] =
+ * mass flow in, mass flow out, total-pressure ratio, isentropic efficiency, |m_in - m_out|/m_in */
+int gb_integrals(gb_solver *h, int level, double *out);
+/* n iterations of the reference driver loop (source/Structured_FV3D.cpp:142-219: Solver() and
+ * the integrals), replayed as CUDA graphs. hist (may be NULL) receives n * n_solves rows of 12:
+ * iter, Res(dens,xmom,ymom,zmom,ener), m_in, m_out, PR, eta, m_ratio, CFL. */
+int gb_iterate(gb_solver *h, int n, double *hist);
+/* per-solve status words (bit 1: non-finite residual or integral, bit 2: limiter active in the
+ * last step, bit 4: limiter list overflow); out[n_solves] */
+int gb_get_status(gb_solver *h, int *out);
+
+/* Copies a named array of one solve and level to out (row-major, components fastest):
+ * "cv" (IM+1,JM+1,KM+1,5) and "pv" (..,6), "mut" (..,1) including ghosts; "res","dq" and
+ * "dt","omega","lamcI".."lamvK" over the cells; "FcI","FvI" (IM,JM-1,KM-1,5) and J, K;
+ * "faceI" (IM,JM-1,KM-1,18), "faceJ", "faceK", "cell" (IM-1,JM-1,KM-1,13), "totalvol";
+ * "dIS_cv".."dKP_pv" reconstruction layers. Returns the count written (>= 0) or < 0. */
+long gb_get_field(gb_solver *h, int solve, int level, const char *name, double *out, long cap);
+/* overwrites the interior conserved variables (IM-1,JM-1,KM-1,5) and the primitive variables */
+int gb_set_cv(gb_solver *h, int solve, int level, const double *cv, long n);
+
+/* waits for the handle's stream */
+int gb_sync(gb_solver *h);
+/* 0 disables graph replay in gb_iterate (eager launches) */
+int gb_set_graphs(gb_solver *h, int enable);
+/* device time of everything enqueued between the two calls, in milliseconds (events on the
+ * handle's stream) */
+int gb_timer_start(gb_solver *h);
+int gb_timer_stop(gb_solver *h, float *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,90 @@
+"""Regenerates the golden fixtures of tests/golden/ from the reference solver itself.
+
+For each case below: writes the case files (config.dat, BoundaryDefinition.dat, grid.dat) with
+the package's mesh generator into tests/golden/<name>/, runs the reference's own CPU code through
+oracle/_ref/ref_harness (built by oracle/build_ref.sh from the reference sources) for the given
+number of driver iterations, and stores the history, the final state and one residual
+evaluation at that state (every intermediate array) in tests/golden/<name>.npz.
+
+Only runs where the reference sources and a C++ compiler exist; the fixtures it writes are
+committed so the tests need neither.
+
+    python tests/golden/make_golden.py [name ...]
+"""
+from __future__ import annotations
+
+import importlib.util
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+PKG = os.path.join(ROOT, "3d-fluid-numerical-simulation-software_gb300")
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+
+def _meshgen():
+    spec = importlib.util.spec_from_file_location("gb_meshgen", os.path.join(PKG, "meshgen.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["gb_meshgen"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+# name -> (generator, kwargs, options, iterations)
+CASES = {
+    "duct_9x9x17": ("annular_duct", dict(IM=9, JM=9, KM=17), {}, 20),
+    "duct_9x9x17_sw_nnd": ("annular_duct", dict(IM=9, JM=9, KM=17), {"scheme": "200", "recon": "100"}, 12),
+    "duct_9x9x17_laminar_cons": ("annular_duct", dict(IM=9, JM=9, KM=17),
+                                 {"recon_var": "100", "recon": "400", "turb": "0"}, 12),
+    "duct_9x9x17_muscl2u_global": ("annular_duct", dict(IM=9, JM=9, KM=17),
+                                   {"recon": "200", "timestep": "G", "limiter": "N"}, 10),
+    "rotor_9x9x33": ("rotor_passage", dict(IM=9, JM=9, KM=33), {}, 20),
+    "rotor_9x9x33_mg": ("rotor_passage", dict(IM=9, JM=9, KM=33), {"multigrid": "Y", "coarse_iter": "5"}, 14),
+}
+
+KEEP_R = ["cv", "pv", "mut", "omega", "lamcI", "lamcJ", "lamcK", "lamvI", "lamvJ", "lamvK", "dt", "FcI", "FcJ",
+          "FcK", "FvI", "FvJ", "FvK", "res", "dIS_pv", "dIP_pv", "dJS_pv", "dJP_pv", "dKS_pv", "dKP_pv", "dIS_cv",
+          "dKP_cv"]
+
+
+def make(name: str) -> None:
+    mg = _meshgen()
+    gen, kw, opts, n_iter = CASES[name]
+    case = getattr(mg, gen)(**kw, options=opts, name=name)
+    cdir = os.path.join(HERE, name)
+    if os.path.isdir(cdir):
+        shutil.rmtree(cdir)
+    mg.write_case(case, cdir)
+    with tempfile.TemporaryDirectory() as tmp:
+        for f in os.listdir(cdir):
+            shutil.copy(os.path.join(cdir, f), tmp)
+        out = os.path.join(tmp, "out")
+        subprocess.run([HARNESS, str(n_iter), out, "1"], cwd=tmp, check=True, stdout=subprocess.DEVNULL)
+        data = {}
+        base_case = name in ("duct_9x9x17", "rotor_9x9x33")
+        for f in sorted(os.listdir(out)):
+            key = f[:-4]
+            if key.startswith("r1_") and key[3:] not in KEEP_R:
+                continue
+            if key.startswith("s") or key.startswith("g2_"):
+                continue                       # state after the loop is r1_cv's interior
+            if key.startswith("g1_") and not base_case:
+                continue                       # geometry is pinned on the two base cases
+            if not base_case and key.startswith("r1_d"):
+                continue
+            data[key] = np.load(os.path.join(out, f))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **data)
+    print(name, "iterations:", int(data["history"].shape[0]))
+
+
+if __name__ == "__main__":
+    if not os.path.exists(HARNESS):
+        sys.exit("build the reference harness first: oracle/build_ref.sh")
+    for n in (sys.argv[1:] or list(CASES)):
+        make(n)
