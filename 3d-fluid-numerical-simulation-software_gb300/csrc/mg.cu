@@ -113,9 +113,11 @@ __global__ void __launch_bounds__(256) k_interpolate(Batch Bf, Batch Bc, Flow<T>
     const Lvl F = Bf.lv[s], C = Bc.lv[s];
     int i, j, k;
     if (!box_index(F.IM - 1, F.JM - 1, F.KM - 1, i, j, k)) return;
-    const int ia1 = (i % 2 == 0) ? i / 2 : i / 2 + 1, ia2 = (i % 2 == 0) ? i / 2 + 1 : i / 2;
-    const int ja1 = (j % 2 == 0) ? j / 2 : j / 2 + 1, ja2 = (j % 2 == 0) ? j / 2 + 1 : j / 2;
-    const int ka1 = (k % 2 == 0) ? k / 2 : k / 2 + 1, ka2 = (k % 2 == 0) ? k / 2 + 1 : k / 2;
+    // nearest coarse cell and the next one (source/Prolong_Interpolate.cpp:90-119): for an odd
+    // fine index n, (n+1)/2 and (n-1)/2; for an even one, n/2 and n/2+1
+    const int ia1 = (i + 1) >> 1, ia2 = (i & 1) ? (i - 1) >> 1 : (i >> 1) + 1;
+    const int ja1 = (j + 1) >> 1, ja2 = (j & 1) ? (j - 1) >> 1 : (j >> 1) + 1;
+    const int ka1 = (k + 1) >> 1, ka2 = (k & 1) ? (k - 1) >> 1 : (k >> 1) + 1;
     const long long c111 = ix(C, ia1, ja1, ka1), c112 = ix(C, ia1, ja1, ka2), c121 = ix(C, ia1, ja2, ka1),
                     c211 = ix(C, ia2, ja1, ka1), c221 = ix(C, ia2, ja2, ka1), c122 = ix(C, ia1, ja2, ka2),
                     c212 = ix(C, ia2, ja1, ka2), c222 = ix(C, ia2, ja2, ka2);

@@ -29,14 +29,17 @@ def golden_dir(name):
     return os.path.join(GOLDEN, name)
 
 
-def rel_err(a, b):
-    """normwise relative error per trailing component, max over components"""
-    a = np.asarray(a, dtype=np.float64).reshape(-1, a.shape[-1]) if np.ndim(a) > 1 else np.atleast_2d(a).T
+def rel_err(a, b, floor=1e-6):
+    """Normwise relative error per trailing component, max over components. A component whose
+    norm is below `floor` times the largest component's norm (rounding noise of a quantity that
+    is zero in exact arithmetic) is measured against that floor instead of its own norm."""
+    a = np.asarray(a, dtype=np.float64)
+    a = a.reshape(-1, a.shape[-1]) if a.ndim > 1 else a.reshape(-1, 1)
     b = np.asarray(b, dtype=np.float64).reshape(a.shape)
     num = np.linalg.norm(a - b, axis=0)
     den = np.linalg.norm(b, axis=0)
-    out = np.where(den > 0, num / np.where(den > 0, den, 1), num)
-    return float(np.max(out))
+    den = np.maximum(den, floor * max(float(den.max()), 1e-300))
+    return float(np.max(num / den))
 
 
 @pytest.fixture(scope="session")
