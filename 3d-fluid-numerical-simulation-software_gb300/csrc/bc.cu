@@ -65,22 +65,30 @@ __global__ void k_bc_inlet(Batch B, Phys P, Geo G, Flow<T> W, const DevInOut *pa
 // equilibrium marched from p_out at i = IM/2 using the previous ghost density, then ghosts
 // extrapolated from the last interior layer
 template <typename T>
-__global__ void k_bc_outlet(Batch B, Phys P, Geo G, Flow<T> W, const DevInOut *pat)
+__global__ void __launch_bounds__(256) k_bc_outlet(Batch B, Phys P, Geo G, Flow<T> W, const DevInOut *pat)
 {
     extern __shared__ double cu[];
     const DevInOut pt = pat[blockIdx.x];
     const Lvl L = B.lv[pt.solve];
     const int IM = L.IM, JM = L.JM, KM = L.KM;
-    for (int i = 1 + threadIdx.x; i <= IM - 1; i += blockDim.x) {
+    // one warp per radial row i: lanes over the pitch, area-weighted swirl and area summed
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int i = 1 + warp; i <= IM - 1; i += nw) {
         double acc = 0.0, sa = 0.0;
-        for (int j = 1; j <= JM - 1; j++) {
+        for (int j = 1 + lane; j <= JM - 1; j += 32) {
             const long long p = ix(L, i, j, KM - 1), f = ix(L, i, j, KM);
             const double th = G.th[2][f];
-            const double ct = -1.0 * (double)W.pv[PU][p] * sin(th) + (double)W.pv[PV][p] * cos(th);
+            double sn, cs;
+            sincos(th, &sn, &cs);
+            const double ct = -1.0 * (double)W.pv[PU][p] * sn + (double)W.pv[PV][p] * cs;
             acc = acc + ct * G.s[2][f];
             sa = sa + G.s[2][f];
         }
-        cu[i] = acc / sa;
+        for (int o = 16; o > 0; o >>= 1) {
+            acc += __shfl_down_sync(0xffffffffu, acc, o);
+            sa += __shfl_down_sync(0xffffffffu, sa, o);
+        }
+        if (lane == 0) cu[i] = acc / sa;
     }
     __syncthreads();
     const int iref = (int)(0.5 * IM);

@@ -152,6 +152,19 @@ int gb_sync(gb_solver *h)
     return guard([&] { gbt::check_cuda(cudaStreamSynchronize(h->s->stream), "cudaStreamSynchronize"); });
 }
 
+int gb_profile_begin(gb_solver *h) { NEED(h); return guard([&] { h->s->profile_begin(); }); }
+
+int gb_profile_end(gb_solver *h, char *buf, int buflen)
+{
+    NEED(h);
+    if (!buf || buflen < 1) { g_err = "null buffer"; return GB_ERR_ARG; }
+    return guard([&] {
+        std::string r = h->s->profile_end();
+        std::strncpy(buf, r.c_str(), (size_t)buflen - 1);
+        buf[buflen - 1] = 0;
+    });
+}
+
 int gb_set_graphs(gb_solver *h, int enable) { NEED(h); h->s->use_graphs = enable != 0; return GB_OK; }
 
 int gb_timer_start(gb_solver *h)

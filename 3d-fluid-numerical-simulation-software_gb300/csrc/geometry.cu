@@ -196,7 +196,7 @@ __global__ void k_face_metrics(Batch B, Geo G, int f)
 }
 
 // total volume per solve (ComputeAllBlockVars.cpp:28-33), one block per solve
-__global__ void k_total_volume(Batch B, Geo G, double *out)
+__global__ void __launch_bounds__(1024) k_total_volume(Batch B, Geo G, double *out)
 {
     const Lvl L = B.lv[blockIdx.y];
     int nI = L.IM - 1, nJ = L.JM - 1, nK = L.KM - 1;

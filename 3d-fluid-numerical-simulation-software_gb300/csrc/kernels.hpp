@@ -1,5 +1,6 @@
 // Host-side declarations of the kernel launchers (one translation unit per stage).
 #pragma once
+#include <vector>
 #include "gbt_common.cuh"
 
 namespace gbt {
@@ -11,6 +12,11 @@ struct LaunchCtx {
     cudaStream_t stream;
     int maxIM = 0, maxJM = 0, maxKM = 0;     // maxima over the solves of this level
     long long pool_n = 0;                     // elements of one field pool of this level
+    // optional stage profiler: called before (begin = 1) and after (begin = 0) a group of
+    // launches with the group's name and the number of kernel launches in it
+    void (*hook)(void *user, const char *stage, int begin, int launches) = nullptr;
+    void *hook_user = nullptr;
+    void mark(const char *stage, int begin, int launches = 1) const { if (hook) hook(hook_user, stage, begin, launches); }
     dim3 grid_n(long long n, int bs) const { return dim3((unsigned)((n + bs - 1) / bs), batch.nsolve); }
     dim3 grid_cells(int bs) const { return grid_n((long long)(maxIM - 1) * (maxJM - 1) * (maxKM - 1), bs); }
     dim3 grid_faces(int f, int bs) const
@@ -39,6 +45,14 @@ struct BcTables {
     const DevInOut *inlet_first = nullptr, *outlet_first = nullptr;   // per solve: Inlet[1], Outlet[1]
 };
 
+// cells of every i+j+k hyperplane of every solve: pairs[start[s*stride + plane] ..
+// start[s*stride + plane + 1]) hold (i << 16) | j; max_count[plane] is the largest plane over solves
+struct PlaneTables {
+    const int *pairs = nullptr, *start = nullptr;
+    int stride = 0, max_plane = 0;
+    std::vector<int> max_count;
+};
+
 void launch_geometry(const LaunchCtx &ctx, const Geo &G, double *totalvol);
 
 template <typename T>
@@ -50,7 +64,7 @@ void launch_resflux(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> F
                     int level, T *scratch_dtmin);
 
 template <typename T>
-void launch_lusgs_sweeps(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> F, int max_plane);
+void launch_lusgs_sweeps(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> F, const PlaneTables &pt);
 
 template <typename T>
 void launch_update(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> F, int level,

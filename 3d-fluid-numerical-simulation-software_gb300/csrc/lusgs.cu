@@ -35,65 +35,78 @@ __device__ __forceinline__ void delt_fn(const Phys &P, const Geo &G, const Flow<
     out[4] = ((ne + pn) * dn + pn * ve) - ((oe + po) * dov + po * ve);
 }
 
+// One warp per block handles ten cells of a plane with three lanes per cell, lane d computing
+// the off-diagonal term of neighbour direction d; the three terms are combined on the first lane
+// in the reference's order (-R + A_I + A_J + A_K + V_I + V_J + V_K). Cells of a plane come from a
+// compact per-solve list, so a plane of ~1,300 cells spreads over ~130 SMs.
 template <typename T, int DIR>      // DIR = +1 forward (lower neighbours), -1 backward
-__global__ void __launch_bounds__(128) k_sweep(Batch B, Phys P, Geo G, Flow<T> W, int plane)
+__global__ void __launch_bounds__(32) k_sweep(Batch B, Phys P, Geo G, Flow<T> W, const int *__restrict__ pairs,
+                                              const int *__restrict__ pstart, int pstride, int plane)
 {
+    const int lane = threadIdx.x, slot = lane / 3, d = lane - 3 * slot;
     const int s = blockIdx.y;
     const Lvl L = B.lv[s];
-    const int nI = L.IM - 1, nJ = L.JM - 1, nK = L.KM - 1;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    // cells of the plane: i in [max(1, plane-nJ-nK), min(nI, plane-2)], j then k = plane-i-j
-    const int ilo = max(1, plane - nJ - nK), ihi = min(nI, plane - 2);
-    if (ilo > ihi) return;
-    const int i = ilo + t / nJ, j = 1 + t % nJ;
-    if (i > ihi) return;
-    const int k = plane - i - j;
-    if (k < 1 || k > nK) return;
-    const long long p = ix(L, i, j, k);
-    const long long stv[3] = {(long long)L.NJ * L.NK, (long long)L.NK, 1LL};
-    const int idx[3] = {i, j, k}, top[3] = {nI, nJ, nK};
-    const T relax = (T)P.relax;
-    const T alpha = (T)G.vol[p] / W.dt[p] + relax * (W.lamc[0][p] + W.lamc[1][p] + W.lamc[2][p]) +
-                    (T)2 * (W.lamv[0][p] + W.lamv[1][p] + W.lamv[2][p]);
-    T aw[3][5], vw[3][5];
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        const bool has = DIR > 0 ? (idx[d] != 1) : (idx[d] != top[d]);
+    const int base = pstart[s * pstride + plane], cnt = pstart[s * pstride + plane + 1] - base;
+    const int idx = blockIdx.x * 10 + slot;
+    const bool active = lane < 30 && idx < cnt;
+    T aw[5] = {(T)0, (T)0, (T)0, (T)0, (T)0}, vw[5] = {(T)0, (T)0, (T)0, (T)0, (T)0};
+    long long p = 0;
+    if (active) {
+        const int ij = pairs[base + idx];
+        const int i = ij >> 16, j = ij & 0xffff, k = plane - i - j;
+        p = ix(L, i, j, k);
+        const int a = d == 0 ? i : (d == 1 ? j : k);
+        const int top = d == 0 ? L.IM - 1 : (d == 1 ? L.JM - 1 : L.KM - 1);
+        const bool has = DIR > 0 ? (a != 1) : (a != top);
         if (has) {
-            const long long nb = DIR > 0 ? p - stv[d] : p + stv[d];
+            const long long sd_ = d == 0 ? (long long)L.NJ * L.NK : (d == 1 ? (long long)L.NK : 1LL);
+            const long long nb = DIR > 0 ? p - sd_ : p + sd_;
             T dF[5];
             delt_fn(P, G, W, d, nb, dF);
             const T sd = (T)G.cs[d][nb];
-            const T rl = relax * W.lamc[d][nb], lv = W.lamv[d][nb];
+            const T rl = (T)P.relax * W.lamc[d][nb], lv = W.lamv[d][nb];
 #pragma unroll
             for (int c = 0; c < 5; c++) {
                 const T dqn = W.dq[c][nb];
-                aw[d][c] = DIR > 0 ? (T)0.5 * (dF[c] * sd + rl * dqn) : (T)0.5 * (dF[c] * sd - rl * dqn);
-                vw[d][c] = lv * dqn;
+                aw[c] = DIR > 0 ? (T)0.5 * (dF[c] * sd + rl * dqn) : (T)0.5 * (dF[c] * sd - rl * dqn);
+                vw[c] = lv * dqn;
             }
-        } else {
-#pragma unroll
-            for (int c = 0; c < 5; c++) { aw[d][c] = (T)0; vw[d][c] = (T)0; }
         }
     }
+    T a1[5], a2[5], v1[5], v2[5];
+#pragma unroll
+    for (int c = 0; c < 5; c++) {
+        a1[c] = __shfl_down_sync(0xffffffffu, aw[c], 1);
+        a2[c] = __shfl_down_sync(0xffffffffu, aw[c], 2);
+        v1[c] = __shfl_down_sync(0xffffffffu, vw[c], 1);
+        v2[c] = __shfl_down_sync(0xffffffffu, vw[c], 2);
+    }
+    if (!active || d != 0) return;
+    const T relax = (T)P.relax;
+    const T alpha = (T)G.vol[p] / W.dt[p] + relax * (W.lamc[0][p] + W.lamc[1][p] + W.lamc[2][p]) +
+                    (T)2 * (W.lamv[0][p] + W.lamv[1][p] + W.lamv[2][p]);
 #pragma unroll
     for (int c = 0; c < 5; c++) {
         T r;
-        if (DIR > 0) r = -W.res[c][p] + aw[0][c] + aw[1][c] + aw[2][c] + vw[0][c] + vw[1][c] + vw[2][c];
-        else r = alpha * W.dq[c][p] - aw[0][c] - aw[1][c] - aw[2][c] + vw[0][c] + vw[1][c] + vw[2][c];
+        if (DIR > 0) r = -W.res[c][p] + aw[c] + a1[c] + a2[c] + vw[c] + v1[c] + v2[c];
+        else r = alpha * W.dq[c][p] - aw[c] - a1[c] - a2[c] + vw[c] + v1[c] + v2[c];
         W.dq[c][p] = r / alpha;
     }
 }
 
 template <typename T>
-void launch_lusgs_sweeps(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, int max_plane)
+void launch_lusgs_sweeps(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const PlaneTables &pt)
 {
     const Batch &B = ctx.batch;
-    // widest plane: at most min(nI, ...) rows of nJ cells; launch nI*nJ threads (rows outside the
-    // plane's i range exit at once)
-    dim3 g = ctx.grid_plane(128);
-    for (int pl = 3; pl <= max_plane; pl++) k_sweep<T, 1><<<g, 128, 0, ctx.stream>>>(B, P, G, W, pl);
-    for (int pl = max_plane; pl >= 3; pl--) k_sweep<T, -1><<<g, 128, 0, ctx.stream>>>(B, P, G, W, pl);
+    const int np = pt.max_plane;
+    ctx.mark("sweep_forward", 1, np - 2);
+    for (int pl = 3; pl <= np; pl++)
+        k_sweep<T, 1><<<dim3(max(1, (pt.max_count[pl] + 9) / 10), B.nsolve), 32, 0, ctx.stream>>>(B, P, G, W, pt.pairs, pt.start, pt.stride, pl);
+    ctx.mark("sweep_forward", 0, np - 2);
+    ctx.mark("sweep_backward", 1, np - 2);
+    for (int pl = np; pl >= 3; pl--)
+        k_sweep<T, -1><<<dim3(max(1, (pt.max_count[pl] + 9) / 10), B.nsolve), 32, 0, ctx.stream>>>(B, P, G, W, pt.pairs, pt.start, pt.stride, pl);
+    ctx.mark("sweep_backward", 0, np - 2);
 }
 
 // primitive variables from the conserved ones
@@ -251,9 +264,11 @@ void launch_update(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W,
 {
     (void)G;
     const Batch &B = ctx.batch;
+    ctx.mark("update_limiter", 1, 2);
     cudaMemsetAsync(bad_count, 0, sizeof(int) * B.nsolve, ctx.stream);
     k_update<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, W, bad_list, bad_cap, bad_count);
     if (P.limiter) k_limiter<T><<<(B.nsolve + 31) / 32, 32, 0, ctx.stream>>>(B, P, W, level, bad_list, bad_cap, bad_count);
+    ctx.mark("update_limiter", 0, 2);
 }
 
 template <typename T>
@@ -324,8 +339,10 @@ template <typename T>
 void launch_res_norm(const LaunchCtx &ctx, const Geo &G, Flow<T> W, const double *totalvol, double *partials, int nblk)
 {
     const Batch &B = ctx.batch;
+    ctx.mark("res_norm", 1, 2);
     k_norm_partial<T><<<dim3(nblk, B.nsolve), 256, 0, ctx.stream>>>(B, G, W, partials, nblk);
     k_norm_final<<<B.nsolve, 32, 0, ctx.stream>>>(B, partials, nblk, totalvol);
+    ctx.mark("res_norm", 0, 2);
 }
 
 // ---- inlet/outlet integrals (source/Ouput.cpp:9-107,282-300), one block per solve ----
@@ -369,7 +386,7 @@ __device__ void section_sums(const Phys &P, const Geo &G, const Flow<T> &W, cons
 }
 
 template <typename T>
-__global__ void k_integrals(Batch B, Phys P, Geo G, Flow<T> W, const DevInOut *inl, const DevInOut *outl)
+__global__ void __launch_bounds__(1024) k_integrals(Batch B, Phys P, Geo G, Flow<T> W, const DevInOut *inl, const DevInOut *outl)
 {
     const int s = blockIdx.x;
     const Lvl L = B.lv[s];
@@ -396,7 +413,7 @@ template <typename T>
 void launch_integrals(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const BcTables &bc)
 {
     // first inlet and first outlet patch of every solve (the reference reports Inlet[1], Outlet[1])
-    k_integrals<T><<<ctx.batch.nsolve, 256, 0, ctx.stream>>>(ctx.batch, P, G, W, bc.inlet_first, bc.outlet_first);
+    k_integrals<T><<<ctx.batch.nsolve, 1024, 0, ctx.stream>>>(ctx.batch, P, G, W, bc.inlet_first, bc.outlet_first);
 }
 
 // CFL ramp of the driver (source/Solver.cpp:49-60): x1.2 whenever the density residual falls
@@ -418,7 +435,7 @@ void launch_cfl_ramp(const LaunchCtx &ctx, int iter)
 }
 
 #define GBT_INST(T)                                                                                                   \
-    template void launch_lusgs_sweeps<T>(const LaunchCtx &, const Phys &, const Geo &, Flow<T>, int);                 \
+    template void launch_lusgs_sweeps<T>(const LaunchCtx &, const Phys &, const Geo &, Flow<T>, const PlaneTables &); \
     template void launch_update<T>(const LaunchCtx &, const Phys &, const Geo &, Flow<T>, int, int *, int, int *);     \
     template void launch_primitive<T>(const LaunchCtx &, const Phys &, Flow<T>);                                       \
     template void launch_limiter<T>(const LaunchCtx &, const Phys &, Flow<T>, int, int *, int, int *);                 \

@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(256) k_cell_a(Batch B, Phys P, Geo G, Flow<T> 
 // mu_t as the minimum over all walls whose lines cross the cell, wall-adjacent cell and its ghost
 // set to zero (source/BL_Model.cpp:101-119).
 template <typename T>
-__global__ void __launch_bounds__(128) k_bl(Batch B, Phys P, Geo G, Flow<T> W, const DevWall *walls, int off)
+__global__ void __launch_bounds__(32) k_bl(Batch B, Phys P, Geo G, Flow<T> W, const DevWall *walls, int off)
 {
     const DevWall wl = walls[off + blockIdx.y];
     const int s = wl.solve;
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(256) k_cell_b(Batch B, Phys P, Geo G, Flow<T> 
 
 // global time stepping: minimum over the solve, then broadcast (source/TimeStep.cpp:64-87)
 template <typename T>
-__global__ void k_dt_min(Batch B, Flow<T> W, T *out)
+__global__ void __launch_bounds__(1024) k_dt_min(Batch B, Flow<T> W, T *out)
 {
     const Lvl L = B.lv[blockIdx.y];
     const int nI = L.IM - 1, nJ = L.JM - 1, nK = L.KM - 1;
@@ -209,27 +209,34 @@ void launch_cell_stages(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<
                         int level, T *scratch)
 {
     const Batch &B = ctx.batch;
+    ctx.mark("spectral_curl", 1);
     k_cell_a<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, G, W);
+    ctx.mark("spectral_curl", 0);
+    ctx.mark("baldwin_lomax", 1, bc.n_wall_slot + 2);
     if (level == 1 && P.turb_bl && bc.n_wall > 0) {
         // first-touch marks of the minimum merge, reset every evaluation
         cudaMemsetAsync(W.flag, 0, (size_t)ctx.pool_n * sizeof(int), ctx.stream);
         for (int q = 0; q < bc.n_wall_slot; q++) {
             int n = bc.wall_slot_off[q + 1] - bc.wall_slot_off[q];
             if (n <= 0) continue;
-            dim3 g((unsigned)((bc.wall_slot_lines[q] + 127) / 128), n);
-            k_bl<T><<<g, 128, 0, ctx.stream>>>(B, P, G, W, bc.wall, bc.wall_slot_off[q]);
+            // one warp per block: the lines of a wall spread over every SM (FP64 throughput per SM is low)
+            dim3 g((unsigned)((bc.wall_slot_lines[q] + 31) / 32), n);
+            k_bl<T><<<g, 32, 0, ctx.stream>>>(B, P, G, W, bc.wall, bc.wall_slot_off[q]);
         }
     }
     if (bc.n_wall > 0) {
         dim3 g((unsigned)((bc.max_wall + 127) / 128), bc.n_wall);
         k_wall_mut<T><<<g, 128, 0, ctx.stream>>>(B, W, bc.wall);
     }
+    ctx.mark("baldwin_lomax", 0, bc.n_wall_slot + 2);
+    ctx.mark("time_step", 1, 2);
     k_cell_b<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, G, W, level);
     if (P.global_dt) {
         k_dt_min<T><<<dim3(1, B.nsolve), 1024, 0, ctx.stream>>>(B, W, scratch);
         k_dt_set<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, W, scratch);
     }
     k_after_timestep<<<(B.nsolve + 127) / 128, 128, 0, ctx.stream>>>(B, level);
+    ctx.mark("time_step", 0, 2);
 }
 
 template void launch_cell_stages<double>(const LaunchCtx &, const Phys &, const Geo &, Flow<double>, const BcTables &, int, double *);

@@ -205,13 +205,19 @@ template <typename T>
 void launch_resflux(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const BcTables &bc, int level,
                     T *scratch)
 {
+    ctx.mark("boundary", 1);
     launch_boundary<T>(ctx, P, G, W, bc);
+    ctx.mark("boundary", 0);
     launch_cell_stages<T>(ctx, P, G, W, bc, level, scratch);
     const Batch &B = ctx.batch;
+    ctx.mark("face_flux", 1, 3);
     k_face<T, 0><<<ctx.grid_faces(0, 128), 128, 0, ctx.stream>>>(B, P, G, W, bc.wall);
     k_face<T, 1><<<ctx.grid_faces(1, 128), 128, 0, ctx.stream>>>(B, P, G, W, bc.wall);
     k_face<T, 2><<<ctx.grid_faces(2, 128), 128, 0, ctx.stream>>>(B, P, G, W, bc.wall);
+    ctx.mark("face_flux", 0, 3);
+    ctx.mark("cell_sum", 1);
     k_cell_sum<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, G, W);
+    ctx.mark("cell_sum", 0);
 }
 
 template void launch_resflux<double>(const LaunchCtx &, const Phys &, const Geo &, Flow<double>, const BcTables &, int, double *);

@@ -53,6 +53,8 @@ struct Level {
     Flow<T> W{};
     double *totalvol = nullptr;
     BcTables bc;
+    PlaneTables planes;
+    DevBuf plane_mem;
     std::vector<DevWall> walls_h;
     bool use_force = false;
     LaunchCtx ctx(const Batch &B, cudaStream_t s) const
@@ -187,13 +189,84 @@ public:
     T *dtmin = nullptr;
     cudaGraphExec_t graphs[3] = {nullptr, nullptr, nullptr};
 
+    // ---- stage profiler
+    struct ProfRec { std::string stage; cudaEvent_t a, b; int launches; };
+    bool profiling = false;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    std::vector<ProfRec> prof;
+    std::vector<std::pair<std::string, cudaEvent_t>> open_marks;
+    cudaEvent_t next_event()
+    {
+        if (ev_used == ev_pool.size()) {
+            cudaEvent_t e;
+            CK(cudaEventCreate(&e));
+            ev_pool.push_back(e);
+        }
+        return ev_pool[ev_used++];
+    }
+    static void hook_fn(void *user, const char *stage, int begin, int launches)
+    {
+        SolverT *self = (SolverT *)user;
+        cudaEvent_t e = self->next_event();
+        CK(cudaEventRecord(e, self->stream));
+        if (begin) self->open_marks.push_back({stage, e});
+        else {
+            for (size_t q = self->open_marks.size(); q-- > 0;)
+                if (self->open_marks[q].first == stage) {
+                    self->prof.push_back({stage, self->open_marks[q].second, e, launches});
+                    self->open_marks.erase(self->open_marks.begin() + q);
+                    break;
+                }
+        }
+    }
+    void profile_begin() override
+    {
+        CK(cudaStreamSynchronize(stream));
+        profiling = true;
+        ev_used = 0;
+        prof.clear();
+        open_marks.clear();
+    }
+    std::string profile_end() override
+    {
+        CK(cudaStreamSynchronize(stream));
+        profiling = false;
+        std::vector<std::string> order;
+        std::map<std::string, std::pair<double, long long>> tot;
+        for (auto &r : prof) {
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, r.a, r.b));
+            if (!tot.count(r.stage)) order.push_back(r.stage);
+            tot[r.stage].first += ms;
+            tot[r.stage].second += r.launches;
+        }
+        std::string out;
+        char buf[256];
+        for (auto &n : order) {
+            snprintf(buf, sizeof buf, "%s:%.6f:%lld;", n.c_str(), tot[n].first, tot[n].second);
+            out += buf;
+        }
+        return out;
+    }
+    struct Mark {
+        const SolverT *s; const char *n; int l;
+        Mark(const SolverT *s_, const char *n_, int l_ = 1) : s(s_), n(n_), l(l_) { if (s->profiling) hook_fn((void *)s, n, 1, l); }
+        ~Mark() { if (s->profiling) hook_fn((void *)s, n, 0, l); }
+    };
+
     Batch batch(int l) const
     {
         Batch B;
         B.lv = lev[l].lv_d; B.sc = lev[l].sc_d; B.st = st_d; B.nsolve = nsolve;
         return B;
     }
-    LaunchCtx ctx(int l) const { return lev[l].ctx(batch(l), stream); }
+    LaunchCtx ctx(int l) const
+    {
+        LaunchCtx c = lev[l].ctx(batch(l), stream);
+        if (profiling) { c.hook = &SolverT::hook_fn; c.hook_user = (void *)this; }
+        return c;
+    }
 
     explicit SolverT(const std::vector<std::string> &dirs, int prec)
     {
@@ -252,6 +325,7 @@ public:
     ~SolverT() override
     {
         for (auto &g : graphs) if (g) cudaGraphExecDestroy(g);
+        for (auto &e : ev_pool) cudaEventDestroy(e);
         if (stream) { cudaStreamSynchronize(stream); cudaStreamDestroy(stream); }
     }
 
@@ -347,9 +421,47 @@ public:
             CK(cudaMemcpy(G.z, hz.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
             build_tables(l, lc, hx, hy);
         }
+        build_planes(l);
         launch_geometry(ctx(l), G, Lv.totalvol);
         CK(cudaStreamSynchronize(stream));
         CK(cudaGetLastError());
+    }
+
+    // compact cell lists of the LU-SGS hyperplanes (source/LU_SGS_Marching.cpp:62-74)
+    void build_planes(int l)
+    {
+        Level<T> &Lv = lev[l];
+        PlaneTables &pt = Lv.planes;
+        pt.max_plane = Lv.max_plane;
+        pt.stride = Lv.max_plane + 2;
+        pt.max_count.assign(pt.stride, 0);
+        std::vector<int> pairs, start((size_t)nsolve * pt.stride + 1, 0);
+        for (int s = 0; s < nsolve; s++) {
+            const Lvl &v = Lv.lv[s];
+            int nI = v.IM - 1, nJ = v.JM - 1, nK = v.KM - 1;
+            if (nI >= 65536 || nJ >= 65536) throw std::runtime_error("block too large for the plane tables");
+            for (int pl = 0; pl < pt.stride; pl++) {
+                start[(size_t)s * pt.stride + pl] = (int)pairs.size();
+                int c = 0;
+                if (pl >= 3)
+                    for (int i = 1; i <= nI; i++)
+                        for (int j = 1; j <= nJ; j++) {
+                            int k = pl - i - j;
+                            if (k >= 1 && k <= nK) { pairs.push_back((i << 16) | j); c++; }
+                        }
+                pt.max_count[pl] = std::max(pt.max_count[pl], c);
+            }
+        }
+        start[(size_t)nsolve * pt.stride] = (int)pairs.size();
+        // start[s*stride + pl + 1] must be the end of plane pl: the last slot of each solve row
+        // (pl = stride-1) is empty, so the next row's first entry closes it
+        Lv.plane_mem.bytes = sizeof(int) * (pairs.size() + start.size()) + 256;
+        CK(cudaMalloc(&Lv.plane_mem.p, Lv.plane_mem.bytes));
+        int *d = (int *)Lv.plane_mem.p;
+        CK(cudaMemcpy(d, pairs.data(), sizeof(int) * pairs.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d + pairs.size(), start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
+        pt.pairs = d;
+        pt.start = d + pairs.size();
     }
 
     void build_tables(int l, const std::vector<LevelCase> &lc, const std::vector<double> &hx, const std::vector<double> &hy)
@@ -513,26 +625,28 @@ public:
         LaunchCtx cx = ctx(l);
         Level<T> &Lv = lev[l];
         if (!Lv.use_force) resflux(l);
-        else launch_forcing<T>(cx, Lv.W);
-        launch_lusgs_sweeps<T>(cx, P, Lv.G, Lv.W, Lv.max_plane);
+        else { Mark m(this, "mg_forcing"); launch_forcing<T>(cx, Lv.W); }
+        launch_lusgs_sweeps<T>(cx, P, Lv.G, Lv.W, Lv.planes);
         launch_update<T>(cx, P, Lv.G, Lv.W, l, bad_list, bad_cap, bad_count);
     }
     void res_calculate(int l) override { launch_res_norm<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, norm_part, norm_blk); }
-    void primitive_vars(int l) override { launch_primitive<T>(ctx(l), P, lev[l].W); }
-    void limit_vars(int l) override { launch_limiter<T>(ctx(l), P, lev[l].W, l, bad_list, bad_cap, bad_count); }
-    void corner_treatment(int l) override { launch_corner<T>(ctx(l), lev[l].W); }
+    void primitive_vars(int l) override { Mark m(this, "primitive"); launch_primitive<T>(ctx(l), P, lev[l].W); }
+    void limit_vars(int l) override { Mark m(this, "limiter", 2); launch_limiter<T>(ctx(l), P, lev[l].W, l, bad_list, bad_cap, bad_count); }
+    void corner_treatment(int l) override { Mark m(this, "mg_corner"); launch_corner<T>(ctx(l), lev[l].W); }
     void restrict_to_coarse() override
     {
         need_mg();
+        Mark m(this, "mg_restrict");
         launch_restrict<T>(ctx(1), ctx(2), lev[1].G, lev[2].G, lev[1].W, lev[2].W);
     }
     void interpolate(int init) override
     {
         need_mg();
+        Mark m(this, "mg_prolong");
         launch_interpolate<T>(ctx(1), ctx(2), lev[1].W, lev[2].W, init);
     }
-    void delta_cons() override { need_mg(); launch_delta<T>(ctx(2), lev[2].W); }
-    void integrals(int l) override { launch_integrals<T>(ctx(l), P, lev[l].G, lev[l].W, lev[l].bc); }
+    void delta_cons() override { need_mg(); Mark m(this, "mg_delta"); launch_delta<T>(ctx(2), lev[2].W); }
+    void integrals(int l) override { Mark m(this, "integrals"); launch_integrals<T>(ctx(l), P, lev[l].G, lev[l].W, lev[l].bc); }
     void set_use_force(int l, bool on) override { lev[l].use_force = on; }
     void need_mg() const { if (ng < 2) throw std::runtime_error("the case runs on a single grid level"); }
 
@@ -576,7 +690,7 @@ public:
         for (int q = 0; q < n; q++) {
             iter++;
             int ph = phase();
-            if (use_graphs && ph >= 0) {
+            if (use_graphs && ph >= 0 && !profiling) {
                 if (!graphs[ph]) {
                     cudaGraph_t g;
                     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));

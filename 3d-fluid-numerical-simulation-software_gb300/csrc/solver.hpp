@@ -47,6 +47,10 @@ public:
     virtual void set_cv(int solve, int level, const double *in, long n) = 0;
     virtual void states(SolveState *out) = 0;
     virtual void set_use_force(int level, bool on) = 0;
+    // stage profiler: while on, iterations run eagerly and every stage is bracketed by events
+    virtual void profile_begin() = 0;
+    // "stage:milliseconds:launches;..." totals since profile_begin
+    virtual std::string profile_end() = 0;
 };
 
 std::unique_ptr<SolverBase> make_solver(const std::vector<std::string> &dirs, int precision);

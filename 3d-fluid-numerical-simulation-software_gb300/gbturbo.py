@@ -55,6 +55,8 @@ def load() -> ctypes.CDLL:
         "gb_set_cv": ([vp, ip, ip, dp, ctypes.c_long], ip),
         "gb_sync": ([vp], ip),
         "gb_set_graphs": ([vp, ip], ip),
+        "gb_profile_begin": ([vp], ip),
+        "gb_profile_end": ([vp, ctypes.c_char_p, ip], ip),
         "gb_timer_start": ([vp], ip),
         "gb_timer_stop": ([vp, ctypes.POINTER(ctypes.c_float)], ip),
     }
@@ -70,7 +72,7 @@ EXPORTED = ["gb_solver_create", "gb_solver_destroy", "gb_last_error", "gb_dims",
             "gb_resflux", "gb_time_marching", "gb_res_calculate", "gb_primitive_vars", "gb_limit_vars",
             "gb_corner_treatment", "gb_restrict", "gb_interpolate", "gb_delta_cons", "gb_set_use_force",
             "gb_solver_step", "gb_integrals", "gb_iterate", "gb_get_status", "gb_get_field", "gb_set_cv",
-            "gb_sync", "gb_set_graphs", "gb_timer_start", "gb_timer_stop"]
+            "gb_sync", "gb_set_graphs", "gb_timer_start", "gb_timer_stop", "gb_profile_begin", "gb_profile_end"]
 
 
 class GBError(RuntimeError):
@@ -224,6 +226,19 @@ class Solver:
 
     def set_graphs(self, on: bool) -> None:
         self._ck(self._L.gb_set_graphs(self.h, int(on)))
+
+    def profile_begin(self) -> None:
+        self._ck(self._L.gb_profile_begin(self.h))
+
+    def profile_end(self) -> dict:
+        buf = ctypes.create_string_buffer(8192)
+        self._ck(self._L.gb_profile_end(self.h, buf, 8192))
+        out = {}
+        for item in buf.value.decode().split(";"):
+            if item:
+                name, ms, n = item.split(":")
+                out[name] = (float(ms), int(n))
+        return out
 
     def timer_start(self) -> None:
         self._ck(self._L.gb_timer_start(self.h))

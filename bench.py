@@ -1,0 +1,340 @@
+"""Benchmark of the residual-and-update path on one GB300 (or N replicas under torchrun).
+
+Workload (default): the synthetic compressor-rotor passage of 129 x 49 x 49 nodes (axial x pitch
+x span; 294,912 fine cells), 22 blades, 16000 rpm, back pressure 1.20 x inlet total, Roe + MUSCL3
+on primitive variables, Baldwin-Lomax, LU-SGS, two-level multigrid (the reference's maximum),
+FP64. A step is one multigrid cycle of the reference driver (CSolver::Solver + integrals); the
+metric is fine-grid cell updates per second (cells x cycles / time).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed] [--batch B]
+  python bench.py --impl reference ...   (the CPU implementation of the path on the host cores)
+
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "3d-fluid-numerical-simulation-software_gb300")
+for _p in (PKG, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--batch", type=int, default=1, help="operating points per GPU")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def make_cases(root: str, n: int, seed_offset: int = 0):
+    """configs[1] passage; in a batch the back pressure varies over [1.05, 1.30] x p_t"""
+    import meshgen as mg
+    dirs = []
+    for q in range(n):
+        pb = 1.20 if n == 1 else 1.05 + 0.25 * ((q + seed_offset) % n) / max(n - 1, 1)
+        case = mg.rotor_passage(IM=49, JM=49, KM=129, options={
+            "Pout": "%.1f" % (pb * 101325.0), "multigrid": "Y", "coarse_iter": "2", "Ma0": "0.45"})
+        d = os.path.join(root, f"op{q}")
+        mg.write_case(case, d)
+        dirs.append(d)
+    return dirs, case.n_cells
+
+
+# ---------------------------------------------------------------------------------------------
+# algorithmic bytes per kernel launch (each input/output element counted once; "geo" and "cv"
+# are FP64 in both forms, "w" is the working precision). unit: "cell" (fine cells), "face"
+# (faces of one family, about one per cell), "plane_cell" (cells of one hyperplane)
+# ---------------------------------------------------------------------------------------------
+ALG = {
+    # S(3) s nrm(3) t1(3) t2(3) qe metrics(9) = 23 geo; prim 6 + mu_t 1 of one cell; 10 fluxes out
+    "face_flux": {"unit": "face", "geo": 23, "cv": 0, "w": 17, "int": 1},
+    # vol dt lamc(3) lamv(3) + res or dq (5) + neighbour cv(5) dq(5) p(1) + mean normal(3) area
+    # entrainment, per direction amortised to one cell: cn 9 cs 3 cve 3; dq out 5
+    "sweep_forward": {"unit": "plane_cell", "geo": 16, "cv": 5, "w": 24, "int": 0},
+    "sweep_backward": {"unit": "plane_cell", "geo": 16, "cv": 5, "w": 24, "int": 0},
+}
+
+
+def alg_bytes_per_launch(stage, cells, planes, wsize, launches_per_call):
+    a = ALG[stage]
+    per_unit = 8 * a["geo"] + 8 * a["cv"] + wsize * a["w"] + 4 * a["int"]
+    if a["unit"] == "plane_cell":
+        return per_unit * cells / planes
+    return per_unit * cells        # one launch per face family, ~cells faces each
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region"""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        if not shutil.which("nvidia-smi"):
+            return
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        self.f = open(self.path, "w")
+        self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                      "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 9:
+                rows.append(p)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        idx = rows[0][0] if not dev.isdigit() else dev
+        rows = [r for r in rows if r[0] == idx] or rows
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in rows for q in range(4) if r[5 + q].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        return rank, world, dist
+    return 0, 1, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allmax(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------------------------
+# CPU arms
+# ---------------------------------------------------------------------------------------------
+def _oracle_worker(args):
+    case_dir, warm, steps = args
+    import pyoracle
+    o = pyoracle.Oracle(case_dir)
+    for _ in range(warm):
+        o.iterate()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.iterate()
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(case_dir, cells, warm, steps):
+    """the oracle port, one thread, bounded sample of the same workload"""
+    import pyoracle
+    pyoracle.build()
+    t = _oracle_worker((case_dir, warm, steps))
+    return {"value": cells * steps / t, "unit": "cell-updates/s", "cores": 1, "kind": "port",
+            "sample": f"{steps} multigrid cycles of one {cells}-cell passage after {warm} untimed iterations, "
+                      f"CPU oracle (single thread, FP64)"}
+
+
+def run_reference(args, rank, world, dist):
+    if rank != 0:
+        return 0
+    import pyoracle
+    pyoracle.build()
+    cores = os.cpu_count() or 1
+    tmp = tempfile.mkdtemp(prefix="gbt_ref_")
+    try:
+        dirs, cells = make_cases(tmp, 1)
+        steps = max(1, min(args.steps, 6))
+        warm = max(args.warmup, 3)
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(cores) as pool:
+            times = pool.map(_oracle_worker, [(dirs[0], warm, steps)] * cores)
+        t = max(times)
+        value = cores * cells * steps / t
+        line = {
+            "impl": "reference", "metric": "cell_updates_per_s", "value": value, "unit": "cell-updates/s",
+            "n_gpus": args.gpus, "steps": steps, "warmup": warm, "ms_per_step": 1000.0 * t / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_block(args, cells, 1),
+            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": cores, "kind": "port",
+                             "sample": f"{cores} independent single-thread CPU solves (the reference's CPU path "
+                                       f"restated in C), {steps} multigrid cycles each after {warm} untimed"},
+            "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line), flush=True)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return 0
+
+
+def config_block(args, cells, nsolve):
+    return {"workload": "rotor_passage_129x49x49_2level_multigrid", "mesh_nodes": "129x49x49 (axial x pitch x span)",
+            "cells_per_solve": cells, "solves_per_gpu": nsolve, "precision": args.precision,
+            "scheme": "Roe + MUSCL3 (primitive), Baldwin-Lomax, LU-SGS, 2-level FAS (reference maximum)",
+            "l2": "inputs larger than L2 (FP64 working set well above 129 MB), no flush",
+            "parallelism": "replicas"}
+
+
+# ---------------------------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------------------------
+def run_gpu(args, rank, world, dist):
+    import build as pkg_build
+    pkg_build.build()
+    import gbturbo
+    prec = gbturbo.FP64 if args.precision == "fp64" else gbturbo.MIXED
+    wsize = 8 if prec == gbturbo.FP64 else 4
+    tmp = tempfile.mkdtemp(prefix=f"gbt_bench_{rank}_")
+    try:
+        dirs, cells = make_cases(tmp, args.batch, seed_offset=rank)
+        nsolve = len(dirs)
+        grid_bytes = sum(os.path.getsize(os.path.join(d, "grid.dat")) for d in dirs)
+
+        # --- device-resident throughput (value)
+        s = gbturbo.Solver(dirs, prec)
+        s.init_uniform()
+        s.iterate(max(args.warmup, 3), history=False)
+        s.sync()
+        barrier(dist)
+        clk = ClockSampler()
+        clk.start()
+        s.timer_start()
+        s.iterate(args.steps, history=False)
+        ms = s.timer_stop()
+        clocks = clk.stop()
+        barrier(dist)
+        ms = allmax(dist, ms)
+        value = cells * nsolve * world * args.steps / (ms / 1000.0)
+        status = [int(x) for x in s.status()]
+
+        # --- stage profile of a few cycles (eager launches, events around every stage)
+        nprof = min(5, args.steps)
+        s.profile_begin()
+        s.iterate(nprof, history=False)
+        prof = s.profile_end()
+        I, J, K, _ = s.dims(0, 1)
+        planes = I + J + K - 5
+        total_prof = sum(v[0] for v in prof.values())
+        launches_per_step = sum(v[1] for v in prof.values()) / nprof
+        dom = max((k for k in prof if k in ALG), key=lambda k: prof[k][0])
+        dom_ms, dom_launches = prof[dom]
+        avg_launch_s = dom_ms / 1000.0 / dom_launches
+        bytes_per_launch = alg_bytes_per_launch(dom, cells * nsolve, planes, wsize, 1)
+        achieved = bytes_per_launch / avg_launch_s / 1e9
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except Exception:
+            pass
+        peak = float(peaks.get("hbm_gbs", 6800.0))
+        traffic = None
+        try:
+            for line in open(os.path.join(ROOT, "profiles", "dram_traffic_per_launch.txt")):
+                f = line.split()
+                if len(f) >= 4 and not line.startswith("#") and f[0] == dom and f[1] == args.precision and int(f[2]) == nsolve:
+                    traffic = float(f[3])
+        except FileNotFoundError:
+            pass
+        s.close()
+
+        # --- end to end through the C-ABI: case files on the host -> handle (upload + geometry)
+        # -> iterations with the history row read back every step
+        barrier(dist)
+        t0 = time.perf_counter()
+        e = gbturbo.Solver(dirs, prec)
+        e.init_uniform()
+        e.iterate(max(args.warmup, 3), history=True)
+        for _ in range(args.steps):
+            e.iterate(1, history=True)
+        e.close()
+        t_e2e = allmax(dist, time.perf_counter() - t0)
+        barrier(dist)
+        n_e2e = max(args.warmup, 3) + args.steps
+        e2e_value = cells * nsolve * world * n_e2e / t_e2e
+
+        base = None
+        if rank == 0 and not args.no_cpu_baseline:
+            base = cpu_baseline(dirs[0], cells, warm=3, steps=2)
+
+        if rank == 0:
+            stages = {k: {"ms_per_step": round(v[0] / nprof, 4), "launches_per_step": round(v[1] / nprof, 1),
+                          "share": round(v[0] / total_prof, 4)} for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+            line = {
+                "metric": "cell_updates_per_s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
+                "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if prec == gbturbo.FP64 else "f32+f64", "data": "synthetic",
+                "config": config_block(args, cells, nsolve),
+                "clocks": clocks,
+                "e2e": {"value": e2e_value, "unit": "cell-updates/s",
+                        "h2d_bytes_per_step": int(grid_bytes / n_e2e), "d2h_bytes_per_step": 96 * nsolve},
+                "gpu_launches": int(round(launches_per_step * args.steps)),
+                "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": traffic,
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800 GB/s",
+                             "note": "FP64 on GB300 is bound by the FP64 pipe, not HBM" if prec == gbturbo.FP64 else ""},
+                "stages": stages,
+                "cpu_baseline": base,
+                "status": status,
+            }
+            print(json.dumps(line), flush=True)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return 0
+
+
+def main():
+    args = parse()
+    rank, world, dist = dist_init()
+    if args.impl == "reference":
+        rc = run_reference(args, rank, world, dist)
+    else:
+        rc = run_gpu(args, rank, world, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -87,6 +87,11 @@ int gb_set_cv(gb_solver *h, int solve, int level, const double *cv, long n);
 int gb_sync(gb_solver *h);
 /* 0 disables graph replay in gb_iterate (eager launches) */
 int gb_set_graphs(gb_solver *h, int enable);
+/* stage profiler: between the two calls iterations run without graphs and every stage of the
+ * path is bracketed by CUDA events on the handle's stream; gb_profile_end writes
+ * "stage:milliseconds:kernel launches;..." totals into buf */
+int gb_profile_begin(gb_solver *h);
+int gb_profile_end(gb_solver *h, char *buf, int buflen);
 /* device time of everything enqueued between the two calls, in milliseconds (events on the
  * handle's stream) */
 int gb_timer_start(gb_solver *h);
