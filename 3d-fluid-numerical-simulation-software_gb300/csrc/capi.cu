@@ -94,6 +94,16 @@ int gb_res_calculate(gb_solver *h, int level, double *out)
     });
 }
 
+int gb_res_calculate_noalloc(gb_solver *h, int level, double *out)
+{
+    NEED(h); LEVEL(h, level);
+    if (h->s->nsolve > GB_NOALLOC_MAX_SOLVES) {
+        g_err = "gb_res_calculate_noalloc: the batch has more solves than the static scratch holds (GB_NOALLOC_MAX_SOLVES)";
+        return GB_ERR_ARG;
+    }
+    return guard([&] { h->s->res_calculate_static(level, out); });
+}
+
 int gb_integrals(gb_solver *h, int level, double *out)
 {
     NEED(h); LEVEL(h, level);

@@ -630,6 +630,10 @@ public:
         launch_update<T>(cx, P, Lv.G, Lv.W, l, bad_list, bad_cap, bad_count);
     }
     void res_calculate(int l) override { launch_res_norm<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, norm_part, norm_blk); }
+    void res_calculate_static(int l, double *host_out) override
+    {
+        launch_res_norm_static<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, host_out);
+    }
     void primitive_vars(int l) override { Mark m(this, "primitive"); launch_primitive<T>(ctx(l), P, lev[l].W); }
     void limit_vars(int l) override { Mark m(this, "limiter", 2); launch_limiter<T>(ctx(l), P, lev[l].W, l, bad_list, bad_cap, bad_count); }
     void corner_treatment(int l) override { Mark m(this, "mg_corner"); launch_corner<T>(ctx(l), lev[l].W); }

@@ -32,6 +32,8 @@ public:
     virtual void resflux(int level) = 0;
     virtual void time_marching(int level) = 0;
     virtual void res_calculate(int level) = 0;
+    // res_calculate with static scratch and no allocation; norms to host_out (5 per solve) if given
+    virtual void res_calculate_static(int level, double *host_out) = 0;
     virtual void primitive_vars(int level) = 0;
     virtual void limit_vars(int level) = 0;
     virtual void corner_treatment(int level) = 0;

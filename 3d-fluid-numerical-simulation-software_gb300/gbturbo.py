@@ -40,6 +40,7 @@ def load() -> ctypes.CDLL:
         "gb_resflux": ([vp, ip], ip),
         "gb_time_marching": ([vp, ip], ip),
         "gb_res_calculate": ([vp, ip, dp], ip),
+        "gb_res_calculate_noalloc": ([vp, ip, dp], ip),
         "gb_primitive_vars": ([vp, ip], ip),
         "gb_limit_vars": ([vp, ip], ip),
         "gb_corner_treatment": ([vp, ip], ip),
@@ -72,7 +73,8 @@ EXPORTED = ["gb_solver_create", "gb_solver_destroy", "gb_last_error", "gb_dims",
             "gb_resflux", "gb_time_marching", "gb_res_calculate", "gb_primitive_vars", "gb_limit_vars",
             "gb_corner_treatment", "gb_restrict", "gb_interpolate", "gb_delta_cons", "gb_set_use_force",
             "gb_solver_step", "gb_integrals", "gb_iterate", "gb_get_status", "gb_get_field", "gb_set_cv",
-            "gb_sync", "gb_set_graphs", "gb_timer_start", "gb_timer_stop", "gb_profile_begin", "gb_profile_end"]
+            "gb_sync", "gb_set_graphs", "gb_timer_start", "gb_timer_stop", "gb_profile_begin", "gb_profile_end",
+            "gb_res_calculate_noalloc"]
 
 
 class GBError(RuntimeError):
@@ -163,6 +165,12 @@ class Solver:
     def res_calculate(self, level: int = 1) -> np.ndarray:
         out = np.zeros(5 * self.n)
         self._ck(self._L.gb_res_calculate(self.h, level, _dp(out)))
+        return out.reshape(self.n, 5)
+
+    def res_calculate_noalloc(self, level: int = 1) -> np.ndarray:
+        """gb_res_calculate_noalloc: the same norms with the library's static scratch, no allocation."""
+        out = np.zeros(5 * self.n)
+        self._ck(self._L.gb_res_calculate_noalloc(self.h, level, _dp(out)))
         return out.reshape(self.n, 5)
 
     def primitive_vars(self, level: int = 1) -> None:

@@ -97,6 +97,18 @@ int gb_profile_end(gb_solver *h, char *buf, int buflen);
 int gb_timer_start(gb_solver *h);
 int gb_timer_stop(gb_solver *h, float *ms);
 
+/* Residual norm of gb_res_calculate (same arguments, same values in out and in the solve states)
+ * computed with no allocation on success: its scratch is a static device array of fixed size
+ * inside the library. It has no counterpart in the reference; it exists for callers that may not
+ * allocate between iterations (a convergence monitor of a batch whose device memory is committed
+ * to the solve pools, a host thread under a no-heap rule). Batches of more than
+ * GB_NOALLOC_MAX_SOLVES solves are rejected with GB_ERR_ARG. All calls on a device share the one
+ * array, so calls that overlap in time race and must be serialised by the caller. The first call
+ * on a device looks the array up and zeroes it: make that call before any stream capture begins.
+ * Call it with the handle's device current. */
+#define GB_NOALLOC_MAX_SOLVES 128
+int gb_res_calculate_noalloc(gb_solver *h, int level, double *out);
+
 #ifdef __cplusplus
 }
 #endif
