@@ -61,70 +61,85 @@ __global__ void k_bc_inlet(Batch B, Phys P, Geo G, Flow<T> W, const DevInOut *pa
     for (int nd = 1; nd <= P.ndummy; nd++) st_state(W, ix(L, i, j, low ? -nd : L.KM + nd), c, q);
 }
 
-// axial outlet, one block per outlet patch: mass-weighted swirl per radial row, radial
-// equilibrium marched from p_out at i = IM/2 using the previous ghost density, then ghosts
-// extrapolated from the last interior layer
+// axial outlet in three launches spread over the SMs: mass-weighted swirl per radial row (one
+// warp per row, lanes over the pitch), radial equilibrium marched from p_out at i = IM/2 using
+// the previous ghost density (one thread per pitch line), then ghosts extrapolated from the last
+// interior layer (one thread per face)
 template <typename T>
-__global__ void __launch_bounds__(256) k_bc_outlet(Batch B, Phys P, Geo G, Flow<T> W, const DevInOut *pat)
+__global__ void __launch_bounds__(256) k_outlet_swirl(Batch B, Geo G, Flow<T> W, const DevInOut *pat, double *cu_all,
+                                                      int cu_stride)
 {
-    extern __shared__ double cu[];
-    const DevInOut pt = pat[blockIdx.x];
+    const DevInOut pt = pat[blockIdx.y];
     const Lvl L = B.lv[pt.solve];
-    const int IM = L.IM, JM = L.JM, KM = L.KM;
-    // one warp per radial row i: lanes over the pitch, area-weighted swirl and area summed
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int i = 1 + warp; i <= IM - 1; i += nw) {
-        double acc = 0.0, sa = 0.0;
-        for (int j = 1 + lane; j <= JM - 1; j += 32) {
-            const long long p = ix(L, i, j, KM - 1), f = ix(L, i, j, KM);
-            const double th = G.th[2][f];
-            double sn, cs;
-            sincos(th, &sn, &cs);
-            const double ct = -1.0 * (double)W.pv[PU][p] * sn + (double)W.pv[PV][p] * cs;
-            acc = acc + ct * G.s[2][f];
-            sa = sa + G.s[2][f];
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            acc += __shfl_down_sync(0xffffffffu, acc, o);
-            sa += __shfl_down_sync(0xffffffffu, sa, o);
-        }
-        if (lane == 0) cu[i] = acc / sa;
+    const int JM = L.JM, KM = L.KM;
+    const int lane = threadIdx.x & 31;
+    const int i = 1 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i > L.IM - 1) return;
+    double acc = 0.0, sa = 0.0;
+    for (int j = 1 + lane; j <= JM - 1; j += 32) {
+        const long long p = ix(L, i, j, KM - 1), f = ix(L, i, j, KM);
+        const double th = G.th[2][f];
+        double sn, cs;
+        sincos(th, &sn, &cs);
+        const double ct = -1.0 * (double)W.pv[PU][p] * sn + (double)W.pv[PV][p] * cs;
+        acc = acc + ct * G.s[2][f];
+        sa = sa + G.s[2][f];
     }
-    __syncthreads();
+    for (int o = 16; o > 0; o >>= 1) {
+        acc += __shfl_down_sync(0xffffffffu, acc, o);
+        sa += __shfl_down_sync(0xffffffffu, sa, o);
+    }
+    if (lane == 0) cu_all[(long long)blockIdx.y * cu_stride + i] = acc / sa;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32) k_outlet_march(Batch B, Geo G, Flow<T> W, const DevInOut *pat, const double *cu_all,
+                                                     int cu_stride)
+{
+    const DevInOut pt = pat[blockIdx.y];
+    const Lvl L = B.lv[pt.solve];
+    const int IM = L.IM, KM = L.KM;
+    const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (j > L.JM - 1) return;
+    const double *cu = cu_all + (long long)blockIdx.y * cu_stride;
     const int iref = (int)(0.5 * IM);
     const double pout = B.sc[pt.solve].pout;
-    for (int j = 1 + threadIdx.x; j <= JM - 1; j += blockDim.x) {
-        double pr = pout;
-        W.pv[PP][ix(L, iref, j, KM)] = (T)pr;
-        for (int i = iref - 1; i >= 1; i--) {
-            const double rn = G.r[2][ix(L, i, j, KM)], rn1 = G.r[2][ix(L, i + 1, j, KM)];
-            const double dpdr = W.cv[0][ix(L, i, j, KM)] * cu[i] * cu[i] / rn;
-            pr = pr - dpdr * (rn1 - rn);
-            W.pv[PP][ix(L, i, j, KM)] = (T)pr;
-        }
-        pr = pout;
-        for (int i = iref + 1; i <= IM - 1; i++) {
-            // radii of the k = KM-1 face row here, as the reference takes them
-            const double rn1 = G.r[2][ix(L, i, j, KM - 1)], rn = G.r[2][ix(L, i - 1, j, KM - 1)];
-            const double dpdr = W.cv[0][ix(L, i, j, KM)] * cu[i] * cu[i] / rn;
-            pr = pr + dpdr * (rn1 - rn);
-            W.pv[PP][ix(L, i, j, KM)] = (T)pr;
-        }
+    double pr = pout;
+    W.pv[PP][ix(L, iref, j, KM)] = (T)pr;
+    for (int i = iref - 1; i >= 1; i--) {
+        const double rn = G.r[2][ix(L, i, j, KM)], rn1 = G.r[2][ix(L, i + 1, j, KM)];
+        const double dpdr = W.cv[0][ix(L, i, j, KM)] * cu[i] * cu[i] / rn;
+        pr = pr - dpdr * (rn1 - rn);
+        W.pv[PP][ix(L, i, j, KM)] = (T)pr;
     }
-    __syncthreads();
-    const int n = (IM - 1) * (JM - 1);
+    pr = pout;
+    for (int i = iref + 1; i <= IM - 1; i++) {
+        // radii of the k = KM-1 face row here, as the reference takes them
+        const double rn1 = G.r[2][ix(L, i, j, KM - 1)], rn = G.r[2][ix(L, i - 1, j, KM - 1)];
+        const double dpdr = W.cv[0][ix(L, i, j, KM)] * cu[i] * cu[i] / rn;
+        pr = pr + dpdr * (rn1 - rn);
+        W.pv[PP][ix(L, i, j, KM)] = (T)pr;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_outlet_fill(Batch B, Phys P, Flow<T> W, const DevInOut *pat)
+{
+    const DevInOut pt = pat[blockIdx.y];
+    const Lvl L = B.lv[pt.solve];
+    const int IM = L.IM, JM = L.JM, KM = L.KM;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (IM - 1) * (JM - 1)) return;
     const double g1 = P.gamma - 1.0;
-    for (int t = threadIdx.x; t < n; t += blockDim.x) {
-        const int i = 1 + t / (JM - 1), j = 1 + t % (JM - 1);
-        const long long g = ix(L, i, j, KM), p = ix(L, i, j, KM - 1);
-        const double d = W.cv[0][p];
-        const double pr = (double)W.pv[PP][g];
-        const double u = W.pv[PU][p], v = W.pv[PV][p], w = W.pv[PW][p];
-        const double c[5] = {d, W.cv[1][p], W.cv[2][p], W.cv[3][p], pr / g1 + d * (u * u + v * v + w * w) / 2.0};
-        const T q[6] = {(T)d, (T)u, (T)v, (T)w, (T)pr, (T)(pr / P.rgas / d)};
-        st_state(W, g, c, q);
-        for (int nd = 1; nd <= P.ndummy; nd++) st_state(W, ix(L, i, j, KM + nd), c, q);
-    }
+    const int i = 1 + t / (JM - 1), j = 1 + t % (JM - 1);
+    const long long g = ix(L, i, j, KM), p = ix(L, i, j, KM - 1);
+    const double d = W.cv[0][p];
+    const double pr = (double)W.pv[PP][g];
+    const double u = W.pv[PU][p], v = W.pv[PV][p], w = W.pv[PW][p];
+    const double c[5] = {d, W.cv[1][p], W.cv[2][p], W.cv[3][p], pr / g1 + d * (u * u + v * v + w * w) / 2.0};
+    const T q[6] = {(T)d, (T)u, (T)v, (T)w, (T)pr, (T)(pr / P.rgas / d)};
+    st_state(W, g, c, q);
+    for (int nd = 1; nd <= P.ndummy; nd++) st_state(W, ix(L, i, j, KM + nd), c, q);
 }
 
 // no-slip wall: ghost keeps p, T, rho, rho*E of the first cell, relative velocity reflected;
@@ -198,8 +213,12 @@ void launch_boundary(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> 
 {
     const Batch &B = ctx.batch;
     if (bc.n_inlet) k_bc_inlet<T><<<dim3((bc.max_inlet + 127) / 128, bc.n_inlet), 128, 0, ctx.stream>>>(B, P, G, W, bc.inlet);
-    if (bc.n_outlet)
-        k_bc_outlet<T><<<bc.n_outlet, 256, (size_t)(bc.max_outlet_im + 1) * sizeof(double), ctx.stream>>>(B, P, G, W, bc.outlet);
+    if (bc.n_outlet) {
+        const int cs = bc.max_outlet_im + 1;
+        k_outlet_swirl<T><<<dim3((bc.max_outlet_im + 7) / 8, bc.n_outlet), 256, 0, ctx.stream>>>(B, G, W, bc.outlet, bc.outlet_cu, cs);
+        k_outlet_march<T><<<dim3((bc.max_outlet_jm + 31) / 32, bc.n_outlet), 32, 0, ctx.stream>>>(B, G, W, bc.outlet, bc.outlet_cu, cs);
+        k_outlet_fill<T><<<dim3((bc.max_outlet_im * bc.max_outlet_jm + 255) / 256, bc.n_outlet), 256, 0, ctx.stream>>>(B, P, W, bc.outlet);
+    }
     if (bc.n_wall) k_bc_wall<T><<<dim3((bc.max_wall + 127) / 128, bc.n_wall), 128, 0, ctx.stream>>>(B, P, G, W, bc.wall);
     if (bc.n_per)
         k_bc_periodic<T><<<(unsigned)((bc.n_per + 255) / 256), 256, 0, ctx.stream>>>(B, W, bc.per_dst, bc.per_src, bc.per_meta, bc.n_per);

@@ -41,9 +41,13 @@ struct BcTables {
     const long long *per_dst = nullptr, *per_src = nullptr;
     const int *per_meta = nullptr;                // solve * 4 + (sign + 1)
     long long n_per = 0;
-    int max_outlet_im = 0;
+    int max_outlet_im = 0, max_outlet_jm = 0;
+    double *outlet_cu = nullptr;                  // per outlet patch: mass-weighted swirl of each radial row
+    double *integ_part = nullptr;                 // per solve and section: kIntegralBlocks partial sums of 3
     const DevInOut *inlet_first = nullptr, *outlet_first = nullptr;   // per solve: Inlet[1], Outlet[1]
 };
+
+constexpr int kIntegralBlocks = 16;             // blocks per inlet/outlet section in the integrals
 
 // cells of every i+j+k hyperplane of every solve: pairs[start[s*stride + plane] ..
 // start[s*stride + plane + 1]) hold (i << 16) | j; max_count[plane] is the largest plane over solves

@@ -11,34 +11,18 @@
 
 namespace gbt {
 
-// flux difference F_n(Q+dQ) - F_n(Q) of neighbour cell nb across its mean normal in direction d
-template <typename T>
-__device__ __forceinline__ void delt_fn(const Phys &P, const Geo &G, const Flow<T> &W, int d, long long nb, T out[5])
-{
-    const T nx = (T)G.cn[d][0][nb], ny = (T)G.cn[d][1][nb], nz = (T)G.cn[d][2][nb];
-    const T ve = (T)G.cve[d][nb];
-    const T od = (T)W.cv[0][nb], omx = (T)W.cv[1][nb], omy = (T)W.cv[2][nb], omz = (T)W.cv[3][nb], oe = (T)W.cv[4][nb];
-    const T nd = od + W.dq[0][nb], nmx = omx + W.dq[1][nb], nmy = omy + W.dq[2][nb], nmz = omz + W.dq[3][nb],
-            ne = oe + W.dq[4][nb];
-    const T inv = (T)1 / nd;
-    const T u = nmx * inv, v = nmy * inv, w = nmz * inv, E = ne * inv;
-    const T pn = ((T)P.gamma - (T)1) * nd * (E - (T)0.5 * (u * u + v * v + w * w));
-    const T po = W.pv[PP][nb];
-    const T oinv = (T)1 / od;
-    const T Vo = omx * oinv * nx + omy * oinv * ny + omz * oinv * nz;
-    const T Vn = u * nx + v * ny + w * nz;
-    const T dn = Vn - ve, dov = Vo - ve;
-    out[0] = nd * dn - od * dov;
-    out[1] = (nmx * dn + pn * nx) - (omx * dov + po * nx);
-    out[2] = (nmy * dn + pn * ny) - (omy * dov + po * ny);
-    out[3] = (nmz * dn + pn * nz) - (omz * dov + po * nz);
-    out[4] = ((ne + pn) * dn + pn * ve) - ((oe + po) * dov + po * ve);
-}
+// Programmatic dependent launch: each plane's kernel is launched while the previous plane's is
+// still running; it reads everything the sweep does not write (indices, geometry, Q, spectral
+// radii, residual) first, then waits for the previous plane's grid to finish before it reads dQ.
+__device__ __forceinline__ void wait_previous_plane() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void release_next_plane() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 // One warp per block handles ten cells of a plane with three lanes per cell, lane d computing
 // the off-diagonal term of neighbour direction d; the three terms are combined on the first lane
 // in the reference's order (-R + A_I + A_J + A_K + V_I + V_J + V_K). Cells of a plane come from a
-// compact per-solve list, so a plane of ~1,300 cells spreads over ~130 SMs.
+// compact per-solve list, so a plane of ~1,300 cells spreads over ~130 SMs. The neighbour's old
+// flux F_n(Q) and the diagonal 1/alpha do not depend on dQ and are formed before the wait, so
+// only the new flux F_n(Q + dQ) and the combination sit on the plane-to-plane critical path.
 template <typename T, int DIR>      // DIR = +1 forward (lower neighbours), -1 backward
 __global__ void __launch_bounds__(32) k_sweep(Batch B, Phys P, Geo G, Flow<T> W, const int *__restrict__ pairs,
                                               const int *__restrict__ pstart, int pstride, int plane)
@@ -49,28 +33,71 @@ __global__ void __launch_bounds__(32) k_sweep(Batch B, Phys P, Geo G, Flow<T> W,
     const int base = pstart[s * pstride + plane], cnt = pstart[s * pstride + plane + 1] - base;
     const int idx = blockIdx.x * 10 + slot;
     const bool active = lane < 30 && idx < cnt;
-    T aw[5] = {(T)0, (T)0, (T)0, (T)0, (T)0}, vw[5] = {(T)0, (T)0, (T)0, (T)0, (T)0};
-    long long p = 0;
+    bool has = false;
+    long long p = 0, nb = 0;
+    T nx = 0, ny = 0, nz = 0, ve = 0, od = 0, omx = 0, omy = 0, omz = 0, oe = 0, sd = 0, rl = 0, lv = 0;
+    T fo[5] = {(T)0, (T)0, (T)0, (T)0, (T)0}, rhs[5] = {(T)0, (T)0, (T)0, (T)0, (T)0};
+    T alpha = (T)1, inva = (T)1;
     if (active) {
         const int ij = pairs[base + idx];
         const int i = ij >> 16, j = ij & 0xffff, k = plane - i - j;
         p = ix(L, i, j, k);
         const int a = d == 0 ? i : (d == 1 ? j : k);
         const int top = d == 0 ? L.IM - 1 : (d == 1 ? L.JM - 1 : L.KM - 1);
-        const bool has = DIR > 0 ? (a != 1) : (a != top);
+        has = DIR > 0 ? (a != 1) : (a != top);
         if (has) {
             const long long sd_ = d == 0 ? (long long)L.NJ * L.NK : (d == 1 ? (long long)L.NK : 1LL);
-            const long long nb = DIR > 0 ? p - sd_ : p + sd_;
-            T dF[5];
-            delt_fn(P, G, W, d, nb, dF);
-            const T sd = (T)G.cs[d][nb];
-            const T rl = (T)P.relax * W.lamc[d][nb], lv = W.lamv[d][nb];
+            nb = DIR > 0 ? p - sd_ : p + sd_;
+            nx = (T)G.cn[d][0][nb]; ny = (T)G.cn[d][1][nb]; nz = (T)G.cn[d][2][nb];
+            ve = (T)G.cve[d][nb];
+            od = (T)W.cv[0][nb]; omx = (T)W.cv[1][nb]; omy = (T)W.cv[2][nb]; omz = (T)W.cv[3][nb]; oe = (T)W.cv[4][nb];
+            const T po = W.pv[PP][nb];
+            const T oinv = (T)1 / od;
+            const T Vo = omx * oinv * nx + omy * oinv * ny + omz * oinv * nz;
+            const T dov = Vo - ve;
+            fo[0] = od * dov;
+            fo[1] = omx * dov + po * nx;
+            fo[2] = omy * dov + po * ny;
+            fo[3] = omz * dov + po * nz;
+            fo[4] = (oe + po) * dov + po * ve;
+            sd = (T)G.cs[d][nb];
+            rl = (T)P.relax * W.lamc[d][nb];
+            lv = W.lamv[d][nb];
+        }
+        if (d == 0) {
+            alpha = (T)G.vol[p] / W.dt[p] + (T)P.relax * (W.lamc[0][p] + W.lamc[1][p] + W.lamc[2][p]) +
+                    (T)2 * (W.lamv[0][p] + W.lamv[1][p] + W.lamv[2][p]);
+            inva = (T)1 / alpha;
+            if (DIR > 0) {
 #pragma unroll
-            for (int c = 0; c < 5; c++) {
-                const T dqn = W.dq[c][nb];
-                aw[c] = DIR > 0 ? (T)0.5 * (dF[c] * sd + rl * dqn) : (T)0.5 * (dF[c] * sd - rl * dqn);
-                vw[c] = lv * dqn;
+                for (int c = 0; c < 5; c++) rhs[c] = -W.res[c][p];
             }
+        }
+    }
+    wait_previous_plane();
+    release_next_plane();
+    T aw[5] = {(T)0, (T)0, (T)0, (T)0, (T)0}, vw[5] = {(T)0, (T)0, (T)0, (T)0, (T)0};
+    if (has) {
+        T dqn[5];
+#pragma unroll
+        for (int c = 0; c < 5; c++) dqn[c] = W.dq[c][nb];
+        // flux difference F_n(Q+dQ) - F_n(Q) of the neighbour across its mean normal
+        const T nd = od + dqn[0], nmx = omx + dqn[1], nmy = omy + dqn[2], nmz = omz + dqn[3], ne = oe + dqn[4];
+        const T inv = (T)1 / nd;
+        const T u = nmx * inv, v = nmy * inv, w = nmz * inv, E = ne * inv;
+        const T pn = ((T)P.gamma - (T)1) * nd * (E - (T)0.5 * (u * u + v * v + w * w));
+        const T Vn = u * nx + v * ny + w * nz;
+        const T dn = Vn - ve;
+        T dF[5];
+        dF[0] = nd * dn - fo[0];
+        dF[1] = (nmx * dn + pn * nx) - fo[1];
+        dF[2] = (nmy * dn + pn * ny) - fo[2];
+        dF[3] = (nmz * dn + pn * nz) - fo[3];
+        dF[4] = ((ne + pn) * dn + pn * ve) - fo[4];
+#pragma unroll
+        for (int c = 0; c < 5; c++) {
+            aw[c] = DIR > 0 ? (T)0.5 * (dF[c] * sd + rl * dqn[c]) : (T)0.5 * (dF[c] * sd - rl * dqn[c]);
+            vw[c] = lv * dqn[c];
         }
     }
     T a1[5], a2[5], v1[5], v2[5];
@@ -82,30 +109,41 @@ __global__ void __launch_bounds__(32) k_sweep(Batch B, Phys P, Geo G, Flow<T> W,
         v2[c] = __shfl_down_sync(0xffffffffu, vw[c], 2);
     }
     if (!active || d != 0) return;
-    const T relax = (T)P.relax;
-    const T alpha = (T)G.vol[p] / W.dt[p] + relax * (W.lamc[0][p] + W.lamc[1][p] + W.lamc[2][p]) +
-                    (T)2 * (W.lamv[0][p] + W.lamv[1][p] + W.lamv[2][p]);
 #pragma unroll
     for (int c = 0; c < 5; c++) {
         T r;
-        if (DIR > 0) r = -W.res[c][p] + aw[c] + a1[c] + a2[c] + vw[c] + v1[c] + v2[c];
+        if (DIR > 0) r = rhs[c] + aw[c] + a1[c] + a2[c] + vw[c] + v1[c] + v2[c];
         else r = alpha * W.dq[c][p] - aw[c] - a1[c] - a2[c] + vw[c] + v1[c] + v2[c];
-        W.dq[c][p] = r / alpha;
+        W.dq[c][p] = r * inva;
     }
+}
+
+template <typename T, int DIR>
+static void launch_plane(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const PlaneTables &pt, int pl,
+                         bool first)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(max(1, (pt.max_count[pl] + 9) / 10), ctx.batch.nsolve);
+    cfg.blockDim = dim3(32);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = ctx.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = first ? 0 : 1;     // the first plane of a sweep waits for everything before it
+    cudaLaunchKernelEx(&cfg, k_sweep<T, DIR>, ctx.batch, P, G, W, pt.pairs, pt.start, pt.stride, pl);
 }
 
 template <typename T>
 void launch_lusgs_sweeps(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const PlaneTables &pt)
 {
-    const Batch &B = ctx.batch;
     const int np = pt.max_plane;
     ctx.mark("sweep_forward", 1, np - 2);
-    for (int pl = 3; pl <= np; pl++)
-        k_sweep<T, 1><<<dim3(max(1, (pt.max_count[pl] + 9) / 10), B.nsolve), 32, 0, ctx.stream>>>(B, P, G, W, pt.pairs, pt.start, pt.stride, pl);
+    for (int pl = 3; pl <= np; pl++) launch_plane<T, 1>(ctx, P, G, W, pt, pl, pl == 3);
     ctx.mark("sweep_forward", 0, np - 2);
     ctx.mark("sweep_backward", 1, np - 2);
-    for (int pl = np; pl >= 3; pl--)
-        k_sweep<T, -1><<<dim3(max(1, (pt.max_count[pl] + 9) / 10), B.nsolve), 32, 0, ctx.stream>>>(B, P, G, W, pt.pairs, pt.start, pt.stride, pl);
+    for (int pl = np; pl >= 3; pl--) launch_plane<T, -1>(ctx, P, G, W, pt, pl, pl == np);
     ctx.mark("sweep_backward", 0, np - 2);
 }
 
@@ -345,15 +383,20 @@ void launch_res_norm(const LaunchCtx &ctx, const Geo &G, Flow<T> W, const double
     ctx.mark("res_norm", 0, 2);
 }
 
-// ---- inlet/outlet integrals (source/Ouput.cpp:9-107,282-300), one block per solve ----
+// ---- inlet/outlet integrals (source/Ouput.cpp:9-107,282-300) ----
+// partial sums over one section (inlet or outlet k face): mass flow, sum Pt^((g-1)/g) * m and
+// sum Tt * m; grid (kIntegralBlocks, solves, 2 sections), so the FP64 powers spread over the SMs
 template <typename T>
-__device__ void section_sums(const Phys &P, const Geo &G, const Flow<T> &W, const Lvl &L, int K, double out[3])
+__global__ void __launch_bounds__(128) k_section_partial(Batch B, Phys P, Geo G, Flow<T> W, const DevInOut *inl,
+                                                         const DevInOut *outl, double *part)
 {
-    // out: mass flow, sum Pt^((g-1)/g) * m, sum Tt * m (all over the same faces)
+    const int s = blockIdx.y, sec = blockIdx.z;
+    const Lvl L = B.lv[s];
+    const int K = sec == 0 ? inl[s].ks : outl[s].ks;
     const int nI = L.IM - 1, nJ = L.JM - 1;
     const double g = P.gamma, g1 = g - 1.0, R = P.rgas;
     double m = 0, pm = 0, tm = 0;
-    for (int t = threadIdx.x; t < nI * nJ; t += blockDim.x) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nI * nJ; t += kIntegralBlocks * blockDim.x) {
         const int i = 1 + t / nJ, j = 1 + t % nJ;
         const long long p = ix(L, i, j, K), q = ix(L, i, j, K - 1);
         const double d = 0.5 * ((double)W.pv[PD][p] + (double)W.pv[PD][q]);
@@ -369,7 +412,7 @@ __device__ void section_sums(const Phys &P, const Geo &G, const Flow<T> &W, cons
         pm += pow(Pt, g1 / g) * mc;
         tm += (double)W.pv[PT][p] * fac * mc;
     }
-    __shared__ double sh[3][32];
+    __shared__ double sh[3][4];
     double v3[3] = {m, pm, tm};
     for (int c = 0; c < 3; c++) {
         double v = v3[c];
@@ -377,23 +420,24 @@ __device__ void section_sums(const Phys &P, const Geo &G, const Flow<T> &W, cons
         if ((threadIdx.x & 31) == 0) sh[c][threadIdx.x >> 5] = v;
     }
     __syncthreads();
-    for (int c = 0; c < 3; c++) {
+    if (threadIdx.x < 3) {
         double v = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += sh[c][w];
-        out[c] = v;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += sh[threadIdx.x][w];
+        part[(((long long)s * 2 + sec) * kIntegralBlocks + blockIdx.x) * 3 + threadIdx.x] = v;
     }
-    __syncthreads();
 }
 
-template <typename T>
-__global__ void __launch_bounds__(1024) k_integrals(Batch B, Phys P, Geo G, Flow<T> W, const DevInOut *inl, const DevInOut *outl)
+// inlet/outlet integrals (source/Ouput.cpp:9-107,282-300): partials summed in block order
+__global__ void k_integrals(Batch B, Phys P, const double *part)
 {
-    const int s = blockIdx.x;
-    const Lvl L = B.lv[s];
-    double a[3], b[3];
-    section_sums(P, G, W, L, inl[s].ks, a);
-    section_sums(P, G, W, L, outl[s].ks, b);
-    if (threadIdx.x != 0) return;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= B.nsolve) return;
+    double a[3] = {0, 0, 0}, b[3] = {0, 0, 0};
+    for (int blk = 0; blk < kIntegralBlocks; blk++)
+        for (int c = 0; c < 3; c++) {
+            a[c] += part[(((long long)s * 2 + 0) * kIntegralBlocks + blk) * 3 + c];
+            b[c] += part[(((long long)s * 2 + 1) * kIntegralBlocks + blk) * 3 + c];
+        }
     const double g = P.gamma, g1 = g - 1.0, R = P.rgas;
     const double nbl = B.sc[s].nblade;
     const double mi = a[0] * P.dens_ref * P.vel_ref * nbl, mo = b[0] * P.dens_ref * P.vel_ref * nbl;
@@ -413,7 +457,10 @@ template <typename T>
 void launch_integrals(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const BcTables &bc)
 {
     // first inlet and first outlet patch of every solve (the reference reports Inlet[1], Outlet[1])
-    k_integrals<T><<<ctx.batch.nsolve, 1024, 0, ctx.stream>>>(ctx.batch, P, G, W, bc.inlet_first, bc.outlet_first);
+    const Batch &B = ctx.batch;
+    k_section_partial<T><<<dim3(kIntegralBlocks, B.nsolve, 2), 128, 0, ctx.stream>>>(B, P, G, W, bc.inlet_first,
+                                                                                      bc.outlet_first, bc.integ_part);
+    k_integrals<<<(B.nsolve + 31) / 32, 32, 0, ctx.stream>>>(B, P, bc.integ_part);
 }
 
 // CFL ramp of the driver (source/Solver.cpp:49-60): x1.2 whenever the density residual falls

@@ -41,13 +41,21 @@ __global__ void __launch_bounds__(256) k_cell_a(Batch B, Phys P, Geo G, Flow<T> 
     W.omega[p] = tsqrt(h * ((w_y - v_z) * (w_y - v_z) + (u_z - w_x) * (u_z - w_x) + (v_x - u_y) * (v_x - u_y)));
 }
 
-// One thread per wall-normal line of one wall patch. The line runs across the whole block from
-// the wall face; Baldwin-Lomax inner/outer viscosity (source/BL_Model.cpp:283-329), merged into
-// mu_t as the minimum over all walls whose lines cross the cell, wall-adjacent cell and its ghost
-// set to zero (source/BL_Model.cpp:101-119).
+// Baldwin-Lomax inner/outer viscosity (source/BL_Model.cpp:283-329) along the wall-normal lines
+// of one wall patch; each line runs across the whole block from the wall face. A block holds 32
+// lines on its lanes (the coalesced tangential index) and BL_WARPS warps that split the points
+// of every line; the line maxima go through shared memory. mu_t is merged as the minimum over
+// all walls whose lines cross the cell; the wall-adjacent cell and its ghost are set to zero
+// (source/BL_Model.cpp:101-119). The maxima keep the reference's first-occurrence rule (strict
+// ">" in line order), so the result does not depend on how the points are split.
+constexpr int BL_WARPS = 8;
+
 template <typename T>
-__global__ void __launch_bounds__(32) k_bl(Batch B, Phys P, Geo G, Flow<T> W, const DevWall *walls, int off)
+__global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, Phys P, Geo G, Flow<T> W, const DevWall *walls, int off)
 {
+    __shared__ T sh_a[BL_WARPS][32], sh_b[BL_WARPS][32], sh_u[BL_WARPS][32];
+    __shared__ int sh_n[BL_WARPS][32];
+    __shared__ T sh_d1[32], sh_m1[32], sh_ret[32], sh_ymax[32], sh_fwake[32];
     const DevWall wl = walls[off + blockIdx.y];
     const int s = wl.solve;
     const Lvl L = B.lv[s];
@@ -57,9 +65,11 @@ __global__ void __launch_bounds__(32) k_bl(Batch B, Phys P, Geo G, Flow<T> W, co
     else if (dirn == 1) { a0 = wl.ks; a1 = wl.ke; b0 = wl.is; b1 = wl.ie; }
     else { a0 = wl.js; a1 = wl.je; b0 = wl.is; b1 = wl.ie; }
     const int na = a1 - a0 + 1, nb = b1 - b0 + 1;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)na * nb) return;
-    const int a = a0 + (int)(t % na), b = b0 + (int)(t / na);
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const long long t = (long long)blockIdx.x * 32 + lane;
+    if ((long long)blockIdx.x * 32 >= (long long)na * nb) return;      // whole block past the patch
+    const bool live = t < (long long)na * nb;
+    const int a = a0 + (int)(live ? t % na : 0), b = b0 + (int)(live ? t / na : 0);
     const int N = dirn == 0 ? L.IM : (dirn == 1 ? L.JM : L.KM);
     const long long sn = dirn == 0 ? (long long)L.NJ * L.NK : (dirn == 1 ? (long long)L.NK : 1LL);
     long long p0;                        // cell n = 0 of the line; cell n is p0 + n*sn
@@ -67,50 +77,96 @@ __global__ void __launch_bounds__(32) k_bl(Batch B, Phys P, Geo G, Flow<T> W, co
     if (dirn == 0) { p0 = ix(L, 0, b, a); fw = ix(L, lo ? 1 : L.IM, b, a); }
     else if (dirn == 1) { p0 = ix(L, b, 0, a); fw = ix(L, b, lo ? 1 : L.JM, a); }
     else { p0 = ix(L, b, a, 0); fw = ix(L, b, a, lo ? 1 : L.KM); }
-    const double fx = G.c[dirn][0][fw], fy = G.c[dirn][1][fw], fz = G.c[dirn][2][fw];
-    // walk in the reference's line order n0 = 1..N-1 (n0 = 1 next to the wall)
+    double fx = 0, fy = 0, fz = 0;
+    if (live) { fx = G.c[dirn][0][fw]; fy = G.c[dirn][1][fw]; fz = G.c[dirn][2][fw]; }
+    // line order n0 = 1..N-1 (n0 = 1 next to the wall); warp wp takes n0 = 1 + wp, 1 + wp + BL_WARPS, ...
 #define CELL(n0) (p0 + (long long)(lo ? (n0) : N - (n0)) * sn)
-    T Tw = (T)0, dens1 = (T)0, mul1 = (T)1;
-    for (int n0 = 1; n0 < N; n0++) {
-        long long p = CELL(n0);
-        T ml = sutherland(P, W.pv[PT][p]);
-        T tw = tabs(W.omega[p] * ml);
-        if (n0 == 1) { Tw = tw; dens1 = W.pv[PD][p]; mul1 = ml; }
-        else if (tw > Tw) Tw = tw;
+    // pass 1: wall shear, taken as the largest |omega * mu_l| along the line
+    T tmax = (T)0;
+    bool any = false;
+    if (live) {
+        for (int n0 = 1 + wp; n0 < N; n0 += BL_WARPS) {
+            const long long p = CELL(n0);
+            const T ml = sutherland(P, W.pv[PT][p]);
+            const T tw = tabs(W.omega[p] * ml);
+            if (n0 == 1) { sh_d1[lane] = W.pv[PD][p]; sh_m1[lane] = ml; }     // first cell: density, mu_l
+            if (!any || tw > tmax) tmax = tw;
+            any = true;
+        }
     }
-    const T Ret = tsqrt(dens1 * Tw) / mul1;
+    sh_a[wp][lane] = tmax;
+    sh_n[wp][lane] = any;
+    __syncthreads();
+    if (wp == 0 && live) {
+        T Tw = (T)0;
+        bool got = false;
+        for (int w = 0; w < BL_WARPS; w++)
+            if (sh_n[w][lane] && (!got || sh_a[w][lane] > Tw)) { Tw = sh_a[w][lane]; got = true; }
+        sh_ret[lane] = tsqrt(sh_d1[lane] * Tw) / sh_m1[lane];
+    }
+    __syncthreads();
+    const T Ret = sh_ret[lane];
     const T Aplus = (T)26.0, kap = (T)(double)0.4f, Ckleb = (T)(double)0.3f;
     const T aCcp = (T)((double)0.0168f * (double)1.6f);
+    // pass 2: largest speed, and F = y |omega| (1 - exp(-y+/A+)) with its first maximiser
     T Fmax = (T)0, ymax = (T)0, Udif = (T)0;
-    for (int n0 = 1; n0 < N; n0++) {
-        long long p = CELL(n0);
-        T dx = (T)(G.cc[0][p] - fx), dy = (T)(G.cc[1][p] - fy), dz = (T)(G.cc[2][p] - fz);
-        T dis = tsqrt(dx * dx + dy * dy + dz * dz);
-        T u = W.pv[PU][p], v = W.pv[PV][p], w = W.pv[PW][p];
-        T V = tsqrt(u * u + v * v + w * w);
-        if (V > Udif) Udif = V;
-        T F = dis * tabs(W.omega[p]) * ((T)1 - exp(-(dis * Ret) / Aplus));
-        if (F > Fmax) { Fmax = F; ymax = dis; }
+    int nmax = 0x7fffffff;
+    if (live) {
+        for (int n0 = 1 + wp; n0 < N; n0 += BL_WARPS) {
+            const long long p = CELL(n0);
+            const T dx = (T)(G.cc[0][p] - fx), dy = (T)(G.cc[1][p] - fy), dz = (T)(G.cc[2][p] - fz);
+            const T dis = tsqrt(dx * dx + dy * dy + dz * dz);
+            const T u = W.pv[PU][p], v = W.pv[PV][p], w = W.pv[PW][p];
+            const T V = tsqrt(u * u + v * v + w * w);
+            if (V > Udif) Udif = V;
+            const T F = dis * tabs(W.omega[p]) * ((T)1 - exp(-(dis * Ret) / Aplus));
+            if (F > Fmax) { Fmax = F; ymax = dis; nmax = n0; }
+        }
     }
-    T q = ymax * Udif * Udif / Fmax;
-    T Fwake = (ymax * Fmax < q) ? ymax * Fmax : q;
-    for (int n0 = 1; n0 < N; n0++) {
-        long long p = CELL(n0);
-        T dx = (T)(G.cc[0][p] - fx), dy = (T)(G.cc[1][p] - fy), dz = (T)(G.cc[2][p] - fz);
-        T dis = tsqrt(dx * dx + dy * dy + dz * dz);
-        T bL = kap * dis * ((T)1 - exp(-(Ret * dis) / Aplus));
-        T om = W.omega[p], rho = W.pv[PD][p];
-        T m_in = rho * bL * bL * om;
-        T r = Ckleb * dis / ymax;
-        T r2 = r * r;
-        T Fk = (T)1 / ((T)1 + (T)5.5 * (r2 * r2 * r2));
-        T m_out = aCcp * rho * Fwake * Fk;
-        T mt = (tabs(m_in) > tabs(m_out)) ? m_out : m_in;
+    __syncthreads();
+    sh_a[wp][lane] = Fmax;
+    sh_b[wp][lane] = ymax;
+    sh_n[wp][lane] = nmax;
+    sh_u[wp][lane] = Udif;
+    __syncthreads();
+    if (wp == 0 && live) {
+        T F = (T)0, y = (T)0, U = (T)0;
+        int n = 0x7fffffff;
+        for (int w = 0; w < BL_WARPS; w++) {
+            if (sh_u[w][lane] > U) U = sh_u[w][lane];
+            const T f = sh_a[w][lane];
+            const int m = sh_n[w][lane];
+            if (f > F || (f == F && m < n && f > (T)0)) { F = f; y = sh_b[w][lane]; n = m; }
+        }
+        const T q = y * U * U / F;
+        sh_ymax[lane] = y;
+        sh_fwake[lane] = (y * F < q) ? y * F : q;
+    }
+    __syncthreads();
+    if (!live) return;
+    const T ym = sh_ymax[lane], Fwake = sh_fwake[lane];
+    // pass 3: inner and outer viscosity, the smaller one merged into mu_t
+    for (int n0 = 1 + wp; n0 < N; n0 += BL_WARPS) {
+        const long long p = CELL(n0);
+        const T dx = (T)(G.cc[0][p] - fx), dy = (T)(G.cc[1][p] - fy), dz = (T)(G.cc[2][p] - fz);
+        const T dis = tsqrt(dx * dx + dy * dy + dz * dz);
+        const T bL = kap * dis * ((T)1 - exp(-(Ret * dis) / Aplus));
+        const T om = W.omega[p], rho = W.pv[PD][p];
+        const T m_in = rho * bL * bL * om;
+        const T r = Ckleb * dis / ym;
+        const T r2 = r * r;
+        const T Fk = (T)1 / ((T)1 + (T)5.5 * (r2 * r2 * r2));
+        const T m_out = aCcp * rho * Fwake * Fk;
+        const T mt = (tabs(m_in) > tabs(m_out)) ? m_out : m_in;
+        if (n0 == 1) {
+            W.mut[p] = (T)0;                                   // wall-adjacent cell
+            W.mut[p0 + (long long)(lo ? 0 : N) * sn] = (T)0;   // its ghost
+            W.flag[p] = 1;
+            continue;
+        }
         if (W.flag[p] == 0) { W.flag[p] = 1; W.mut[p] = mt; }
-        else { T old = W.mut[p]; W.mut[p] = (old < mt) ? old : mt; }
+        else { const T old = W.mut[p]; W.mut[p] = (old < mt) ? old : mt; }
     }
-    W.mut[CELL(1)] = (T)0;
-    W.mut[p0 + (long long)(lo ? 0 : N) * sn] = (T)0;
 #undef CELL
 }
 
@@ -219,9 +275,9 @@ void launch_cell_stages(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<
         for (int q = 0; q < bc.n_wall_slot; q++) {
             int n = bc.wall_slot_off[q + 1] - bc.wall_slot_off[q];
             if (n <= 0) continue;
-            // one warp per block: the lines of a wall spread over every SM (FP64 throughput per SM is low)
+            // 32 lines per block, the points of each line split over BL_WARPS warps
             dim3 g((unsigned)((bc.wall_slot_lines[q] + 31) / 32), n);
-            k_bl<T><<<g, 32, 0, ctx.stream>>>(B, P, G, W, bc.wall, bc.wall_slot_off[q]);
+            k_bl<T><<<g, 32 * BL_WARPS, 0, ctx.stream>>>(B, P, G, W, bc.wall, bc.wall_slot_off[q]);
         }
     }
     if (bc.n_wall > 0) {

@@ -205,9 +205,10 @@ template <typename T>
 void launch_resflux(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const BcTables &bc, int level,
                     T *scratch)
 {
-    ctx.mark("boundary", 1);
+    const int nbc = (bc.n_inlet > 0) + 3 * (bc.n_outlet > 0) + (bc.n_wall > 0) + (bc.n_per > 0);
+    ctx.mark("boundary", 1, nbc);
     launch_boundary<T>(ctx, P, G, W, bc);
-    ctx.mark("boundary", 0);
+    ctx.mark("boundary", 0, nbc);
     launch_cell_stages<T>(ctx, P, G, W, bc, level, scratch);
     const Batch &B = ctx.batch;
     ctx.mark("face_flux", 1, 3);

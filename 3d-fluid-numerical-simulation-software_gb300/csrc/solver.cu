@@ -488,6 +488,7 @@ public:
             inl1.push_back(inl[inl.size() - c.in.size()]);
             outl1.push_back(outl.back());
             bc.max_outlet_im = std::max(bc.max_outlet_im, c.IM);
+            bc.max_outlet_jm = std::max(bc.max_outlet_jm, c.JM);
         }
         // walls ordered by their position in each case's list, then by solve
         bc.n_wall_slot = (int)max_walls;
@@ -570,7 +571,8 @@ public:
         auto bytes = [](size_t n, size_t sz) { return (n * sz + 255) & ~(size_t)255; };
         size_t tot = bytes(inl.size(), sizeof(DevInOut)) + bytes(outl.size(), sizeof(DevInOut)) + bytes(inl1.size(), sizeof(DevInOut)) +
                      bytes(outl1.size(), sizeof(DevInOut)) + bytes(walls.size(), sizeof(DevWall)) + bytes(pdst.size(), 8) * 2 +
-                     bytes(pmeta.size(), 4) + 256;
+                     bytes(pmeta.size(), 4) + bytes(outl.size() * (size_t)(bc.max_outlet_im + 1), 8) +
+                     bytes((size_t)nsolve * 2 * kIntegralBlocks * 3, 8) + 256;
         CK(cudaMalloc(&Lv.tab_mem.p, tot));
         char *q = (char *)Lv.tab_mem.p;
         auto up = [&](const void *h, size_t n, size_t sz) {
@@ -588,6 +590,8 @@ public:
         bc.per_src = (const long long *)up(psrc.data(), psrc.size(), 8);
         bc.per_meta = (const int *)up(pmeta.data(), pmeta.size(), 4);
         bc.n_per = (long long)pdst.size();
+        bc.outlet_cu = (double *)up(nullptr, 0, 8); q += bytes(outl.size() * (size_t)(bc.max_outlet_im + 1), 8);
+        bc.integ_part = (double *)up(nullptr, 0, 8); q += bytes((size_t)nsolve * 2 * kIntegralBlocks * 3, 8);
         for (int f = 0; f < 3; f++)
             CK(cudaMemcpy((void *)Lv.W.wallf[f], wallf[f].data(), sizeof(int) * (size_t)Lv.pool_n, cudaMemcpyHostToDevice));
         Lv.walls_h = walls;
@@ -650,7 +654,7 @@ public:
         launch_interpolate<T>(ctx(1), ctx(2), lev[1].W, lev[2].W, init);
     }
     void delta_cons() override { need_mg(); Mark m(this, "mg_delta"); launch_delta<T>(ctx(2), lev[2].W); }
-    void integrals(int l) override { Mark m(this, "integrals"); launch_integrals<T>(ctx(l), P, lev[l].G, lev[l].W, lev[l].bc); }
+    void integrals(int l) override { Mark m(this, "integrals", 2); launch_integrals<T>(ctx(l), P, lev[l].G, lev[l].W, lev[l].bc); }
     void set_use_force(int l, bool on) override { lev[l].use_force = on; }
     void need_mg() const { if (ng < 2) throw std::runtime_error("the case runs on a single grid level"); }
 
