@@ -21,7 +21,7 @@ __device__ __forceinline__ void st_state(Flow<T> &W, long long g, const double c
 
 // inlet: Riemann invariant from the interior, total pressure/temperature and flow direction
 template <typename T>
-__global__ void k_bc_inlet(Batch B, Phys P, Geo G, Flow<T> W, const DevInOut *pat)
+__global__ void __launch_bounds__(32) k_bc_inlet(Batch B, Phys P, Geo G, Flow<T> W, const DevInOut *pat)
 {
     const DevInOut pt = pat[blockIdx.y];
     const Lvl L = B.lv[pt.solve];
@@ -106,17 +106,18 @@ __global__ void __launch_bounds__(32) k_outlet_march(Batch B, Geo G, Flow<T> W, 
     const double pout = B.sc[pt.solve].pout;
     double pr = pout;
     W.pv[PP][ix(L, iref, j, KM)] = (T)pr;
+    // read-only loads (__ldg) so that they are not ordered behind the pressure stores
     for (int i = iref - 1; i >= 1; i--) {
-        const double rn = G.r[2][ix(L, i, j, KM)], rn1 = G.r[2][ix(L, i + 1, j, KM)];
-        const double dpdr = W.cv[0][ix(L, i, j, KM)] * cu[i] * cu[i] / rn;
+        const double rn = __ldg(&G.r[2][ix(L, i, j, KM)]), rn1 = __ldg(&G.r[2][ix(L, i + 1, j, KM)]);
+        const double dpdr = __ldg(&W.cv[0][ix(L, i, j, KM)]) * __ldg(&cu[i]) * __ldg(&cu[i]) / rn;
         pr = pr - dpdr * (rn1 - rn);
         W.pv[PP][ix(L, i, j, KM)] = (T)pr;
     }
     pr = pout;
     for (int i = iref + 1; i <= IM - 1; i++) {
         // radii of the k = KM-1 face row here, as the reference takes them
-        const double rn1 = G.r[2][ix(L, i, j, KM - 1)], rn = G.r[2][ix(L, i - 1, j, KM - 1)];
-        const double dpdr = W.cv[0][ix(L, i, j, KM)] * cu[i] * cu[i] / rn;
+        const double rn1 = __ldg(&G.r[2][ix(L, i, j, KM - 1)]), rn = __ldg(&G.r[2][ix(L, i - 1, j, KM - 1)]);
+        const double dpdr = __ldg(&W.cv[0][ix(L, i, j, KM)]) * __ldg(&cu[i]) * __ldg(&cu[i]) / rn;
         pr = pr + dpdr * (rn1 - rn);
         W.pv[PP][ix(L, i, j, KM)] = (T)pr;
     }
@@ -212,7 +213,8 @@ template <typename T>
 void launch_boundary(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const BcTables &bc)
 {
     const Batch &B = ctx.batch;
-    if (bc.n_inlet) k_bc_inlet<T><<<dim3((bc.max_inlet + 127) / 128, bc.n_inlet), 128, 0, ctx.stream>>>(B, P, G, W, bc.inlet);
+    // 32-thread blocks: the FP64 powers and roots of the inlet state spread over many SMs
+    if (bc.n_inlet) k_bc_inlet<T><<<dim3((bc.max_inlet + 31) / 32, bc.n_inlet), 32, 0, ctx.stream>>>(B, P, G, W, bc.inlet);
     if (bc.n_outlet) {
         const int cs = bc.max_outlet_im + 1;
         k_outlet_swirl<T><<<dim3((bc.max_outlet_im + 7) / 8, bc.n_outlet), 256, 0, ctx.stream>>>(B, G, W, bc.outlet, bc.outlet_cu, cs);

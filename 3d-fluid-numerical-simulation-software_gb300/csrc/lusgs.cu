@@ -11,9 +11,11 @@
 
 namespace gbt {
 
-// Programmatic dependent launch: each plane's kernel is launched while the previous plane's is
-// still running; it reads everything the sweep does not write (indices, geometry, Q, spectral
-// radii, residual) first, then waits for the previous plane's grid to finish before it reads dQ.
+// Programmatic dependent launch: every plane's kernel lets the next plane's kernel start as soon
+// as all of its own blocks are resident, so the kernels of many planes are in flight at once; each
+// reads everything the sweep does not write (indices, geometry, Q, spectral radii, residual)
+// first, then waits for the previous plane's grid to finish before it reads dQ. The resident set
+// is always a prefix of the plane sequence, so the oldest resident plane can always finish.
 __device__ __forceinline__ void wait_previous_plane() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void release_next_plane() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
@@ -27,6 +29,7 @@ template <typename T, int DIR>      // DIR = +1 forward (lower neighbours), -1 b
 __global__ void __launch_bounds__(32) k_sweep(Batch B, Phys P, Geo G, Flow<T> W, const int *__restrict__ pairs,
                                               const int *__restrict__ pstart, int pstride, int plane)
 {
+    release_next_plane();
     const int lane = threadIdx.x, slot = lane / 3, d = lane - 3 * slot;
     const int s = blockIdx.y;
     const Lvl L = B.lv[s];
@@ -75,7 +78,11 @@ __global__ void __launch_bounds__(32) k_sweep(Batch B, Phys P, Geo G, Flow<T> W,
         }
     }
     wait_previous_plane();
-    release_next_plane();
+    T dqp[5];                            // backward sweep: this cell's forward-sweep dQ
+    if (DIR < 0 && active && d == 0) {
+#pragma unroll
+        for (int c = 0; c < 5; c++) dqp[c] = W.dq[c][p];
+    }
     T aw[5] = {(T)0, (T)0, (T)0, (T)0, (T)0}, vw[5] = {(T)0, (T)0, (T)0, (T)0, (T)0};
     if (has) {
         T dqn[5];
@@ -113,7 +120,7 @@ __global__ void __launch_bounds__(32) k_sweep(Batch B, Phys P, Geo G, Flow<T> W,
     for (int c = 0; c < 5; c++) {
         T r;
         if (DIR > 0) r = rhs[c] + aw[c] + a1[c] + a2[c] + vw[c] + v1[c] + v2[c];
-        else r = alpha * W.dq[c][p] - aw[c] - a1[c] - a2[c] + vw[c] + v1[c] + v2[c];
+        else r = alpha * dqp[c] - aw[c] - a1[c] - a2[c] + vw[c] + v1[c] + v2[c];
         W.dq[c][p] = r * inva;
     }
 }

@@ -4,6 +4,7 @@
 // corner fill of the coarse ghosts, trilinear 27/9/3/1 prolongation.
 #include "gbt_common.cuh"
 #include "kernels.hpp"
+#include <algorithm>
 
 namespace gbt {
 
@@ -59,49 +60,59 @@ __global__ void __launch_bounds__(256) k_delta(Batch B, Flow<T> W)
     for (int c = 0; c < NQ; c++) W.dq2h[c][p] = (T)(W.cv[c][p] - W.cv2h[c][p]);
 }
 
-// 12 edges then 8 corners of the ghost layer, for Q and for the coarse correction; one block per
-// solve (edges first, then corners that read them)
+// 12 edges then 8 corners of the ghost layer, for Q and for the coarse correction
+// (source/Corner_Treatment.cpp): edges in one launch (one thread per edge cell, all values read
+// before any is written), then the corners, which read the edges, in a second one
 template <typename T>
-__global__ void k_corner(Batch B, Flow<T> W)
+__global__ void __launch_bounds__(64) k_edges(Batch B, Flow<T> W)
+{
+    const Lvl L = B.lv[blockIdx.z];
+    const int IM = L.IM, JM = L.JM, KM = L.KM;
+    const int e = blockIdx.y, n = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    long long dst, a, b;
+    switch (e) {
+    case 0: if (n > IM - 1) return; dst = ix(L, n, 0, 0); a = ix(L, n, 1, 0); b = ix(L, n, 0, 1); break;
+    case 1: if (n > IM - 1) return; dst = ix(L, n, JM, 0); a = ix(L, n, JM - 1, 0); b = ix(L, n, JM, 1); break;
+    case 2: if (n > IM - 1) return; dst = ix(L, n, 0, KM); a = ix(L, n, 0, KM - 1); b = ix(L, n, 1, KM); break;
+    case 3: if (n > IM - 1) return; dst = ix(L, n, JM, KM); a = ix(L, n, JM - 1, KM); b = ix(L, n, JM, KM - 1); break;
+    case 4: if (n > JM - 1) return; dst = ix(L, 0, n, 0); a = ix(L, 1, n, 0); b = ix(L, 0, n, 1); break;
+    case 5: if (n > JM - 1) return; dst = ix(L, 0, n, KM); a = ix(L, 1, n, KM); b = ix(L, 0, n, KM - 1); break;
+    case 6: if (n > JM - 1) return; dst = ix(L, IM, n, KM); a = ix(L, IM - 1, n, KM); b = ix(L, IM, n, KM - 1); break;
+    case 7: if (n > JM - 1) return; dst = ix(L, IM, n, 0); a = ix(L, IM - 1, n, 0); b = ix(L, IM, n, 1); break;
+    case 8: if (n > KM - 1) return; dst = ix(L, 0, 0, n); a = ix(L, 1, 0, n); b = ix(L, 0, 1, n); break;
+    case 9: if (n > KM - 1) return; dst = ix(L, IM, 0, n); a = ix(L, IM, 1, n); b = ix(L, IM - 1, 0, n); break;
+    case 10: if (n > KM - 1) return; dst = ix(L, 0, JM, n); a = ix(L, 1, JM, n); b = ix(L, 0, JM - 1, n); break;
+    default: if (n > KM - 1) return; dst = ix(L, IM, JM, n); a = ix(L, IM - 1, JM, n); b = ix(L, IM, JM - 1, n); break;
+    }
+    double qa[NQ], qb[NQ];
+    T da[NQ], db[NQ];
+#pragma unroll
+    for (int c = 0; c < NQ; c++) { qa[c] = W.cv[c][a]; qb[c] = W.cv[c][b]; da[c] = W.dq2h[c][a]; db[c] = W.dq2h[c][b]; }
+#pragma unroll
+    for (int c = 0; c < NQ; c++) {
+        W.cv[c][dst] = 0.5 * (qa[c] + qb[c]);
+        W.dq2h[c][dst] = (T)0.5 * (da[c] + db[c]);
+    }
+}
+
+// corner (ci,cj,ck) from its three edge neighbours and three face-diagonal neighbours; thread
+// corner * NQ + c of the block of its solve
+template <typename T>
+__global__ void __launch_bounds__(64) k_corners(Batch B, Flow<T> W)
 {
     const Lvl L = B.lv[blockIdx.x];
     const int IM = L.IM, JM = L.JM, KM = L.KM;
-    auto edge = [&](long long dst, long long a, long long b) {
-        for (int c = 0; c < NQ; c++) {
-            W.cv[c][dst] = 0.5 * (W.cv[c][a] + W.cv[c][b]);
-            W.dq2h[c][dst] = (T)0.5 * (W.dq2h[c][a] + W.dq2h[c][b]);
-        }
-    };
-    for (int i = 1 + threadIdx.x; i <= IM - 1; i += blockDim.x) {
-        edge(ix(L, i, 0, 0), ix(L, i, 1, 0), ix(L, i, 0, 1));
-        edge(ix(L, i, JM, 0), ix(L, i, JM - 1, 0), ix(L, i, JM, 1));
-        edge(ix(L, i, 0, KM), ix(L, i, 0, KM - 1), ix(L, i, 1, KM));
-        edge(ix(L, i, JM, KM), ix(L, i, JM - 1, KM), ix(L, i, JM, KM - 1));
-    }
-    for (int j = 1 + threadIdx.x; j <= JM - 1; j += blockDim.x) {
-        edge(ix(L, 0, j, 0), ix(L, 1, j, 0), ix(L, 0, j, 1));
-        edge(ix(L, 0, j, KM), ix(L, 1, j, KM), ix(L, 0, j, KM - 1));
-        edge(ix(L, IM, j, KM), ix(L, IM - 1, j, KM), ix(L, IM, j, KM - 1));
-        edge(ix(L, IM, j, 0), ix(L, IM - 1, j, 0), ix(L, IM, j, 1));
-    }
-    for (int k = 1 + threadIdx.x; k <= KM - 1; k += blockDim.x) {
-        edge(ix(L, 0, 0, k), ix(L, 1, 0, k), ix(L, 0, 1, k));
-        edge(ix(L, IM, 0, k), ix(L, IM, 1, k), ix(L, IM - 1, 0, k));
-        edge(ix(L, 0, JM, k), ix(L, 1, JM, k), ix(L, 0, JM - 1, k));
-        edge(ix(L, IM, JM, k), ix(L, IM - 1, JM, k), ix(L, IM, JM - 1, k));
-    }
-    __syncthreads();
-    if (threadIdx.x >= 8) return;
-    // corner (ci,cj,ck) from its three edge neighbours and three face-diagonal neighbours
-    const int ci = (threadIdx.x & 1) ? IM : 0, cj = (threadIdx.x & 2) ? JM : 0, ck = (threadIdx.x & 4) ? KM : 0;
+    if (threadIdx.x >= 8 * NQ) return;
+    const int corner = threadIdx.x / NQ, c = threadIdx.x % NQ;
+    const int ci = (corner & 1) ? IM : 0, cj = (corner & 2) ? JM : 0, ck = (corner & 4) ? KM : 0;
     const int i1 = ci ? IM - 1 : 1, j1 = cj ? JM - 1 : 1, k1 = ck ? KM - 1 : 1;
     const long long e1 = ix(L, i1, cj, ck), e2 = ix(L, ci, j1, ck), e3 = ix(L, ci, cj, k1);
     const long long d1 = ix(L, i1, j1, ck), d2 = ix(L, i1, cj, k1), d3 = ix(L, ci, j1, k1);
     const long long dst = ix(L, ci, cj, ck);
-    for (int c = 0; c < NQ; c++) {
-        W.cv[c][dst] = (2.0 * (W.cv[c][e1] + W.cv[c][e2] + W.cv[c][e3]) - (W.cv[c][d1] + W.cv[c][d2] + W.cv[c][d3])) / 3.0;
-        W.dq2h[c][dst] = ((T)2 * (W.dq2h[c][e1] + W.dq2h[c][e2] + W.dq2h[c][e3]) - (W.dq2h[c][d1] + W.dq2h[c][d2] + W.dq2h[c][d3])) / (T)3;
-    }
+    const double q = (2.0 * (W.cv[c][e1] + W.cv[c][e2] + W.cv[c][e3]) - (W.cv[c][d1] + W.cv[c][d2] + W.cv[c][d3])) / 3.0;
+    const T d = ((T)2 * (W.dq2h[c][e1] + W.dq2h[c][e2] + W.dq2h[c][e3]) - (W.dq2h[c][d1] + W.dq2h[c][d2] + W.dq2h[c][d3])) / (T)3;
+    W.cv[c][dst] = q;
+    W.dq2h[c][dst] = d;
 }
 
 // fine Q (+)= sum of 27/64, 9/64, 3/64, 1/64 weighted coarse values around the fine cell; the
@@ -157,7 +168,9 @@ void launch_delta(const LaunchCtx &cc, Flow<T> Fc)
 template <typename T>
 void launch_corner(const LaunchCtx &cc, Flow<T> Fc)
 {
-    k_corner<T><<<cc.batch.nsolve, 256, 0, cc.stream>>>(cc.batch, Fc);
+    const int mx = std::max(cc.maxIM, std::max(cc.maxJM, cc.maxKM));
+    k_edges<T><<<dim3((mx + 63) / 64, 12, cc.batch.nsolve), 64, 0, cc.stream>>>(cc.batch, Fc);
+    k_corners<T><<<cc.batch.nsolve, 64, 0, cc.stream>>>(cc.batch, Fc);
 }
 template <typename T>
 void launch_interpolate(const LaunchCtx &cf, const LaunchCtx &cc, Flow<T> Ff, Flow<T> Fc, int init)

@@ -58,9 +58,9 @@ cudaError_t scratch_for_current_device(double **out)
     return cudaSuccess;
 }
 
-// One launch per call: every block folds its share of the cells exactly as the two-stage norm
-// does (same strided order, same warp tree), the last block of each solve to arrive adds the 64
-// partials in block order, so the result equals the two-launch norm bit for bit.
+// One launch per call: every block folds a strided share of the cells (the same per-cell terms as
+// the two-launch norm), the last block of each solve to arrive adds the 64 partials in block
+// order. The two-launch norm uses more blocks, so the two agree to rounding, not bit for bit.
 template <typename T>
 __global__ void __launch_bounds__(256) k_norm_onepass(Batch B, Geo G, Flow<T> W, const double *__restrict__ totalvol,
                                                       double *partials, double *norms, unsigned *arrivals)

@@ -185,7 +185,7 @@ public:
     int *bad_list = nullptr, *bad_count = nullptr;
     const int bad_cap = 4096;
     double *norm_part = nullptr;
-    const int norm_blk = 64;
+    const int norm_blk = 304;            // two blocks per SM: the FP64 divisions spread over all SMs
     T *dtmin = nullptr;
     cudaGraphExec_t graphs[3] = {nullptr, nullptr, nullptr};
 
@@ -640,7 +640,7 @@ public:
     }
     void primitive_vars(int l) override { Mark m(this, "primitive"); launch_primitive<T>(ctx(l), P, lev[l].W); }
     void limit_vars(int l) override { Mark m(this, "limiter", 2); launch_limiter<T>(ctx(l), P, lev[l].W, l, bad_list, bad_cap, bad_count); }
-    void corner_treatment(int l) override { Mark m(this, "mg_corner"); launch_corner<T>(ctx(l), lev[l].W); }
+    void corner_treatment(int l) override { Mark m(this, "mg_corner", 2); launch_corner<T>(ctx(l), lev[l].W); }
     void restrict_to_coarse() override
     {
         need_mg();
