@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(32) k_bc_inlet(Batch B, Phys P, Geo G, Flow<T>
 
 // axial outlet in three launches spread over the SMs: mass-weighted swirl per radial row (one
 // warp per row, lanes over the pitch), radial equilibrium marched from p_out at i = IM/2 using
-// the previous ghost density (one thread per pitch line), then ghosts extrapolated from the last
+// the previous ghost density (one warp per pitch line), then ghosts extrapolated from the last
 // interior layer (one thread per face)
 template <typename T>
 __global__ void __launch_bounds__(256) k_outlet_swirl(Batch B, Geo G, Flow<T> W, const DevInOut *pat, double *cu_all,
@@ -92,6 +92,10 @@ __global__ void __launch_bounds__(256) k_outlet_swirl(Batch B, Geo G, Flow<T> W,
     if (lane == 0) cu_all[(long long)blockIdx.y * cu_stride + i] = acc / sa;
 }
 
+// The march p_i = p_(i+1) - t_i (towards the hub) and p_i = p_(i-1) + u_i (towards the casing)
+// has increments that do not depend on p, so one warp per pitch line forms them for 32 radial
+// rows at a time and adds them up with a warp scan (a different association of the same sums
+// than the reference's running total).
 template <typename T>
 __global__ void __launch_bounds__(32) k_outlet_march(Batch B, Geo G, Flow<T> W, const DevInOut *pat, const double *cu_all,
                                                      int cu_stride)
@@ -99,27 +103,45 @@ __global__ void __launch_bounds__(32) k_outlet_march(Batch B, Geo G, Flow<T> W, 
     const DevInOut pt = pat[blockIdx.y];
     const Lvl L = B.lv[pt.solve];
     const int IM = L.IM, KM = L.KM;
-    const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.x, lane = threadIdx.x;
     if (j > L.JM - 1) return;
     const double *cu = cu_all + (long long)blockIdx.y * cu_stride;
     const int iref = (int)(0.5 * IM);
     const double pout = B.sc[pt.solve].pout;
-    double pr = pout;
-    W.pv[PP][ix(L, iref, j, KM)] = (T)pr;
-    // read-only loads (__ldg) so that they are not ordered behind the pressure stores
-    for (int i = iref - 1; i >= 1; i--) {
-        const double rn = __ldg(&G.r[2][ix(L, i, j, KM)]), rn1 = __ldg(&G.r[2][ix(L, i + 1, j, KM)]);
-        const double dpdr = __ldg(&W.cv[0][ix(L, i, j, KM)]) * __ldg(&cu[i]) * __ldg(&cu[i]) / rn;
-        pr = pr - dpdr * (rn1 - rn);
-        W.pv[PP][ix(L, i, j, KM)] = (T)pr;
+    if (lane == 0) W.pv[PP][ix(L, iref, j, KM)] = (T)pout;
+    // towards the hub: i = iref-1, iref-2, ..., 1
+    double carry = 0.0;
+    for (int base = 0; base < iref - 1; base += 32) {
+        const int i = iref - 1 - base - lane;
+        double t = 0.0;
+        if (i >= 1) {
+            const double rn = G.r[2][ix(L, i, j, KM)], rn1 = G.r[2][ix(L, i + 1, j, KM)];
+            const double dpdr = W.cv[0][ix(L, i, j, KM)] * cu[i] * cu[i] / rn;
+            t = dpdr * (rn1 - rn);
+        }
+        for (int o = 1; o < 32; o <<= 1) {
+            const double v = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += v;
+        }
+        if (i >= 1) W.pv[PP][ix(L, i, j, KM)] = (T)(pout - (carry + t));
+        carry += __shfl_sync(0xffffffffu, t, 31);
     }
-    pr = pout;
-    for (int i = iref + 1; i <= IM - 1; i++) {
-        // radii of the k = KM-1 face row here, as the reference takes them
-        const double rn1 = __ldg(&G.r[2][ix(L, i, j, KM - 1)]), rn = __ldg(&G.r[2][ix(L, i - 1, j, KM - 1)]);
-        const double dpdr = __ldg(&W.cv[0][ix(L, i, j, KM)]) * __ldg(&cu[i]) * __ldg(&cu[i]) / rn;
-        pr = pr + dpdr * (rn1 - rn);
-        W.pv[PP][ix(L, i, j, KM)] = (T)pr;
+    // towards the casing: i = iref+1, ..., IM-1, radii of the k = KM-1 face row as the reference takes them
+    carry = 0.0;
+    for (int base = 0; base < IM - 1 - iref; base += 32) {
+        const int i = iref + 1 + base + lane;
+        double u = 0.0;
+        if (i <= IM - 1) {
+            const double rn1 = G.r[2][ix(L, i, j, KM - 1)], rn = G.r[2][ix(L, i - 1, j, KM - 1)];
+            const double dpdr = W.cv[0][ix(L, i, j, KM)] * cu[i] * cu[i] / rn;
+            u = dpdr * (rn1 - rn);
+        }
+        for (int o = 1; o < 32; o <<= 1) {
+            const double v = __shfl_up_sync(0xffffffffu, u, o);
+            if (lane >= o) u += v;
+        }
+        if (i <= IM - 1) W.pv[PP][ix(L, i, j, KM)] = (T)(pout + (carry + u));
+        carry += __shfl_sync(0xffffffffu, u, 31);
     }
 }
 
@@ -218,7 +240,7 @@ void launch_boundary(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> 
     if (bc.n_outlet) {
         const int cs = bc.max_outlet_im + 1;
         k_outlet_swirl<T><<<dim3((bc.max_outlet_im + 7) / 8, bc.n_outlet), 256, 0, ctx.stream>>>(B, G, W, bc.outlet, bc.outlet_cu, cs);
-        k_outlet_march<T><<<dim3((bc.max_outlet_jm + 31) / 32, bc.n_outlet), 32, 0, ctx.stream>>>(B, G, W, bc.outlet, bc.outlet_cu, cs);
+        k_outlet_march<T><<<dim3(bc.max_outlet_jm, bc.n_outlet), 32, 0, ctx.stream>>>(B, G, W, bc.outlet, bc.outlet_cu, cs);
         k_outlet_fill<T><<<dim3((bc.max_outlet_im * bc.max_outlet_jm + 255) / 256, bc.n_outlet), 256, 0, ctx.stream>>>(B, P, W, bc.outlet);
     }
     if (bc.n_wall) k_bc_wall<T><<<dim3((bc.max_wall + 127) / 128, bc.n_wall), 128, 0, ctx.stream>>>(B, P, G, W, bc.wall);

@@ -42,11 +42,13 @@ def parse():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=1, help="operating points per GPU")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the secondary measurements of the mixed-precision and batched forms")
     return ap.parse_args()
 
 
 def make_cases(root: str, n: int, seed_offset: int = 0):
-    """configs[1] passage; in a batch the back pressure varies over [1.05, 1.30] x p_t"""
+    """the 129 x 49 x 49 rotor passage; in a batch the back pressure varies over [1.05, 1.30] x p_t"""
     import meshgen as mg
     dirs = []
     for q in range(n):
@@ -74,12 +76,21 @@ ALG = {
 }
 
 
-def alg_bytes_per_launch(stage, cells, planes, wsize, launches_per_call):
+def alg_units_per_step(stage, level_dims):
+    """units of ALG[stage] processed in one multigrid cycle: each level's residual and sweeps run
+    once per cycle; level_dims holds the (IM, JM, KM) node counts of every level of every solve"""
+    n = 0
+    for I, J, K in level_dims:
+        if ALG[stage]["unit"] == "face":
+            n += I * (J - 1) * (K - 1) + (I - 1) * J * (K - 1) + (I - 1) * (J - 1) * K
+        else:
+            n += (I - 1) * (J - 1) * (K - 1)
+    return n
+
+
+def alg_bytes_per_unit(stage, wsize):
     a = ALG[stage]
-    per_unit = 8 * a["geo"] + 8 * a["cv"] + wsize * a["w"] + 4 * a["int"]
-    if a["unit"] == "plane_cell":
-        return per_unit * cells / planes
-    return per_unit * cells        # one launch per face family, ~cells faces each
+    return 8 * a["geo"] + 8 * a["cv"] + wsize * a["w"] + 4 * a["int"]
 
 
 class ClockSampler:
@@ -208,6 +219,38 @@ def run_reference(args, rank, world, dist):
     return 0
 
 
+def measure_forms(gbturbo, dirs, cells, n_ref, ref_int, steps, tmp):
+    """secondary numbers beside the FP64 headline: the mixed-precision form on the same passage
+    (device-timed cycles, and its integrals after the same number of cycles as the FP64 run,
+    relative to the FP64 values), and a batch of 8 operating points in the mixed form"""
+    out = {}
+    m = gbturbo.Solver(dirs, gbturbo.MIXED)
+    m.init_uniform()
+    m.iterate(3, history=False)
+    m.timer_start()
+    m.iterate(steps, history=False)
+    ms = m.timer_stop()
+    m.iterate(n_ref - 3 - steps, history=False)
+    got = m.integrals(1)[0]
+    m.close()
+    names = ["m_in", "m_out", "PR", "eta"]
+    out["mixed"] = {"value": cells * steps / (ms / 1000.0), "unit": "cell-updates/s", "ms_per_step": ms / steps,
+                    "steps": steps, "cycles_compared": n_ref,
+                    "rel_err_vs_fp64": {n: abs(float(got[q] - ref_int[q]) / float(ref_int[q])) for q, n in enumerate(names)}}
+    bdirs, _ = make_cases(os.path.join(tmp, "batch8"), 8)
+    b = gbturbo.Solver(bdirs, gbturbo.MIXED)
+    b.init_uniform()
+    b.iterate(3, history=False)
+    b.timer_start()
+    b.iterate(steps, history=False)
+    ms = b.timer_stop()
+    b.close()
+    out["mixed_batch8"] = {"value": 8 * cells * steps / (ms / 1000.0), "unit": "cell-updates/s",
+                           "ms_per_step": ms / steps, "steps": steps,
+                           "operating_points": "back pressure 1.05-1.30 x inlet total (seeded)"}
+    return out
+
+
 def config_block(args, cells, nsolve):
     return {"workload": "rotor_passage_129x49x49_2level_multigrid", "mesh_nodes": "129x49x49 (axial x pitch x span)",
             "cells_per_solve": cells, "solves_per_gpu": nsolve, "precision": args.precision,
@@ -253,15 +296,16 @@ def run_gpu(args, rank, world, dist):
         s.profile_begin()
         s.iterate(nprof, history=False)
         prof = s.profile_end()
-        I, J, K, _ = s.dims(0, 1)
-        planes = I + J + K - 5
+        level_dims = [s.dims(q, l)[:3] for q in range(nsolve) for l in range(1, s.ng + 1)]
         total_prof = sum(v[0] for v in prof.values())
         launches_per_step = sum(v[1] for v in prof.values()) / nprof
         dom = max((k for k in prof if k in ALG), key=lambda k: prof[k][0])
         dom_ms, dom_launches = prof[dom]
-        avg_launch_s = dom_ms / 1000.0 / dom_launches
-        bytes_per_launch = alg_bytes_per_launch(dom, cells * nsolve, planes, wsize, 1)
-        achieved = bytes_per_launch / avg_launch_s / 1e9
+        # algorithmic bytes of the stage per cycle / its device time per cycle (events around the
+        # stage's launches, eager); per launch = per cycle / launches per cycle
+        bytes_per_step = alg_units_per_step(dom, level_dims) * alg_bytes_per_unit(dom, wsize)
+        achieved = bytes_per_step / (dom_ms / nprof / 1000.0) / 1e9
+        bytes_per_launch = bytes_per_step / (dom_launches / nprof)
         peaks = {}
         try:
             peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -273,9 +317,13 @@ def run_gpu(args, rank, world, dist):
             for line in open(os.path.join(ROOT, "profiles", "dram_traffic_per_launch.txt")):
                 f = line.split()
                 if len(f) >= 4 and not line.startswith("#") and f[0] == dom and f[1] == args.precision and int(f[2]) == nsolve:
-                    traffic = float(f[3])
+                    traffic = float(f[3])        # DRAM read + write bytes per launch (ncu), same averaging
         except FileNotFoundError:
             pass
+        forms = None
+        if rank == 0 and world == 1 and not args.no_forms and prec == gbturbo.FP64 and nsolve == 1:
+            n_ref = max(args.warmup, 3) + args.steps + nprof
+            forms = measure_forms(gbturbo, dirs, cells, n_ref, s.integrals(1)[0], min(args.steps, 50), tmp)
         s.close()
 
         # --- end to end through the C-ABI: case files on the host -> handle (upload + geometry)
@@ -311,10 +359,11 @@ def run_gpu(args, rank, world, dist):
                         "h2d_bytes_per_step": int(grid_bytes / n_e2e), "d2h_bytes_per_step": 96 * nsolve},
                 "gpu_launches": int(round(launches_per_step * args.steps)),
                 "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": traffic,
+                             "frac": achieved / peak, "traffic": traffic, "alg_bytes_per_launch": bytes_per_launch,
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800 GB/s",
                              "note": "FP64 on GB300 is bound by the FP64 pipe, not HBM" if prec == gbturbo.FP64 else ""},
                 "stages": stages,
+                "forms": forms,
                 "cpu_baseline": base,
                 "status": status,
             }
