@@ -49,12 +49,28 @@ struct BcTables {
 
 constexpr int kIntegralBlocks = 16;             // blocks per inlet/outlet section in the integrals
 
-// cells of every i+j+k hyperplane of every solve: pairs[start[s*stride + plane] ..
-// start[s*stride + plane + 1]) hold (i << 16) | j; max_count[plane] is the largest plane over solves
+// Cells of every i+j+k hyperplane of every solve, in "plane order": q runs over the planes of
+// solve 0, then those of solve 1, ...; inside a plane by i, then j. start[s*stride + plane] ..
+// start[s*stride + plane + 1] are the q of one plane of solve s; max_count[plane] is the largest
+// plane over the solves.
 struct PlaneTables {
-    const int *pairs = nullptr, *start = nullptr;
+    const int *start = nullptr;
     int stride = 0, max_plane = 0;
+    long long nq = 0;
     std::vector<int> max_count;
+};
+
+// Everything the LU-SGS sweeps read, copied into plane order so that the cells of one plane and
+// their neighbours in the previous plane are dense in memory (in the k-contiguous box they are
+// scattered, one sector per value). Geometry is copied once; the flow inputs before every forward
+// sweep; dQ lives here during the sweeps and is scattered back to the box afterwards.
+template <typename T>
+struct SweepData {
+    const long long *cell = nullptr;               // q -> box index (including the solve's base)
+    const int *nb[2][3] = {};                      // [0] lower (forward), [1] upper (backward) neighbour q, or -1
+    T *gn[3][3] = {}, *gs[3] = {}, *gve[3] = {}, *gvol = nullptr;   // per direction: mean normal, |S|, entrainment
+    T *cv[NQ] = {}, *pp = nullptr, *lamc[3] = {}, *lamv[3] = {}, *dt = nullptr, *res[NQ] = {};
+    T *dq[NQ] = {};
 };
 
 void launch_geometry(const LaunchCtx &ctx, const Geo &G, double *totalvol);
@@ -68,7 +84,11 @@ void launch_resflux(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> F
                     int level, T *scratch_dtmin);
 
 template <typename T>
-void launch_lusgs_sweeps(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> F, const PlaneTables &pt);
+void launch_lusgs_sweeps(const LaunchCtx &ctx, const Phys &P, Flow<T> F, const PlaneTables &pt, const SweepData<T> &S);
+
+// plane-order copy of the sweep's geometry (once per level, after the geometry kernels)
+template <typename T>
+void launch_sweep_geometry(const LaunchCtx &ctx, const Geo &G, const PlaneTables &pt, const SweepData<T> &S);
 
 template <typename T>
 void launch_update(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> F, int level,

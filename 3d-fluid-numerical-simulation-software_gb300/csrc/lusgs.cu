@@ -21,40 +21,33 @@ __device__ __forceinline__ void release_next_plane() { asm volatile("griddepcont
 
 // One warp per block handles ten cells of a plane with three lanes per cell, lane d computing
 // the off-diagonal term of neighbour direction d; the three terms are combined on the first lane
-// in the reference's order (-R + A_I + A_J + A_K + V_I + V_J + V_K). Cells of a plane come from a
-// compact per-solve list, so a plane of ~1,300 cells spreads over ~130 SMs. The neighbour's old
-// flux F_n(Q) and the diagonal 1/alpha do not depend on dQ and are formed before the wait, so
-// only the new flux F_n(Q + dQ) and the combination sit on the plane-to-plane critical path.
+// in the reference's order (-R + A_I + A_J + A_K + V_I + V_J + V_K). A plane's cells and their
+// neighbours are read from the plane-order copy (SweepData), so a warp's loads are dense. The
+// neighbour's old flux F_n(Q) and the diagonal 1/alpha do not depend on dQ and are formed before
+// the wait, so only the new flux F_n(Q + dQ) and the combination sit on the plane-to-plane
+// critical path.
 template <typename T, int DIR>      // DIR = +1 forward (lower neighbours), -1 backward
-__global__ void __launch_bounds__(32) k_sweep(Batch B, Phys P, Geo G, Flow<T> W, const int *__restrict__ pairs,
-                                              const int *__restrict__ pstart, int pstride, int plane)
+__global__ void __launch_bounds__(32) k_sweep(Phys P, SweepData<T> S, const int *__restrict__ pstart, int pstride,
+                                              int plane)
 {
     release_next_plane();
     const int lane = threadIdx.x, slot = lane / 3, d = lane - 3 * slot;
     const int s = blockIdx.y;
-    const Lvl L = B.lv[s];
     const int base = pstart[s * pstride + plane], cnt = pstart[s * pstride + plane + 1] - base;
     const int idx = blockIdx.x * 10 + slot;
     const bool active = lane < 30 && idx < cnt;
-    bool has = false;
-    long long p = 0, nb = 0;
+    const int q = base + idx;
+    int nb = -1;
     T nx = 0, ny = 0, nz = 0, ve = 0, od = 0, omx = 0, omy = 0, omz = 0, oe = 0, sd = 0, rl = 0, lv = 0;
     T fo[5] = {(T)0, (T)0, (T)0, (T)0, (T)0}, rhs[5] = {(T)0, (T)0, (T)0, (T)0, (T)0};
     T alpha = (T)1, inva = (T)1;
     if (active) {
-        const int ij = pairs[base + idx];
-        const int i = ij >> 16, j = ij & 0xffff, k = plane - i - j;
-        p = ix(L, i, j, k);
-        const int a = d == 0 ? i : (d == 1 ? j : k);
-        const int top = d == 0 ? L.IM - 1 : (d == 1 ? L.JM - 1 : L.KM - 1);
-        has = DIR > 0 ? (a != 1) : (a != top);
-        if (has) {
-            const long long sd_ = d == 0 ? (long long)L.NJ * L.NK : (d == 1 ? (long long)L.NK : 1LL);
-            nb = DIR > 0 ? p - sd_ : p + sd_;
-            nx = (T)G.cn[d][0][nb]; ny = (T)G.cn[d][1][nb]; nz = (T)G.cn[d][2][nb];
-            ve = (T)G.cve[d][nb];
-            od = (T)W.cv[0][nb]; omx = (T)W.cv[1][nb]; omy = (T)W.cv[2][nb]; omz = (T)W.cv[3][nb]; oe = (T)W.cv[4][nb];
-            const T po = W.pv[PP][nb];
+        nb = S.nb[DIR > 0 ? 0 : 1][d][q];
+        if (nb >= 0) {
+            nx = S.gn[d][0][nb]; ny = S.gn[d][1][nb]; nz = S.gn[d][2][nb];
+            ve = S.gve[d][nb];
+            od = S.cv[0][nb]; omx = S.cv[1][nb]; omy = S.cv[2][nb]; omz = S.cv[3][nb]; oe = S.cv[4][nb];
+            const T po = S.pp[nb];
             const T oinv = (T)1 / od;
             const T Vo = omx * oinv * nx + omy * oinv * ny + omz * oinv * nz;
             const T dov = Vo - ve;
@@ -63,17 +56,17 @@ __global__ void __launch_bounds__(32) k_sweep(Batch B, Phys P, Geo G, Flow<T> W,
             fo[2] = omy * dov + po * ny;
             fo[3] = omz * dov + po * nz;
             fo[4] = (oe + po) * dov + po * ve;
-            sd = (T)G.cs[d][nb];
-            rl = (T)P.relax * W.lamc[d][nb];
-            lv = W.lamv[d][nb];
+            sd = S.gs[d][nb];
+            rl = (T)P.relax * S.lamc[d][nb];
+            lv = S.lamv[d][nb];
         }
         if (d == 0) {
-            alpha = (T)G.vol[p] / W.dt[p] + (T)P.relax * (W.lamc[0][p] + W.lamc[1][p] + W.lamc[2][p]) +
-                    (T)2 * (W.lamv[0][p] + W.lamv[1][p] + W.lamv[2][p]);
+            alpha = S.gvol[q] / S.dt[q] + (T)P.relax * (S.lamc[0][q] + S.lamc[1][q] + S.lamc[2][q]) +
+                    (T)2 * (S.lamv[0][q] + S.lamv[1][q] + S.lamv[2][q]);
             inva = (T)1 / alpha;
             if (DIR > 0) {
 #pragma unroll
-                for (int c = 0; c < 5; c++) rhs[c] = -W.res[c][p];
+                for (int c = 0; c < 5; c++) rhs[c] = -S.res[c][q];
             }
         }
     }
@@ -81,13 +74,13 @@ __global__ void __launch_bounds__(32) k_sweep(Batch B, Phys P, Geo G, Flow<T> W,
     T dqp[5];                            // backward sweep: this cell's forward-sweep dQ
     if (DIR < 0 && active && d == 0) {
 #pragma unroll
-        for (int c = 0; c < 5; c++) dqp[c] = W.dq[c][p];
+        for (int c = 0; c < 5; c++) dqp[c] = S.dq[c][q];
     }
     T aw[5] = {(T)0, (T)0, (T)0, (T)0, (T)0}, vw[5] = {(T)0, (T)0, (T)0, (T)0, (T)0};
-    if (has) {
+    if (nb >= 0) {
         T dqn[5];
 #pragma unroll
-        for (int c = 0; c < 5; c++) dqn[c] = W.dq[c][nb];
+        for (int c = 0; c < 5; c++) dqn[c] = S.dq[c][nb];
         // flux difference F_n(Q+dQ) - F_n(Q) of the neighbour across its mean normal
         const T nd = od + dqn[0], nmx = omx + dqn[1], nmy = omy + dqn[2], nmz = omz + dqn[3], ne = oe + dqn[4];
         const T inv = (T)1 / nd;
@@ -121,12 +114,55 @@ __global__ void __launch_bounds__(32) k_sweep(Batch B, Phys P, Geo G, Flow<T> W,
         T r;
         if (DIR > 0) r = rhs[c] + aw[c] + a1[c] + a2[c] + vw[c] + v1[c] + v2[c];
         else r = alpha * dqp[c] - aw[c] - a1[c] - a2[c] + vw[c] + v1[c] + v2[c];
-        W.dq[c][p] = r * inva;
+        S.dq[c][q] = r * inva;
     }
 }
 
+// flow inputs of the sweeps into plane order (before every forward sweep)
+template <typename T>
+__global__ void __launch_bounds__(256) k_sweep_gather(Flow<T> W, SweepData<T> S, long long nq)
+{
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const long long p = S.cell[q];
+#pragma unroll
+    for (int c = 0; c < 5; c++) { S.cv[c][q] = (T)W.cv[c][p]; S.res[c][q] = W.res[c][p]; }
+#pragma unroll
+    for (int d = 0; d < 3; d++) { S.lamc[d][q] = W.lamc[d][p]; S.lamv[d][q] = W.lamv[d][p]; }
+    S.pp[q] = W.pv[PP][p];
+    S.dt[q] = W.dt[p];
+}
+
+// dQ back into the box (after the backward sweep)
+template <typename T>
+__global__ void __launch_bounds__(256) k_sweep_scatter(Flow<T> W, SweepData<T> S, long long nq)
+{
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const long long p = S.cell[q];
+#pragma unroll
+    for (int c = 0; c < 5; c++) W.dq[c][p] = S.dq[c][q];
+}
+
+// geometry of the sweeps into plane order, in the working precision (once per level)
+template <typename T>
+__global__ void __launch_bounds__(256) k_sweep_geometry(Geo G, SweepData<T> S, long long nq)
+{
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const long long p = S.cell[q];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) S.gn[d][c][q] = (T)G.cn[d][c][p];
+        S.gs[d][q] = (T)G.cs[d][p];
+        S.gve[d][q] = (T)G.cve[d][p];
+    }
+    S.gvol[q] = (T)G.vol[p];
+}
+
 template <typename T, int DIR>
-static void launch_plane(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const PlaneTables &pt, int pl,
+static void launch_plane(const LaunchCtx &ctx, const Phys &P, const PlaneTables &pt, const SweepData<T> &S, int pl,
                          bool first)
 {
     cudaLaunchConfig_t cfg = {};
@@ -139,19 +175,28 @@ static void launch_plane(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = first ? 0 : 1;     // the first plane of a sweep waits for everything before it
-    cudaLaunchKernelEx(&cfg, k_sweep<T, DIR>, ctx.batch, P, G, W, pt.pairs, pt.start, pt.stride, pl);
+    cudaLaunchKernelEx(&cfg, k_sweep<T, DIR>, P, S, pt.start, pt.stride, pl);
 }
 
 template <typename T>
-void launch_lusgs_sweeps(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const PlaneTables &pt)
+void launch_lusgs_sweeps(const LaunchCtx &ctx, const Phys &P, Flow<T> W, const PlaneTables &pt, const SweepData<T> &S)
 {
     const int np = pt.max_plane;
-    ctx.mark("sweep_forward", 1, np - 2);
-    for (int pl = 3; pl <= np; pl++) launch_plane<T, 1>(ctx, P, G, W, pt, pl, pl == 3);
-    ctx.mark("sweep_forward", 0, np - 2);
-    ctx.mark("sweep_backward", 1, np - 2);
-    for (int pl = np; pl >= 3; pl--) launch_plane<T, -1>(ctx, P, G, W, pt, pl, pl == np);
-    ctx.mark("sweep_backward", 0, np - 2);
+    const unsigned gq = (unsigned)((pt.nq + 255) / 256);
+    ctx.mark("sweep_forward", 1, np - 1);
+    k_sweep_gather<T><<<gq, 256, 0, ctx.stream>>>(W, S, pt.nq);
+    for (int pl = 3; pl <= np; pl++) launch_plane<T, 1>(ctx, P, pt, S, pl, pl == 3);
+    ctx.mark("sweep_forward", 0, np - 1);
+    ctx.mark("sweep_backward", 1, np - 1);
+    for (int pl = np; pl >= 3; pl--) launch_plane<T, -1>(ctx, P, pt, S, pl, pl == np);
+    k_sweep_scatter<T><<<gq, 256, 0, ctx.stream>>>(W, S, pt.nq);
+    ctx.mark("sweep_backward", 0, np - 1);
+}
+
+template <typename T>
+void launch_sweep_geometry(const LaunchCtx &ctx, const Geo &G, const PlaneTables &pt, const SweepData<T> &S)
+{
+    k_sweep_geometry<T><<<(unsigned)((pt.nq + 255) / 256), 256, 0, ctx.stream>>>(G, S, pt.nq);
 }
 
 // primitive variables from the conserved ones
@@ -489,7 +534,8 @@ void launch_cfl_ramp(const LaunchCtx &ctx, int iter)
 }
 
 #define GBT_INST(T)                                                                                                   \
-    template void launch_lusgs_sweeps<T>(const LaunchCtx &, const Phys &, const Geo &, Flow<T>, const PlaneTables &); \
+    template void launch_lusgs_sweeps<T>(const LaunchCtx &, const Phys &, Flow<T>, const PlaneTables &, const SweepData<T> &); \
+    template void launch_sweep_geometry<T>(const LaunchCtx &, const Geo &, const PlaneTables &, const SweepData<T> &); \
     template void launch_update<T>(const LaunchCtx &, const Phys &, const Geo &, Flow<T>, int, int *, int, int *);     \
     template void launch_primitive<T>(const LaunchCtx &, const Phys &, Flow<T>);                                       \
     template void launch_limiter<T>(const LaunchCtx &, const Phys &, Flow<T>, int, int *, int, int *);                 \

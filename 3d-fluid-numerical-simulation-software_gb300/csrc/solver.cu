@@ -54,6 +54,7 @@ struct Level {
     double *totalvol = nullptr;
     BcTables bc;
     PlaneTables planes;
+    SweepData<T> sweep;
     DevBuf plane_mem;
     std::vector<DevWall> walls_h;
     bool use_force = false;
@@ -423,11 +424,13 @@ public:
         }
         build_planes(l);
         launch_geometry(ctx(l), G, Lv.totalvol);
+        launch_sweep_geometry<T>(ctx(l), G, Lv.planes, Lv.sweep);
         CK(cudaStreamSynchronize(stream));
         CK(cudaGetLastError());
     }
 
-    // compact cell lists of the LU-SGS hyperplanes (source/LU_SGS_Marching.cpp:62-74)
+    // cells of the LU-SGS hyperplanes (source/LU_SGS_Marching.cpp:62-74) in plane order, with the
+    // plane-order neighbour tables and the plane-order copies of the sweep's inputs
     void build_planes(int l)
     {
         Level<T> &Lv = lev[l];
@@ -435,33 +438,82 @@ public:
         pt.max_plane = Lv.max_plane;
         pt.stride = Lv.max_plane + 2;
         pt.max_count.assign(pt.stride, 0);
-        std::vector<int> pairs, start((size_t)nsolve * pt.stride + 1, 0);
+        std::vector<long long> cell;
+        std::vector<int> start((size_t)nsolve * pt.stride + 1, 0);
+        std::vector<int> nbq[2][3];
         for (int s = 0; s < nsolve; s++) {
             const Lvl &v = Lv.lv[s];
-            int nI = v.IM - 1, nJ = v.JM - 1, nK = v.KM - 1;
-            if (nI >= 65536 || nJ >= 65536) throw std::runtime_error("block too large for the plane tables");
+            const int nI = v.IM - 1, nJ = v.JM - 1, nK = v.KM - 1;
+            // q of interior cell (i,j,k) of this solve
+            std::vector<int> qof((size_t)nI * nJ * nK, -1);
+            auto at = [&](int i, int j, int k) -> int & { return qof[((size_t)(i - 1) * nJ + (j - 1)) * nK + (k - 1)]; };
             for (int pl = 0; pl < pt.stride; pl++) {
-                start[(size_t)s * pt.stride + pl] = (int)pairs.size();
+                start[(size_t)s * pt.stride + pl] = (int)cell.size();
                 int c = 0;
                 if (pl >= 3)
                     for (int i = 1; i <= nI; i++)
                         for (int j = 1; j <= nJ; j++) {
-                            int k = pl - i - j;
-                            if (k >= 1 && k <= nK) { pairs.push_back((i << 16) | j); c++; }
+                            const int k = pl - i - j;
+                            if (k < 1 || k > nK) continue;
+                            at(i, j, k) = (int)cell.size();
+                            cell.push_back(ix(v, i, j, k));
+                            c++;
                         }
                 pt.max_count[pl] = std::max(pt.max_count[pl], c);
             }
+            if (cell.size() > (size_t)0x7fffffff) throw std::runtime_error("batch too large for the plane tables");
+            for (int dir = 0; dir < 2; dir++)
+                for (int d = 0; d < 3; d++) nbq[dir][d].resize(cell.size(), -1);
+            for (int i = 1; i <= nI; i++)
+                for (int j = 1; j <= nJ; j++)
+                    for (int k = 1; k <= nK; k++) {
+                        const int q = at(i, j, k);
+                        if (i > 1) nbq[0][0][q] = at(i - 1, j, k);
+                        if (j > 1) nbq[0][1][q] = at(i, j - 1, k);
+                        if (k > 1) nbq[0][2][q] = at(i, j, k - 1);
+                        if (i < nI) nbq[1][0][q] = at(i + 1, j, k);
+                        if (j < nJ) nbq[1][1][q] = at(i, j + 1, k);
+                        if (k < nK) nbq[1][2][q] = at(i, j, k + 1);
+                    }
         }
-        start[(size_t)nsolve * pt.stride] = (int)pairs.size();
+        start[(size_t)nsolve * pt.stride] = (int)cell.size();
         // start[s*stride + pl + 1] must be the end of plane pl: the last slot of each solve row
         // (pl = stride-1) is empty, so the next row's first entry closes it
-        Lv.plane_mem.bytes = sizeof(int) * (pairs.size() + start.size()) + 256;
+        const size_t nq = cell.size();
+        pt.nq = (long long)nq;
+        auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+        const size_t n_t = 16 + 18 + NQ;                   // geometry, flow inputs, dQ
+        Lv.plane_mem.bytes = al(sizeof(int) * start.size()) + al(sizeof(long long) * nq) + 6 * al(sizeof(int) * nq) +
+                             n_t * al(sizeof(T) * nq) + 256;
         CK(cudaMalloc(&Lv.plane_mem.p, Lv.plane_mem.bytes));
-        int *d = (int *)Lv.plane_mem.p;
-        CK(cudaMemcpy(d, pairs.data(), sizeof(int) * pairs.size(), cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d + pairs.size(), start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
-        pt.pairs = d;
-        pt.start = d + pairs.size();
+        char *q = (char *)Lv.plane_mem.p;
+        auto take = [&](size_t b) { char *r = q; q += al(b); return r; };
+        int *dstart = (int *)take(sizeof(int) * start.size());
+        CK(cudaMemcpy(dstart, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
+        pt.start = dstart;
+        SweepData<T> &S = Lv.sweep;
+        long long *dcell = (long long *)take(sizeof(long long) * nq);
+        CK(cudaMemcpy(dcell, cell.data(), sizeof(long long) * nq, cudaMemcpyHostToDevice));
+        S.cell = dcell;
+        for (int dir = 0; dir < 2; dir++)
+            for (int d = 0; d < 3; d++) {
+                int *t = (int *)take(sizeof(int) * nq);
+                CK(cudaMemcpy(t, nbq[dir][d].data(), sizeof(int) * nq, cudaMemcpyHostToDevice));
+                S.nb[dir][d] = t;
+            }
+        auto arr = [&]() { return (T *)take(sizeof(T) * nq); };
+        for (int d = 0; d < 3; d++) {
+            for (int c = 0; c < 3; c++) S.gn[d][c] = arr();
+            S.gs[d] = arr();
+            S.gve[d] = arr();
+        }
+        S.gvol = arr();
+        for (int c = 0; c < NQ; c++) S.cv[c] = arr();
+        S.pp = arr();
+        for (int d = 0; d < 3; d++) { S.lamc[d] = arr(); S.lamv[d] = arr(); }
+        S.dt = arr();
+        for (int c = 0; c < NQ; c++) S.res[c] = arr();
+        for (int c = 0; c < NQ; c++) S.dq[c] = arr();
     }
 
     void build_tables(int l, const std::vector<LevelCase> &lc, const std::vector<double> &hx, const std::vector<double> &hy)
@@ -630,7 +682,7 @@ public:
         Level<T> &Lv = lev[l];
         if (!Lv.use_force) resflux(l);
         else { Mark m(this, "mg_forcing"); launch_forcing<T>(cx, Lv.W); }
-        launch_lusgs_sweeps<T>(cx, P, Lv.G, Lv.W, Lv.planes);
+        launch_lusgs_sweeps<T>(cx, P, Lv.W, Lv.planes, Lv.sweep);
         launch_update<T>(cx, P, Lv.G, Lv.W, l, bad_list, bad_cap, bad_count);
     }
     void res_calculate(int l) override { launch_res_norm<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, norm_part, norm_blk); }

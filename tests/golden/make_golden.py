@@ -9,7 +9,7 @@ evaluation at that state (every intermediate array) in tests/golden/<name>.npz.
 Only runs where the reference sources and a C++ compiler exist; the fixtures it writes are
 committed so the tests need neither.
 
-    python tests/golden/make_golden.py [name ...]
+    python tests/golden/make_golden.py [name ...]      (default: every short case; long cases by name)
 """
 from __future__ import annotations
 
@@ -48,12 +48,34 @@ CASES = {
     "rotor_9x9x33_mg": ("rotor_passage", dict(IM=9, JM=9, KM=33), {"multigrid": "Y", "coarse_iter": "5"}, 14),
 }
 
+# long runs: only the driver history is kept, and the case is regenerated by the tests from the
+# same generator call (its grid file is several MB)
+LONG = {
+    "duct_33x33x65_2000": ("annular_duct", dict(IM=33, JM=33, KM=65), {}, 2000),
+}
+
 KEEP_R = ["cv", "pv", "mut", "omega", "lamcI", "lamcJ", "lamcK", "lamvI", "lamvJ", "lamvK", "dt", "FcI", "FcJ",
           "FcK", "FvI", "FvJ", "FvK", "res", "dIS_pv", "dIP_pv", "dJS_pv", "dJP_pv", "dKS_pv", "dKP_pv", "dIS_cv",
           "dKP_cv"]
 
 
+def make_long(name: str) -> None:
+    mg = _meshgen()
+    gen, kw, opts, n_iter = LONG[name]
+    case = getattr(mg, gen)(**kw, options=opts, name=name)
+    with tempfile.TemporaryDirectory() as tmp:
+        mg.write_case(case, tmp)
+        out = os.path.join(tmp, "out")
+        subprocess.run([HARNESS, str(n_iter), out, "0"], cwd=tmp, check=True, stdout=subprocess.DEVNULL)
+        hist = np.load(os.path.join(out, "history.npy"))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), history=hist)
+    print(name, "iterations:", int(hist.shape[0]))
+
+
 def make(name: str) -> None:
+    if name in LONG:
+        make_long(name)
+        return
     mg = _meshgen()
     gen, kw, opts, n_iter = CASES[name]
     case = getattr(mg, gen)(**kw, options=opts, name=name)
