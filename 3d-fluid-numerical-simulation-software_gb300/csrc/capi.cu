@@ -175,6 +175,14 @@ int gb_profile_end(gb_solver *h, char *buf, int buflen)
     });
 }
 
+int gb_sweep_tuning(gb_solver *h, int level, int *cells_per_warp)
+{
+    NEED(h); LEVEL(h, level);
+    if (!cells_per_warp) { g_err = "null buffer"; return GB_ERR_ARG; }
+    *cells_per_warp = h->s->sweep_cells_per_warp(level);
+    return GB_OK;
+}
+
 int gb_set_graphs(gb_solver *h, int enable) { NEED(h); h->s->use_graphs = enable != 0; return GB_OK; }
 
 int gb_timer_start(gb_solver *h)

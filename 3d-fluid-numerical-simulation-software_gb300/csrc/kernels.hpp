@@ -57,6 +57,7 @@ struct PlaneTables {
     const int *start = nullptr;
     int stride = 0, max_plane = 0;
     long long nq = 0;
+    int cpw = 10;                                 // cells per warp of the sweep kernels (autotuned)
     std::vector<int> max_count;
 };
 
@@ -85,6 +86,11 @@ void launch_resflux(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> F
 
 template <typename T>
 void launch_lusgs_sweeps(const LaunchCtx &ctx, const Phys &P, Flow<T> F, const PlaneTables &pt, const SweepData<T> &S);
+
+// fastest cells-per-warp of the sweep kernels for this level (times the plane chains on benign
+// inputs in the plane-order scratch; synchronises the stream)
+template <typename T>
+int tune_sweep_cpw(const LaunchCtx &ctx, const Phys &P, const PlaneTables &pt, const SweepData<T> &S);
 
 // plane-order copy of the sweep's geometry (once per level, after the geometry kernels)
 template <typename T>

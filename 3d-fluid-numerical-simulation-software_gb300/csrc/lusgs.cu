@@ -19,14 +19,14 @@ namespace gbt {
 __device__ __forceinline__ void wait_previous_plane() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void release_next_plane() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
-// One warp per block handles ten cells of a plane with three lanes per cell, lane d computing
+// One warp per block handles CPW cells of a plane with three lanes per cell, lane d computing
 // the off-diagonal term of neighbour direction d; the three terms are combined on the first lane
 // in the reference's order (-R + A_I + A_J + A_K + V_I + V_J + V_K). A plane's cells and their
 // neighbours are read from the plane-order copy (SweepData), so a warp's loads are dense. The
 // neighbour's old flux F_n(Q) and the diagonal 1/alpha do not depend on dQ and are formed before
 // the wait, so only the new flux F_n(Q + dQ) and the combination sit on the plane-to-plane
 // critical path.
-template <typename T, int DIR>      // DIR = +1 forward (lower neighbours), -1 backward
+template <typename T, int DIR, int CPW>   // DIR = +1 forward (lower neighbours), -1 backward; CPW cells per warp
 __global__ void __launch_bounds__(32) k_sweep(Phys P, SweepData<T> S, const int *__restrict__ pstart, int pstride,
                                               int plane)
 {
@@ -34,8 +34,8 @@ __global__ void __launch_bounds__(32) k_sweep(Phys P, SweepData<T> S, const int 
     const int lane = threadIdx.x, slot = lane / 3, d = lane - 3 * slot;
     const int s = blockIdx.y;
     const int base = pstart[s * pstride + plane], cnt = pstart[s * pstride + plane + 1] - base;
-    const int idx = blockIdx.x * 10 + slot;
-    const bool active = lane < 30 && idx < cnt;
+    const int idx = blockIdx.x * CPW + slot;
+    const bool active = lane < 3 * CPW && idx < cnt;
     const int q = base + idx;
     int nb = -1;
     T nx = 0, ny = 0, nz = 0, ve = 0, od = 0, omx = 0, omy = 0, omz = 0, oe = 0, sd = 0, rl = 0, lv = 0;
@@ -161,12 +161,12 @@ __global__ void __launch_bounds__(256) k_sweep_geometry(Geo G, SweepData<T> S, l
     S.gvol[q] = (T)G.vol[p];
 }
 
-template <typename T, int DIR>
-static void launch_plane(const LaunchCtx &ctx, const Phys &P, const PlaneTables &pt, const SweepData<T> &S, int pl,
-                         bool first)
+template <typename T, int DIR, int CPW>
+static void launch_plane_cpw(const LaunchCtx &ctx, const Phys &P, const PlaneTables &pt, const SweepData<T> &S, int pl,
+                             bool first)
 {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(max(1, (pt.max_count[pl] + 9) / 10), ctx.batch.nsolve);
+    cfg.gridDim = dim3(max(1, (pt.max_count[pl] + CPW - 1) / CPW), ctx.batch.nsolve);
     cfg.blockDim = dim3(32);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = ctx.stream;
@@ -175,7 +175,70 @@ static void launch_plane(const LaunchCtx &ctx, const Phys &P, const PlaneTables 
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = first ? 0 : 1;     // the first plane of a sweep waits for everything before it
-    cudaLaunchKernelEx(&cfg, k_sweep<T, DIR>, P, S, pt.start, pt.stride, pl);
+    cudaLaunchKernelEx(&cfg, k_sweep<T, DIR, CPW>, P, S, pt.start, pt.stride, pl);
+}
+
+// cells per warp of the sweep kernels; the autotuner picks one per level
+constexpr int kSweepCpw[] = {1, 2, 4, 10};
+
+template <typename T, int DIR>
+static void launch_plane(const LaunchCtx &ctx, const Phys &P, const PlaneTables &pt, const SweepData<T> &S, int pl,
+                         bool first)
+{
+    switch (pt.cpw) {
+    case 1: launch_plane_cpw<T, DIR, 1>(ctx, P, pt, S, pl, first); break;
+    case 2: launch_plane_cpw<T, DIR, 2>(ctx, P, pt, S, pl, first); break;
+    case 4: launch_plane_cpw<T, DIR, 4>(ctx, P, pt, S, pl, first); break;
+    default: launch_plane_cpw<T, DIR, 10>(ctx, P, pt, S, pl, first); break;
+    }
+}
+
+// benign sweep inputs for timing (Q = rest state, unit time step and radii, zero residual)
+template <typename T>
+__global__ void __launch_bounds__(256) k_sweep_fill(SweepData<T> S, long long nq)
+{
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    S.cv[0][q] = (T)1; S.cv[1][q] = (T)0.1; S.cv[2][q] = (T)0.1; S.cv[3][q] = (T)0.1; S.cv[4][q] = (T)2.5;
+    S.pp[q] = (T)0.7;
+    for (int d = 0; d < 3; d++) { S.lamc[d][q] = (T)1; S.lamv[d][q] = (T)0.1; }
+    S.dt[q] = (T)1;
+    for (int c = 0; c < NQ; c++) { S.res[c][q] = (T)1e-3; S.dq[c][q] = (T)0; }
+}
+
+// Autotuner of the sweep's cells per warp: times the forward and backward plane chains of this
+// level on benign inputs written into the plane-order scratch (which every time step gathers
+// afresh, so the solver's state is untouched) and returns the fastest candidate. Results do not
+// depend on the choice: every cell is computed the same way.
+template <typename T>
+int tune_sweep_cpw(const LaunchCtx &ctx, const Phys &P, const PlaneTables &pt0, const SweepData<T> &S)
+{
+    PlaneTables pt = pt0;
+    const int np = pt.max_plane;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    k_sweep_fill<T><<<(unsigned)((pt.nq + 255) / 256), 256, 0, ctx.stream>>>(S, pt.nq);
+    int best = 10;
+    float best_ms = 1e30f;
+    for (int cpw : kSweepCpw) {
+        pt.cpw = cpw;
+        float ms = 0.f;
+        for (int rep = 0; rep < 3; rep++) {
+            cudaEventRecord(e0, ctx.stream);
+            for (int pl = 3; pl <= np; pl++) launch_plane<T, 1>(ctx, P, pt, S, pl, pl == 3);
+            for (int pl = np; pl >= 3; pl--) launch_plane<T, -1>(ctx, P, pt, S, pl, pl == np);
+            cudaEventRecord(e1, ctx.stream);
+            cudaEventSynchronize(e1);
+            float t = 0.f;
+            cudaEventElapsedTime(&t, e0, e1);
+            if (rep > 0) ms += t;           // first repetition warms up
+        }
+        if (ms < best_ms) { best_ms = ms; best = cpw; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return best;
 }
 
 template <typename T>
@@ -536,6 +599,7 @@ void launch_cfl_ramp(const LaunchCtx &ctx, int iter)
 #define GBT_INST(T)                                                                                                   \
     template void launch_lusgs_sweeps<T>(const LaunchCtx &, const Phys &, Flow<T>, const PlaneTables &, const SweepData<T> &); \
     template void launch_sweep_geometry<T>(const LaunchCtx &, const Geo &, const PlaneTables &, const SweepData<T> &); \
+    template int tune_sweep_cpw<T>(const LaunchCtx &, const Phys &, const PlaneTables &, const SweepData<T> &); \
     template void launch_update<T>(const LaunchCtx &, const Phys &, const Geo &, Flow<T>, int, int *, int, int *);     \
     template void launch_primitive<T>(const LaunchCtx &, const Phys &, Flow<T>);                                       \
     template void launch_limiter<T>(const LaunchCtx &, const Phys &, Flow<T>, int, int *, int, int *);                 \

@@ -425,6 +425,7 @@ public:
         build_planes(l);
         launch_geometry(ctx(l), G, Lv.totalvol);
         launch_sweep_geometry<T>(ctx(l), G, Lv.planes, Lv.sweep);
+        Lv.planes.cpw = tune_sweep_cpw<T>(ctx(l), P, Lv.planes, Lv.sweep);
         CK(cudaStreamSynchronize(stream));
         CK(cudaGetLastError());
     }
@@ -686,6 +687,7 @@ public:
         launch_update<T>(cx, P, Lv.G, Lv.W, l, bad_list, bad_cap, bad_count);
     }
     void res_calculate(int l) override { launch_res_norm<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, norm_part, norm_blk); }
+    int sweep_cells_per_warp(int l) const override { return lev[l].planes.cpw; }
     void res_calculate_static(int l, double *host_out) override
     {
         launch_res_norm_static<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, host_out);

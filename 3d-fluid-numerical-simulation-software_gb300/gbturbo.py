@@ -56,6 +56,7 @@ def load() -> ctypes.CDLL:
         "gb_set_cv": ([vp, ip, ip, dp, ctypes.c_long], ip),
         "gb_sync": ([vp], ip),
         "gb_set_graphs": ([vp, ip], ip),
+        "gb_sweep_tuning": ([vp, ip, ctypes.POINTER(ip)], ip),
         "gb_profile_begin": ([vp], ip),
         "gb_profile_end": ([vp, ctypes.c_char_p, ip], ip),
         "gb_timer_start": ([vp], ip),
@@ -74,7 +75,7 @@ EXPORTED = ["gb_solver_create", "gb_solver_destroy", "gb_last_error", "gb_dims",
             "gb_corner_treatment", "gb_restrict", "gb_interpolate", "gb_delta_cons", "gb_set_use_force",
             "gb_solver_step", "gb_integrals", "gb_iterate", "gb_get_status", "gb_get_field", "gb_set_cv",
             "gb_sync", "gb_set_graphs", "gb_timer_start", "gb_timer_stop", "gb_profile_begin", "gb_profile_end",
-            "gb_res_calculate_noalloc"]
+            "gb_res_calculate_noalloc", "gb_sweep_tuning"]
 
 
 class GBError(RuntimeError):
@@ -231,6 +232,12 @@ class Solver:
 
     def sync(self) -> None:
         self._ck(self._L.gb_sync(self.h))
+
+    def sweep_tuning(self, level: int = 1) -> int:
+        """cells per warp the sweep autotuner chose for a level"""
+        v = ctypes.c_int()
+        self._ck(self._L.gb_sweep_tuning(self.h, level, ctypes.byref(v)))
+        return int(v.value)
 
     def set_graphs(self, on: bool) -> None:
         self._ck(self._L.gb_set_graphs(self.h, int(on)))

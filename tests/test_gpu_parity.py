@@ -165,3 +165,11 @@ def test_prolongation_of_a_synthetic_coarse_field(gpu_lib):
                                   + 3 / 64 * (C[a2, b2, c1] + C[a1, b2, c2] + C[a2, b1, c2]) + 1 / 64 * C[a2, b2, c2])
         sl = (slice(1, -1),) * 3
         assert rel_err(F[sl], P[sl]) < 1e-14
+
+
+def test_sweep_autotuner_picks_a_candidate(gpu_lib):
+    with gpu_lib.Solver(golden_dir("rotor_9x9x33_mg"), gpu_lib.MIXED) as s:
+        assert s.sweep_tuning(1) in (1, 2, 4, 10)
+        assert s.sweep_tuning(2) in (1, 2, 4, 10)
+        with pytest.raises(gpu_lib.GBError):
+            s.sweep_tuning(3)
