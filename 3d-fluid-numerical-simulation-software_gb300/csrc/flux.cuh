@@ -50,8 +50,11 @@ __device__ __forceinline__ void recon1(int type, T eta, T FF, T F, T B, T BB, T 
         T a = F - FF, b = B - F, c = BB - B;
         T SL = ((T)2 * a * b + eps) / (a * a + b * b + eps);
         T SR = ((T)2 * c * b + eps) / (c * c + b * b + eps);
-        L = F + SL / (T)4 * (((T)1 - SL / (T)3) * a + (SL / (T)3 + (T)1) * b);
-        R = B - SR / (T)4 * (((T)1 - SR / (T)3) * c + (SR / (T)3 + (T)1) * b);
+        // S/3 as a product with 1/3 (the FP64 divide is the costly instruction here; within rounding)
+        const T third = (T)(1.0 / 3.0);
+        const T sl3 = SL * third, sr3 = SR * third;
+        L = F + SL * (T)0.25 * (((T)1 - sl3) * a + (sl3 + (T)1) * b);
+        R = B - SR * (T)0.25 * (((T)1 - sr3) * c + (sr3 + (T)1) * b);
     }
 }
 
@@ -69,11 +72,11 @@ __device__ __forceinline__ void recon_prim(int type, T gamma, const P6<T> &FF, c
     recon1(type, eta, FF.p, F.p, B.p, BB.p, l.p, r.p);
     if (l.d <= lz || l.p <= lz) l = F;
     if (r.d <= lz || r.p <= lz) r = B;
-    const T gm1 = gamma - (T)1;
+    const T rgm1 = (T)1 / (gamma - (T)1);
     cl.d = l.d; cl.mx = l.d * l.u; cl.my = l.d * l.v; cl.mz = l.d * l.w;
-    cl.e = l.p / gm1 + l.d * (l.u * l.u + l.v * l.v + l.w * l.w) / (T)2;
+    cl.e = l.p * rgm1 + l.d * (l.u * l.u + l.v * l.v + l.w * l.w) * (T)0.5;
     cr.d = r.d; cr.mx = r.d * r.u; cr.my = r.d * r.v; cr.mz = r.d * r.w;
-    cr.e = r.p / gm1 + r.d * (r.u * r.u + r.v * r.v + r.w * r.w) / (T)2;
+    cr.e = r.p * rgm1 + r.d * (r.u * r.u + r.v * r.v + r.w * r.w) * (T)0.5;
 }
 
 template <typename T>
@@ -102,14 +105,15 @@ template <typename T>
 __device__ __forceinline__ C5<T> roe(T gamma, const C5<T> &QL, const C5<T> &QR, T qe)
 {
     const T g1 = gamma - (T)1;
-    T dL = QL.d, uL = QL.mx / dL, vL = QL.my / dL, wL = QL.mz / dL, EL = QL.e / dL;
+    // divisions by the densities as products with their reciprocals (within rounding)
+    T dL = QL.d, rdL = (T)1 / dL, uL = QL.mx * rdL, vL = QL.my * rdL, wL = QL.mz * rdL, EL = QL.e * rdL;
     T pL = g1 * dL * (EL - (T)0.5 * (uL * uL + vL * vL + wL * wL));
-    T HL = EL + pL / dL;
-    T dR = QR.d, uR = QR.mx / dR, vR = QR.my / dR, wR = QR.mz / dR, ER = QR.e / dR;
+    T HL = EL + pL * rdL;
+    T dR = QR.d, rdR = (T)1 / dR, uR = QR.mx * rdR, vR = QR.my * rdR, wR = QR.mz * rdR, ER = QR.e * rdR;
     T pR = g1 * dR * (ER - (T)0.5 * (uR * uR + vR * vR + wR * wR));
-    T HR = ER + pR / dR;
+    T HR = ER + pR * rdR;
     T unL = uL - qe, unR = uR - qe;
-    T tmp = tsqrt(dR / dL);
+    T tmp = tsqrt(dR * rdL);
     T inv = (T)1 / ((T)1 + tmp);
     T ua = (uL + tmp * uR) * inv, va = (vL + tmp * vR) * inv, wa = (wL + tmp * wR) * inv, Ha = (HL + tmp * HR) * inv;
     T q2 = ua * ua + va * va + wa * wa;
@@ -120,8 +124,9 @@ __device__ __forceinline__ C5<T> roe(T gamma, const C5<T> &QL, const C5<T> &QR, 
     T dd = dR - dL, dmx = QR.mx - QL.mx, dmy = QR.my - QL.my, dmz = QR.mz - QL.mz, de = QR.e - QL.e;
     T a2 = dmy / (va + (T)(double)1E-8f) - dd;
     T a3 = dmz / (wa + (T)(double)1E-8f) - dd;
-    T a4 = g1 * (dd * (Ha - ua * ua - va * va - wa * wa) + ua * dmx + va * dmy + wa * dmz - de) / (ca * ca);
-    T a1 = ((ua + ca) * dd - dmx - ca * a4) / ((T)2 * ca);
+    const T rca = (T)1 / ca;
+    T a4 = g1 * (dd * (Ha - ua * ua - va * va - wa * wa) + ua * dmx + va * dmy + wa * dmz - de) * (rca * rca);
+    T a1 = ((ua + ca) * dd - dmx - ca * a4) * ((T)0.5 * rca);
     T a5 = dd - (a1 + a4);
     C5<T> F;
     F.d = (T)0.5 * (QL.d * unL + QR.d * unR) - (T)0.5 * (l1 * a1 + l2 * a4 + l5 * a5);

@@ -109,11 +109,13 @@ __global__ void __launch_bounds__(32) k_sweep(Phys P, SweepData<T> S, const int 
         v2[c] = __shfl_down_sync(0xffffffffu, vw[c], 2);
     }
     if (!active || d != 0) return;
+    // the reference's left-to-right sums regrouped as a tree: three dependent additions instead
+    // of six on the plane-to-plane critical path (same terms, rounding differs)
 #pragma unroll
     for (int c = 0; c < 5; c++) {
         T r;
-        if (DIR > 0) r = rhs[c] + aw[c] + a1[c] + a2[c] + vw[c] + v1[c] + v2[c];
-        else r = alpha * dqp[c] - aw[c] - a1[c] - a2[c] + vw[c] + v1[c] + v2[c];
+        if (DIR > 0) r = ((rhs[c] + aw[c]) + (a1[c] + a2[c])) + ((vw[c] + v1[c]) + v2[c]);
+        else r = ((alpha * dqp[c] - aw[c]) - (a1[c] + a2[c])) + ((vw[c] + v1[c]) + v2[c]);
         S.dq[c][q] = r * inva;
     }
 }

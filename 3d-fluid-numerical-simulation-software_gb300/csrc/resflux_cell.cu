@@ -49,6 +49,7 @@ __global__ void __launch_bounds__(256) k_cell_a(Batch B, Phys P, Geo G, Flow<T> 
 // (source/BL_Model.cpp:101-119). The maxima keep the reference's first-occurrence rule (strict
 // ">" in line order), so the result does not depend on how the points are split.
 constexpr int BL_WARPS = 8;
+constexpr int BL_CACHE = 16;         // points per thread whose distance and damping pass 2 keeps for pass 3
 
 template <typename T>
 __global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, Phys P, Geo G, Flow<T> W, const DevWall *walls, int off)
@@ -111,15 +112,20 @@ __global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, Phys P, Geo G, Fl
     // pass 2: largest speed, and F = y |omega| (1 - exp(-y+/A+)) with its first maximiser
     T Fmax = (T)0, ymax = (T)0, Udif = (T)0;
     int nmax = 0x7fffffff;
+    // wall distance and van Driest damping of this thread's first BL_CACHE points, reused by pass 3
+    T c_dis[BL_CACHE], c_damp[BL_CACHE];
     if (live) {
-        for (int n0 = 1 + wp; n0 < N; n0 += BL_WARPS) {
+        int ci = 0;
+        for (int n0 = 1 + wp; n0 < N; n0 += BL_WARPS, ci++) {
             const long long p = CELL(n0);
             const T dx = (T)(G.cc[0][p] - fx), dy = (T)(G.cc[1][p] - fy), dz = (T)(G.cc[2][p] - fz);
             const T dis = tsqrt(dx * dx + dy * dy + dz * dz);
             const T u = W.pv[PU][p], v = W.pv[PV][p], w = W.pv[PW][p];
             const T V = tsqrt(u * u + v * v + w * w);
             if (V > Udif) Udif = V;
-            const T F = dis * tabs(W.omega[p]) * ((T)1 - exp(-(dis * Ret) / Aplus));
+            const T damp = (T)1 - exp(-(dis * Ret) / Aplus);
+            if (ci < BL_CACHE) { c_dis[ci] = dis; c_damp[ci] = damp; }
+            const T F = dis * tabs(W.omega[p]) * damp;
             if (F > Fmax) { Fmax = F; ymax = dis; nmax = n0; }
         }
     }
@@ -145,12 +151,21 @@ __global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, Phys P, Geo G, Fl
     __syncthreads();
     if (!live) return;
     const T ym = sh_ymax[lane], Fwake = sh_fwake[lane];
+    // (Ret * dis) equals (dis * Ret) exactly, so the cached damping is the value pass 3 would form
     // pass 3: inner and outer viscosity, the smaller one merged into mu_t
-    for (int n0 = 1 + wp; n0 < N; n0 += BL_WARPS) {
+    int ci = 0;
+    for (int n0 = 1 + wp; n0 < N; n0 += BL_WARPS, ci++) {
         const long long p = CELL(n0);
-        const T dx = (T)(G.cc[0][p] - fx), dy = (T)(G.cc[1][p] - fy), dz = (T)(G.cc[2][p] - fz);
-        const T dis = tsqrt(dx * dx + dy * dy + dz * dz);
-        const T bL = kap * dis * ((T)1 - exp(-(Ret * dis) / Aplus));
+        T dis, damp;
+        if (ci < BL_CACHE) {
+            dis = c_dis[ci];
+            damp = c_damp[ci];
+        } else {
+            const T dx = (T)(G.cc[0][p] - fx), dy = (T)(G.cc[1][p] - fy), dz = (T)(G.cc[2][p] - fz);
+            dis = tsqrt(dx * dx + dy * dy + dz * dz);
+            damp = (T)1 - exp(-(Ret * dis) / Aplus);
+        }
+        const T bL = kap * dis * damp;
         const T om = W.omega[p], rho = W.pv[PD][p];
         const T m_in = rho * bL * bL * om;
         const T r = Ckleb * dis / ym;
