@@ -268,10 +268,20 @@ void launch_sweep_geometry(const LaunchCtx &ctx, const Geo &G, const PlaneTables
 template <typename T>
 __device__ __forceinline__ void prim_from_cons(const Phys &P, const double c[5], T q[6])
 {
-    const double d = c[0], u = c[1] / d, v = c[2] / d, w = c[3] / d;
-    const double V2 = u * u + v * v + w * w;
-    const double pr = (P.gamma - 1.0) * (c[4] - d * V2 / 2.0);
-    q[PD] = (T)d; q[PU] = (T)u; q[PV] = (T)v; q[PW] = (T)w; q[PP] = (T)pr; q[PT] = (T)(pr / d / P.rgas);
+    if constexpr (sizeof(T) == 4) {
+        // mixed form: primitives are stored in FP32, so they are formed in FP32 from the FP64 Q
+        const float d = (float)c[0], rd = 1.0f / d;
+        const float u = (float)c[1] * rd, v = (float)c[2] * rd, w = (float)c[3] * rd;
+        const float V2 = u * u + v * v + w * w;
+        const float pr = ((float)P.gamma - 1.0f) * ((float)c[4] - d * V2 * 0.5f);
+        q[PD] = d; q[PU] = u; q[PV] = v; q[PW] = w; q[PP] = pr; q[PT] = pr * rd / (float)P.rgas;
+    } else {
+        // one FP64 division by the density, products with its reciprocal (within rounding)
+        const double d = c[0], rd = 1.0 / d, u = c[1] * rd, v = c[2] * rd, w = c[3] * rd;
+        const double V2 = u * u + v * v + w * w;
+        const double pr = (P.gamma - 1.0) * (c[4] - d * V2 * 0.5);
+        q[PD] = (T)d; q[PU] = (T)u; q[PV] = (T)v; q[PW] = (T)w; q[PP] = (T)pr; q[PT] = (T)(pr * rd / P.rgas);
+    }
 }
 
 template <typename T>

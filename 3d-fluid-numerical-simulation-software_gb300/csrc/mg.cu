@@ -143,8 +143,16 @@ __global__ void __launch_bounds__(256) k_interpolate(Batch Bf, Batch Bc, Flow<T>
             Wf.cv[c][p] = v;
         } else {
             const T *q = Wc.dq2h[c];
-            v = a1 * (double)q[c111] + a2 * ((double)q[c112] + (double)q[c121] + (double)q[c211]) +
-                a3 * ((double)q[c221] + (double)q[c122] + (double)q[c212]) + a4 * (double)q[c222];
+            if constexpr (sizeof(T) == 4) {
+                // mixed form: the correction is summed in FP32 (the weights are exact there) and
+                // accumulated into the FP64 Q
+                const T w = (T)a1 * q[c111] + (T)a2 * (q[c112] + q[c121] + q[c211]) +
+                            (T)a3 * (q[c221] + q[c122] + q[c212]) + (T)a4 * q[c222];
+                v = (double)w;
+            } else {
+                v = a1 * (double)q[c111] + a2 * ((double)q[c112] + (double)q[c121] + (double)q[c211]) +
+                    a3 * ((double)q[c221] + (double)q[c122] + (double)q[c212]) + a4 * (double)q[c222];
+            }
             Wf.cv[c][p] = Wf.cv[c][p] + v;
         }
     }
