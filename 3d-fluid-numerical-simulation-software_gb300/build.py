@@ -60,7 +60,7 @@ def build(verbose: bool = False) -> str:
     with concurrent.futures.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
     if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        cmd = [nvcc(), "-shared"] + ARCH + objs + ["-o", LIB, "-lcudart"]
+        cmd = [nvcc(), "-shared"] + ARCH + objs + ["-o", LIB, "-lcudart", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -107,6 +107,17 @@ template <> __device__ __forceinline__ double tsqrt<double>(double x) { return s
 template <> __device__ __forceinline__ float tsqrt<float>(float x) { return sqrtf(x); }
 
 // Sutherland law of the reference (include/FluidProps.h:107-112); T^1.5 as T*sqrt(T).
+// |(o - c) / o| for the residual norm: the reciprocal of o is seeded by an FP32 division and
+// refined by one Newton-Raphson step, r1 = r0 (2 - o r0), which takes the 2^-24 relative error of
+// the seed to about 1e-14 for two FP64 fused multiply-adds instead of an FP64 division (the norm
+// sums some 1e5 such terms, so this is far below what it resolves).
+__device__ __forceinline__ double rel_change(double o, double c)
+{
+    const double r0 = (double)(1.0f / (float)o);
+    const double r1 = r0 * fma(-o, r0, 2.0);
+    return fabs((o - c) * r1);
+}
+
 template <typename T>
 __device__ __forceinline__ T sutherland(const Phys &P, T temp)
 {

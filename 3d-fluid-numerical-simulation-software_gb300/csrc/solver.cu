@@ -5,6 +5,9 @@
 #include "solver.hpp"
 #include <cmath>
 #include <cstring>
+#include <atomic>
+#include <exception>
+#include <thread>
 #include <map>
 #include <stdexcept>
 #include <algorithm>
@@ -274,7 +277,23 @@ public:
         precision = prec;
         nsolve = (int)dirs.size();
         if (nsolve < 1) throw std::runtime_error("no case directories given");
-        for (auto &d : dirs) cases.push_back(read_case(d));
+        // the case files of a batch are parsed in parallel host threads (text grids of large
+        // batches run to gigabytes)
+        cases.resize(nsolve);
+        {
+            std::vector<std::exception_ptr> errs(nsolve);
+            std::atomic<int> next{0};
+            const unsigned nt = std::min<unsigned>((unsigned)nsolve, std::max(1u, std::thread::hardware_concurrency()));
+            std::vector<std::thread> pool;
+            for (unsigned t = 0; t < nt; t++)
+                pool.emplace_back([&] {
+                    for (int i = next++; i < nsolve; i = next++) {
+                        try { cases[i] = read_case(dirs[i]); } catch (...) { errs[i] = std::current_exception(); }
+                    }
+                });
+            for (auto &t : pool) t.join();
+            for (auto &e : errs) if (e) std::rethrow_exception(e);
+        }
         const CaseSpec &c0 = cases[0];
         for (auto &c : cases) {
             if (c.ng != c0.ng || c.coarse_iter != c0.coarse_iter || c.scheme != c0.scheme || c.recon != c0.recon ||

@@ -61,6 +61,29 @@ def make_cases(root: str, n: int, seed_offset: int = 0):
     return dirs, case.n_cells
 
 
+def make_sampled_cases(root: str, n: int, seed: int = 2024):
+    """n operating points from the seeded sampler of the batched form: back pressure U[1.05, 1.30]
+    x p_t, speed {0.8, 0.9, 1.0} x 16000 rpm, mesh {97x41x41, 129x49x49, 161x65x65}, stagger
+    offset N(0, 1 deg); two-level multigrid, mixed form options as the single passage"""
+    import meshgen as mg
+    jobs = [(os.path.join(root, f"sp{q}"), op) for q, op in enumerate(mg.sample_operating_points(n, seed))]
+    # the text grids are slow to format: generate in parallel worker processes (spawned, since
+    # this process already holds a CUDA context)
+    with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
+        cells = pool.map(_write_sampled_case, jobs)
+    return [d for d, _ in jobs], cells
+
+
+def _write_sampled_case(job):
+    d, op = job
+    import meshgen as mg
+    case = mg.rotor_passage(IM=op["IM"], JM=op["JM"], KM=op["KM"], rpm=op["rpm"], stagger_offset=op["stagger_offset"],
+                            options={"Pout": "%.1f" % (op["pb"] * 101325.0), "multigrid": "Y", "coarse_iter": "2",
+                                     "Ma0": "0.45"})
+    mg.write_case(case, d)
+    return case.n_cells
+
+
 # ---------------------------------------------------------------------------------------------
 # algorithmic bytes per kernel launch (each input/output element counted once; "geo" and "cv"
 # are FP64 in both forms, "w" is the working precision). unit: "cell" (fine cells), "face"
@@ -248,6 +271,24 @@ def measure_forms(gbturbo, dirs, cells, n_ref, ref_int, steps, tmp):
     out["mixed_batch8"] = {"value": 8 * cells * steps / (ms / 1000.0), "unit": "cell-updates/s",
                            "ms_per_step": ms / steps, "steps": steps,
                            "operating_points": "back pressure 1.05-1.30 x inlet total (seeded)"}
+    # 64 sampled operating points on three mesh sizes in one batch
+    t0 = time.perf_counter()
+    sdirs, scells = make_sampled_cases(os.path.join(tmp, "batch64"), 64)
+    b = gbturbo.Solver(sdirs, gbturbo.MIXED)
+    t_setup = time.perf_counter() - t0
+    b.init_uniform()
+    b.iterate(3, history=False)
+    b.timer_start()
+    b.iterate(steps // 2, history=False)
+    ms = b.timer_stop()
+    b.close()
+    shutil.rmtree(os.path.join(tmp, "batch64"), ignore_errors=True)
+    out["mixed_batch64_sampled"] = {"value": sum(scells) * (steps // 2) / (ms / 1000.0), "unit": "cell-updates/s",
+                                    "ms_per_step": ms / (steps // 2), "steps": steps // 2,
+                                    "fine_cells": int(sum(scells)), "setup_s": round(t_setup, 1),
+                                    "operating_points": "seeded sampler: back pressure U[1.05,1.30] x p_t, "
+                                                        "rpm {0.8,0.9,1.0} x 16000, meshes 97x41x41 / 129x49x49 / "
+                                                        "161x65x65, stagger offset N(0,1 deg)"}
     return out
 
 
