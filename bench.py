@@ -41,6 +41,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=1, help="operating points per GPU")
+    ap.add_argument("--sampled", action="store_true",
+                    help="draw the batch from the seeded operating-point sampler (three mesh sizes)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the secondary measurements of the mixed-precision and batched forms")
@@ -293,7 +295,11 @@ def measure_forms(gbturbo, dirs, cells, n_ref, ref_int, steps, tmp):
 
 
 def config_block(args, cells, nsolve):
-    return {"workload": "rotor_passage_129x49x49_2level_multigrid", "mesh_nodes": "129x49x49 (axial x pitch x span)",
+    if getattr(args, "sampled", False):
+        wl, mesh = "sampled_rotor_passages_2level_multigrid", "97x41x41 / 129x49x49 / 161x65x65 (seeded sampler)"
+    else:
+        wl, mesh = "rotor_passage_129x49x49_2level_multigrid", "129x49x49 (axial x pitch x span)"
+    return {"workload": wl, "mesh_nodes": mesh,
             "cells_per_solve": cells, "solves_per_gpu": nsolve, "precision": args.precision,
             "scheme": "Roe + MUSCL3 (primitive), Baldwin-Lomax, LU-SGS, 2-level FAS (reference maximum)",
             "l2": "inputs larger than L2 (FP64 working set well above 129 MB), no flush",
@@ -311,7 +317,11 @@ def run_gpu(args, rank, world, dist):
     wsize = 8 if prec == gbturbo.FP64 else 4
     tmp = tempfile.mkdtemp(prefix=f"gbt_bench_{rank}_")
     try:
-        dirs, cells = make_cases(tmp, args.batch, seed_offset=rank)
+        if args.sampled:
+            dirs, cell_list = make_sampled_cases(tmp, args.batch, seed=2024 + rank)
+            cells = sum(cell_list) / len(cell_list)     # mean per solve; totals below multiply by nsolve
+        else:
+            dirs, cells = make_cases(tmp, args.batch, seed_offset=rank)
         nsolve = len(dirs)
         grid_bytes = sum(os.path.getsize(os.path.join(d, "grid.dat")) for d in dirs)
 
