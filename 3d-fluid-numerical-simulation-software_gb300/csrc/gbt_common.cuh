@@ -95,6 +95,41 @@ struct Phys {
     int equation_ns, turb_bl, recon_var, recon, scheme, limiter, global_dt, ndummy;
 };
 
+// Geometry in the working precision T, the copy the T-arithmetic kernels (face fluxes, spectral
+// radii, curl, time step, residual sum) read: for T = double the pointers alias the FP64 arrays
+// of Geo; for T = float they point at FP32 copies made once at set-up, holding exactly the values
+// that converting the FP64 arrays at every use would give. (Converting at use costs one FP64-pipe
+// instruction per value, and the FP64 pipe is GB300's narrowest.)
+template <typename T>
+struct GeoW {
+    T *S[3][3], *s[3], *c[3][2], *nrm[3][3], *t1[3][3], *t2[3][3], *qe[3], *m[3][9];   // faces
+    T *vol, *cc[2], *sb[3][3], *cm[9];                                                 // cells
+};
+
+// Physical constants in the working precision, converted (and the reciprocal Reynolds number
+// formed) once on the host.
+template <typename T>
+struct PhysW {
+    T gamma, gm1, rgas, pr_lam, pr_tur, c_timestep, relax, inv_re, suth_c1, suth_c2;
+};
+
+template <typename T>
+inline PhysW<T> phys_working(const Phys &P)
+{
+    PhysW<T> w;
+    w.gamma = (T)P.gamma;
+    w.gm1 = w.gamma - (T)1;
+    w.rgas = (T)P.rgas;
+    w.pr_lam = (T)P.pr_lam;
+    w.pr_tur = (T)P.pr_tur;
+    w.c_timestep = (T)P.c_timestep;
+    w.relax = (T)P.relax;
+    w.inv_re = (T)(1.0 / P.re_ref);
+    w.suth_c1 = (T)P.suth_c1;
+    w.suth_c2 = (T)P.suth_c2;
+    return w;
+}
+
 // Status bits reported per solve.
 enum {
     GBT_STATUS_NAN = 1,          // a residual norm or an integral is not finite
@@ -116,6 +151,12 @@ __device__ __forceinline__ double rel_change(double o, double c)
     const double r0 = (double)(1.0f / (float)o);
     const double r1 = r0 * fma(-o, r0, 2.0);
     return fabs((o - c) * r1);
+}
+
+template <typename T>
+__device__ __forceinline__ T sutherland(const PhysW<T> &P, T temp)
+{
+    return P.inv_re * (temp * tsqrt(temp)) * P.suth_c1 / (temp + P.suth_c2);
 }
 
 template <typename T>

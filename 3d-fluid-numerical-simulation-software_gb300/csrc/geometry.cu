@@ -7,6 +7,7 @@
 // expression the reference evaluates in place.
 #include "gbt_common.cuh"
 #include "kernels.hpp"
+#include <algorithm>
 
 namespace gbt {
 
@@ -230,6 +231,33 @@ void launch_geometry(const LaunchCtx &ctx, const Geo &G, double *totalvol)
     for (int f = 0; f < 3; f++)
         k_face_metrics<<<ctx.grid_faces(f, 256), blk, 0, ctx.stream>>>(B, G, f);
     k_total_volume<<<dim3(1, B.nsolve), dim3(1024), 0, ctx.stream>>>(B, G, totalvol);
+}
+
+// ---- FP32 copies of the geometry read by the working-precision kernels (mixed form) ----
+__global__ void __launch_bounds__(256) k_to_float(const double *__restrict__ src, float *__restrict__ dst, long long n)
+{
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        dst[t] = (float)src[t];
+}
+
+void launch_geometry_working(const LaunchCtx &ctx, const Geo &G, const GeoW<float> &W)
+{
+    const long long n = ctx.pool_n;
+    const unsigned g = (unsigned)std::min<long long>((n + 255) / 256, 152LL * 16);
+    auto cv = [&](const double *a, float *b) { k_to_float<<<g, 256, 0, ctx.stream>>>(a, b, n); };
+    for (int f = 0; f < 3; f++) {
+        for (int c = 0; c < 3; c++) {
+            cv(G.S[f][c], W.S[f][c]); cv(G.nrm[f][c], W.nrm[f][c]); cv(G.t1[f][c], W.t1[f][c]); cv(G.t2[f][c], W.t2[f][c]);
+            cv(G.sb[f][c], W.sb[f][c]);
+        }
+        for (int c = 0; c < 2; c++) cv(G.c[f][c], W.c[f][c]);
+        cv(G.s[f], W.s[f]);
+        cv(G.qe[f], W.qe[f]);
+        for (int c = 0; c < 9; c++) cv(G.m[f][c], W.m[f][c]);
+    }
+    cv(G.vol, W.vol);
+    for (int c = 0; c < 2; c++) cv(G.cc[c], W.cc[c]);
+    for (int c = 0; c < 9; c++) cv(G.cm[c], W.cm[c]);
 }
 
 }  // namespace gbt

@@ -81,16 +81,19 @@ void launch_boundary(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> 
 
 // residual stages; level = 1 for the fine mesh (turbulence model only there)
 template <typename T>
-void launch_resflux(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> F, const BcTables &bc,
-                    int level, T *scratch_dtmin);
+void launch_resflux(const LaunchCtx &ctx, const Phys &P, const PhysW<T> &PC, const Geo &G, const GeoW<T> &GW, Flow<T> F,
+                    const BcTables &bc, int level, T *scratch_dtmin);
 
 template <typename T>
-void launch_lusgs_sweeps(const LaunchCtx &ctx, const Phys &P, Flow<T> F, const PlaneTables &pt, const SweepData<T> &S);
+void launch_lusgs_sweeps(const LaunchCtx &ctx, const PhysW<T> &P, Flow<T> F, const PlaneTables &pt, const SweepData<T> &S);
 
 // fastest cells-per-warp of the sweep kernels for this level (times the plane chains on benign
 // inputs in the plane-order scratch; synchronises the stream)
 template <typename T>
-int tune_sweep_cpw(const LaunchCtx &ctx, const Phys &P, const PlaneTables &pt, const SweepData<T> &S);
+int tune_sweep_cpw(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneTables &pt, const SweepData<T> &S);
+
+// FP32 copies of the geometry the working-precision kernels read (mixed form; once per level)
+void launch_geometry_working(const LaunchCtx &ctx, const Geo &G, const GeoW<float> &GW);
 
 // plane-order copy of the sweep's geometry (once per level, after the geometry kernels)
 template <typename T>

@@ -27,7 +27,7 @@ __device__ __forceinline__ void release_next_plane() { asm volatile("griddepcont
 // the wait, so only the new flux F_n(Q + dQ) and the combination sit on the plane-to-plane
 // critical path.
 template <typename T, int DIR, int CPW>   // DIR = +1 forward (lower neighbours), -1 backward; CPW cells per warp
-__global__ void __launch_bounds__(32) k_sweep(Phys P, SweepData<T> S, const int *__restrict__ pstart, int pstride,
+__global__ void __launch_bounds__(32) k_sweep(PhysW<T> P, SweepData<T> S, const int *__restrict__ pstart, int pstride,
                                               int plane)
 {
     release_next_plane();
@@ -57,11 +57,11 @@ __global__ void __launch_bounds__(32) k_sweep(Phys P, SweepData<T> S, const int 
             fo[3] = omz * dov + po * nz;
             fo[4] = (oe + po) * dov + po * ve;
             sd = S.gs[d][nb];
-            rl = (T)P.relax * S.lamc[d][nb];
+            rl = P.relax * S.lamc[d][nb];
             lv = S.lamv[d][nb];
         }
         if (d == 0) {
-            alpha = S.gvol[q] / S.dt[q] + (T)P.relax * (S.lamc[0][q] + S.lamc[1][q] + S.lamc[2][q]) +
+            alpha = S.gvol[q] / S.dt[q] + P.relax * (S.lamc[0][q] + S.lamc[1][q] + S.lamc[2][q]) +
                     (T)2 * (S.lamv[0][q] + S.lamv[1][q] + S.lamv[2][q]);
             inva = (T)1 / alpha;
             if (DIR > 0) {
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(32) k_sweep(Phys P, SweepData<T> S, const int 
         const T nd = od + dqn[0], nmx = omx + dqn[1], nmy = omy + dqn[2], nmz = omz + dqn[3], ne = oe + dqn[4];
         const T inv = (T)1 / nd;
         const T u = nmx * inv, v = nmy * inv, w = nmz * inv, E = ne * inv;
-        const T pn = ((T)P.gamma - (T)1) * nd * (E - (T)0.5 * (u * u + v * v + w * w));
+        const T pn = P.gm1 * nd * (E - (T)0.5 * (u * u + v * v + w * w));
         const T Vn = u * nx + v * ny + w * nz;
         const T dn = Vn - ve;
         T dF[5];
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(256) k_sweep_geometry(Geo G, SweepData<T> S, l
 }
 
 template <typename T, int DIR, int CPW>
-static void launch_plane_cpw(const LaunchCtx &ctx, const Phys &P, const PlaneTables &pt, const SweepData<T> &S, int pl,
+static void launch_plane_cpw(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneTables &pt, const SweepData<T> &S, int pl,
                              bool first)
 {
     cudaLaunchConfig_t cfg = {};
@@ -184,7 +184,7 @@ static void launch_plane_cpw(const LaunchCtx &ctx, const Phys &P, const PlaneTab
 constexpr int kSweepCpw[] = {1, 2, 4, 10};
 
 template <typename T, int DIR>
-static void launch_plane(const LaunchCtx &ctx, const Phys &P, const PlaneTables &pt, const SweepData<T> &S, int pl,
+static void launch_plane(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneTables &pt, const SweepData<T> &S, int pl,
                          bool first)
 {
     switch (pt.cpw) {
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(256) k_sweep_fill(SweepData<T> S, long long nq
 // afresh, so the solver's state is untouched) and returns the fastest candidate. Results do not
 // depend on the choice: every cell is computed the same way.
 template <typename T>
-int tune_sweep_cpw(const LaunchCtx &ctx, const Phys &P, const PlaneTables &pt0, const SweepData<T> &S)
+int tune_sweep_cpw(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneTables &pt0, const SweepData<T> &S)
 {
     PlaneTables pt = pt0;
     const int np = pt.max_plane;
@@ -244,7 +244,7 @@ int tune_sweep_cpw(const LaunchCtx &ctx, const Phys &P, const PlaneTables &pt0, 
 }
 
 template <typename T>
-void launch_lusgs_sweeps(const LaunchCtx &ctx, const Phys &P, Flow<T> W, const PlaneTables &pt, const SweepData<T> &S)
+void launch_lusgs_sweeps(const LaunchCtx &ctx, const PhysW<T> &P, Flow<T> W, const PlaneTables &pt, const SweepData<T> &S)
 {
     const int np = pt.max_plane;
     const unsigned gq = (unsigned)((pt.nq + 255) / 256);
@@ -609,9 +609,9 @@ void launch_cfl_ramp(const LaunchCtx &ctx, int iter)
 }
 
 #define GBT_INST(T)                                                                                                   \
-    template void launch_lusgs_sweeps<T>(const LaunchCtx &, const Phys &, Flow<T>, const PlaneTables &, const SweepData<T> &); \
+    template void launch_lusgs_sweeps<T>(const LaunchCtx &, const PhysW<T> &, Flow<T>, const PlaneTables &, const SweepData<T> &); \
     template void launch_sweep_geometry<T>(const LaunchCtx &, const Geo &, const PlaneTables &, const SweepData<T> &); \
-    template int tune_sweep_cpw<T>(const LaunchCtx &, const Phys &, const PlaneTables &, const SweepData<T> &); \
+    template int tune_sweep_cpw<T>(const LaunchCtx &, const PhysW<T> &, const PlaneTables &, const SweepData<T> &); \
     template void launch_update<T>(const LaunchCtx &, const Phys &, const Geo &, Flow<T>, int, int *, int, int *);     \
     template void launch_primitive<T>(const LaunchCtx &, const Phys &, Flow<T>);                                       \
     template void launch_limiter<T>(const LaunchCtx &, const Phys &, Flow<T>, int, int *, int, int *);                 \

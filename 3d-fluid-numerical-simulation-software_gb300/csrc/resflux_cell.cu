@@ -10,7 +10,7 @@ namespace gbt {
 
 // lambda_c per direction and |curl V| (needs ghosts of the velocity)
 template <typename T>
-__global__ void __launch_bounds__(256) k_cell_a(Batch B, Phys P, Geo G, Flow<T> W)
+__global__ void __launch_bounds__(256) k_cell_a(Batch B, Phys P, PhysW<T> PC, GeoW<T> G, Flow<T> W)
 {
     const int s = blockIdx.y;
     const Lvl L = B.lv[s];
@@ -19,12 +19,12 @@ __global__ void __launch_bounds__(256) k_cell_a(Batch B, Phys P, Geo G, Flow<T> 
     const long long p = ix(L, i, j, k);
     const T w_rot = (T)B.sc[s].w_rot;
     const T u = W.pv[PU][p], v = W.pv[PV][p], w = W.pv[PW][p];
-    const T ur = u + w_rot * (T)G.cc[1][p];
-    const T vr = v - w_rot * (T)G.cc[0][p];
-    const T cs = tsqrt((T)P.gamma * (T)P.rgas * W.pv[PT][p]);
+    const T ur = u + w_rot * G.cc[1][p];
+    const T vr = v - w_rot * G.cc[0][p];
+    const T cs = tsqrt(PC.gamma * PC.rgas * W.pv[PT][p]);
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-        T sx = (T)G.sb[d][0][p], sy = (T)G.sb[d][1][p], sz = (T)G.sb[d][2][p];
+        T sx = G.sb[d][0][p], sy = G.sb[d][1][p], sz = G.sb[d][2][p];
         W.lamc[d][p] = tabs(ur * sx + vr * sy + w * sz) + cs * tsqrt(sx * sx + sy * sy + sz * sz);
     }
     if (!P.equation_ns) return;
@@ -33,8 +33,8 @@ __global__ void __launch_bounds__(256) k_cell_a(Batch B, Phys P, Geo G, Flow<T> 
     T uk = h * (W.pv[PU][p + sI] - W.pv[PU][p - sI]), vk = h * (W.pv[PV][p + sI] - W.pv[PV][p - sI]), wk = h * (W.pv[PW][p + sI] - W.pv[PW][p - sI]);
     T ue = h * (W.pv[PU][p + sJ] - W.pv[PU][p - sJ]), ve = h * (W.pv[PV][p + sJ] - W.pv[PV][p - sJ]), we = h * (W.pv[PW][p + sJ] - W.pv[PW][p - sJ]);
     T uz = h * (W.pv[PU][p + 1] - W.pv[PU][p - 1]), vz = h * (W.pv[PV][p + 1] - W.pv[PV][p - 1]), wz = h * (W.pv[PW][p + 1] - W.pv[PW][p - 1]);
-    T m0 = (T)G.cm[0][p], m1 = (T)G.cm[1][p], m2 = (T)G.cm[2][p], m3 = (T)G.cm[3][p], m4 = (T)G.cm[4][p],
-      m5 = (T)G.cm[5][p], m6 = (T)G.cm[6][p], m7 = (T)G.cm[7][p], m8 = (T)G.cm[8][p];
+    T m0 = G.cm[0][p], m1 = G.cm[1][p], m2 = G.cm[2][p], m3 = G.cm[3][p], m4 = G.cm[4][p],
+      m5 = G.cm[5][p], m6 = G.cm[6][p], m7 = G.cm[7][p], m8 = G.cm[8][p];
     T v_x = vk * m0 + ve * m3 + vz * m6, w_x = wk * m0 + we * m3 + wz * m6;
     T u_y = uk * m1 + ue * m4 + uz * m7, w_y = wk * m1 + we * m4 + wz * m7;
     T u_z = uk * m2 + ue * m5 + uz * m8, v_z = vk * m2 + ve * m5 + vz * m8;
@@ -52,7 +52,7 @@ constexpr int BL_WARPS = 8;
 constexpr int BL_CACHE = 16;         // points per thread whose distance and damping pass 2 keeps for pass 3
 
 template <typename T>
-__global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, Phys P, Geo G, Flow<T> W, const DevWall *walls, int off)
+__global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, PhysW<T> PC, Geo G, Flow<T> W, const DevWall *walls, int off)
 {
     __shared__ T sh_a[BL_WARPS][32], sh_b[BL_WARPS][32], sh_u[BL_WARPS][32];
     __shared__ int sh_n[BL_WARPS][32];
@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, Phys P, Geo G, Fl
     if (live) {
         for (int n0 = 1 + wp; n0 < N; n0 += BL_WARPS) {
             const long long p = CELL(n0);
-            const T ml = sutherland(P, W.pv[PT][p]);
+            const T ml = sutherland(PC, W.pv[PT][p]);
             const T tw = tabs(W.omega[p] * ml);
             if (n0 == 1) { sh_d1[lane] = W.pv[PD][p]; sh_m1[lane] = ml; }     // first cell: density, mu_l
             if (!any || tw > tmax) tmax = tw;
@@ -204,7 +204,7 @@ __global__ void k_wall_mut(Batch B, Flow<T> W, const DevWall *walls)
 
 // viscous spectral radii and the local time step
 template <typename T>
-__global__ void __launch_bounds__(256) k_cell_b(Batch B, Phys P, Geo G, Flow<T> W, int level)
+__global__ void __launch_bounds__(256) k_cell_b(Batch B, Phys P, PhysW<T> PC, GeoW<T> G, Flow<T> W, int level)
 {
     const int s = blockIdx.y;
     const Lvl L = B.lv[s];
@@ -213,25 +213,25 @@ __global__ void __launch_bounds__(256) k_cell_b(Batch B, Phys P, Geo G, Flow<T> 
     const long long p = ix(L, i, j, k);
     const int fl = B.st[s].flag_low_dt[level];
     const double dtf = fl == 0 ? 1.0 : (double)(1.0f / (1.0f + (float)fl));
-    const T vol = (T)G.vol[p];
+    const T vol = G.vol[p];
     T lc = W.lamc[0][p] + W.lamc[1][p] + W.lamc[2][p];
     T lv = (T)0;
     if (P.equation_ns) {
-        const T ml = sutherland(P, W.pv[PT][p]);
+        const T ml = sutherland(PC, W.pv[PT][p]);
         const T mt = W.mut[p];
         const T rho = W.pv[PD][p];
-        const T a = (T)(double)(4.0f / 3.0f) / rho, b = (T)P.gamma / rho;
-        const T coef = (a > b ? a : b) * (ml / (T)P.pr_lam + mt / (T)P.pr_tur);
+        const T a = (T)(double)(4.0f / 3.0f) / rho, b = PC.gamma / rho;
+        const T coef = (a > b ? a : b) * (ml / PC.pr_lam + mt / PC.pr_tur);
         T l[3];
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-            T sx = (T)G.sb[d][0][p], sy = (T)G.sb[d][1][p], sz = (T)G.sb[d][2][p];
+            T sx = G.sb[d][0][p], sy = G.sb[d][1][p], sz = G.sb[d][2][p];
             l[d] = coef * (sx * sx + sy * sy + sz * sz) / vol;
             W.lamv[d][p] = l[d];
         }
         lv = l[0] + l[1] + l[2];
     }
-    W.dt[p] = (T)(dtf * B.st[s].cfl) * vol / (lc + (T)P.c_timestep * lv);
+    W.dt[p] = (T)(dtf * B.st[s].cfl) * vol / (lc + PC.c_timestep * lv);
 }
 
 // global time stepping: minimum over the solve, then broadcast (source/TimeStep.cpp:64-87)
@@ -276,12 +276,13 @@ __global__ void k_after_timestep(Batch B, int level)
 }
 
 template <typename T>
-void launch_cell_stages(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const BcTables &bc,
+void launch_cell_stages(const LaunchCtx &ctx, const Phys &P, const PhysW<T> &PC, const Geo &G, const GeoW<T> &GW,
+                        Flow<T> W, const BcTables &bc,
                         int level, T *scratch)
 {
     const Batch &B = ctx.batch;
     ctx.mark("spectral_curl", 1);
-    k_cell_a<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, G, W);
+    k_cell_a<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, PC, GW, W);
     ctx.mark("spectral_curl", 0);
     ctx.mark("baldwin_lomax", 1, bc.n_wall_slot + 2);
     if (level == 1 && P.turb_bl && bc.n_wall > 0) {
@@ -292,7 +293,7 @@ void launch_cell_stages(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<
             if (n <= 0) continue;
             // 32 lines per block, the points of each line split over BL_WARPS warps
             dim3 g((unsigned)((bc.wall_slot_lines[q] + 31) / 32), n);
-            k_bl<T><<<g, 32 * BL_WARPS, 0, ctx.stream>>>(B, P, G, W, bc.wall, bc.wall_slot_off[q]);
+            k_bl<T><<<g, 32 * BL_WARPS, 0, ctx.stream>>>(B, PC, G, W, bc.wall, bc.wall_slot_off[q]);
         }
     }
     if (bc.n_wall > 0) {
@@ -301,7 +302,7 @@ void launch_cell_stages(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<
     }
     ctx.mark("baldwin_lomax", 0, bc.n_wall_slot + 2);
     ctx.mark("time_step", 1, 2);
-    k_cell_b<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, G, W, level);
+    k_cell_b<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, PC, GW, W, level);
     if (P.global_dt) {
         k_dt_min<T><<<dim3(1, B.nsolve), 1024, 0, ctx.stream>>>(B, W, scratch);
         k_dt_set<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, W, scratch);
@@ -310,7 +311,9 @@ void launch_cell_stages(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<
     ctx.mark("time_step", 0, 2);
 }
 
-template void launch_cell_stages<double>(const LaunchCtx &, const Phys &, const Geo &, Flow<double>, const BcTables &, int, double *);
-template void launch_cell_stages<float>(const LaunchCtx &, const Phys &, const Geo &, Flow<float>, const BcTables &, int, float *);
+template void launch_cell_stages<double>(const LaunchCtx &, const Phys &, const PhysW<double> &, const Geo &,
+                                         const GeoW<double> &, Flow<double>, const BcTables &, int, double *);
+template void launch_cell_stages<float>(const LaunchCtx &, const Phys &, const PhysW<float> &, const Geo &,
+                                        const GeoW<float> &, Flow<float>, const BcTables &, int, float *);
 
 }  // namespace gbt

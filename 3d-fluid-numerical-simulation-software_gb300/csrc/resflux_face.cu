@@ -50,7 +50,7 @@ __device__ __forceinline__ T tan_diff(const T *__restrict__ c, long long p, long
 }
 
 template <typename T, int F>
-__global__ void __launch_bounds__(128) k_face(Batch B, Phys P, Geo G, Flow<T> W, const DevWall *walls)
+__global__ void __launch_bounds__(128) k_face(Batch B, Phys P, PhysW<T> PC, GeoW<T> G, Flow<T> W, const DevWall *walls)
 {
     const int s = blockIdx.y;
     const Lvl L = B.lv[s];
@@ -62,8 +62,8 @@ __global__ void __launch_bounds__(128) k_face(Batch B, Phys P, Geo G, Flow<T> W,
     const long long sn = F == 0 ? sI : (F == 1 ? sJ : sK);
     const int NN = F == 0 ? L.IM : (F == 1 ? L.JM : L.KM);
     const int a = F == 0 ? i : (F == 1 ? j : k);
-    const T gamma = (T)P.gamma, g1 = gamma - (T)1;
-    const T Sx = (T)G.S[F][0][p], Sy = (T)G.S[F][1][p], Sz = (T)G.S[F][2][p];
+    const T gamma = PC.gamma, g1 = PC.gm1;
+    const T Sx = G.S[F][0][p], Sy = G.S[F][1][p], Sz = G.S[F][2][p];
     const int wq = W.wallf[F][p];
     T f0, f1, f2, f3, f4;
     if (wq) {
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(128) k_face(Batch B, Phys P, Geo G, Flow<T> W,
         const P6<T> A = ld_pv(W, p), Bq = ld_pv(W, m);
         const T d = (T)0.5 * (A.d + Bq.d), u = (T)0.5 * (A.u + Bq.u), v = (T)0.5 * (A.v + Bq.v),
                 w = (T)0.5 * (A.w + Bq.w), pr = (T)0.5 * (A.p + Bq.p);
-        const T ue = -(T)G.c[F][1][p] * rot, ve = (T)G.c[F][0][p] * rot;
+        const T ue = -G.c[F][1][p] * rot, ve = G.c[F][0][p] * rot;
         const T Vna = u * Sx + v * Sy + w * Sz, Vne = ue * Sx + ve * Sy;
         const T e = pr / g1 + d * (u * u + v * v + w * w) / (T)2;
         const T dv = Vna - Vne;
@@ -89,21 +89,21 @@ __global__ void __launch_bounds__(128) k_face(Batch B, Phys P, Geo G, Flow<T> W,
         C5<T> cl, cr;
         if (P.recon_var == 100) recon_cons(P.recon, gamma, ld_cv(W, q0), ld_cv(W, q1), ld_cv(W, q2), ld_cv(W, q3), cl, cr);
         else recon_prim(P.recon, gamma, ld_pv(W, q0), ld_pv(W, q1), ld_pv(W, q2), ld_pv(W, q3), cl, cr);
-        const T nx = (T)G.nrm[F][0][p], ny = (T)G.nrm[F][1][p], nz = (T)G.nrm[F][2][p];
-        const T ax = (T)G.t1[F][0][p], ay = (T)G.t1[F][1][p], az = (T)G.t1[F][2][p];
-        const T bx = (T)G.t2[F][0][p], by = (T)G.t2[F][1][p], bz = (T)G.t2[F][2][p];
+        const T nx = G.nrm[F][0][p], ny = G.nrm[F][1][p], nz = G.nrm[F][2][p];
+        const T ax = G.t1[F][0][p], ay = G.t1[F][1][p], az = G.t1[F][2][p];
+        const T bx = G.t2[F][0][p], by = G.t2[F][1][p], bz = G.t2[F][2][p];
         C5<T> QL = {cl.d, cl.mx * nx + cl.my * ny + cl.mz * nz, cl.mx * ax + cl.my * ay + cl.mz * az,
                     cl.mx * bx + cl.my * by + cl.mz * bz, cl.e};
         C5<T> QR = {cr.d, cr.mx * nx + cr.my * ny + cr.mz * nz, cr.mx * ax + cr.my * ay + cr.mz * az,
                     cr.mx * bx + cr.my * by + cr.mz * bz, cr.e};
-        const T qe = (T)G.qe[F][p];
+        const T qe = G.qe[F][p];
         C5<T> Fc;
         if (P.scheme == 300) Fc = roe(gamma, QL, QR, qe);
         else {
             C5<T> fp = sw_half(gamma, QL, qe, (T)1), fm = sw_half(gamma, QR, qe, (T)-1);
             Fc.d = fp.d + fm.d; Fc.mx = fp.mx + fm.mx; Fc.my = fp.my + fm.my; Fc.mz = fp.mz + fm.mz; Fc.e = fp.e + fm.e;
         }
-        const T sa = (T)G.s[F][p];
+        const T sa = G.s[F][p];
         f0 = Fc.d * sa;
         f1 = (Fc.mx * nx + Fc.my * ax + Fc.mz * bx) * sa;
         f2 = (Fc.mx * ny + Fc.my * ay + Fc.mz * by) * sa;
@@ -135,9 +135,8 @@ __global__ void __launch_bounds__(128) k_face(Batch B, Phys P, Geo G, Flow<T> W,
         else if (F == 1) { dk[q] = d1[q]; de[q] = dn[q]; dz[q] = d2[q]; }
         else { dk[q] = d1[q]; de[q] = d2[q]; dz[q] = dn[q]; }
     }
-    const T m0 = (T)G.m[F][0][p], m1 = (T)G.m[F][1][p], m2 = (T)G.m[F][2][p], m3 = (T)G.m[F][3][p],
-            m4 = (T)G.m[F][4][p], m5 = (T)G.m[F][5][p], m6 = (T)G.m[F][6][p], m7 = (T)G.m[F][7][p],
-            m8 = (T)G.m[F][8][p];
+    const T m0 = G.m[F][0][p], m1 = G.m[F][1][p], m2 = G.m[F][2][p], m3 = G.m[F][3][p], m4 = G.m[F][4][p],
+            m5 = G.m[F][5][p], m6 = G.m[F][6][p], m7 = G.m[F][7][p], m8 = G.m[F][8][p];
     T gx[4], gy[4], gz[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
@@ -149,13 +148,13 @@ __global__ void __launch_bounds__(128) k_face(Batch B, Phys P, Geo G, Flow<T> W,
     const T h = (T)0.5;
     const T uf = h * (W.pv[PU][p] + W.pv[PU][m]), vf = h * (W.pv[PV][p] + W.pv[PV][m]);
     const T wf = h * (W.pv[PW][p] + W.pv[PW][m]), tf = h * (W.pv[PT][p] + W.pv[PT][m]);
-    const T mul = sutherland(P, tf);
-    const T gR = gamma * (T)P.rgas / g1;
-    T mu = mul, cond = mul * gR / (T)P.pr_lam;
+    const T mul = sutherland(PC, tf);
+    const T gR = gamma * PC.rgas / g1;
+    T mu = mul, cond = mul * gR / PC.pr_lam;
     if (P.turb_bl) {
         const T mt = (W.mut[m] + W.mut[p]) / (T)2;
         mu = mul + mt;
-        cond = cond + mt * gR / (T)P.pr_tur;
+        cond = cond + mt * gR / PC.pr_tur;
     }
     const T c43 = (T)(double)(4.0f / 3.0f), c23 = (T)(double)(2.0f / 3.0f);
     const T txx = mu * (c43 * gx[0] - c23 * (gy[1] + gz[2]));
@@ -176,7 +175,7 @@ __global__ void __launch_bounds__(128) k_face(Batch B, Phys P, Geo G, Flow<T> W,
 
 // face sums, rotation source, residual R = Fc - Fv
 template <typename T>
-__global__ void __launch_bounds__(256) k_cell_sum(Batch B, Phys P, Geo G, Flow<T> W)
+__global__ void __launch_bounds__(256) k_cell_sum(Batch B, Phys P, GeoW<T> G, Flow<T> W)
 {
     const int s = blockIdx.y;
     const Lvl L = B.lv[s];
@@ -185,7 +184,7 @@ __global__ void __launch_bounds__(256) k_cell_sum(Batch B, Phys P, Geo G, Flow<T
     const long long p = ix(L, i, j, k);
     const long long pI = p + (long long)L.NJ * L.NK, pJ = p + L.NK, pK = p + 1;
     const T w = (T)B.sc[s].w_rot;
-    const T rv = W.pv[PD][p] * (T)G.vol[p];
+    const T rv = W.pv[PD][p] * G.vol[p];
     T src[5] = {(T)0, rv * (w * W.pv[PV][p]), -(rv * (w * W.pv[PU][p])), (T)0, (T)0};
 #pragma unroll
     for (int c = 0; c < NQ; c++) {
@@ -198,30 +197,32 @@ __global__ void __launch_bounds__(256) k_cell_sum(Batch B, Phys P, Geo G, Flow<T
 }
 
 template <typename T>
-void launch_cell_stages(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const BcTables &bc,
-                        int level, T *scratch);
+void launch_cell_stages(const LaunchCtx &ctx, const Phys &P, const PhysW<T> &PC, const Geo &G, const GeoW<T> &GW,
+                        Flow<T> W, const BcTables &bc, int level, T *scratch);
 
 template <typename T>
-void launch_resflux(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const BcTables &bc, int level,
-                    T *scratch)
+void launch_resflux(const LaunchCtx &ctx, const Phys &P, const PhysW<T> &PC, const Geo &G, const GeoW<T> &GW, Flow<T> W,
+                    const BcTables &bc, int level, T *scratch)
 {
     const int nbc = (bc.n_inlet > 0) + 3 * (bc.n_outlet > 0) + (bc.n_wall > 0) + (bc.n_per > 0);
     ctx.mark("boundary", 1, nbc);
     launch_boundary<T>(ctx, P, G, W, bc);
     ctx.mark("boundary", 0, nbc);
-    launch_cell_stages<T>(ctx, P, G, W, bc, level, scratch);
+    launch_cell_stages<T>(ctx, P, PC, G, GW, W, bc, level, scratch);
     const Batch &B = ctx.batch;
     ctx.mark("face_flux", 1, 3);
-    k_face<T, 0><<<ctx.grid_faces(0, 128), 128, 0, ctx.stream>>>(B, P, G, W, bc.wall);
-    k_face<T, 1><<<ctx.grid_faces(1, 128), 128, 0, ctx.stream>>>(B, P, G, W, bc.wall);
-    k_face<T, 2><<<ctx.grid_faces(2, 128), 128, 0, ctx.stream>>>(B, P, G, W, bc.wall);
+    k_face<T, 0><<<ctx.grid_faces(0, 128), 128, 0, ctx.stream>>>(B, P, PC, GW, W, bc.wall);
+    k_face<T, 1><<<ctx.grid_faces(1, 128), 128, 0, ctx.stream>>>(B, P, PC, GW, W, bc.wall);
+    k_face<T, 2><<<ctx.grid_faces(2, 128), 128, 0, ctx.stream>>>(B, P, PC, GW, W, bc.wall);
     ctx.mark("face_flux", 0, 3);
     ctx.mark("cell_sum", 1);
-    k_cell_sum<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, G, W);
+    k_cell_sum<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, GW, W);
     ctx.mark("cell_sum", 0);
 }
 
-template void launch_resflux<double>(const LaunchCtx &, const Phys &, const Geo &, Flow<double>, const BcTables &, int, double *);
-template void launch_resflux<float>(const LaunchCtx &, const Phys &, const Geo &, Flow<float>, const BcTables &, int, float *);
+template void launch_resflux<double>(const LaunchCtx &, const Phys &, const PhysW<double> &, const Geo &,
+                                     const GeoW<double> &, Flow<double>, const BcTables &, int, double *);
+template void launch_resflux<float>(const LaunchCtx &, const Phys &, const PhysW<float> &, const Geo &,
+                                    const GeoW<float> &, Flow<float>, const BcTables &, int, float *);
 
 }  // namespace gbt

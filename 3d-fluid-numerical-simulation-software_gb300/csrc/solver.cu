@@ -53,6 +53,8 @@ struct Level {
     int maxIM = 0, maxJM = 0, maxKM = 0, max_plane = 0;
     DevBuf geo_mem, flow_d_mem, flow_t_mem, int_mem, tab_mem, meta_mem;
     Geo G{};
+    GeoW<T> GW{};                         // working-precision geometry (aliases in FP64, FP32 copies in mixed)
+    DevBuf geow_mem;
     Flow<T> W{};
     double *totalvol = nullptr;
     BcTables bc;
@@ -185,6 +187,7 @@ class SolverT : public SolverBase {
 public:
     Level<T> lev[3];
     DevBuf st_mem, scratch_mem;
+    PhysW<T> PC{};                        // physical constants in the working precision
     SolveState *st_d = nullptr;
     int *bad_list = nullptr, *bad_count = nullptr;
     const int bad_cap = 4096;
@@ -317,6 +320,7 @@ public:
         P.equation_ns = c0.equation_ns; P.turb_bl = c0.turb == 100; P.recon_var = c0.recon_var; P.recon = c0.recon;
         P.scheme = c0.scheme; P.limiter = c0.limiter; P.global_dt = c0.global_dt;
         P.ndummy = c0.recon == 0 ? 3 : 2;
+        PC = phys_working<T>(P);
 
         CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         // per-solve state
@@ -443,10 +447,55 @@ public:
         }
         build_planes(l);
         launch_geometry(ctx(l), G, Lv.totalvol);
+        build_geometry_working(l);
         launch_sweep_geometry<T>(ctx(l), G, Lv.planes, Lv.sweep);
-        Lv.planes.cpw = tune_sweep_cpw<T>(ctx(l), P, Lv.planes, Lv.sweep);
+        Lv.planes.cpw = tune_sweep_cpw<T>(ctx(l), PC, Lv.planes, Lv.sweep);
         CK(cudaStreamSynchronize(stream));
         CK(cudaGetLastError());
+    }
+
+    // geometry in the working precision: aliases of the FP64 arrays in the FP64 form, FP32 copies
+    // (made on the device, once) in the mixed form
+    void build_geometry_working(int l)
+    {
+        Level<T> &Lv = lev[l];
+        const Geo &G = Lv.G;
+        GeoW<T> &W = Lv.GW;
+        if constexpr (sizeof(T) == 8) {
+            for (int f = 0; f < 3; f++) {
+                for (int c = 0; c < 3; c++) {
+                    W.S[f][c] = G.S[f][c]; W.nrm[f][c] = G.nrm[f][c]; W.t1[f][c] = G.t1[f][c]; W.t2[f][c] = G.t2[f][c];
+                    W.sb[f][c] = G.sb[f][c];
+                }
+                for (int c = 0; c < 2; c++) W.c[f][c] = G.c[f][c];
+                W.s[f] = G.s[f];
+                W.qe[f] = G.qe[f];
+                for (int c = 0; c < 9; c++) W.m[f][c] = G.m[f][c];
+            }
+            W.vol = G.vol;
+            for (int c = 0; c < 2; c++) W.cc[c] = G.cc[c];
+            for (int c = 0; c < 9; c++) W.cm[c] = G.cm[c];
+        } else {
+            const long long N = Lv.pool_n;
+            const int NW = 3 * (5 * 3 + 2 + 1 + 1 + 9) + 1 + 2 + 9;
+            Lv.geow_mem.bytes = sizeof(T) * (size_t)N * NW;
+            CK(cudaMalloc(&Lv.geow_mem.p, Lv.geow_mem.bytes));
+            T *g = (T *)Lv.geow_mem.p;
+            auto take = [&]() { T *r = g; g += N; return r; };
+            for (int f = 0; f < 3; f++) {
+                for (int c = 0; c < 3; c++) {
+                    W.S[f][c] = take(); W.nrm[f][c] = take(); W.t1[f][c] = take(); W.t2[f][c] = take(); W.sb[f][c] = take();
+                }
+                for (int c = 0; c < 2; c++) W.c[f][c] = take();
+                W.s[f] = take();
+                W.qe[f] = take();
+                for (int c = 0; c < 9; c++) W.m[f][c] = take();
+            }
+            W.vol = take();
+            for (int c = 0; c < 2; c++) W.cc[c] = take();
+            for (int c = 0; c < 9; c++) W.cm[c] = take();
+            launch_geometry_working(ctx(l), G, W);
+        }
     }
 
     // cells of the LU-SGS hyperplanes (source/LU_SGS_Marching.cpp:62-74) in plane order, with the
@@ -694,7 +743,7 @@ public:
     }
     void resflux(int l) override
     {
-        launch_resflux<T>(ctx(l), P, lev[l].G, lev[l].W, lev[l].bc, l, dtmin);
+        launch_resflux<T>(ctx(l), P, PC, lev[l].G, lev[l].GW, lev[l].W, lev[l].bc, l, dtmin);
     }
     void time_marching(int l) override
     {
@@ -702,7 +751,7 @@ public:
         Level<T> &Lv = lev[l];
         if (!Lv.use_force) resflux(l);
         else { Mark m(this, "mg_forcing"); launch_forcing<T>(cx, Lv.W); }
-        launch_lusgs_sweeps<T>(cx, P, Lv.W, Lv.planes, Lv.sweep);
+        launch_lusgs_sweeps<T>(cx, PC, Lv.W, Lv.planes, Lv.sweep);
         launch_update<T>(cx, P, Lv.G, Lv.W, l, bad_list, bad_cap, bad_count);
     }
     void res_calculate(int l) override { launch_res_norm<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, norm_part, norm_blk); }
