@@ -175,11 +175,11 @@ int gb_profile_end(gb_solver *h, char *buf, int buflen)
     });
 }
 
-int gb_sweep_tuning(gb_solver *h, int level, int *cells_per_warp)
+int gb_sweep_tuning(gb_solver *h, int level, int out[2])
 {
     NEED(h); LEVEL(h, level);
-    if (!cells_per_warp) { g_err = "null buffer"; return GB_ERR_ARG; }
-    *cells_per_warp = h->s->sweep_cells_per_warp(level);
+    if (!out) { g_err = "null buffer"; return GB_ERR_ARG; }
+    h->s->sweep_shape(level, out);
     return GB_OK;
 }
 

@@ -57,7 +57,7 @@ struct PlaneTables {
     const int *start = nullptr;
     int stride = 0, max_plane = 0;
     long long nq = 0;
-    int cpw = 10;                                 // cells per warp of the sweep kernels (autotuned)
+    int cpw = 10, wpb = 1;                        // sweep block shape: cells per warp, warps per block (autotuned)
     std::vector<int> max_count;
 };
 
@@ -87,8 +87,8 @@ void launch_resflux(const LaunchCtx &ctx, const Phys &P, const PhysW<T> &PC, con
 template <typename T>
 void launch_lusgs_sweeps(const LaunchCtx &ctx, const PhysW<T> &P, Flow<T> F, const PlaneTables &pt, const SweepData<T> &S);
 
-// fastest cells-per-warp of the sweep kernels for this level (times the plane chains on benign
-// inputs in the plane-order scratch; synchronises the stream)
+// fastest block shape of the sweep kernels for this level, as cells_per_warp * 16 + warps_per_block
+// (times the plane chains on benign inputs in the plane-order scratch; synchronises the stream)
 template <typename T>
 int tune_sweep_cpw(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneTables &pt, const SweepData<T> &S);
 

@@ -19,22 +19,22 @@ namespace gbt {
 __device__ __forceinline__ void wait_previous_plane() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void release_next_plane() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
-// One warp per block handles CPW cells of a plane with three lanes per cell, lane d computing
+// Each warp handles CPW cells of a plane with three lanes per cell, lane d computing
 // the off-diagonal term of neighbour direction d; the three terms are combined on the first lane
 // in the reference's order (-R + A_I + A_J + A_K + V_I + V_J + V_K). A plane's cells and their
 // neighbours are read from the plane-order copy (SweepData), so a warp's loads are dense. The
 // neighbour's old flux F_n(Q) and the diagonal 1/alpha do not depend on dQ and are formed before
 // the wait, so only the new flux F_n(Q + dQ) and the combination sit on the plane-to-plane
 // critical path.
-template <typename T, int DIR, int CPW>   // DIR = +1 forward (lower neighbours), -1 backward; CPW cells per warp
-__global__ void __launch_bounds__(32) k_sweep(PhysW<T> P, SweepData<T> S, const int *__restrict__ pstart, int pstride,
-                                              int plane)
+template <typename T, int DIR, int CPW, int WPB>   // DIR = +1 forward, -1 backward; CPW cells per warp, WPB warps per block
+__global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, const int *__restrict__ pstart,
+                                                    int pstride, int plane)
 {
     release_next_plane();
-    const int lane = threadIdx.x, slot = lane / 3, d = lane - 3 * slot;
+    const int lane = threadIdx.x & 31, slot = lane / 3, d = lane - 3 * slot;
     const int s = blockIdx.y;
     const int base = pstart[s * pstride + plane], cnt = pstart[s * pstride + plane + 1] - base;
-    const int idx = blockIdx.x * CPW + slot;
+    const int idx = (blockIdx.x * WPB + (int)(threadIdx.x >> 5)) * CPW + slot;
     const bool active = lane < 3 * CPW && idx < cnt;
     const int q = base + idx;
     int nb = -1;
@@ -163,13 +163,13 @@ __global__ void __launch_bounds__(256) k_sweep_geometry(Geo G, SweepData<T> S, l
     S.gvol[q] = (T)G.vol[p];
 }
 
-template <typename T, int DIR, int CPW>
-static void launch_plane_cpw(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneTables &pt, const SweepData<T> &S, int pl,
-                             bool first)
+template <typename T, int DIR, int CPW, int WPB>
+static void launch_plane_v(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneTables &pt, const SweepData<T> &S, int pl,
+                           bool first)
 {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(max(1, (pt.max_count[pl] + CPW - 1) / CPW), ctx.batch.nsolve);
-    cfg.blockDim = dim3(32);
+    cfg.gridDim = dim3(max(1, (pt.max_count[pl] + CPW * WPB - 1) / (CPW * WPB)), ctx.batch.nsolve);
+    cfg.blockDim = dim3(32 * WPB);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = ctx.stream;
     cudaLaunchAttribute attr[1];
@@ -177,21 +177,26 @@ static void launch_plane_cpw(const LaunchCtx &ctx, const PhysW<T> &P, const Plan
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = first ? 0 : 1;     // the first plane of a sweep waits for everything before it
-    cudaLaunchKernelEx(&cfg, k_sweep<T, DIR, CPW>, P, S, pt.start, pt.stride, pl);
+    cudaLaunchKernelEx(&cfg, k_sweep<T, DIR, CPW, WPB>, P, S, pt.start, pt.stride, pl);
 }
 
-// cells per warp of the sweep kernels; the autotuner picks one per level
-constexpr int kSweepCpw[] = {1, 2, 4, 10};
+// (cells per warp, warps per block) variants of the sweep kernels; the autotuner picks one per level
+struct SweepShape { int cpw, wpb; };
+constexpr SweepShape kSweepShapes[] = {{1, 1}, {2, 1}, {4, 1}, {10, 1}, {4, 4}, {10, 4}, {10, 8}};
 
 template <typename T, int DIR>
 static void launch_plane(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneTables &pt, const SweepData<T> &S, int pl,
                          bool first)
 {
-    switch (pt.cpw) {
-    case 1: launch_plane_cpw<T, DIR, 1>(ctx, P, pt, S, pl, first); break;
-    case 2: launch_plane_cpw<T, DIR, 2>(ctx, P, pt, S, pl, first); break;
-    case 4: launch_plane_cpw<T, DIR, 4>(ctx, P, pt, S, pl, first); break;
-    default: launch_plane_cpw<T, DIR, 10>(ctx, P, pt, S, pl, first); break;
+    const int v = pt.cpw * 16 + pt.wpb;
+    switch (v) {
+    case 1 * 16 + 1: launch_plane_v<T, DIR, 1, 1>(ctx, P, pt, S, pl, first); break;
+    case 2 * 16 + 1: launch_plane_v<T, DIR, 2, 1>(ctx, P, pt, S, pl, first); break;
+    case 4 * 16 + 1: launch_plane_v<T, DIR, 4, 1>(ctx, P, pt, S, pl, first); break;
+    case 4 * 16 + 4: launch_plane_v<T, DIR, 4, 4>(ctx, P, pt, S, pl, first); break;
+    case 10 * 16 + 4: launch_plane_v<T, DIR, 10, 4>(ctx, P, pt, S, pl, first); break;
+    case 10 * 16 + 8: launch_plane_v<T, DIR, 10, 8>(ctx, P, pt, S, pl, first); break;
+    default: launch_plane_v<T, DIR, 10, 1>(ctx, P, pt, S, pl, first); break;
     }
 }
 
@@ -208,10 +213,11 @@ __global__ void __launch_bounds__(256) k_sweep_fill(SweepData<T> S, long long nq
     for (int c = 0; c < NQ; c++) { S.res[c][q] = (T)1e-3; S.dq[c][q] = (T)0; }
 }
 
-// Autotuner of the sweep's cells per warp: times the forward and backward plane chains of this
+// Autotuner of the sweep's block shape (cells per warp, warps per block): times the forward and
+// backward plane chains of this
 // level on benign inputs written into the plane-order scratch (which every time step gathers
-// afresh, so the solver's state is untouched) and returns the fastest candidate. Results do not
-// depend on the choice: every cell is computed the same way.
+// afresh, so the solver's state is untouched) and returns the fastest candidate as
+// cpw * 16 + wpb. Results do not depend on the choice: every cell is computed the same way.
 template <typename T>
 int tune_sweep_cpw(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneTables &pt0, const SweepData<T> &S)
 {
@@ -221,10 +227,11 @@ int tune_sweep_cpw(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneTables &p
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     k_sweep_fill<T><<<(unsigned)((pt.nq + 255) / 256), 256, 0, ctx.stream>>>(S, pt.nq);
-    int best = 10;
+    SweepShape best = {10, 1};
     float best_ms = 1e30f;
-    for (int cpw : kSweepCpw) {
-        pt.cpw = cpw;
+    for (const SweepShape &sh : kSweepShapes) {
+        pt.cpw = sh.cpw;
+        pt.wpb = sh.wpb;
         float ms = 0.f;
         for (int rep = 0; rep < 3; rep++) {
             cudaEventRecord(e0, ctx.stream);
@@ -236,11 +243,11 @@ int tune_sweep_cpw(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneTables &p
             cudaEventElapsedTime(&t, e0, e1);
             if (rep > 0) ms += t;           // first repetition warms up
         }
-        if (ms < best_ms) { best_ms = ms; best = cpw; }
+        if (ms < best_ms) { best_ms = ms; best = sh; }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    return best;
+    return best.cpw * 16 + best.wpb;
 }
 
 template <typename T>

@@ -449,7 +449,11 @@ public:
         launch_geometry(ctx(l), G, Lv.totalvol);
         build_geometry_working(l);
         launch_sweep_geometry<T>(ctx(l), G, Lv.planes, Lv.sweep);
-        Lv.planes.cpw = tune_sweep_cpw<T>(ctx(l), PC, Lv.planes, Lv.sweep);
+        {
+            const int v = tune_sweep_cpw<T>(ctx(l), PC, Lv.planes, Lv.sweep);
+            Lv.planes.cpw = v / 16;
+            Lv.planes.wpb = v % 16;
+        }
         CK(cudaStreamSynchronize(stream));
         CK(cudaGetLastError());
     }
@@ -755,7 +759,7 @@ public:
         launch_update<T>(cx, P, Lv.G, Lv.W, l, bad_list, bad_cap, bad_count);
     }
     void res_calculate(int l) override { launch_res_norm<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, norm_part, norm_blk); }
-    int sweep_cells_per_warp(int l) const override { return lev[l].planes.cpw; }
+    void sweep_shape(int l, int out[2]) const override { out[0] = lev[l].planes.cpw; out[1] = lev[l].planes.wpb; }
     void res_calculate_static(int l, double *host_out) override
     {
         launch_res_norm_static<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, host_out);

@@ -49,8 +49,8 @@ public:
     virtual void set_cv(int solve, int level, const double *in, long n) = 0;
     virtual void states(SolveState *out) = 0;
     virtual void set_use_force(int level, bool on) = 0;
-    // cells per warp the sweep autotuner chose for a level
-    virtual int sweep_cells_per_warp(int level) const = 0;
+    // block shape the sweep autotuner chose for a level: cells per warp, warps per block
+    virtual void sweep_shape(int level, int out[2]) const = 0;
     // stage profiler: while on, iterations run eagerly and every stage is bracketed by events
     virtual void profile_begin() = 0;
     // "stage:milliseconds:launches;..." totals since profile_begin

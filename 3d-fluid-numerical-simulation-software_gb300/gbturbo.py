@@ -233,11 +233,11 @@ class Solver:
     def sync(self) -> None:
         self._ck(self._L.gb_sync(self.h))
 
-    def sweep_tuning(self, level: int = 1) -> int:
-        """cells per warp the sweep autotuner chose for a level"""
-        v = ctypes.c_int()
-        self._ck(self._L.gb_sweep_tuning(self.h, level, ctypes.byref(v)))
-        return int(v.value)
+    def sweep_tuning(self, level: int = 1) -> tuple:
+        """(cells per warp, warps per block) the sweep autotuner chose for a level"""
+        v = (ctypes.c_int * 2)()
+        self._ck(self._L.gb_sweep_tuning(self.h, level, v))
+        return int(v[0]), int(v[1])
 
     def set_graphs(self, on: bool) -> None:
         self._ck(self._L.gb_set_graphs(self.h, int(on)))

@@ -348,7 +348,7 @@ def run_gpu(args, rank, world, dist):
         s.iterate(nprof, history=False)
         prof = s.profile_end()
         level_dims = [s.dims(q, l)[:3] for q in range(nsolve) for l in range(1, s.ng + 1)]
-        tuning = {f"level{l}": s.sweep_tuning(l) for l in range(1, s.ng + 1)}
+        tuning = {f"level{l}": list(s.sweep_tuning(l)) for l in range(1, s.ng + 1)}
         total_prof = sum(v[0] for v in prof.values())
         launches_per_step = sum(v[1] for v in prof.values()) / nprof
         dom = max((k for k in prof if k in ALG), key=lambda k: prof[k][0])
@@ -414,7 +414,7 @@ def run_gpu(args, rank, world, dist):
                              "frac": achieved / peak, "traffic": traffic, "alg_bytes_per_launch": bytes_per_launch,
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800 GB/s",
                              "note": "FP64 on GB300 is bound by the FP64 pipe, not HBM" if prec == gbturbo.FP64 else ""},
-                "sweep_cells_per_warp": tuning,
+                "sweep_shape_cells_per_warp_warps_per_block": tuning,
                 "stages": stages,
                 "forms": forms,
                 "cpu_baseline": base,

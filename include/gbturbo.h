@@ -85,9 +85,10 @@ int gb_set_cv(gb_solver *h, int solve, int level, const double *cv, long n);
 
 /* waits for the handle's stream */
 int gb_sync(gb_solver *h);
-/* cells per warp of the LU-SGS sweep kernels on a level, chosen at create by timing the plane
- * chains for each candidate (1, 2, 4, 10); the choice changes timing only, not results */
-int gb_sweep_tuning(gb_solver *h, int level, int *cells_per_warp);
+/* block shape of the LU-SGS sweep kernels on a level: out[0] cells per warp, out[1] warps per
+ * block, chosen at create by timing the plane chains of each candidate shape; the choice changes
+ * timing only, not results */
+int gb_sweep_tuning(gb_solver *h, int level, int out[2]);
 /* 0 disables graph replay in gb_iterate (eager launches) */
 int gb_set_graphs(gb_solver *h, int enable);
 /* stage profiler: between the two calls iterations run without graphs and every stage of the
