@@ -22,12 +22,17 @@ __global__ void __launch_bounds__(256) k_cell_a(Batch B, Phys P, PhysW<T> PC, Ge
     const T ur = u + w_rot * G.cc[1][p];
     const T vr = v - w_rot * G.cc[0][p];
     const T cs = tsqrt(PC.gamma * PC.rgas * W.pv[PT][p]);
+    T lam[3];                                  // stored after the curl's loads
 #pragma unroll
     for (int d = 0; d < 3; d++) {
         T sx = G.sb[d][0][p], sy = G.sb[d][1][p], sz = G.sb[d][2][p];
-        W.lamc[d][p] = tabs(ur * sx + vr * sy + w * sz) + cs * tsqrt(sx * sx + sy * sy + sz * sz);
+        lam[d] = tabs(ur * sx + vr * sy + w * sz) + cs * tsqrt(sx * sx + sy * sy + sz * sz);
     }
-    if (!P.equation_ns) return;
+    if (!P.equation_ns) {
+#pragma unroll
+        for (int d = 0; d < 3; d++) W.lamc[d][p] = lam[d];
+        return;
+    }
     const long long sI = (long long)L.NJ * L.NK, sJ = L.NK;
     const T h = (T)0.5;
     T uk = h * (W.pv[PU][p + sI] - W.pv[PU][p - sI]), vk = h * (W.pv[PV][p + sI] - W.pv[PV][p - sI]), wk = h * (W.pv[PW][p + sI] - W.pv[PW][p - sI]);
@@ -38,7 +43,10 @@ __global__ void __launch_bounds__(256) k_cell_a(Batch B, Phys P, PhysW<T> PC, Ge
     T v_x = vk * m0 + ve * m3 + vz * m6, w_x = wk * m0 + we * m3 + wz * m6;
     T u_y = uk * m1 + ue * m4 + uz * m7, w_y = wk * m1 + we * m4 + wz * m7;
     T u_z = uk * m2 + ue * m5 + uz * m8, v_z = vk * m2 + ve * m5 + vz * m8;
-    W.omega[p] = tsqrt(h * ((w_y - v_z) * (w_y - v_z) + (u_z - w_x) * (u_z - w_x) + (v_x - u_y) * (v_x - u_y)));
+    const T om = tsqrt(h * ((w_y - v_z) * (w_y - v_z) + (u_z - w_x) * (u_z - w_x) + (v_x - u_y) * (v_x - u_y)));
+#pragma unroll
+    for (int d = 0; d < 3; d++) W.lamc[d][p] = lam[d];
+    W.omega[p] = om;
 }
 
 // Baldwin-Lomax inner/outer viscosity (source/BL_Model.cpp:283-329) along the wall-normal lines
@@ -212,6 +220,7 @@ __global__ void __launch_bounds__(256) k_cell_b(Batch B, Phys P, PhysW<T> PC, Ge
     if (!box_index(L.IM - 1, L.JM - 1, L.KM - 1, i, j, k)) return;
     const long long p = ix(L, i, j, k);
     const int fl = B.st[s].flag_low_dt[level];
+    const double cfl = B.st[s].cfl;
     const double dtf = fl == 0 ? 1.0 : (double)(1.0f / (1.0f + (float)fl));
     const T vol = G.vol[p];
     T lc = W.lamc[0][p] + W.lamc[1][p] + W.lamc[2][p];
@@ -227,11 +236,12 @@ __global__ void __launch_bounds__(256) k_cell_b(Batch B, Phys P, PhysW<T> PC, Ge
         for (int d = 0; d < 3; d++) {
             T sx = G.sb[d][0][p], sy = G.sb[d][1][p], sz = G.sb[d][2][p];
             l[d] = coef * (sx * sx + sy * sy + sz * sz) / vol;
-            W.lamv[d][p] = l[d];
         }
+#pragma unroll
+        for (int d = 0; d < 3; d++) W.lamv[d][p] = l[d];
         lv = l[0] + l[1] + l[2];
     }
-    W.dt[p] = (T)(dtf * B.st[s].cfl) * vol / (lc + PC.c_timestep * lv);
+    W.dt[p] = (T)(dtf * cfl) * vol / (lc + PC.c_timestep * lv);
 }
 
 // global time stepping: minimum over the solve, then broadcast (source/TimeStep.cpp:64-87)

@@ -49,9 +49,12 @@ __device__ __forceinline__ T tan_diff(const T *__restrict__ c, long long p, long
     return plus - minus;
 }
 
-template <typename T, int F>
+// MODE 1 is the default scheme (MUSCL3 on primitive variables, Roe) with the option switches
+// resolved at compile time; MODE 0 reads them from P
+template <typename T, int F, int MODE>
 __global__ void __launch_bounds__(128) k_face(Batch B, Phys P, PhysW<T> PC, GeoW<T> G, Flow<T> W, const DevWall *walls)
 {
+    const int recon_var = MODE ? 200 : P.recon_var, recon = MODE ? 500 : P.recon, scheme = MODE ? 300 : P.scheme;
     const int s = blockIdx.y;
     const Lvl L = B.lv[s];
     int ni, nj, nk, i, j, k;
@@ -87,8 +90,8 @@ __global__ void __launch_bounds__(128) k_face(Batch B, Phys P, PhysW<T> PC, GeoW
         auto rm = [NN](int c) { return c <= 0 ? c - 1 : (c >= NN ? c + 1 : c); };
         const long long q0 = p0 + rm(a - 2) * sn, q1 = p0 + rm(a - 1) * sn, q2 = p0 + rm(a) * sn, q3 = p0 + rm(a + 1) * sn;
         C5<T> cl, cr;
-        if (P.recon_var == 100) recon_cons(P.recon, gamma, ld_cv(W, q0), ld_cv(W, q1), ld_cv(W, q2), ld_cv(W, q3), cl, cr);
-        else recon_prim(P.recon, gamma, ld_pv(W, q0), ld_pv(W, q1), ld_pv(W, q2), ld_pv(W, q3), cl, cr);
+        if (recon_var == 100) recon_cons(recon, gamma, ld_cv(W, q0), ld_cv(W, q1), ld_cv(W, q2), ld_cv(W, q3), cl, cr);
+        else recon_prim(recon, gamma, ld_pv(W, q0), ld_pv(W, q1), ld_pv(W, q2), ld_pv(W, q3), cl, cr);
         const T nx = G.nrm[F][0][p], ny = G.nrm[F][1][p], nz = G.nrm[F][2][p];
         const T ax = G.t1[F][0][p], ay = G.t1[F][1][p], az = G.t1[F][2][p];
         const T bx = G.t2[F][0][p], by = G.t2[F][1][p], bz = G.t2[F][2][p];
@@ -98,7 +101,7 @@ __global__ void __launch_bounds__(128) k_face(Batch B, Phys P, PhysW<T> PC, GeoW
                     cr.mx * bx + cr.my * by + cr.mz * bz, cr.e};
         const T qe = G.qe[F][p];
         C5<T> Fc;
-        if (P.scheme == 300) Fc = roe(gamma, QL, QR, qe);
+        if (scheme == 300) Fc = roe(gamma, QL, QR, qe);
         else {
             C5<T> fp = sw_half(gamma, QL, qe, (T)1), fm = sw_half(gamma, QR, qe, (T)-1);
             Fc.d = fp.d + fm.d; Fc.mx = fp.mx + fm.mx; Fc.my = fp.my + fm.my; Fc.mz = fp.mz + fm.mz; Fc.e = fp.e + fm.e;
@@ -110,8 +113,12 @@ __global__ void __launch_bounds__(128) k_face(Batch B, Phys P, PhysW<T> PC, GeoW
         f3 = (Fc.mx * nz + Fc.my * az + Fc.mz * bz) * sa;
         f4 = Fc.e * sa;
     }
-    W.Ff[F][0][p] = f0; W.Ff[F][1][p] = f1; W.Ff[F][2][p] = f2; W.Ff[F][3][p] = f3; W.Ff[F][4][p] = f4;
-    if (!P.equation_ns) return;
+    // the flux is stored after every load of the viscous part (the compiler cannot move those loads
+    // above a store to memory it cannot tell apart)
+    if (!P.equation_ns) {
+        W.Ff[F][0][p] = f0; W.Ff[F][1][p] = f1; W.Ff[F][2][p] = f2; W.Ff[F][3][p] = f3; W.Ff[F][4][p] = f4;
+        return;
+    }
 
     // ---- viscous flux ----
     const int iD1 = F == 0 ? 1 : 0, iD2 = F == 2 ? 1 : 2;   // tangential directions (kesi/yita/zita order)
@@ -166,6 +173,7 @@ __global__ void __launch_bounds__(128) k_face(Batch B, Phys P, PhysW<T> PC, GeoW
     const T qx = uf * txx + vf * txy + wf * txz + cond * gx[3];
     const T qy = uf * txy + vf * tyy + wf * tyz + cond * gy[3];
     const T qz = uf * txz + vf * tyz + wf * tzz + cond * gz[3];
+    W.Ff[F][0][p] = f0; W.Ff[F][1][p] = f1; W.Ff[F][2][p] = f2; W.Ff[F][3][p] = f3; W.Ff[F][4][p] = f4;
     W.Vf[F][0][p] = (T)0;
     W.Vf[F][1][p] = txx * Sx + txy * Sy + txz * Sz;
     W.Vf[F][2][p] = txy * Sx + tyy * Sy + tyz * Sz;
@@ -186,14 +194,17 @@ __global__ void __launch_bounds__(256) k_cell_sum(Batch B, Phys P, GeoW<T> G, Fl
     const T w = (T)B.sc[s].w_rot;
     const T rv = W.pv[PD][p] * G.vol[p];
     T src[5] = {(T)0, rv * (w * W.pv[PV][p]), -(rv * (w * W.pv[PU][p])), (T)0, (T)0};
+    T r[NQ];                                   // all loads first, then the stores
 #pragma unroll
     for (int c = 0; c < NQ; c++) {
         T fc = W.Ff[0][c][pI] - W.Ff[0][c][p] + W.Ff[1][c][pJ] - W.Ff[1][c][p] + W.Ff[2][c][pK] - W.Ff[2][c][p] - src[c];
         T fv = (T)0;
         if (P.equation_ns)
             fv = W.Vf[0][c][pI] - W.Vf[0][c][p] + W.Vf[1][c][pJ] - W.Vf[1][c][p] + W.Vf[2][c][pK] - W.Vf[2][c][p];
-        W.res[c][p] = fc - fv;
+        r[c] = fc - fv;
     }
+#pragma unroll
+    for (int c = 0; c < NQ; c++) W.res[c][p] = r[c];
 }
 
 template <typename T>
@@ -211,9 +222,15 @@ void launch_resflux(const LaunchCtx &ctx, const Phys &P, const PhysW<T> &PC, con
     launch_cell_stages<T>(ctx, P, PC, G, GW, W, bc, level, scratch);
     const Batch &B = ctx.batch;
     ctx.mark("face_flux", 1, 3);
-    k_face<T, 0><<<ctx.grid_faces(0, 128), 128, 0, ctx.stream>>>(B, P, PC, GW, W, bc.wall);
-    k_face<T, 1><<<ctx.grid_faces(1, 128), 128, 0, ctx.stream>>>(B, P, PC, GW, W, bc.wall);
-    k_face<T, 2><<<ctx.grid_faces(2, 128), 128, 0, ctx.stream>>>(B, P, PC, GW, W, bc.wall);
+    if (P.recon_var == 200 && P.recon == 500 && P.scheme == 300) {
+        k_face<T, 0, 1><<<ctx.grid_faces(0, 128), 128, 0, ctx.stream>>>(B, P, PC, GW, W, bc.wall);
+        k_face<T, 1, 1><<<ctx.grid_faces(1, 128), 128, 0, ctx.stream>>>(B, P, PC, GW, W, bc.wall);
+        k_face<T, 2, 1><<<ctx.grid_faces(2, 128), 128, 0, ctx.stream>>>(B, P, PC, GW, W, bc.wall);
+    } else {
+        k_face<T, 0, 0><<<ctx.grid_faces(0, 128), 128, 0, ctx.stream>>>(B, P, PC, GW, W, bc.wall);
+        k_face<T, 1, 0><<<ctx.grid_faces(1, 128), 128, 0, ctx.stream>>>(B, P, PC, GW, W, bc.wall);
+        k_face<T, 2, 0><<<ctx.grid_faces(2, 128), 128, 0, ctx.stream>>>(B, P, PC, GW, W, bc.wall);
+    }
     ctx.mark("face_flux", 0, 3);
     ctx.mark("cell_sum", 1);
     k_cell_sum<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, GW, W);
