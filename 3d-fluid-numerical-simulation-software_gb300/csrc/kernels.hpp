@@ -44,6 +44,11 @@ struct BcTables {
     int max_outlet_im = 0, max_outlet_jm = 0;
     double *outlet_cu = nullptr;                  // per outlet patch: mass-weighted swirl of each radial row
     double *integ_part = nullptr;                 // per solve and section: kIntegralBlocks partial sums of 3
+    // Baldwin-Lomax wall distances (fine level): record w holds, for point n0 = 1..N-1 of each of
+    // its wall-normal lines t, the distance of cell n0 from the line's wall-face centre at
+    // wall_dist[wall_dist_off[w] + (n0 - 1) * lines(w) + t], in the working precision
+    void *wall_dist = nullptr;
+    const long long *wall_dist_off = nullptr;
     const DevInOut *inlet_first = nullptr, *outlet_first = nullptr;   // per solve: Inlet[1], Outlet[1]
 };
 
@@ -91,6 +96,10 @@ void launch_lusgs_sweeps(const LaunchCtx &ctx, const PhysW<T> &P, Flow<T> F, con
 // (times the plane chains on benign inputs in the plane-order scratch; synchronises the stream)
 template <typename T>
 int tune_sweep_cpw(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneTables &pt, const SweepData<T> &S);
+
+// Baldwin-Lomax wall distances of every wall line point (fine level, once; see BcTables)
+template <typename T>
+void launch_wall_distances(const LaunchCtx &ctx, const Geo &G, const BcTables &bc);
 
 // FP32 copies of the geometry the working-precision kernels read (mixed form; once per level)
 void launch_geometry_working(const LaunchCtx &ctx, const Geo &G, const GeoW<float> &GW);

@@ -57,37 +57,84 @@ __global__ void __launch_bounds__(256) k_cell_a(Batch B, Phys P, PhysW<T> PC, Ge
 // (source/BL_Model.cpp:101-119). The maxima keep the reference's first-occurrence rule (strict
 // ">" in line order), so the result does not depend on how the points are split.
 constexpr int BL_WARPS = 8;
-constexpr int BL_CACHE = 16;         // points per thread whose distance and damping pass 2 keeps for pass 3
+constexpr int BL_CACHE = 16;         // points per thread whose damping pass 2 keeps for pass 3
+
+// geometry of one wall-normal line of wall record wl (shared by the distance and BL kernels)
+struct BlLine {
+    int dirn, lo, N, lines;
+    long long p0, sn, fw;
+    bool live;
+    long long t;
+};
+__device__ __forceinline__ BlLine bl_line(const Lvl &L, const DevWall &wl, int blk, int lane)
+{
+    BlLine r;
+    r.dirn = (wl.face - 1) / 2;
+    r.lo = wl.face % 2 == 1;
+    int a0, a1, b0, b1;                  // a: fast (coalesced) tangential index, b: the other one
+    if (r.dirn == 0) { a0 = wl.ks; a1 = wl.ke; b0 = wl.js; b1 = wl.je; }
+    else if (r.dirn == 1) { a0 = wl.ks; a1 = wl.ke; b0 = wl.is; b1 = wl.ie; }
+    else { a0 = wl.js; a1 = wl.je; b0 = wl.is; b1 = wl.ie; }
+    const int na = a1 - a0 + 1, nb = b1 - b0 + 1;
+    r.lines = na * nb;
+    r.t = (long long)blk * 32 + lane;
+    r.live = r.t < (long long)r.lines;
+    const int a = a0 + (int)(r.live ? r.t % na : 0), b = b0 + (int)(r.live ? r.t / na : 0);
+    r.N = r.dirn == 0 ? L.IM : (r.dirn == 1 ? L.JM : L.KM);
+    r.sn = r.dirn == 0 ? (long long)L.NJ * L.NK : (r.dirn == 1 ? (long long)L.NK : 1LL);
+    if (r.dirn == 0) { r.p0 = ix(L, 0, b, a); r.fw = ix(L, r.lo ? 1 : L.IM, b, a); }
+    else if (r.dirn == 1) { r.p0 = ix(L, b, 0, a); r.fw = ix(L, b, r.lo ? 1 : L.JM, a); }
+    else { r.p0 = ix(L, b, a, 0); r.fw = ix(L, b, a, r.lo ? 1 : L.KM); }
+    return r;
+}
+
+// distance of every line point from its wall-face centre, formed exactly as the BL kernel would
+template <typename T>
+__global__ void __launch_bounds__(32 * BL_WARPS) k_wall_dist(Batch B, Geo G, const DevWall *walls,
+                                                             const long long *off, T *dist)
+{
+    const DevWall wl = walls[blockIdx.y];
+    const Lvl L = B.lv[wl.solve];
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const BlLine ln = bl_line(L, wl, blockIdx.x, lane);
+    if (!ln.live) return;
+    const double fx = G.c[ln.dirn][0][ln.fw], fy = G.c[ln.dirn][1][ln.fw], fz = G.c[ln.dirn][2][ln.fw];
+    T *d = dist + off[blockIdx.y];
+    for (int n0 = 1 + wp; n0 < ln.N; n0 += BL_WARPS) {
+        const long long p = ln.p0 + (long long)(ln.lo ? n0 : ln.N - n0) * ln.sn;
+        const T dx = (T)(G.cc[0][p] - fx), dy = (T)(G.cc[1][p] - fy), dz = (T)(G.cc[2][p] - fz);
+        d[(long long)(n0 - 1) * ln.lines + ln.t] = tsqrt(dx * dx + dy * dy + dz * dz);
+    }
+}
 
 template <typename T>
-__global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, PhysW<T> PC, Geo G, Flow<T> W, const DevWall *walls, int off)
+void launch_wall_distances(const LaunchCtx &ctx, const Geo &G, const BcTables &bc)
+{
+    if (!bc.n_wall || !bc.wall_dist) return;
+    dim3 g((unsigned)((bc.max_wall + 31) / 32), bc.n_wall);
+    k_wall_dist<T><<<g, 32 * BL_WARPS, 0, ctx.stream>>>(ctx.batch, G, bc.wall, bc.wall_dist_off, (T *)bc.wall_dist);
+}
+template void launch_wall_distances<double>(const LaunchCtx &, const Geo &, const BcTables &);
+template void launch_wall_distances<float>(const LaunchCtx &, const Geo &, const BcTables &);
+
+template <typename T>
+__global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, PhysW<T> PC, Flow<T> W, const DevWall *walls, int off,
+                                                      const long long *dist_off, const T *dist_all)
 {
     __shared__ T sh_a[BL_WARPS][32], sh_b[BL_WARPS][32], sh_u[BL_WARPS][32];
     __shared__ int sh_n[BL_WARPS][32];
     __shared__ T sh_d1[32], sh_m1[32], sh_ret[32], sh_ymax[32], sh_fwake[32];
     const DevWall wl = walls[off + blockIdx.y];
-    const int s = wl.solve;
-    const Lvl L = B.lv[s];
-    const int dirn = (wl.face - 1) / 2, lo = wl.face % 2 == 1;
-    int a0, a1, b0, b1;                  // a: fast (coalesced) tangential index, b: the other one
-    if (dirn == 0) { a0 = wl.ks; a1 = wl.ke; b0 = wl.js; b1 = wl.je; }
-    else if (dirn == 1) { a0 = wl.ks; a1 = wl.ke; b0 = wl.is; b1 = wl.ie; }
-    else { a0 = wl.js; a1 = wl.je; b0 = wl.is; b1 = wl.ie; }
-    const int na = a1 - a0 + 1, nb = b1 - b0 + 1;
+    const Lvl L = B.lv[wl.solve];
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-    const long long t = (long long)blockIdx.x * 32 + lane;
-    if ((long long)blockIdx.x * 32 >= (long long)na * nb) return;      // whole block past the patch
-    const bool live = t < (long long)na * nb;
-    const int a = a0 + (int)(live ? t % na : 0), b = b0 + (int)(live ? t / na : 0);
-    const int N = dirn == 0 ? L.IM : (dirn == 1 ? L.JM : L.KM);
-    const long long sn = dirn == 0 ? (long long)L.NJ * L.NK : (dirn == 1 ? (long long)L.NK : 1LL);
-    long long p0;                        // cell n = 0 of the line; cell n is p0 + n*sn
-    long long fw;                        // wall face
-    if (dirn == 0) { p0 = ix(L, 0, b, a); fw = ix(L, lo ? 1 : L.IM, b, a); }
-    else if (dirn == 1) { p0 = ix(L, b, 0, a); fw = ix(L, b, lo ? 1 : L.JM, a); }
-    else { p0 = ix(L, b, a, 0); fw = ix(L, b, a, lo ? 1 : L.KM); }
-    double fx = 0, fy = 0, fz = 0;
-    if (live) { fx = G.c[dirn][0][fw]; fy = G.c[dirn][1][fw]; fz = G.c[dirn][2][fw]; }
+    const BlLine ln = bl_line(L, wl, blockIdx.x, lane);
+    if ((long long)blockIdx.x * 32 >= (long long)ln.lines) return;      // whole block past the patch
+    const bool live = ln.live;
+    const int N = ln.N, lo = ln.lo;
+    const long long p0 = ln.p0, sn = ln.sn;
+    // wall distance of point n0 of this line (precomputed once from the geometry)
+    const T *dist = dist_all + dist_off[off + blockIdx.y] + ln.t;
+#define DIST(n0) dist[(long long)((n0) - 1) * ln.lines]
     // line order n0 = 1..N-1 (n0 = 1 next to the wall); warp wp takes n0 = 1 + wp, 1 + wp + BL_WARPS, ...
 #define CELL(n0) (p0 + (long long)(lo ? (n0) : N - (n0)) * sn)
     // pass 1: wall shear, taken as the largest |omega * mu_l| along the line
@@ -120,19 +167,18 @@ __global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, PhysW<T> PC, Geo 
     // pass 2: largest speed, and F = y |omega| (1 - exp(-y+/A+)) with its first maximiser
     T Fmax = (T)0, ymax = (T)0, Udif = (T)0;
     int nmax = 0x7fffffff;
-    // wall distance and van Driest damping of this thread's first BL_CACHE points, reused by pass 3
-    T c_dis[BL_CACHE], c_damp[BL_CACHE];
+    // van Driest damping of this thread's first BL_CACHE points, reused by pass 3
+    T c_damp[BL_CACHE];
     if (live) {
         int ci = 0;
         for (int n0 = 1 + wp; n0 < N; n0 += BL_WARPS, ci++) {
             const long long p = CELL(n0);
-            const T dx = (T)(G.cc[0][p] - fx), dy = (T)(G.cc[1][p] - fy), dz = (T)(G.cc[2][p] - fz);
-            const T dis = tsqrt(dx * dx + dy * dy + dz * dz);
+            const T dis = DIST(n0);
             const T u = W.pv[PU][p], v = W.pv[PV][p], w = W.pv[PW][p];
             const T V = tsqrt(u * u + v * v + w * w);
             if (V > Udif) Udif = V;
             const T damp = (T)1 - exp(-(dis * Ret) / Aplus);
-            if (ci < BL_CACHE) { c_dis[ci] = dis; c_damp[ci] = damp; }
+            if (ci < BL_CACHE) c_damp[ci] = damp;
             const T F = dis * tabs(W.omega[p]) * damp;
             if (F > Fmax) { Fmax = F; ymax = dis; nmax = n0; }
         }
@@ -164,15 +210,8 @@ __global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, PhysW<T> PC, Geo 
     int ci = 0;
     for (int n0 = 1 + wp; n0 < N; n0 += BL_WARPS, ci++) {
         const long long p = CELL(n0);
-        T dis, damp;
-        if (ci < BL_CACHE) {
-            dis = c_dis[ci];
-            damp = c_damp[ci];
-        } else {
-            const T dx = (T)(G.cc[0][p] - fx), dy = (T)(G.cc[1][p] - fy), dz = (T)(G.cc[2][p] - fz);
-            dis = tsqrt(dx * dx + dy * dy + dz * dz);
-            damp = (T)1 - exp(-(Ret * dis) / Aplus);
-        }
+        const T dis = DIST(n0);
+        const T damp = ci < BL_CACHE ? c_damp[ci] : (T)1 - exp(-(Ret * dis) / Aplus);
         const T bL = kap * dis * damp;
         const T om = W.omega[p], rho = W.pv[PD][p];
         const T m_in = rho * bL * bL * om;
@@ -191,6 +230,7 @@ __global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, PhysW<T> PC, Geo 
         else { const T old = W.mut[p]; W.mut[p] = (old < mt) ? old : mt; }
     }
 #undef CELL
+#undef DIST
 }
 
 // ghost mu_t mirrored across every wall face (source/WallFlux.cpp:106-109,137-140,168-171)
@@ -303,7 +343,8 @@ void launch_cell_stages(const LaunchCtx &ctx, const Phys &P, const PhysW<T> &PC,
             if (n <= 0) continue;
             // 32 lines per block, the points of each line split over BL_WARPS warps
             dim3 g((unsigned)((bc.wall_slot_lines[q] + 31) / 32), n);
-            k_bl<T><<<g, 32 * BL_WARPS, 0, ctx.stream>>>(B, PC, G, W, bc.wall, bc.wall_slot_off[q]);
+            k_bl<T><<<g, 32 * BL_WARPS, 0, ctx.stream>>>(B, PC, W, bc.wall, bc.wall_slot_off[q], bc.wall_dist_off,
+                                                         (const T *)bc.wall_dist);
         }
     }
     if (bc.n_wall > 0) {

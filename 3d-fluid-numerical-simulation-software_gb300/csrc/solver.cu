@@ -55,6 +55,7 @@ struct Level {
     Geo G{};
     GeoW<T> GW{};                         // working-precision geometry (aliases in FP64, FP32 copies in mixed)
     DevBuf geow_mem;
+    DevBuf wdist_mem;                     // Baldwin-Lomax wall distances (fine level)
     Flow<T> W{};
     double *totalvol = nullptr;
     BcTables bc;
@@ -448,6 +449,7 @@ public:
         build_planes(l);
         launch_geometry(ctx(l), G, Lv.totalvol);
         build_geometry_working(l);
+        build_wall_distances(l);
         launch_sweep_geometry<T>(ctx(l), G, Lv.planes, Lv.sweep);
         {
             const int v = tune_sweep_cpw<T>(ctx(l), PC, Lv.planes, Lv.sweep);
@@ -456,6 +458,32 @@ public:
         }
         CK(cudaStreamSynchronize(stream));
         CK(cudaGetLastError());
+    }
+
+    // Baldwin-Lomax wall distances of the fine level (constant geometry, computed once)
+    void build_wall_distances(int l)
+    {
+        Level<T> &Lv = lev[l];
+        BcTables &bc = Lv.bc;
+        if (l != 1 || !P.turb_bl || bc.n_wall == 0) return;
+        std::vector<long long> off(bc.n_wall);
+        long long tot = 0;
+        for (int w = 0; w < bc.n_wall; w++) {
+            const DevWall &wl = Lv.walls_h[w];
+            const Lvl &v = Lv.lv[wl.solve];
+            const int dirn = (wl.face - 1) / 2;
+            const long long lines = (long long)(wl.ie - wl.is + 1) * (wl.je - wl.js + 1) * (wl.ke - wl.ks + 1);
+            const int N = dirn == 0 ? v.IM : (dirn == 1 ? v.JM : v.KM);
+            off[w] = tot;
+            tot += lines * (N - 1);
+        }
+        const size_t ob = (sizeof(long long) * off.size() + 255) & ~(size_t)255;
+        Lv.wdist_mem.bytes = ob + sizeof(T) * (size_t)tot;
+        CK(cudaMalloc(&Lv.wdist_mem.p, Lv.wdist_mem.bytes));
+        CK(cudaMemcpy(Lv.wdist_mem.p, off.data(), sizeof(long long) * off.size(), cudaMemcpyHostToDevice));
+        bc.wall_dist_off = (const long long *)Lv.wdist_mem.p;
+        bc.wall_dist = (char *)Lv.wdist_mem.p + ob;
+        launch_wall_distances<T>(ctx(l), Lv.G, bc);
     }
 
     // geometry in the working precision: aliases of the FP64 arrays in the FP64 form, FP32 copies
