@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbturbo.so")
 SOURCES = ["geometry.cu", "bc.cu", "resflux_cell.cu", "resflux_face.cu", "lusgs.cu", "mg.cu", "solver.cu",
-           "capi.cu", "case_io.cpp", "noalloc.cu"]
+           "capi.cu", "case_io.cpp", "noalloc.cu", "restart_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -45,7 +45,7 @@ def _compile(src: str, verbose: bool) -> str:
         return obj
     cmd = [nvcc()] + _flags(verbose) + ["-c", path, "-o", obj]
     if src.endswith(".cpp"):
-        cmd = [nvcc(), "-x", "c++"] + _flags(False)[:] + ["-c", path, "-o", obj]
+        cmd = [nvcc(), "-x", "c++"] + _flags(False)[:] + ["-Xcompiler", "-ffp-contract=off", "-c", path, "-o", obj]
         cmd = [c for c in cmd if c not in ARCH]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -156,6 +156,23 @@ int gb_set_cv(gb_solver *h, int solve, int level, const double *cv, long n)
     return guard([&] { h->s->set_cv(solve, level, cv, n); });
 }
 
+static std::string path_or_empty(const char *p) { return p ? std::string(p) : std::string(); }
+int gb_read_restart(gb_solver *h, int solve, const char *path)
+{
+    NEED(h);
+    return guard([&] { h->s->read_restart(solve, path_or_empty(path)); });
+}
+int gb_write_restart(gb_solver *h, int solve, const char *path)
+{
+    NEED(h);
+    return guard([&] { h->s->write_restart(solve, path_or_empty(path)); });
+}
+int gb_write_solution(gb_solver *h, int solve, const char *path)
+{
+    NEED(h);
+    return guard([&] { h->s->write_solution(solve, path_or_empty(path)); });
+}
+
 int gb_sync(gb_solver *h)
 {
     NEED(h);

@@ -268,7 +268,6 @@ void validate(const CaseSpec &c)
     if (c.turb != 0 && c.turb != 100)
         throw std::runtime_error("turbulence model " + std::to_string(c.turb) + " is not on this path (none 0, Baldwin-Lomax 100)");
     if (c.irs) throw std::runtime_error("implicit residual smoothing is not on this path");
-    if (c.restart) throw std::runtime_error("restart from RestartSolution.dat is not supported by this reader");
     if (!c.turbo_axial) throw std::runtime_error("only the axial outlet is on this path");
     if (c.use_mg && c.coarse_iter < 1)
         throw std::runtime_error("multigrid needs at least one coarse-grid iteration (the fine level is initialised from it)");

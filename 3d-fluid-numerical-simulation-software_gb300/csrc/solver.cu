@@ -3,6 +3,7 @@
 // source/ComputeAllBlockVars.cpp:223-255) as kernel launches on one stream, replayed through
 // CUDA graphs.
 #include "solver.hpp"
+#include "restart_io.hpp"
 #include <cmath>
 #include <cstring>
 #include <atomic>
@@ -189,6 +190,8 @@ public:
     Level<T> lev[3];
     DevBuf st_mem, scratch_mem;
     PhysW<T> PC{};                        // physical constants in the working precision
+    NonDim nd_ref{};                      // reference scales of the batch (shared gas and inlet options)
+    bool reuse = false;                   // the cases start from a restart file (config "use previous solution")
     SolveState *st_d = nullptr;
     int *bad_list = nullptr, *bad_count = nullptr;
     const int bad_cap = 4096;
@@ -303,6 +306,7 @@ public:
             if (c.ng != c0.ng || c.coarse_iter != c0.coarse_iter || c.scheme != c0.scheme || c.recon != c0.recon ||
                 c.recon_var != c0.recon_var || c.turb != c0.turb || c.equation_ns != c0.equation_ns ||
                 c.limiter != c0.limiter || c.global_dt != c0.global_dt || c.Gamma != c0.Gamma || c.Rgas != c0.Rgas ||
+                c.restart != c0.restart ||
                 c.Pr_lam != c0.Pr_lam || c.Pr_tur != c0.Pr_tur || c.Ptin != c0.Ptin || c.Ttin != c0.Ttin ||
                 c.Len_ref != c0.Len_ref || c.relax != c0.relax || c.C_timestep != c0.C_timestep ||
                 std::memcmp(c.inlet_dir, c0.inlet_dir, sizeof c.inlet_dir) != 0)
@@ -310,7 +314,9 @@ public:
         }
         ng = c0.ng;
         coarse_iter = c0.coarse_iter;
+        reuse = c0.restart;
         NonDim nd0 = nondimensionalise(c0);
+        nd_ref = nd0;
         P.gamma = c0.Gamma; P.rgas = nd0.rgas; P.pr_lam = c0.Pr_lam; P.pr_tur = c0.Pr_tur; P.re_ref = nd0.re_ref;
         P.ptin = nd0.ptin; P.ttin = nd0.ttin; P.dens_ref = nd0.dens_ref; P.vel_ref = nd0.vel_ref; P.temp_ref = nd0.temp_ref;
         for (int d = 0; d < 3; d++) P.inlet_dir[d] = c0.inlet_dir[d];
@@ -818,8 +824,8 @@ public:
     void step_body()
     {
         if (ng == 1) { time_marching(1); res_calculate(1); return; }
-        if (iter < coarse_iter) { time_marching(2); res_calculate(2); }
-        else if (iter == coarse_iter) {
+        if (!reuse && iter < coarse_iter) { time_marching(2); res_calculate(2); }
+        else if (!reuse && iter == coarse_iter) {
             time_marching(2); res_calculate(2); corner_treatment(2);
             interpolate(1); primitive_vars(1); limit_vars(1);
         } else {
@@ -836,7 +842,14 @@ public:
         }
     }
     int report_level() const { return (ng != 1 && iter <= coarse_iter) ? 2 : 1; }
-    int phase() const { return ng == 1 ? 0 : (iter < coarse_iter ? 1 : (iter == coarse_iter ? -1 : 2)); }
+    // driver phase: single grid; coarse-only start-up; the start-up's last cycle (eager); FAS. A
+    // restarted multigrid run goes straight to FAS cycles (source/Solver.cpp:67-140)
+    int phase() const
+    {
+        if (ng == 1) return 0;
+        if (reuse) return 2;
+        return iter < coarse_iter ? 1 : (iter == coarse_iter ? -1 : 2);
+    }
 
     void solver_step() override
     {
@@ -1006,6 +1019,79 @@ public:
             return cnt;
         }
         return -1;
+    }
+
+    // ---- the reference's solution files (source/Ouput.cpp:109-259, source/UserInput.cpp:1118-1159)
+    std::string default_path(int solve, const std::string &path, const char *name) const
+    {
+        return path.empty() ? cases[solve].dir + "/" + name : path;
+    }
+    void fine_state(int solve, std::vector<double> &pv, std::vector<double> &cv, std::vector<double> *mut)
+    {
+        const Lvl &v = lev[1].lv[solve];
+        const size_t nb = (size_t)(v.IM + 1) * (v.JM + 1) * (v.KM + 1);
+        pv.resize(nb * 6);
+        cv.resize(nb * 5);
+        if (get_field(solve, 1, "pv", pv.data(), (long)pv.size()) < 0 || get_field(solve, 1, "cv", cv.data(), (long)cv.size()) < 0)
+            throw std::runtime_error("state download failed");
+        if (mut) {
+            mut->resize(nb);
+            if (get_field(solve, 1, "mut", mut->data(), (long)mut->size()) < 0) throw std::runtime_error("state download failed");
+        }
+    }
+    void write_restart(int solve, const std::string &path) override
+    {
+        if (solve < 0 || solve >= nsolve) throw std::runtime_error("bad solve");
+        const Lvl &v = lev[1].lv[solve];
+        std::vector<double> pv, cv;
+        fine_state(solve, pv, cv, nullptr);
+        write_restart_file(default_path(solve, path, "RestartSolution.dat"), v.IM, v.JM, v.KM, pv.data(), cv.data());
+    }
+    void write_solution(int solve, const std::string &path) override
+    {
+        if (solve < 0 || solve >= nsolve) throw std::runtime_error("bad solve");
+        const Lvl &v = lev[1].lv[solve];
+        std::vector<double> pv, cv, mut;
+        fine_state(solve, pv, cv, &mut);
+        const CaseSpec &c = cases[solve];
+        SolutionScales sc;
+        sc.gamma = P.gamma; sc.rgas = P.rgas;
+        sc.len_ref = c.Len_ref; sc.dens_ref = nd_ref.dens_ref; sc.vel_ref = nd_ref.vel_ref; sc.temp_ref = nd_ref.temp_ref;
+        sc.mue_ref = nd_ref.mue_ref; sc.re_ref = nd_ref.re_ref;
+        sc.w_rot = lev[1].sc[solve].w_rot; sc.delta_th = lev[1].sc[solve].delta_th;
+        write_solution_file(default_path(solve, path, "RelativeSolution.plt"), v.IM, v.JM, v.KM, c.x.data(), c.y.data(),
+                            c.z.data(), pv.data(), mut.data(), sc);
+    }
+    void read_restart(int solve, const std::string &path) override
+    {
+        if (solve < 0 || solve >= nsolve) throw std::runtime_error("bad solve");
+        const Lvl &v = lev[1].lv[solve];
+        const size_t n = (size_t)(v.IM - 1) * (v.JM - 1) * (v.KM - 1);
+        std::vector<double> cv(n * 5), pv(n * 6);
+        read_restart_file(default_path(solve, path, "RestartSolution.dat"), v.IM, v.JM, v.KM, cv.data(), pv.data());
+        // Q and the primitive variables exactly as read (CUserInput::ReadSolution sets both)
+        CK(cudaStreamSynchronize(stream));
+        const long long bn = box_size(v.IM, v.JM, v.KM);
+        Lvl z = v; z.base = 0;
+        Flow<T> &W = lev[1].W;
+        for (int c = 0; c < 5; c++) {
+            std::vector<double> h((size_t)bn);
+            CK(cudaMemcpy(h.data(), W.cv[c] + v.base, sizeof(double) * bn, cudaMemcpyDeviceToHost));
+            size_t q = c;
+            for (int i = 1; i <= v.IM - 1; i++)
+                for (int j = 1; j <= v.JM - 1; j++)
+                    for (int k = 1; k <= v.KM - 1; k++, q += 5) h[(size_t)ix(z, i, j, k)] = cv[q];
+            CK(cudaMemcpy(W.cv[c] + v.base, h.data(), sizeof(double) * bn, cudaMemcpyHostToDevice));
+        }
+        for (int c = 0; c < 6; c++) {
+            std::vector<T> h((size_t)bn);
+            CK(cudaMemcpy(h.data(), W.pv[c] + v.base, sizeof(T) * bn, cudaMemcpyDeviceToHost));
+            size_t q = c;
+            for (int i = 1; i <= v.IM - 1; i++)
+                for (int j = 1; j <= v.JM - 1; j++)
+                    for (int k = 1; k <= v.KM - 1; k++, q += 6) h[(size_t)ix(z, i, j, k)] = (T)pv[q];
+            CK(cudaMemcpy(W.pv[c] + v.base, h.data(), sizeof(T) * bn, cudaMemcpyHostToDevice));
+        }
     }
 
     void set_cv(int solve, int l, const double *in, long n) override

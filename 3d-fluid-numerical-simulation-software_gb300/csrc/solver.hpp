@@ -47,6 +47,11 @@ public:
     virtual void dims(int solve, int level, int out[4]) const = 0;
     virtual long get_field(int solve, int level, const std::string &name, double *out, long cap) = 0;
     virtual void set_cv(int solve, int level, const double *in, long n) = 0;
+    // the reference's solution files for one solve (fine level): RestartSolution.dat in and out,
+    // RelativeSolution.plt out; an empty path means the file of that name in the case directory
+    virtual void read_restart(int solve, const std::string &path) = 0;
+    virtual void write_restart(int solve, const std::string &path) = 0;
+    virtual void write_solution(int solve, const std::string &path) = 0;
     virtual void states(SolveState *out) = 0;
     virtual void set_use_force(int level, bool on) = 0;
     // block shape the sweep autotuner chose for a level: cells per warp, warps per block

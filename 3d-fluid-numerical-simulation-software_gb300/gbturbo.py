@@ -55,6 +55,9 @@ def load() -> ctypes.CDLL:
         "gb_get_field": ([vp, ip, ip, ctypes.c_char_p, dp, ctypes.c_long], ctypes.c_long),
         "gb_set_cv": ([vp, ip, ip, dp, ctypes.c_long], ip),
         "gb_sync": ([vp], ip),
+        "gb_read_restart": ([vp, ip, ctypes.c_char_p], ip),
+        "gb_write_restart": ([vp, ip, ctypes.c_char_p], ip),
+        "gb_write_solution": ([vp, ip, ctypes.c_char_p], ip),
         "gb_set_graphs": ([vp, ip], ip),
         "gb_sweep_tuning": ([vp, ip, ctypes.POINTER(ip)], ip),
         "gb_profile_begin": ([vp], ip),
@@ -75,7 +78,8 @@ EXPORTED = ["gb_solver_create", "gb_solver_destroy", "gb_last_error", "gb_dims",
             "gb_corner_treatment", "gb_restrict", "gb_interpolate", "gb_delta_cons", "gb_set_use_force",
             "gb_solver_step", "gb_integrals", "gb_iterate", "gb_get_status", "gb_get_field", "gb_set_cv",
             "gb_sync", "gb_set_graphs", "gb_timer_start", "gb_timer_stop", "gb_profile_begin", "gb_profile_end",
-            "gb_res_calculate_noalloc", "gb_sweep_tuning"]
+            "gb_res_calculate_noalloc", "gb_sweep_tuning", "gb_read_restart", "gb_write_restart",
+            "gb_write_solution"]
 
 
 class GBError(RuntimeError):
@@ -229,6 +233,16 @@ class Solver:
     def set_cv(self, cv: np.ndarray, solve: int = 0, level: int = 1) -> None:
         a = np.ascontiguousarray(cv, dtype=np.float64).ravel()
         self._ck(self._L.gb_set_cv(self.h, solve, level, _dp(a), a.size))
+
+    # ---- the reference's solution files (a None path: the file in the solve's case directory)
+    def read_restart(self, solve: int = 0, path: Optional[str] = None) -> None:
+        self._ck(self._L.gb_read_restart(self.h, solve, path.encode() if path else None))
+
+    def write_restart(self, solve: int = 0, path: Optional[str] = None) -> None:
+        self._ck(self._L.gb_write_restart(self.h, solve, path.encode() if path else None))
+
+    def write_solution(self, solve: int = 0, path: Optional[str] = None) -> None:
+        self._ck(self._L.gb_write_solution(self.h, solve, path.encode() if path else None))
 
     def sync(self) -> None:
         self._ck(self._L.gb_sync(self.h))

@@ -83,6 +83,18 @@ long gb_get_field(gb_solver *h, int solve, int level, const char *name, double *
 /* overwrites the interior conserved variables (IM-1,JM-1,KM-1,5) and the primitive variables */
 int gb_set_cv(gb_solver *h, int solve, int level, const double *cv, long n);
 
+/* The reference's solution files for one solve (fine level). A NULL path means the file of that
+ * name in the solve's case directory.
+ * gb_read_restart: CUserInput::ReadSolution (source/UserInput.cpp:1118-1159): reads
+ *   RestartSolution.dat and sets Q and the primitive variables as read; it takes the place of
+ *   gb_init_uniform for cases whose config asks for the previous solution, for which the driver
+ *   runs full multigrid cycles from the first iteration (source/Solver.cpp:113-138).
+ * gb_write_restart: COutput::OutputRestartSolution (source/Ouput.cpp:227-259).
+ * gb_write_solution: COutput::OutputSolution (source/Ouput.cpp:109-225), RelativeSolution.plt. */
+int gb_read_restart(gb_solver *h, int solve, const char *path);
+int gb_write_restart(gb_solver *h, int solve, const char *path);
+int gb_write_solution(gb_solver *h, int solve, const char *path);
+
 /* waits for the handle's stream */
 int gb_sync(gb_solver *h);
 /* block shape of the LU-SGS sweep kernels on a level: out[0] cells per warp, out[1] warps per

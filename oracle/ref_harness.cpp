@@ -7,7 +7,7 @@
 // the hot path produces as .npy files so that the CPU oracle and the GPU path can be compared
 // against the reference itself.
 //
-//   ref_harness <n_iter> <out_dir> [dump_resflux=1]
+//   ref_harness <n_iter> <out_dir> [dump_resflux=1] [write_outputs=0]
 //
 // run from a directory holding config.dat, BoundaryDefinition.dat and the grid file.
 // This file is compiled with -Dprivate=public to read members the reference keeps private.
@@ -172,10 +172,11 @@ static void dump_resflux(CMesh &M, const std::string &p)
 
 int main(int argc, char **argv)
 {
-    if (argc < 3) { fprintf(stderr, "usage: ref_harness n_iter out_dir [dump_resflux]\n"); return 2; }
+    if (argc < 3) { fprintf(stderr, "usage: ref_harness n_iter out_dir [dump_resflux] [write_outputs]\n"); return 2; }
     int n_iter = atoi(argv[1]);
     g_out = argv[2];
     int dump_rf = argc > 3 ? atoi(argv[3]) : 1;
+    int write_out = argc > 4 ? atoi(argv[4]) : 0;      // the reference's solution and restart files
     mkdir(g_out.c_str(), 0755);
 
     CSolver Solver;
@@ -187,7 +188,10 @@ int main(int argc, char **argv)
     for (int i = 1; i <= Solver.NG; i++) Solver.Mesh[i].AllocateMemory();
     if (Solver.NG == 2) Solver.Mesh[2].AllocateMemory_Pro_Inter_Vars();
     for (int i = 1; i <= Solver.NG; i++) Solver.Mesh[i].Geometry();
-    if (Solver.NG == 1) Solver.Mesh[1].Initial();
+    // start: uniform field, or the reference's restart file when the case asks for it
+    // (source/Structured_FV3D.cpp:86-102)
+    if (Solver.reUseSolution) CUserInput::ReadSolution(Solver.Mesh[1]);
+    else if (Solver.NG == 1) Solver.Mesh[1].Initial();
     else Solver.Mesh[2].Initial();
 
     dump_geometry(Solver.Mesh[1], "g1_");
@@ -212,6 +216,11 @@ int main(int argc, char **argv)
         if (Solver.Res.dens <= Solver.ConvTol && Solver.MassFlow_ratio <= 0.003) break;
     }
     npy_write("history", hist, {(size_t)done, 12});
+    if (write_out) {
+        // RelativeSolution.plt and RestartSolution.dat in the working directory (source/Ouput.cpp:109-259)
+        COutput::OutputSolution(Solver.Mesh[1]);
+        COutput::OutputRestartSolution(Solver.Mesh[1]);
+    }
     dump_state(Solver.Mesh[1], "s1_");
     if (Solver.NG == 2) dump_state(Solver.Mesh[2], "s2_");
     if (dump_rf) {

@@ -9,7 +9,8 @@ evaluation at that state (every intermediate array) in tests/golden/<name>.npz.
 Only runs where the reference sources and a C++ compiler exist; the fixtures it writes are
 committed so the tests need neither.
 
-    python tests/golden/make_golden.py [name ...]      (default: every short case; long cases by name)
+    python tests/golden/make_golden.py [name ...]      (default: every short case and the restart case;
+                                                        long cases by name)
 """
 from __future__ import annotations
 
@@ -54,6 +55,13 @@ LONG = {
     "duct_33x33x65_2000": ("annular_duct", dict(IM=33, JM=33, KM=65), {}, 2000),
 }
 
+# restart round trip: the reference runs n1 iterations and writes its solution and restart files,
+# then a second run of the same case with "use previous solution" reads the restart file and runs
+# n2 more; both case directories are kept (the second holds the restart file it starts from)
+RESTART = {
+    "rotor_9x9x33_restart": ("rotor_passage", dict(IM=9, JM=9, KM=33), {}, 10, 10),
+}
+
 KEEP_R = ["cv", "pv", "mut", "omega", "lamcI", "lamcJ", "lamcK", "lamvI", "lamvJ", "lamvK", "dt", "FcI", "FcJ",
           "FcK", "FvI", "FvJ", "FvK", "res", "dIS_pv", "dIP_pv", "dJS_pv", "dJP_pv", "dKS_pv", "dKP_pv", "dIS_cv",
           "dKP_cv"]
@@ -72,7 +80,40 @@ def make_long(name: str) -> None:
     print(name, "iterations:", int(hist.shape[0]))
 
 
+def make_restart(name: str) -> None:
+    mg = _meshgen()
+    gen, kw, opts, n1, n2 = RESTART[name]
+    cdir, rdir = os.path.join(HERE, name), os.path.join(HERE, name + "_reuse")
+    for d in (cdir, rdir):
+        if os.path.isdir(d):
+            shutil.rmtree(d)
+    mg.write_case(getattr(mg, gen)(**kw, options=dict(opts), name=name), cdir)
+    mg.write_case(getattr(mg, gen)(**kw, options=dict(opts, restart="Y"), name=name), rdir)
+    data = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for f in os.listdir(cdir):
+            shutil.copy(os.path.join(cdir, f), tmp)
+        out = os.path.join(tmp, "out")
+        subprocess.run([HARNESS, str(n1), out, "0", "1"], cwd=tmp, check=True, stdout=subprocess.DEVNULL)
+        data["history1"] = np.load(os.path.join(out, "history.npy"))
+        for key, f in (("restart_file", "RestartSolution.dat"), ("solution_file", "RelativeSolution.plt")):
+            data[key] = np.frombuffer(open(os.path.join(tmp, f), "rb").read(), dtype=np.uint8)
+        shutil.copy(os.path.join(tmp, "RestartSolution.dat"), rdir)
+    with tempfile.TemporaryDirectory() as tmp:
+        for f in os.listdir(rdir):
+            shutil.copy(os.path.join(rdir, f), tmp)
+        out = os.path.join(tmp, "out")
+        subprocess.run([HARNESS, str(n2), out, "0"], cwd=tmp, check=True, stdout=subprocess.DEVNULL)
+        data["history2"] = np.load(os.path.join(out, "history.npy"))
+        data["s1_cv"] = np.load(os.path.join(out, "s1_cv.npy"))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **data)
+    print(name, "iterations:", n1, "+", n2)
+
+
 def make(name: str) -> None:
+    if name in RESTART:
+        make_restart(name)
+        return
     if name in LONG:
         make_long(name)
         return
@@ -108,5 +149,5 @@ def make(name: str) -> None:
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: oracle/build_ref.sh")
-    for n in (sys.argv[1:] or list(CASES)):
+    for n in (sys.argv[1:] or list(CASES) + list(RESTART)):
         make(n)
