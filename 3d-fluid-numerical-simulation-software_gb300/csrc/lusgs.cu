@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
             ve = S.gve[d][nb];
             od = S.cv[0][nb]; omx = S.cv[1][nb]; omy = S.cv[2][nb]; omz = S.cv[3][nb]; oe = S.cv[4][nb];
             const T po = S.pp[nb];
-            const T oinv = (T)1 / od;
+            const T oinv = rcp_nr(od);
             const T Vo = omx * oinv * nx + omy * oinv * ny + omz * oinv * nz;
             const T dov = Vo - ve;
             fo[0] = od * dov;
@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
         if (d == 0) {
             alpha = S.gvol[q] / S.dt[q] + P.relax * (S.lamc[0][q] + S.lamc[1][q] + S.lamc[2][q]) +
                     (T)2 * (S.lamv[0][q] + S.lamv[1][q] + S.lamv[2][q]);
-            inva = (T)1 / alpha;
+            inva = rcp_nr(alpha);
             if (DIR > 0) {
 #pragma unroll
                 for (int c = 0; c < 5; c++) rhs[c] = -S.res[c][q];
@@ -81,13 +81,15 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
         T dqn[5];
 #pragma unroll
         for (int c = 0; c < 5; c++) dqn[c] = S.dq[c][nb];
-        // flux difference F_n(Q+dQ) - F_n(Q) of the neighbour across its mean normal
+        // flux difference F_n(Q+dQ) - F_n(Q) of the neighbour across its mean normal. The momentum
+        // projections and |m|^2 are formed while the reciprocal of the density is computed, so that
+        // only V_n = (m.n)/rho and p = (g-1)(rho E - |m|^2/(2 rho)) follow it on the plane-to-plane
+        // critical path (the same quantities as the reference's u = m_x/rho, ..., regrouped).
         const T nd = od + dqn[0], nmx = omx + dqn[1], nmy = omy + dqn[2], nmz = omz + dqn[3], ne = oe + dqn[4];
-        const T inv = (T)1 / nd;
-        const T u = nmx * inv, v = nmy * inv, w = nmz * inv, E = ne * inv;
-        const T pn = P.gm1 * nd * (E - (T)0.5 * (u * u + v * v + w * w));
-        const T Vn = u * nx + v * ny + w * nz;
-        const T dn = Vn - ve;
+        const T mn = nmx * nx + nmy * ny + nmz * nz, m2 = nmx * nmx + nmy * nmy + nmz * nmz;
+        const T inv = rcp_nr(nd);
+        const T pn = P.gm1 * (ne - (T)0.5 * (m2 * inv));
+        const T dn = mn * inv - ve;
         T dF[5];
         dF[0] = nd * dn - fo[0];
         dF[1] = (nmx * dn + pn * nx) - fo[1];
@@ -467,12 +469,11 @@ __global__ void __launch_bounds__(256) k_norm_partial(Batch B, Geo G, Flow<T> W,
     const int s = blockIdx.y;
     const Lvl L = B.lv[s];
     const int nI = L.IM - 1, nJ = L.JM - 1, nK = L.KM - 1;
-    const long long n = (long long)nI * nJ * nK;
+    const unsigned n = (unsigned)nI * (unsigned)nJ * (unsigned)nK;
     double acc[5] = {0, 0, 0, 0, 0};
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)nblk * blockDim.x) {
-        const int k = (int)(t % nK) + 1;
-        const long long q = t / nK;
-        const int j = (int)(q % nJ) + 1, i = (int)(q / nJ) + 1;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (unsigned)nblk * blockDim.x) {
+        const unsigned q = t / (unsigned)nK, r = q / (unsigned)nJ;
+        const int k = (int)(t - q * (unsigned)nK) + 1, j = (int)(q - r * (unsigned)nJ) + 1, i = (int)r + 1;
         const long long p = ix(L, i, j, k);
         const double vol = G.vol[p];
 #pragma unroll

@@ -79,7 +79,8 @@ __device__ __forceinline__ BlLine bl_line(const Lvl &L, const DevWall &wl, int b
     r.lines = na * nb;
     r.t = (long long)blk * 32 + lane;
     r.live = r.t < (long long)r.lines;
-    const int a = a0 + (int)(r.live ? r.t % na : 0), b = b0 + (int)(r.live ? r.t / na : 0);
+    const unsigned tq = r.live ? (unsigned)r.t / (unsigned)na : 0u;
+    const int a = a0 + (int)(r.live ? (unsigned)r.t - tq * (unsigned)na : 0u), b = b0 + (int)tq;
     r.N = r.dirn == 0 ? L.IM : (r.dirn == 1 ? L.JM : L.KM);
     r.sn = r.dirn == 0 ? (long long)L.NJ * L.NK : (r.dirn == 1 ? (long long)L.NK : 1LL);
     if (r.dirn == 0) { r.p0 = ix(L, 0, b, a); r.fw = ix(L, r.lo ? 1 : L.IM, b, a); }
@@ -290,12 +291,11 @@ __global__ void __launch_bounds__(1024) k_dt_min(Batch B, Flow<T> W, T *out)
 {
     const Lvl L = B.lv[blockIdx.y];
     const int nI = L.IM - 1, nJ = L.JM - 1, nK = L.KM - 1;
-    const long long n = (long long)nI * nJ * nK;
+    const unsigned n = (unsigned)nI * (unsigned)nJ * (unsigned)nK;
     T m = (T)1E10;
-    for (long long t = threadIdx.x; t < n; t += blockDim.x) {
-        int k = (int)(t % nK) + 1;
-        long long q = t / nK;
-        int j = (int)(q % nJ) + 1, i = (int)(q / nJ) + 1;
+    for (unsigned t = threadIdx.x; t < n; t += blockDim.x) {
+        const unsigned q = t / (unsigned)nK, r = q / (unsigned)nJ;
+        const int k = (int)(t - q * (unsigned)nK) + 1, j = (int)(q - r * (unsigned)nJ) + 1, i = (int)r + 1;
         T v = W.dt[ix(L, i, j, k)];
         m = (m < v) ? m : v;
     }
