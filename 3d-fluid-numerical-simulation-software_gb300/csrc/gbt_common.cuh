@@ -146,19 +146,6 @@ template <> __device__ __forceinline__ float tsqrt<float>(float x) { return sqrt
 // refined by one Newton-Raphson step, r1 = r0 (2 - o r0), which takes the 2^-24 relative error of
 // the seed to about 1e-14 for two FP64 fused multiply-adds instead of an FP64 division (the norm
 // sums some 1e5 such terms, so this is far below what it resolves).
-// Reciprocal in the working precision. FP64: an FP32 seed refined by two Newton-Raphson steps,
-// r <- r + r (1 - x r), each squaring the relative error (2^-24 -> ~1e-14 -> rounding), so the
-// result is within an ulp or two of 1/x with four dependent fused multiply-adds; FP32: the
-// division itself.
-__device__ __forceinline__ double rcp_nr(double x)
-{
-    double r = (double)(1.0f / (float)x);
-    r = fma(r, fma(-x, r, 1.0), r);
-    r = fma(r, fma(-x, r, 1.0), r);
-    return r;
-}
-__device__ __forceinline__ float rcp_nr(float x) { return 1.0f / x; }
-
 __device__ __forceinline__ double rel_change(double o, double c)
 {
     const double r0 = (double)(1.0f / (float)o);

@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
             ve = S.gve[d][nb];
             od = S.cv[0][nb]; omx = S.cv[1][nb]; omy = S.cv[2][nb]; omz = S.cv[3][nb]; oe = S.cv[4][nb];
             const T po = S.pp[nb];
-            const T oinv = rcp_nr(od);
+            const T oinv = (T)1 / od;
             const T Vo = omx * oinv * nx + omy * oinv * ny + omz * oinv * nz;
             const T dov = Vo - ve;
             fo[0] = od * dov;
@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
         if (d == 0) {
             alpha = S.gvol[q] / S.dt[q] + P.relax * (S.lamc[0][q] + S.lamc[1][q] + S.lamc[2][q]) +
                     (T)2 * (S.lamv[0][q] + S.lamv[1][q] + S.lamv[2][q]);
-            inva = rcp_nr(alpha);
+            inva = (T)1 / alpha;
             if (DIR > 0) {
 #pragma unroll
                 for (int c = 0; c < 5; c++) rhs[c] = -S.res[c][q];
@@ -81,15 +81,24 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
         T dqn[5];
 #pragma unroll
         for (int c = 0; c < 5; c++) dqn[c] = S.dq[c][nb];
-        // flux difference F_n(Q+dQ) - F_n(Q) of the neighbour across its mean normal. The momentum
-        // projections and |m|^2 are formed while the reciprocal of the density is computed, so that
-        // only V_n = (m.n)/rho and p = (g-1)(rho E - |m|^2/(2 rho)) follow it on the plane-to-plane
-        // critical path (the same quantities as the reference's u = m_x/rho, ..., regrouped).
+        // flux difference F_n(Q+dQ) - F_n(Q) of the neighbour across its mean normal
         const T nd = od + dqn[0], nmx = omx + dqn[1], nmy = omy + dqn[2], nmz = omz + dqn[3], ne = oe + dqn[4];
-        const T mn = nmx * nx + nmy * ny + nmz * nz, m2 = nmx * nmx + nmy * nmy + nmz * nmz;
-        const T inv = rcp_nr(nd);
-        const T pn = P.gm1 * (ne - (T)0.5 * (m2 * inv));
-        const T dn = mn * inv - ve;
+        T pn, dn;
+        if constexpr (sizeof(T) == 8) {
+            // FP64 (parity) form: the reference's sequence, u = m_x / rho, ...
+            const T inv = (T)1 / nd;
+            const T u = nmx * inv, v = nmy * inv, w = nmz * inv, E = ne * inv;
+            pn = P.gm1 * nd * (E - (T)0.5 * (u * u + v * v + w * w));
+            dn = (u * nx + v * ny + w * nz) - ve;
+        } else {
+            // mixed form: the momentum projection and |m|^2 are formed while the reciprocal of the
+            // density is computed, so that only V_n = (m.n)/rho and p = (g-1)(rho E - |m|^2/(2 rho))
+            // follow it on the plane-to-plane critical path (the same quantities, regrouped)
+            const T mn = nmx * nx + nmy * ny + nmz * nz, m2 = nmx * nmx + nmy * nmy + nmz * nmz;
+            const T inv = (T)1 / nd;
+            pn = P.gm1 * (ne - (T)0.5 * (m2 * inv));
+            dn = mn * inv - ve;
+        }
         T dF[5];
         dF[0] = nd * dn - fo[0];
         dF[1] = (nmx * dn + pn * nx) - fo[1];
