@@ -94,6 +94,8 @@ void launch_lusgs_sweeps(const LaunchCtx &ctx, const PhysW<T> &P, Flow<T> F, con
 
 // fastest block shape of the sweep kernels for this level, as cells_per_warp * 16 + warps_per_block
 // (times the plane chains on benign inputs in the plane-order scratch; synchronises the stream)
+// whether (cells per warp, warps per block) is one of the compiled sweep shapes
+bool sweep_shape_known(int cpw, int wpb);
 template <typename T>
 int tune_sweep_cpw(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneTables &pt, const SweepData<T> &S);
 

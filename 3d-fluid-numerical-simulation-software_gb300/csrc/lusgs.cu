@@ -195,6 +195,13 @@ static void launch_plane_v(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneT
 struct SweepShape { int cpw, wpb; };
 constexpr SweepShape kSweepShapes[] = {{1, 1}, {2, 1}, {4, 1}, {10, 1}, {4, 4}, {10, 4}, {10, 8}};
 
+bool sweep_shape_known(int cpw, int wpb)
+{
+    for (const SweepShape &sh : kSweepShapes)
+        if (sh.cpw == cpw && sh.wpb == wpb) return true;
+    return false;
+}
+
 template <typename T, int DIR>
 static void launch_plane(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneTables &pt, const SweepData<T> &S, int pl,
                          bool first)

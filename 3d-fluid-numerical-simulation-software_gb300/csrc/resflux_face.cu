@@ -52,7 +52,7 @@ __device__ __forceinline__ T tan_diff(const T *__restrict__ c, long long p, long
 // MODE 1 is the default scheme (MUSCL3 on primitive variables, Roe) with the option switches
 // resolved at compile time; MODE 0 reads them from P
 template <typename T, int F, int MODE>
-__global__ void __launch_bounds__(128) k_face(Batch B, Phys P, PhysW<T> PC, GeoW<T> G, Flow<T> W, const DevWall *walls)
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 4) k_face(Batch B, Phys P, PhysW<T> PC, GeoW<T> G, Flow<T> W, const DevWall *walls)
 {
     const int recon_var = MODE ? 200 : P.recon_var, recon = MODE ? 500 : P.recon, scheme = MODE ? 300 : P.scheme;
     const int s = blockIdx.y;

@@ -6,6 +6,8 @@
 #include "restart_io.hpp"
 #include <cmath>
 #include <cstring>
+#include <cstdio>
+#include <cstdlib>
 #include <atomic>
 #include <exception>
 #include <thread>
@@ -458,9 +460,22 @@ public:
         build_wall_distances(l);
         launch_sweep_geometry<T>(ctx(l), G, Lv.planes, Lv.sweep);
         {
-            const int v = tune_sweep_cpw<T>(ctx(l), PC, Lv.planes, Lv.sweep);
-            Lv.planes.cpw = v / 16;
-            Lv.planes.wpb = v % 16;
+            // block shape of the sweep kernels: GBTURBO_SWEEP_SHAPE="cpw,wpb" pins it; batches of
+            // four or more solves time the candidates; smaller ones, where the candidates are within
+            // run-to-run noise of each other, take ten cells per one-warp block
+            int cpw = 10, wpb = 1;
+            const char *pin = std::getenv("GBTURBO_SWEEP_SHAPE");
+            if (pin && std::sscanf(pin, "%d,%d", &cpw, &wpb) == 2 && sweep_shape_known(cpw, wpb)) {
+            } else if (nsolve >= 4) {
+                const int v = tune_sweep_cpw<T>(ctx(l), PC, Lv.planes, Lv.sweep);
+                cpw = v / 16;
+                wpb = v % 16;
+            } else {
+                cpw = 10;
+                wpb = 1;
+            }
+            Lv.planes.cpw = cpw;
+            Lv.planes.wpb = wpb;
         }
         CK(cudaStreamSynchronize(stream));
         CK(cudaGetLastError());
