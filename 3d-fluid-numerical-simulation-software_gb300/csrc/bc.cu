@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(32) k_outlet_march(Batch B, Geo G, Flow<T> W, 
     if (j > L.JM - 1) return;
     const double *cu = cu_all + (long long)blockIdx.y * cu_stride;
     const int iref = (int)(0.5 * IM);
-    const double pout = B.sc[pt.solve].pout;
+    const double pout = B.st[pt.solve].pout;
     if (lane == 0) W.pv[PP][ix(L, iref, j, KM)] = (T)pout;
     // towards the hub: i = iref-1, iref-2, ..., 1
     double carry = 0.0;

@@ -120,6 +120,15 @@ int gb_integrals(gb_solver *h, int level, double *out)
     });
 }
 
+int gb_mass_flow_imposed(gb_solver *h) { NEED(h); return guard([&] { h->s->mass_flow_imposed(); }); }
+
+int gb_get_outlet_pressure(gb_solver *h, double *out)
+{
+    NEED(h);
+    if (!out) { g_err = "null buffer"; return GB_ERR_ARG; }
+    return guard([&] { h->s->outlet_pressure(out); });
+}
+
 int gb_iterate(gb_solver *h, int n, double *hist)
 {
     NEED(h);

@@ -112,7 +112,13 @@ void read_config(CaseSpec &c)
     }
     r.next();
     c.mass_imposed = is_yes(r.next());
-    r.next();
+    {
+        // read with the stream as the reference does (source/UserInput.cpp:80), not through stof
+        std::istringstream is(r.next());
+        is >> c.m_imposed >> c.relax_press >> c.iter_mass_imp >> c.resc_mass_imp;
+        if (c.mass_imposed && (!is || c.m_imposed <= 0.0 || c.iter_mass_imp < 1))
+            throw std::runtime_error("config.dat: the imposed mass flow line needs a positive mass flow and an iteration step >= 1");
+    }
     r.skip(3);
     c.maxiter = as_int(r.next(), "max iterations");
     c.coarse_iter = as_int(r.next(), "coarse iterations");

@@ -28,6 +28,8 @@ struct CaseSpec {
     double Ptin = 0, Ttin = 0, Pout = 0, P21 = 0, Ma0 = 0, Len_ref = 0, ev_ratio = 0;
     double inlet_dir[3] = {0, 0, 1};
     bool mass_imposed = false;
+    double m_imposed = 0.0, relax_press = 0.0, resc_mass_imp = 0.0;   // imposed mass flow [kg/s], relaxation, residual gate
+    int iter_mass_imp = 1;                                            // iterations between back-pressure updates
     int maxiter = 0, coarse_iter = 0, outstep = 0, nt = 1;
     double convtol = 0;
     bool use_mg = false, restart = false;

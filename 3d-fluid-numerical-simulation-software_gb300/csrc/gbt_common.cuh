@@ -74,6 +74,7 @@ struct SolveState {
     int status;                                      // bit flags, see GBT_STATUS_*
     int limiter_hits;
     int pad_;
+    double pout;                                     // current nondimensional back pressure (mass-flow control moves it)
 };
 
 // Per-solve constants (copied once).
@@ -82,6 +83,9 @@ struct SolveConst {
     double delta_th;                                 // periodic pitch angle (sign as used)
     double pout;                                     // nondimensional back pressure
     double nblade;
+    // imposed mass flow (source/Solver.cpp:142-145, source/Structured_FV3D.cpp:186-193)
+    double m_imposed, relax_press, resc_mass_imp;
+    int iter_mass_imp, mass_imposed;
 };
 
 // Global (per handle) physical constants, in the reference's nondimensional units.

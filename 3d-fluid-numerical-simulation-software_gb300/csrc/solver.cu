@@ -171,6 +171,20 @@ __global__ void k_fill_uniform(Batch B, double *cv0, double *cv1, double *cv2, d
 }
 
 // start of a driver iteration: iteration counter and CFL ramp (source/Solver.cpp:49-60)
+// imposed mass flow after the iteration's output (source/Structured_FV3D.cpp:186-193 with
+// CSolver::MassFlowImposed, source/Solver.cpp:142-145): once the density residual is below the
+// gate and every iter_mass_imp iterations, p_out += relax * p_out * (m_out - m_imposed) / m_imposed
+__global__ void k_mass_control(Batch B)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= B.nsolve) return;
+    const SolveConst &c = B.sc[s];
+    SolveState &st = B.st[s];
+    if (!c.mass_imposed) return;
+    if (st.res[0] <= c.resc_mass_imp && st.iter % c.iter_mass_imp == 0)
+        st.pout = st.pout + c.relax_press * st.pout * (st.m_out - c.m_imposed) / c.m_imposed;
+}
+
 __global__ void k_iter_begin(Batch B)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -194,6 +208,7 @@ public:
     PhysW<T> PC{};                        // physical constants in the working precision
     NonDim nd_ref{};                      // reference scales of the batch (shared gas and inlet options)
     bool reuse = false;                   // the cases start from a restart file (config "use previous solution")
+    bool any_mass = false;                // some case imposes its mass flow through the back pressure
     SolveState *st_d = nullptr;
     int *bad_list = nullptr, *bad_count = nullptr;
     const int bad_cap = 4096;
@@ -317,6 +332,7 @@ public:
         ng = c0.ng;
         coarse_iter = c0.coarse_iter;
         reuse = c0.restart;
+        for (auto &c : cases) any_mass = any_mass || c.mass_imposed;
         NonDim nd0 = nondimensionalise(c0);
         nd_ref = nd0;
         P.gamma = c0.Gamma; P.rgas = nd0.rgas; P.pr_lam = c0.Pr_lam; P.pr_tur = c0.Pr_tur; P.re_ref = nd0.re_ref;
@@ -341,6 +357,7 @@ public:
             std::memset(&st[s], 0, sizeof(SolveState));
             st[s].cfl = cases[s].CFL;
             st[s].cfl_res = (double)1.0E-3f;
+            st[s].pout = nondimensionalise(cases[s]).pout;
         }
         CK(cudaMemcpy(st_d, st.data(), st_mem.bytes, cudaMemcpyHostToDevice));
         // scratch: limiter lists, norm partials, global-dt minima
@@ -380,6 +397,8 @@ public:
             NonDim nd = nondimensionalise(cases[s]);
             SolveConst sc;
             sc.w_rot = nd.w_rot; sc.delta_th = nd.delta_th; sc.pout = nd.pout; sc.nblade = cases[s].nblade;
+            sc.m_imposed = cases[s].m_imposed; sc.relax_press = cases[s].relax_press; sc.resc_mass_imp = cases[s].resc_mass_imp;
+            sc.iter_mass_imp = cases[s].iter_mass_imp; sc.mass_imposed = cases[s].mass_imposed ? 1 : 0;
             Lv.sc.push_back(sc);
             Lv.maxIM = std::max(Lv.maxIM, c.IM); Lv.maxJM = std::max(Lv.maxJM, c.JM); Lv.maxKM = std::max(Lv.maxKM, c.KM);
             Lv.max_plane = std::max(Lv.max_plane, c.IM + c.JM + c.KM - 3);
@@ -834,6 +853,16 @@ public:
     void need_mg() const { if (ng < 2) throw std::runtime_error("the case runs on a single grid level"); }
 
     void begin_iteration() { k_iter_begin<<<(nsolve + 127) / 128, 128, 0, stream>>>(batch(1)); }
+    void mass_flow_imposed() override
+    {
+        if (any_mass) k_mass_control<<<(nsolve + 127) / 128, 128, 0, stream>>>(batch(1));
+    }
+    void outlet_pressure(double *out) override
+    {
+        std::vector<SolveState> st(nsolve);
+        states(st.data());
+        for (int s = 0; s < nsolve; s++) out[s] = st[s].pout;
+    }
 
     // CSolver::Solver (source/Solver.cpp:47-140) for the current iteration number
     void step_body()
@@ -887,6 +916,7 @@ public:
                     begin_iteration();
                     step_body();
                     integrals(report_level());
+                    mass_flow_imposed();
                     CK(cudaStreamEndCapture(stream, &g));
                     CK(cudaGraphInstantiate(&graphs[ph], g, 0));
                     cudaGraphDestroy(g);
@@ -896,6 +926,7 @@ public:
                 begin_iteration();
                 step_body();
                 integrals(report_level());
+                mass_flow_imposed();
             }
             if (hist) {
                 CK(cudaMemcpyAsync(st.data(), st_d, sizeof(SolveState) * nsolve, cudaMemcpyDeviceToHost, stream));

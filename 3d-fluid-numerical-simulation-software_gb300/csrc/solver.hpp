@@ -42,6 +42,10 @@ public:
     virtual void delta_cons() = 0;
     virtual void integrals(int level) = 0;
     virtual void solver_step() = 0;
+    // one back-pressure update of the cases that impose their mass flow (after the integrals)
+    virtual void mass_flow_imposed() = 0;
+    // current nondimensional back pressure of every solve
+    virtual void outlet_pressure(double *out) = 0;
     // n driver iterations; hist (if not null) receives n * nsolve rows of 12 values
     virtual void iterate(int n, double *hist) = 0;
     virtual void dims(int solve, int level, int out[4]) const = 0;

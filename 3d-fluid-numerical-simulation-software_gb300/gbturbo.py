@@ -55,6 +55,8 @@ def load() -> ctypes.CDLL:
         "gb_get_field": ([vp, ip, ip, ctypes.c_char_p, dp, ctypes.c_long], ctypes.c_long),
         "gb_set_cv": ([vp, ip, ip, dp, ctypes.c_long], ip),
         "gb_sync": ([vp], ip),
+        "gb_mass_flow_imposed": ([vp], ip),
+        "gb_get_outlet_pressure": ([vp, dp], ip),
         "gb_read_restart": ([vp, ip, ctypes.c_char_p], ip),
         "gb_write_restart": ([vp, ip, ctypes.c_char_p], ip),
         "gb_write_solution": ([vp, ip, ctypes.c_char_p], ip),
@@ -79,7 +81,7 @@ EXPORTED = ["gb_solver_create", "gb_solver_destroy", "gb_last_error", "gb_dims",
             "gb_solver_step", "gb_integrals", "gb_iterate", "gb_get_status", "gb_get_field", "gb_set_cv",
             "gb_sync", "gb_set_graphs", "gb_timer_start", "gb_timer_stop", "gb_profile_begin", "gb_profile_end",
             "gb_res_calculate_noalloc", "gb_sweep_tuning", "gb_read_restart", "gb_write_restart",
-            "gb_write_solution"]
+            "gb_write_solution", "gb_mass_flow_imposed", "gb_get_outlet_pressure"]
 
 
 class GBError(RuntimeError):
@@ -243,6 +245,15 @@ class Solver:
 
     def write_solution(self, solve: int = 0, path: Optional[str] = None) -> None:
         self._ck(self._L.gb_write_solution(self.h, solve, path.encode() if path else None))
+
+    def mass_flow_imposed(self) -> None:
+        self._ck(self._L.gb_mass_flow_imposed(self.h))
+
+    def outlet_pressure(self) -> np.ndarray:
+        """current nondimensional back pressure of every solve"""
+        out = np.zeros(self.n)
+        self._ck(self._L.gb_get_outlet_pressure(self.h, _dp(out)))
+        return out
 
     def sync(self) -> None:
         self._ck(self._L.gb_sync(self.h))

@@ -95,6 +95,15 @@ int gb_read_restart(gb_solver *h, int solve, const char *path);
 int gb_write_restart(gb_solver *h, int solve, const char *path);
 int gb_write_solution(gb_solver *h, int solve, const char *path);
 
+/* Imposed mass flow (config "use flow mass outlet" and its line of imposed mass flow, relaxation,
+ * iteration step and residual gate): CSolver::MassFlowImposed with the driver's conditions
+ * (source/Solver.cpp:142-145, source/Structured_FV3D.cpp:186-193). gb_iterate applies it after
+ * every iteration's integrals; gb_mass_flow_imposed applies it once, for callers that drive
+ * gb_solver_step and gb_integrals themselves. gb_get_outlet_pressure: the current
+ * nondimensional back pressure of every solve (CBndConds::Pout). */
+int gb_mass_flow_imposed(gb_solver *h);
+int gb_get_outlet_pressure(gb_solver *h, double *out);
+
 /* waits for the handle's stream */
 int gb_sync(gb_solver *h);
 /* block shape of the LU-SGS sweep kernels on a level: out[0] cells per warp, out[1] warps per

@@ -20,6 +20,7 @@
 #include <unistd.h>
 #include "Solver.h"
 #include "Output.h"
+#include "BndConds.h"
 #include "UserInput.h"
 
 static std::string g_out;
@@ -200,6 +201,7 @@ int main(int argc, char **argv)
 
     // history rows: iter, Res.dens, Res.xmom..ener, m_in, m_out, PR, eta, m_ratio, CFL
     std::vector<double> hist;
+    std::vector<double> pout_hist;          // nondimensional back pressure used in each iteration
     int done = 0;
     for (Solver.iter = 1; Solver.iter <= n_iter; Solver.iter++) {
         Solver.Solver();
@@ -213,9 +215,15 @@ int main(int argc, char **argv)
                           (double)CTimeDiscr::CFL};
         hist.insert(hist.end(), row, row + 12);
         done++;
+        pout_hist.push_back((double)CBndConds::Pout);
+        // imposed mass flow, as the driver applies it after the output (source/Structured_FV3D.cpp:186-193)
+        if (Solver.UseFlowMassImposed == 1 && Solver.Res.dens <= Solver.resc_mass_imp &&
+            Solver.iter % Solver.iter_mass_imp == 0)
+            Solver.MassFlowImposed();
         if (Solver.Res.dens <= Solver.ConvTol && Solver.MassFlow_ratio <= 0.003) break;
     }
     npy_write("history", hist, {(size_t)done, 12});
+    npy_write("pout", pout_hist, {(size_t)done});
     if (write_out) {
         // RelativeSolution.plt and RestartSolution.dat in the working directory (source/Ouput.cpp:109-259)
         COutput::OutputSolution(Solver.Mesh[1]);

@@ -47,6 +47,9 @@ CASES = {
                                    {"recon": "200", "timestep": "G", "limiter": "N"}, 10),
     "rotor_9x9x33": ("rotor_passage", dict(IM=9, JM=9, KM=33), {}, 20),
     "rotor_9x9x33_mg": ("rotor_passage", dict(IM=9, JM=9, KM=33), {"multigrid": "Y", "coarse_iter": "5"}, 14),
+    # imposed mass flow: 25 kg/s, relaxation 0.2, every 2 iterations, residual gate 1.0
+    "rotor_9x9x33_massflow": ("rotor_passage", dict(IM=9, JM=9, KM=33),
+                              {"mass_imposed": "Y", "mass_line": "25.0 0.2 2 1.0"}, 20),
 }
 
 # long runs: only the driver history is kept, and the case is regenerated by the tests from the
