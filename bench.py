@@ -24,6 +24,8 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "3d-fluid-numerical-simulation-software_gb300")
 for _p in (PKG, os.path.join(ROOT, "oracle")):
@@ -46,15 +48,24 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the secondary measurements of the mixed-precision and batched forms")
+    ap.add_argument("--study", choices=["precision", "solves"],
+                    help="long runs instead of the benchmark line: 'precision' = the mixed form's integrals "
+                         "against the FP64 solve after 3000 cycles at three back pressures; 'solves' = "
+                         "converged solves per hour of the plain FP64 path and the batched mixed form")
+    ap.add_argument("--cycles", type=int, default=None, help="cycle cap of a study (3000 / 4000 by default)")
+    ap.add_argument("--points", type=int, default=64, help="operating points of the batched form in the solves study")
     return ap.parse_args()
 
 
-def make_cases(root: str, n: int, seed_offset: int = 0):
-    """the 129 x 49 x 49 rotor passage; in a batch the back pressure varies over [1.05, 1.30] x p_t"""
+def make_cases(root: str, n: int, seed_offset: int = 0, back_pressures=None):
+    """the 129 x 49 x 49 rotor passage; in a batch the back pressure varies over [1.05, 1.30] x p_t
+    (or is given, as ratios to the inlet total pressure)"""
     import meshgen as mg
     dirs = []
     for q in range(n):
         pb = 1.20 if n == 1 else 1.05 + 0.25 * ((q + seed_offset) % n) / max(n - 1, 1)
+        if back_pressures is not None:
+            pb = back_pressures[q]
         case = mg.rotor_passage(IM=49, JM=49, KM=129, options={
             "Pout": "%.1f" % (pb * 101325.0), "multigrid": "Y", "coarse_iter": "2", "Ma0": "0.45"})
         d = os.path.join(root, f"op{q}")
@@ -294,6 +305,115 @@ def measure_forms(gbturbo, dirs, cells, n_ref, ref_int, steps, tmp):
     return out
 
 
+# ---------------------------------------------------------------------------------------------
+# long-run studies (one JSON document each; not the benchmark line)
+# ---------------------------------------------------------------------------------------------
+INTEGRAL_COLS = {"m_in": 6, "m_out": 7, "PR": 8, "eta": 9}
+
+
+def study_precision(gbturbo, tmp, cycles):
+    """the mixed-precision form against the FP64 solve on the 129 x 49 x 49 passage at back
+    pressures 1.10, 1.20 and 1.28 x inlet total: both forms run the same cycles from the uniform
+    start (the three points as one batch), and every integral of the mixed form is compared with
+    the FP64 one at the last cycle and averaged over the last 10% of the cycles (the stalled points
+    are unsteady, so the cycle-by-cycle values of both forms wander)"""
+    pbs = [1.10, 1.20, 1.28]
+    dirs, cells = make_cases(os.path.join(tmp, "prec"), 3, back_pressures=pbs)
+    hist, wall = {}, {}
+    for name, prec in (("fp64", gbturbo.FP64), ("mixed", gbturbo.MIXED)):
+        t0 = time.perf_counter()
+        with gbturbo.Solver(dirs, prec) as s:
+            s.init_uniform()
+            hist[name] = s.iterate(cycles)
+        wall[name] = time.perf_counter() - t0
+    tail = max(1, cycles // 10)
+    points = []
+    for q, pb in enumerate(pbs):
+        row = {"back_pressure_over_pt": pb}
+        for form in ("fp64", "mixed"):
+            h = hist[form][:, q, :]
+            row[form] = {"last": {n: float(h[-1, c]) for n, c in INTEGRAL_COLS.items()},
+                         "mean_tail": {n: float(h[-tail:, c].mean()) for n, c in INTEGRAL_COLS.items()},
+                         "res_dens_last": float(h[-1, 1]), "mass_ratio_last": float(h[-1, 10])}
+        for key in ("last", "mean_tail"):
+            row["rel_err_" + key] = {n: abs(row["mixed"][key][n] - row["fp64"][key][n]) / abs(row["fp64"][key][n])
+                                     for n in INTEGRAL_COLS}
+        # largest relative difference of the four integrals at checkpoints along the run
+        d = np.max(np.abs(hist["mixed"][:, q, 6:10] - hist["fp64"][:, q, 6:10]) /
+                   np.abs(hist["fp64"][:, q, 6:10]), axis=1)
+        row["rel_err_at_cycle"] = {str(c): float(d[c - 1]) for c in range(100, cycles + 1, 100) if c % 500 == 0 or c <= 300}
+        points.append(row)
+    return {"study": "precision", "workload": "rotor_passage_129x49x49_2level_multigrid", "cycles": cycles,
+            "cells_per_solve": cells, "wall_s": wall, "points": points}
+
+
+def _timed_run(speedline, dirs, prec, cycles, tol):
+    t0 = time.perf_counter()
+    table = speedline.run(dirs, prec, max_iter=cycles, chunk=100, tol=tol)
+    return time.perf_counter() - t0, table
+
+
+def study_solves(gbturbo, tmp, cycles, npoints):
+    """converged solves per hour, each point run from the uniform start until the reference's rule
+    (density residual <= 1e-6 and mass ratio <= 0.003) or the cycle cap, wall clock through the
+    public API (case reading, geometry, iterations with the history read back every 100 cycles):
+      plain FP64: the 129 x 49 x 49 passage at 1.20 x p_t, one solve at a time, and a seeded
+        subsample of the sampled operating points one at a time;
+      mixed, one solve at a time: the same passage;
+      mixed, batched: the seeded sampler's points as one batch."""
+    import speedline
+    out = {"study": "solves", "cycle_cap": cycles, "tol": 1e-6, "mass_ratio_limit": speedline.MASS_RATIO_LIMIT}
+    dirs, cells = make_cases(os.path.join(tmp, "single"), 1)
+    for name, prec in (("fp64_single_129x49x49", gbturbo.FP64), ("mixed_single_129x49x49", gbturbo.MIXED)):
+        t, table = _timed_run(speedline, dirs, prec, cycles, 1e-6)
+        out[name] = {"wall_s": t, "solves_per_hour": 3600.0 / t, "points": table}
+    sdirs, scells = make_sampled_cases(os.path.join(tmp, "sampled"), npoints)
+    t, table = _timed_run(speedline, sdirs, gbturbo.MIXED, cycles, 1e-6)
+    out["mixed_batch_sampled"] = {"wall_s": t, "points_in_batch": npoints, "fine_cells": int(sum(scells)),
+                                  "solves_per_hour": 3600.0 * npoints / t,
+                                  "converged": sum(1 for r in table if r["converged"]),
+                                  "iterations": [r["iteration"] for r in table]}
+    # plain FP64 on a subsample of the same points: one of each mesh size and one more
+    sizes = {}
+    for q, c in enumerate(scells):
+        sizes.setdefault(c, q)
+    sub = sorted(sizes.values())
+    sub += [q for q in range(npoints) if q not in sub][:4 - len(sub)]
+    t_sub = 0.0
+    rows = []
+    for q in sub:
+        t, table = _timed_run(speedline, [sdirs[q]], gbturbo.FP64, cycles, 1e-6)
+        t_sub += t
+        rows.append(dict(table[0], cells=int(scells[q]), wall_s=t))
+    mean_cells = sum(scells) / len(scells)
+    sub_cells = sum(scells[q] for q in sub) / len(sub)
+    # one FP64 solve of the batch's mean size takes (time per cell of the subsample) x mean cells
+    t_mean = t_sub / len(sub) * (mean_cells / sub_cells)
+    out["fp64_single_sampled"] = {"subsample": sub, "wall_s": t_sub, "points": rows,
+                                  "solves_per_hour": 3600.0 / t_mean,
+                                  "note": "one solve at a time; per-solve time scaled from the subsample to the "
+                                          "batch's mean fine-cell count"}
+    out["batched_mixed_over_plain_fp64_solves_per_hour"] = (out["mixed_batch_sampled"]["solves_per_hour"] /
+                                                           out["fp64_single_sampled"]["solves_per_hour"])
+    return out
+
+
+def run_study(args):
+    import build as pkg_build
+    pkg_build.build()
+    import gbturbo
+    tmp = tempfile.mkdtemp(prefix="gbt_study_")
+    try:
+        if args.study == "precision":
+            res = study_precision(gbturbo, tmp, args.cycles or 3000)
+        else:
+            res = study_solves(gbturbo, tmp, args.cycles or 4000, args.points)
+        print(json.dumps(res), flush=True)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return 0
+
+
 def config_block(args, cells, nsolve):
     if getattr(args, "sampled", False):
         wl, mesh = "sampled_rotor_passages_2level_multigrid", "97x41x41 / 129x49x49 / 161x65x65 (seeded sampler)"
@@ -428,6 +548,8 @@ def run_gpu(args, rank, world, dist):
 
 def main():
     args = parse()
+    if args.study:
+        return run_study(args)
     rank, world, dist = dist_init()
     if args.impl == "reference":
         rc = run_reference(args, rank, world, dist)
