@@ -68,6 +68,24 @@ int gb_dims(gb_solver *h, int solve, int level, int out[4])
     return guard([&] { h->s->dims(solve, level, out); });
 }
 
+int gb_num_blocks(gb_solver *h, int *n_cases, int *n_blocks)
+{
+    NEED(h);
+    if (n_cases) *n_cases = h->s->ncase;
+    if (n_blocks) *n_blocks = h->s->nsolve;
+    return GB_OK;
+}
+
+int gb_case_blocks(gb_solver *h, int solve, int out[2])
+{
+    NEED(h);
+    if (!out) { g_err = "null buffer"; return GB_ERR_ARG; }
+    if (solve < 0 || solve >= h->s->ncase) { g_err = "solve out of range"; return GB_ERR_ARG; }
+    out[0] = h->s->case_first[solve];
+    out[1] = h->s->case_nblk[solve];
+    return GB_OK;
+}
+
 int gb_init_uniform(gb_solver *h) { NEED(h); return guard([&] { h->s->init_uniform(); }); }
 int gb_resflux(gb_solver *h, int level) { NEED(h); LEVEL(h, level); return guard([&] { h->s->resflux(level); }); }
 int gb_time_marching(gb_solver *h, int level) { NEED(h); LEVEL(h, level); return guard([&] { h->s->time_marching(level); }); }
@@ -86,9 +104,9 @@ int gb_res_calculate(gb_solver *h, int level, double *out)
     return guard([&] {
         h->s->res_calculate(level);
         if (out) {
-            std::vector<gbt::SolveState> st(h->s->nsolve);
+            std::vector<gbt::SolveState> st(h->s->ncase);
             h->s->states(st.data());
-            for (int s = 0; s < h->s->nsolve; s++)
+            for (int s = 0; s < h->s->ncase; s++)
                 for (int c = 0; c < 5; c++) out[s * 5 + c] = st[s].res[c];
         }
     });
@@ -98,7 +116,7 @@ int gb_res_calculate_noalloc(gb_solver *h, int level, double *out)
 {
     NEED(h); LEVEL(h, level);
     if (h->s->nsolve > GB_NOALLOC_MAX_SOLVES) {
-        g_err = "gb_res_calculate_noalloc: the batch has more solves than the static scratch holds (GB_NOALLOC_MAX_SOLVES)";
+        g_err = "gb_res_calculate_noalloc: the batch has more blocks than the static scratch holds (GB_NOALLOC_MAX_SOLVES)";
         return GB_ERR_ARG;
     }
     return guard([&] { h->s->res_calculate_static(level, out); });
@@ -110,9 +128,9 @@ int gb_integrals(gb_solver *h, int level, double *out)
     return guard([&] {
         h->s->integrals(level);
         if (out) {
-            std::vector<gbt::SolveState> st(h->s->nsolve);
+            std::vector<gbt::SolveState> st(h->s->ncase);
             h->s->states(st.data());
-            for (int s = 0; s < h->s->nsolve; s++) {
+            for (int s = 0; s < h->s->ncase; s++) {
                 out[s * 5 + 0] = st[s].m_in; out[s * 5 + 1] = st[s].m_out; out[s * 5 + 2] = st[s].pr;
                 out[s * 5 + 3] = st[s].eff; out[s * 5 + 4] = st[s].m_ratio;
             }
@@ -141,9 +159,9 @@ int gb_get_status(gb_solver *h, int *out)
     NEED(h);
     if (!out) { g_err = "null buffer"; return GB_ERR_ARG; }
     return guard([&] {
-        std::vector<gbt::SolveState> st(h->s->nsolve);
+        std::vector<gbt::SolveState> st(h->s->ncase);
         h->s->states(st.data());
-        for (int s = 0; s < h->s->nsolve; s++) out[s] = st[s].status;
+        for (int s = 0; s < h->s->ncase; s++) out[s] = st[s].status;
     });
 }
 

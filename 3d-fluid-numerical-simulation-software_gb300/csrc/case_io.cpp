@@ -158,7 +158,9 @@ void ng_check(int is, int ie, int js, int je, int ks, int ke, int &NG)
     NG = std::min(num, NG);
 }
 
-void read_bc(CaseSpec &c)
+struct BlockRow { int IM, JM, KM, nblade; double rpm; };
+
+void read_bc(CaseSpec &c, std::vector<BlockRow> &blocks)
 {
     LineReader r(c.dir + "/" + c.bc_file, c.bc_file);
     int NG = 4;
@@ -169,8 +171,7 @@ void read_bc(CaseSpec &c)
     for (int q = 0; q < n; q++) {
         auto v = ints(r.next());
         if (v.size() < 9) throw std::runtime_error(c.bc_file + ": bad inlet line");
-        if (v[1] != 1) throw std::runtime_error("multi-block cases are not supported");
-        c.inlets.push_back({v[2], v[3], v[4], v[5], v[6], v[7], v[8]});
+        c.inlets.push_back({v[2], v[3], v[4], v[5], v[6], v[7], v[8], v[1]});
         ng_check(v[3], v[4], v[5], v[6], v[7], v[8], NG);
     }
     r.skip(3);
@@ -179,8 +180,7 @@ void read_bc(CaseSpec &c)
     for (int q = 0; q < n; q++) {
         auto v = ints(r.next());
         if (v.size() < 9) throw std::runtime_error(c.bc_file + ": bad outlet line");
-        if (v[1] != 1) throw std::runtime_error("multi-block cases are not supported");
-        c.outlets.push_back({v[2], v[3], v[4], v[5], v[6], v[7], v[8]});
+        c.outlets.push_back({v[2], v[3], v[4], v[5], v[6], v[7], v[8], v[1]});
         ng_check(v[3], v[4], v[5], v[6], v[7], v[8], NG);
     }
     r.skip(3);
@@ -189,42 +189,47 @@ void read_bc(CaseSpec &c)
     for (int q = 0; q < n; q++) {
         auto v = ints(r.next());
         if (v.size() < 10) throw std::runtime_error(c.bc_file + ": bad wall line");
-        if (v[1] != 1) throw std::runtime_error("multi-block cases are not supported");
-        c.walls.push_back({v[2], v[3] != 0, v[4], v[5], v[6], v[7], v[8], v[9]});
+        c.walls.push_back({v[2], v[3] != 0, v[4], v[5], v[6], v[7], v[8], v[9], v[1]});
         ng_check(v[4], v[5], v[6], v[7], v[8], v[9], NG);
     }
+    // periodic pairs and block interfaces share one line format
+    // (ID orient BID1 FT1 range1 BID2 FT2 range2; source/UserInput.cpp:380-420)
+    auto pair_line = [&](const char *what) {
+        auto v = ints(r.next());
+        if (v.size() < 18) throw std::runtime_error(c.bc_file + ": bad " + what + " line");
+        PeriodicIO p;
+        p.orient = v[1]; p.b1 = v[2]; p.f1 = v[3]; p.b2 = v[10]; p.f2 = v[11];
+        for (int d = 0; d < 6; d++) { p.r1[d] = v[4 + d]; p.r2[d] = v[12 + d]; }
+        ng_check(v[4], v[5], v[6], v[7], v[8], v[9], NG);
+        return p;
+    };
     r.skip(3);
     n = count("periodic count");
     r.next();
-    for (int q = 0; q < n; q++) {
-        auto v = ints(r.next());
-        if (v.size() < 18) throw std::runtime_error(c.bc_file + ": bad periodic line");
-        if (v[2] != 1 || v[10] != 1) throw std::runtime_error("multi-block cases are not supported");
-        PeriodicIO p;
-        p.orient = v[1]; p.f1 = v[3]; p.f2 = v[11];
-        for (int d = 0; d < 6; d++) { p.r1[d] = v[4 + d]; p.r2[d] = v[12 + d]; }
-        c.periodics.push_back(p);
-        ng_check(v[4], v[5], v[6], v[7], v[8], v[9], NG);
-    }
+    for (int q = 0; q < n; q++) c.periodics.push_back(pair_line("periodic"));
     r.skip(3);
-    if (count("interior count") != 0) throw std::runtime_error("block interfaces are not supported (single-block cases only)");
+    n = count("interior count");
     r.next();
+    for (int q = 0; q < n; q++) c.interiors.push_back(pair_line("interior"));
     r.skip(3);
     if (count("mixing-plane count") != 0) throw std::runtime_error("mixing planes are not supported");
     r.next();
     r.skip(3);
-    if (count("block count") != 1) throw std::runtime_error("only single-block cases are supported");
+    const int nb = count("block count");
+    if (nb < 1) throw std::runtime_error(c.bc_file + ": the case needs at least one block");
     r.next();
-    {
+    for (int b = 0; b < nb; b++) {
         // BID IM JM KM NBlade rpm (rpm read by a stream into a REAL: exact decimal parse)
         std::string s = r.next();
         const char *p = s.c_str();
         char *e;
         int v[5];
         for (int q = 0; q < 5; q++) { v[q] = (int)std::strtol(p, &e, 10); p = e; }
-        c.rpm = std::strtod(p, &e);
-        c.IM = v[1]; c.JM = v[2]; c.KM = v[3]; c.nblade = v[4];
-        int IM = c.IM, JM = c.JM, KM = c.KM;
+        BlockRow br;
+        br.rpm = std::strtod(p, &e);
+        br.IM = v[1]; br.JM = v[2]; br.KM = v[3]; br.nblade = v[4];
+        blocks.push_back(br);
+        int IM = br.IM, JM = br.JM, KM = br.KM;
         for (int j = 1; j <= std::min(std::min(IM, JM), KM); j++) {
             int nn = 2 * j;
             if ((IM - 1) % nn == 0 && (JM - 1) % nn == 0 && (KM - 1) % nn == 0 && (IM - 1) / nn > 2 &&
@@ -235,36 +240,74 @@ void read_bc(CaseSpec &c)
         }
     }
     c.ng = c.use_mg ? std::min(NG, 2) : 1;
+    c.nblock = nb;
+    auto in_range = [&](int b, const char *what) {
+        if (b < 1 || b > nb) throw std::runtime_error(c.bc_file + ": " + what + " names block " + std::to_string(b) + " of " + std::to_string(nb));
+    };
+    for (auto &p : c.inlets) in_range(p.block, "an inlet");
+    for (auto &p : c.outlets) in_range(p.block, "an outlet");
+    for (auto &w : c.walls) in_range(w.block, "a wall");
+    for (auto &p : c.periodics) { in_range(p.b1, "a periodic pair"); in_range(p.b2, "a periodic pair"); }
+    for (auto &p : c.interiors) { in_range(p.b1, "an interface"); in_range(p.b2, "an interface"); }
 }
 
-void read_grid(CaseSpec &c)
+// the grid file: block count, then per block its id line, "IM JM KM" and the nodes, i fastest
+// (source/UserInput.cpp:241-290)
+void read_grid(const CaseSpec &c, const std::vector<BlockRow> &rows, std::vector<CaseSpec> &out)
 {
     std::string path = c.dir + "/" + c.grid_file;
     LineReader r(path, c.grid_file);
-    if (as_int(r.next(), "block count") != 1) throw std::runtime_error("only single-block grids are supported");
-    r.next();
-    int IM, JM, KM;
-    {
-        std::istringstream is(r.next());
-        if (!(is >> IM >> JM >> KM)) throw std::runtime_error(c.grid_file + ": bad block size line");
+    const int nb = as_int(r.next(), "block count");
+    if (nb != (int)rows.size()) throw std::runtime_error("grid and boundary file disagree on the number of blocks");
+    for (int b = 1; b <= nb; b++) {
+        if (as_int(r.next(), "block id") != b)
+            throw std::runtime_error(c.grid_file + ": blocks must be numbered 1, 2, ... in file order");
+        int IM, JM, KM;
+        {
+            std::istringstream is(r.next());
+            if (!(is >> IM >> JM >> KM)) throw std::runtime_error(c.grid_file + ": bad block size line");
+        }
+        const BlockRow &br = rows[b - 1];
+        if (IM != br.IM || JM != br.JM || KM != br.KM)
+            throw std::runtime_error("grid and boundary file disagree on the size of block " + std::to_string(b));
+        CaseSpec bs;
+        // options and the case-wide lists, then this block's own patches and grid
+        bs = c;
+        bs.inlets.clear(); bs.outlets.clear(); bs.walls.clear();
+        for (auto &p : c.inlets) if (p.block == b) bs.inlets.push_back(p);
+        for (auto &p : c.outlets) if (p.block == b) bs.outlets.push_back(p);
+        for (auto &w : c.walls) if (w.block == b) bs.walls.push_back(w);
+        bs.block = b;
+        bs.IM = IM; bs.JM = JM; bs.KM = KM; bs.nblade = br.nblade; bs.rpm = br.rpm;
+        size_t n = (size_t)IM * JM * KM;
+        bs.x.resize(n); bs.y.resize(n); bs.z.resize(n);
+        for (size_t q = 0; q < n; q++) {
+            std::string s = r.next();
+            const char *p = s.c_str();
+            char *e;
+            bs.x[q] = std::strtod(p, &e); if (e == p) throw std::runtime_error(c.grid_file + ": bad node line"); p = e;
+            bs.y[q] = std::strtod(p, &e); if (e == p) throw std::runtime_error(c.grid_file + ": bad node line"); p = e;
+            bs.z[q] = std::strtod(p, &e); if (e == p) throw std::runtime_error(c.grid_file + ": bad node line");
+        }
+        out.push_back(std::move(bs));
     }
-    if (IM != c.IM || JM != c.JM || KM != c.KM)
-        throw std::runtime_error("grid and boundary file disagree on the block size");
-    size_t n = (size_t)IM * JM * KM;
-    c.x.resize(n); c.y.resize(n); c.z.resize(n);
-    for (size_t q = 0; q < n; q++) {
-        std::string s = r.next();
-        const char *p = s.c_str();
-        char *e;
-        c.x[q] = std::strtod(p, &e); if (e == p) throw std::runtime_error(c.grid_file + ": bad node line"); p = e;
-        c.y[q] = std::strtod(p, &e); if (e == p) throw std::runtime_error(c.grid_file + ": bad node line"); p = e;
-        c.z[q] = std::strtod(p, &e); if (e == p) throw std::runtime_error(c.grid_file + ": bad node line");
-    }
+}
+
+void validate_block(const CaseSpec &c)
+{
+    const std::string b = c.nblock > 1 ? "block " + std::to_string(c.block) + ": " : "";
+    if (c.IM < 4 || c.JM < 4 || c.KM < 4) throw std::runtime_error(b + "each direction needs at least 4 nodes");
+    for (auto &p : c.inlets)
+        if (p.ks != p.ke || (p.ks != 1 && p.ks != c.KM)) throw std::runtime_error(b + "inlets must be k-faces (k = 1 or KM)");
+    for (auto &p : c.outlets)
+        if (p.ks != p.ke || p.ke != c.KM) throw std::runtime_error(b + "the axial outlet must be the k = KM face");
+    for (auto &w : c.walls)
+        if (c.turb == 100 && (w.face == 5 || w.face == 6))
+            throw std::runtime_error(b + "Baldwin-Lomax with k-face walls is not supported");
 }
 
 void validate(const CaseSpec &c)
 {
-    if (c.IM < 4 || c.JM < 4 || c.KM < 4) throw std::runtime_error("each direction needs at least 4 nodes");
     if (c.scheme != 200 && c.scheme != 300)
         throw std::runtime_error("space scheme " + std::to_string(c.scheme) + " is not on this path (Steger-Warming 200, Roe 300)");
     if (c.recon_var != 100 && c.recon_var != 200)
@@ -278,26 +321,24 @@ void validate(const CaseSpec &c)
     if (c.use_mg && c.coarse_iter < 1)
         throw std::runtime_error("multigrid needs at least one coarse-grid iteration (the fine level is initialised from it)");
     if (c.inlets.empty() || c.outlets.empty()) throw std::runtime_error("the case needs an inlet and an outlet");
-    for (auto &p : c.inlets)
-        if (p.ks != p.ke || (p.ks != 1 && p.ks != c.KM)) throw std::runtime_error("inlets must be k-faces (k = 1 or KM)");
-    for (auto &p : c.outlets)
-        if (p.ks != p.ke || p.ke != c.KM) throw std::runtime_error("the axial outlet must be the k = KM face");
-    for (auto &w : c.walls)
-        if (c.turb == 100 && (w.face == 5 || w.face == 6))
-            throw std::runtime_error("Baldwin-Lomax with k-face walls is not supported");
 }
 
 }  // namespace
 
-CaseSpec read_case(const std::string &dir)
+std::vector<CaseSpec> read_case(const std::string &dir)
 {
     CaseSpec c;
     c.dir = dir;
     read_config(c);
-    read_bc(c);
-    read_grid(c);
+    std::vector<BlockRow> rows;
+    read_bc(c, rows);
     validate(c);
-    return c;
+    c.first_inlet = c.inlets[0];
+    c.first_outlet = c.outlets[0];
+    std::vector<CaseSpec> blocks;
+    read_grid(c, rows, blocks);
+    for (auto &b : blocks) validate_block(b);
+    return blocks;
 }
 
 }  // namespace gbt

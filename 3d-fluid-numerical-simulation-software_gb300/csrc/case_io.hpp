@@ -8,14 +8,18 @@
 
 namespace gbt {
 
-struct PatchIO {               // inlet / outlet
+struct PatchIO {               // inlet / outlet (block: 1-based block of the case)
     int face, is, ie, js, je, ks, ke;
+    int block = 1;
 };
 struct WallIO {
     int face, rotate, is, ie, js, je, ks, ke;
+    int block = 1;
 };
+// periodic pair or block interface: side 1 (block b1, face type f1, node range r1) and side 2
 struct PeriodicIO {
     int orient, f1, r1[6], f2, r2[6];
+    int b1 = 1, b2 = 1;
 };
 
 // Everything the reference reads before its first iteration, with scalar options already
@@ -36,20 +40,25 @@ struct CaseSpec {
     double CFL = 0, C_timestep = 0, relax = 0, epsEntr = 0, k2 = 0, k4 = 0;
     bool irs = false, limiter = false, global_dt = false;
     int recon_var = 200, recon = 500, scheme = 300, time_scheme = 500, turb = 100;
-    // boundary definition (source/UserInput.cpp:336-446)
+    // boundary definition (source/UserInput.cpp:336-446). A case of several blocks is held as one
+    // spec per block: inlets, outlets and walls are those of this block, in file order; periodic
+    // pairs and block interfaces (which join two blocks) are the case's full lists, in file order
     std::vector<PatchIO> inlets, outlets;
     std::vector<WallIO> walls;
-    std::vector<PeriodicIO> periodics;
+    std::vector<PeriodicIO> periodics, interiors;
+    PatchIO first_inlet{}, first_outlet{};       // the case's Inlet[1] and Outlet[1] (the reported sections)
     int nblade = 1;
     double rpm = 0;
     int ng = 1;                                  // levels chosen as the reference does (<= 2)
-    // grid
+    int block = 1, nblock = 1;                   // this spec's block and the case's block count
+    // grid of this block
     int IM = 0, JM = 0, KM = 0;
     std::vector<double> x, y, z;                 // node coordinates, index ((k-1)*JM + (j-1))*IM + (i-1)
 };
 
-// Reads a case directory; throws std::runtime_error with a message naming the problem.
-CaseSpec read_case(const std::string &dir);
+// Reads a case directory into one spec per block (block order of the files); throws
+// std::runtime_error with a message naming the problem.
+std::vector<CaseSpec> read_case(const std::string &dir);
 
 // One line of a reference input file: comment from '#' removed, leading and trailing blanks
 // removed (tabs are kept, as the reference keeps them); a trailing carriage return is dropped.

@@ -86,6 +86,11 @@ struct SolveConst {
     // imposed mass flow (source/Solver.cpp:142-145, source/Structured_FV3D.cpp:186-193)
     double m_imposed, relax_press, resc_mass_imp;
     int iter_mass_imp, mass_imposed;
+    // the case this block belongs to: its first slot and its number of blocks (the case-wide
+    // residual norm and integrals combine these slots; every slot of a case holds the same
+    // case-wide state)
+    int lead, nblk, cix;                             // cix: the case's index
+    int pad_;
 };
 
 // Global (per handle) physical constants, in the reference's nondimensional units.

@@ -120,7 +120,7 @@ void launch_res_norm(const LaunchCtx &ctx, const Geo &G, Flow<T> F, const double
 
 // residual norm with scratch in a static device array; copies the norms to host_out if given
 template <typename T>
-void launch_res_norm_static(const LaunchCtx &ctx, const Geo &G, Flow<T> F, const double *totalvol, double *host_out);
+void launch_res_norm_static(const LaunchCtx &ctx, const Geo &G, Flow<T> F, const double *totalvol, int ncase, double *host_out);
 
 template <typename T>
 void launch_integrals(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> F, const BcTables &bc);

@@ -513,12 +513,16 @@ __global__ void __launch_bounds__(256) k_norm_partial(Batch B, Geo G, Flow<T> W,
     }
 }
 
+// the norm of a case: the partials of its blocks in block order, over the case's volume (every
+// slot of the case computes the same sum and keeps it)
 __global__ void k_norm_final(Batch B, const double *partials, int nblk, const double *totalvol)
 {
     const int s = blockIdx.x;
     if (threadIdx.x >= 5) return;
+    const SolveConst &sc = B.sc[s];
     double v = 0;
-    for (int b = 0; b < nblk; b++) v += partials[((long long)s * nblk + b) * 5 + threadIdx.x];
+    for (int q = sc.lead; q < sc.lead + sc.nblk; q++)
+        for (int b = 0; b < nblk; b++) v += partials[((long long)q * nblk + b) * 5 + threadIdx.x];
     v = v / totalvol[s];
     B.st[s].res[threadIdx.x] = v;
     if (threadIdx.x == 0 && !isfinite(v)) B.st[s].status |= GBT_STATUS_NAN;
@@ -542,8 +546,10 @@ __global__ void __launch_bounds__(128) k_section_partial(Batch B, Phys P, Geo G,
                                                          const DevInOut *outl, double *part)
 {
     const int s = blockIdx.y, sec = blockIdx.z;
-    const Lvl L = B.lv[s];
-    const int K = sec == 0 ? inl[s].ks : outl[s].ks;
+    // the section's block: the case's Inlet[1] / Outlet[1] may lie in any of its blocks
+    const DevInOut &sp = sec == 0 ? inl[s] : outl[s];
+    const Lvl L = B.lv[sp.solve];
+    const int K = sp.ks;
     const int nI = L.IM - 1, nJ = L.JM - 1;
     const double g = P.gamma, g1 = g - 1.0, R = P.rgas;
     double m = 0, pm = 0, tm = 0;
@@ -579,7 +585,7 @@ __global__ void __launch_bounds__(128) k_section_partial(Batch B, Phys P, Geo G,
 }
 
 // inlet/outlet integrals (source/Ouput.cpp:9-107,282-300): partials summed in block order
-__global__ void k_integrals(Batch B, Phys P, const double *part)
+__global__ void k_integrals(Batch B, Phys P, const DevInOut *inl, const DevInOut *outl, const double *part)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= B.nsolve) return;
@@ -590,8 +596,9 @@ __global__ void k_integrals(Batch B, Phys P, const double *part)
             b[c] += part[(((long long)s * 2 + 1) * kIntegralBlocks + blk) * 3 + c];
         }
     const double g = P.gamma, g1 = g - 1.0, R = P.rgas;
-    const double nbl = B.sc[s].nblade;
-    const double mi = a[0] * P.dens_ref * P.vel_ref * nbl, mo = b[0] * P.dens_ref * P.vel_ref * nbl;
+    // blade count of the inlet's and of the outlet's block (source/Ouput.cpp:288,294)
+    const double mi = a[0] * P.dens_ref * P.vel_ref * B.sc[inl[s].solve].nblade;
+    const double mo = b[0] * P.dens_ref * P.vel_ref * B.sc[outl[s].solve].nblade;
     const double pti = pow(a[1] / a[0], g / g1) * P.dens_ref * P.vel_ref * P.vel_ref;
     const double pto = pow(b[1] / b[0], g / g1) * P.dens_ref * P.vel_ref * P.vel_ref;
     const double tti = a[2] / a[0] * P.temp_ref, tto = b[2] / b[0] * P.temp_ref;
@@ -611,7 +618,7 @@ void launch_integrals(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T>
     const Batch &B = ctx.batch;
     k_section_partial<T><<<dim3(kIntegralBlocks, B.nsolve, 2), 128, 0, ctx.stream>>>(B, P, G, W, bc.inlet_first,
                                                                                       bc.outlet_first, bc.integ_part);
-    k_integrals<<<(B.nsolve + 31) / 32, 32, 0, ctx.stream>>>(B, P, bc.integ_part);
+    k_integrals<<<(B.nsolve + 31) / 32, 32, 0, ctx.stream>>>(B, P, bc.inlet_first, bc.outlet_first, bc.integ_part);
 }
 
 // CFL ramp of the driver (source/Solver.cpp:49-60): x1.2 whenever the density residual falls

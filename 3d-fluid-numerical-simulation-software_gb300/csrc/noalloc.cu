@@ -9,8 +9,8 @@
 // into the static array and copies them straight into the caller's buffer.
 //
 // Limits and sharing:
-//  - at most GB_NOALLOC_MAX_SOLVES solves per handle (the array holds 64 partial sums of 5
-//    components for each of them); larger batches are rejected with GB_ERR_ARG;
+//  - at most GB_NOALLOC_MAX_SOLVES blocks (slots) per handle (the array holds 64 partial sums of
+//    5 components for each of them); larger batches are rejected with GB_ERR_ARG;
 //  - every call, from every handle on a device, shares the one array: calls that overlap in time
 //    (two host threads, or two streams in flight at once) race on it and must be serialised by
 //    the caller;
@@ -98,25 +98,29 @@ __global__ void __launch_bounds__(256) k_norm_onepass(Batch B, Geo G, Flow<T> W,
         __threadfence();
     }
     __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(&arrivals[s], 1u) == (unsigned)(kBlocks - 1);
+    // the blocks of all slots of a case count on the case's first slot; the last to arrive adds
+    // the partials of the case's blocks in block order and gives every slot of the case the norm
+    const SolveConst &sc = B.sc[s];
+    if (threadIdx.x == 0) last = atomicAdd(&arrivals[sc.lead], 1u) == (unsigned)(kBlocks * sc.nblk - 1);
     __syncthreads();
     if (!last || threadIdx.x >= 5) return;
     __threadfence();
     double v = 0;
-    for (int b = 0; b < kBlocks; b++) v += __ldcg(&partials[((long long)s * kBlocks + b) * 5 + threadIdx.x]);
+    for (int q = sc.lead; q < sc.lead + sc.nblk; q++)
+        for (int b = 0; b < kBlocks; b++) v += __ldcg(&partials[((long long)q * kBlocks + b) * 5 + threadIdx.x]);
     v = v / totalvol[s];
-    B.st[s].res[threadIdx.x] = v;
-    norms[s * 5 + threadIdx.x] = v;
+    for (int q = sc.lead; q < sc.lead + sc.nblk; q++) B.st[q].res[threadIdx.x] = v;
+    norms[sc.cix * 5 + threadIdx.x] = v;
     if (threadIdx.x == 0) {
-        if (!isfinite(v)) B.st[s].status |= GBT_STATUS_NAN;
-        arrivals[s] = 0u;
+        if (!isfinite(v)) B.st[sc.lead].status |= GBT_STATUS_NAN;
+        arrivals[sc.lead] = 0u;
     }
 }
 
 }  // namespace
 
 template <typename T>
-void launch_res_norm_static(const LaunchCtx &ctx, const Geo &G, Flow<T> W, const double *totalvol, double *host_out)
+void launch_res_norm_static(const LaunchCtx &ctx, const Geo &G, Flow<T> W, const double *totalvol, int ncase, double *host_out)
 {
     const Batch &B = ctx.batch;
     if (B.nsolve > kMaxSolves) throw std::invalid_argument("batch larger than the static norm scratch");
@@ -128,13 +132,13 @@ void launch_res_norm_static(const LaunchCtx &ctx, const Geo &G, Flow<T> W, const
     k_norm_onepass<T><<<dim3(kBlocks, B.nsolve), 256, 0, ctx.stream>>>(B, G, W, totalvol, partials, norms, arrivals);
     check_cuda(cudaGetLastError(), "k_norm_onepass launch");
     if (host_out) {
-        check_cuda(cudaMemcpyAsync(host_out, norms, sizeof(double) * 5 * B.nsolve, cudaMemcpyDeviceToHost, ctx.stream),
+        check_cuda(cudaMemcpyAsync(host_out, norms, sizeof(double) * 5 * ncase, cudaMemcpyDeviceToHost, ctx.stream),
                    "cudaMemcpyAsync");
         check_cuda(cudaStreamSynchronize(ctx.stream), "cudaStreamSynchronize");
     }
 }
 
-template void launch_res_norm_static<double>(const LaunchCtx &, const Geo &, Flow<double>, const double *, double *);
-template void launch_res_norm_static<float>(const LaunchCtx &, const Geo &, Flow<float>, const double *, double *);
+template void launch_res_norm_static<double>(const LaunchCtx &, const Geo &, Flow<double>, const double *, int, double *);
+template void launch_res_norm_static<float>(const LaunchCtx &, const Geo &, Flow<float>, const double *, int, double *);
 
 }  // namespace gbt

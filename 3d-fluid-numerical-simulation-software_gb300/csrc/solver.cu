@@ -60,7 +60,7 @@ struct Level {
     DevBuf geow_mem;
     DevBuf wdist_mem;                     // Baldwin-Lomax wall distances (fine level)
     Flow<T> W{};
-    double *totalvol = nullptr;
+    double *totalvol = nullptr, *blockvol = nullptr;
     BcTables bc;
     PlaneTables planes;
     SweepData<T> sweep;
@@ -88,16 +88,28 @@ struct LevelCase {
     int IM, JM, KM;
     std::vector<PatchIO> in, out;
     std::vector<WallIO> walls;
-    std::vector<PeriodicIO> per;
     std::vector<double> x, y, z;          // nodes, ((k-1)*JM + (j-1))*IM + (i-1)
 };
+
+// a periodic pair or block interface on a level
+static PeriodicIO level_pair(PeriodicIO p, int level)
+{
+    if (level > 1)
+        for (int d = 0; d < 3; d++) { coarse_patch(p.r1[2 * d], p.r1[2 * d + 1]); coarse_patch(p.r2[2 * d], p.r2[2 * d + 1]); }
+    return p;
+}
+static PatchIO level_patch(PatchIO p, int level)
+{
+    if (level > 1) { coarse_patch(p.is, p.ie); coarse_patch(p.js, p.je); coarse_patch(p.ks, p.ke); }
+    return p;
+}
 
 static LevelCase level_case(const CaseSpec &c, int level)
 {
     LevelCase L;
     if (level == 1) {
         L.IM = c.IM; L.JM = c.JM; L.KM = c.KM;
-        L.in = c.inlets; L.out = c.outlets; L.walls = c.walls; L.per = c.periodics;
+        L.in = c.inlets; L.out = c.outlets; L.walls = c.walls;
         L.x = c.x; L.y = c.y; L.z = c.z;
         return L;
     }
@@ -114,10 +126,6 @@ static LevelCase level_case(const CaseSpec &c, int level)
     for (auto p : c.inlets) { coarse_patch(p.is, p.ie); coarse_patch(p.js, p.je); coarse_patch(p.ks, p.ke); L.in.push_back(p); }
     for (auto p : c.outlets) { coarse_patch(p.is, p.ie); coarse_patch(p.js, p.je); coarse_patch(p.ks, p.ke); L.out.push_back(p); }
     for (auto w : c.walls) { coarse_patch(w.is, w.ie); coarse_patch(w.js, w.je); coarse_patch(w.ks, w.ke); L.walls.push_back(w); }
-    for (auto p : c.periodics) {
-        for (int d = 0; d < 3; d++) { coarse_patch(p.r1[2 * d], p.r1[2 * d + 1]); coarse_patch(p.r2[2 * d], p.r2[2 * d + 1]); }
-        L.per.push_back(p);
-    }
     return L;
 }
 
@@ -159,15 +167,28 @@ static void trans(int ori, int l1, int m1, int L1, int M1, int &l2, int &m2)
     }
 }
 
-// interior cells of a level set to the uniform start (source/Initialization.cpp:17-76)
-__global__ void k_fill_uniform(Batch B, double *cv0, double *cv1, double *cv2, double *cv3, double *cv4, double c0,
-                               double c1, double c2, double c3, double c4)
+// interior cells of a level set to the uniform start of their solve (source/Initialization.cpp:17-76):
+// five conserved values per slot in init
+__global__ void k_fill_uniform(Batch B, double *cv0, double *cv1, double *cv2, double *cv3, double *cv4,
+                               const double *init)
 {
     const Lvl L = B.lv[blockIdx.y];
     int i, j, k;
     if (!box_index(L.IM - 1, L.JM - 1, L.KM - 1, i, j, k)) return;
     const long long p = ix(L, i, j, k);
-    cv0[p] = c0; cv1[p] = c1; cv2[p] = c2; cv3[p] = c3; cv4[p] = c4;
+    const double *c = init + 5 * blockIdx.y;
+    cv0[p] = c[0]; cv1[p] = c[1]; cv2[p] = c[2]; cv3[p] = c[3]; cv4[p] = c[4];
+}
+
+// volume of a case: its blocks' volumes summed in block order (source/ComputeAllBlockVars.cpp:32)
+__global__ void k_case_volume(Batch B, const double *blockvol, double *casevol)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= B.nsolve) return;
+    const SolveConst &c = B.sc[s];
+    double v = 0.0;
+    for (int b = 0; b < c.nblk; b++) v = v + blockvol[c.lead + b];
+    casevol[s] = v;
 }
 
 // start of a driver iteration: iteration counter and CFL ramp (source/Solver.cpp:49-60)
@@ -213,6 +234,7 @@ public:
     int *bad_list = nullptr, *bad_count = nullptr;
     const int bad_cap = 4096;
     double *norm_part = nullptr;
+    double *init_q = nullptr;             // uniform start: five conserved values per slot
     const int norm_blk = 304;            // two blocks per SM: the FP64 divisions spread over all SMs
     T *dtmin = nullptr;
     cudaGraphExec_t graphs[3] = {nullptr, nullptr, nullptr};
@@ -299,25 +321,32 @@ public:
     explicit SolverT(const std::vector<std::string> &dirs, int prec)
     {
         precision = prec;
-        nsolve = (int)dirs.size();
-        if (nsolve < 1) throw std::runtime_error("no case directories given");
+        ncase = (int)dirs.size();
+        if (ncase < 1) throw std::runtime_error("no case directories given");
         // the case files of a batch are parsed in parallel host threads (text grids of large
         // batches run to gigabytes)
-        cases.resize(nsolve);
         {
-            std::vector<std::exception_ptr> errs(nsolve);
+            std::vector<std::vector<CaseSpec>> per_case(ncase);
+            std::vector<std::exception_ptr> errs(ncase);
             std::atomic<int> next{0};
-            const unsigned nt = std::min<unsigned>((unsigned)nsolve, std::max(1u, std::thread::hardware_concurrency()));
+            const unsigned nt = std::min<unsigned>((unsigned)ncase, std::max(1u, std::thread::hardware_concurrency()));
             std::vector<std::thread> pool;
             for (unsigned t = 0; t < nt; t++)
                 pool.emplace_back([&] {
-                    for (int i = next++; i < nsolve; i = next++) {
-                        try { cases[i] = read_case(dirs[i]); } catch (...) { errs[i] = std::current_exception(); }
+                    for (int i = next++; i < ncase; i = next++) {
+                        try { per_case[i] = read_case(dirs[i]); } catch (...) { errs[i] = std::current_exception(); }
                     }
                 });
             for (auto &t : pool) t.join();
             for (auto &e : errs) if (e) std::rethrow_exception(e);
+            // one slot per block, the blocks of a case consecutive
+            for (int c = 0; c < ncase; c++) {
+                case_first.push_back((int)cases.size());
+                case_nblk.push_back((int)per_case[c].size());
+                for (auto &b : per_case[c]) cases.push_back(std::move(b));
+            }
         }
+        nsolve = (int)cases.size();
         const CaseSpec &c0 = cases[0];
         for (auto &c : cases) {
             if (c.ng != c0.ng || c.coarse_iter != c0.coarse_iter || c.scheme != c0.scheme || c.recon != c0.recon ||
@@ -361,11 +390,13 @@ public:
         }
         CK(cudaMemcpy(st_d, st.data(), st_mem.bytes, cudaMemcpyHostToDevice));
         // scratch: limiter lists, norm partials, global-dt minima
-        size_t sb = sizeof(int) * (size_t)nsolve * (bad_cap + 1) + sizeof(double) * (size_t)nsolve * norm_blk * 5 + sizeof(T) * nsolve + 256;
+        size_t sb = sizeof(int) * (size_t)nsolve * (bad_cap + 1) + sizeof(double) * (size_t)nsolve * (norm_blk + 1) * 5 +
+                    sizeof(T) * nsolve + 256;
         scratch_mem.bytes = sb;
         CK(cudaMalloc(&scratch_mem.p, sb));
         char *q = (char *)scratch_mem.p;
         norm_part = (double *)q; q += sizeof(double) * (size_t)nsolve * norm_blk * 5;
+        init_q = (double *)q; q += sizeof(double) * (size_t)nsolve * 5;
         bad_list = (int *)q; q += sizeof(int) * (size_t)nsolve * bad_cap;
         bad_count = (int *)q; q += sizeof(int) * nsolve;
         dtmin = (T *)(((uintptr_t)q + 15) & ~(uintptr_t)15);
@@ -399,6 +430,9 @@ public:
             sc.w_rot = nd.w_rot; sc.delta_th = nd.delta_th; sc.pout = nd.pout; sc.nblade = cases[s].nblade;
             sc.m_imposed = cases[s].m_imposed; sc.relax_press = cases[s].relax_press; sc.resc_mass_imp = cases[s].resc_mass_imp;
             sc.iter_mass_imp = cases[s].iter_mass_imp; sc.mass_imposed = cases[s].mass_imposed ? 1 : 0;
+            sc.lead = s - (cases[s].block - 1);
+            sc.nblk = cases[s].nblock;
+            sc.cix = (int)(std::upper_bound(case_first.begin(), case_first.end(), s) - case_first.begin()) - 1;
             Lv.sc.push_back(sc);
             Lv.maxIM = std::max(Lv.maxIM, c.IM); Lv.maxJM = std::max(Lv.maxJM, c.JM); Lv.maxKM = std::max(Lv.maxKM, c.KM);
             Lv.max_plane = std::max(Lv.max_plane, c.IM + c.JM + c.KM - 3);
@@ -413,7 +447,7 @@ public:
         CK(cudaMemcpy(Lv.sc_d, Lv.sc.data(), sizeof(SolveConst) * nsolve, cudaMemcpyHostToDevice));
         // geometry pools (FP64)
         const int NGEO = 124;
-        Lv.geo_mem.bytes = sizeof(double) * N * NGEO + sizeof(double) * nsolve;
+        Lv.geo_mem.bytes = sizeof(double) * N * NGEO + sizeof(double) * 2 * nsolve;
         CK(cudaMalloc(&Lv.geo_mem.p, Lv.geo_mem.bytes));
         CK(cudaMemset(Lv.geo_mem.p, 0, Lv.geo_mem.bytes));
         double *g = (double *)Lv.geo_mem.p;
@@ -430,7 +464,8 @@ public:
         G.vol = take();
         for (int c = 0; c < 3; c++) G.cc[c] = take();
         for (int c = 0; c < 9; c++) G.cm[c] = take();
-        Lv.totalvol = g;
+        Lv.blockvol = g;                   // per slot: the block's volume
+        Lv.totalvol = g + nsolve;          // per slot: the volume of its whole case (CMesh::TotalVol)
         // flow pools
         Lv.flow_d_mem.bytes = sizeof(double) * N * 15;
         CK(cudaMalloc(&Lv.flow_d_mem.p, Lv.flow_d_mem.bytes));
@@ -474,7 +509,8 @@ public:
             build_tables(l, lc, hx, hy);
         }
         build_planes(l);
-        launch_geometry(ctx(l), G, Lv.totalvol);
+        launch_geometry(ctx(l), G, Lv.blockvol);
+        k_case_volume<<<(nsolve + 127) / 128, 128, 0, stream>>>(batch(l), Lv.blockvol, Lv.totalvol);
         build_geometry_working(l);
         build_wall_distances(l);
         launch_sweep_geometry<T>(ctx(l), G, Lv.planes, Lv.sweep);
@@ -677,11 +713,19 @@ public:
                 bc.max_inlet = std::max(bc.max_inlet, (p.ie - p.is + 1) * (p.je - p.js + 1));
             }
             for (auto &p : c.out) outl.push_back({s, p.face, p.is, p.ie, p.js, p.je, p.ks, p.ke});
-            if (c.out.size() != 1) throw std::runtime_error("exactly one axial outlet per case is supported");
-            inl1.push_back(inl[inl.size() - c.in.size()]);
-            outl1.push_back(outl.back());
             bc.max_outlet_im = std::max(bc.max_outlet_im, c.IM);
             bc.max_outlet_jm = std::max(bc.max_outlet_jm, c.JM);
+            // the sections the case reports (its Inlet[1] and Outlet[1]), on the slot of their block
+            const CaseSpec &cs = cases[s];
+            const int lead = s - (cs.block - 1);
+            const PatchIO fi = level_patch(cs.first_inlet, l), fo = level_patch(cs.first_outlet, l);
+            inl1.push_back({lead + fi.block - 1, fi.face, fi.is, fi.ie, fi.js, fi.je, fi.ks, fi.ke});
+            outl1.push_back({lead + fo.block - 1, fo.face, fo.is, fo.ie, fo.js, fo.je, fo.ks, fo.ke});
+        }
+        for (int c = 0; c < ncase; c++) {
+            int nout = 0;
+            for (int b = 0; b < case_nblk[c]; b++) nout += (int)lc[case_first[c] + b].out.size();
+            if (nout != 1) throw std::runtime_error("exactly one axial outlet per case is supported");
         }
         // walls ordered by their position in each case's list, then by solve
         bc.n_wall_slot = (int)max_walls;
@@ -712,48 +756,67 @@ public:
                         for (int k = w.ks; k <= w.ke; k++) wallf[f][ix(Lv.lv[s], i, j, k)] = rec + 1;
             }
         }
-        // periodic gather list, last writer wins as in the reference's sequential copies
-        for (int s = 0; s < nsolve; s++) {
-            const LevelCase &c = lc[s];
-            const Lvl &v = Lv.lv[s];
+        // ghost exchange of block interfaces and periodic pairs as one gather list, in the
+        // reference's order (all interfaces, then all periodic pairs, each in file order;
+        // source/BoundaryCondition.cpp:46-58); the last writer of a cell wins, as in the reference's
+        // sequential copies
+        for (int cix = 0; cix < ncase; cix++) {
+            const int s0 = case_first[cix];
+            const CaseSpec &cs = cases[s0];
             std::map<long long, size_t> last;
-            for (auto &pr : c.per) {
-                long long pa = ix(v, pr.r1[0], pr.r1[2], pr.r1[4]), pb = ix(v, pr.r2[0], pr.r2[2], pr.r2[4]);
-                double th1 = std::atan(hy[pa] / hx[pa]), th2 = std::atan(hy[pb] / hx[pb]);
-                if ((th2 - th1) < 0.0)
-                    throw std::runtime_error("periodic pair listed against the pitch direction (the reference flips the pitch sign on every call then); list the lower-theta face first");
+            std::vector<std::pair<PeriodicIO, bool>> pairs;
+            for (auto &p : cs.interiors) pairs.push_back({level_pair(p, l), false});
+            for (auto &p : cs.periodics) pairs.push_back({level_pair(p, l), true});
+            for (auto &pp : pairs) {
+                const PeriodicIO &pr = pp.first;
+                const bool rotate = pp.second;
+                const int sa = s0 + pr.b1 - 1, sb = s0 + pr.b2 - 1;
+                const Lvl &va = Lv.lv[sa], &vb = Lv.lv[sb];
+                const LevelCase &ca = lc[sa], &cb = lc[sb];
+                if (rotate) {
+                    long long pa = ix(va, pr.r1[0], pr.r1[2], pr.r1[4]), pb = ix(vb, pr.r2[0], pr.r2[2], pr.r2[4]);
+                    double th1 = std::atan(hy[pa] / hx[pa]), th2 = std::atan(hy[pb] / hx[pb]);
+                    if ((th2 - th1) < 0.0)
+                        throw std::runtime_error("periodic pair listed against the pitch direction (the reference flips the pitch sign on every call then); list the lower-theta face first");
+                }
                 for (int nd = 1; nd <= P.ndummy; nd++) {
                     for (int dir = 0; dir < 2; dir++) {
+                        // side 1 -> side 2 rotated by +delta_th of block 1, then side 2 -> side 1 by
+                        // -delta_th; an interface copies without rotation
                         const int *ra = dir == 0 ? pr.r1 : pr.r2, *rb = dir == 0 ? pr.r2 : pr.r1;
                         int fa = dir == 0 ? pr.f1 : pr.f2, fb = dir == 0 ? pr.f2 : pr.f1;
+                        const Lvl &vs = dir == 0 ? va : vb, &vd = dir == 0 ? vb : va;
+                        const LevelCase &cS = dir == 0 ? ca : cb, &cD = dir == 0 ? cb : ca;
                         int La, Ma, Lb, Mb;
-                        auto A = patch_walk(fa, nd, ra, c.IM, c.JM, c.KM, La, Ma);
-                        auto Bw = patch_walk(fb, nd, rb, c.IM, c.JM, c.KM, Lb, Mb);
+                        auto A = patch_walk(fa, nd, ra, cS.IM, cS.JM, cS.KM, La, Ma);
+                        auto Bw = patch_walk(fb, nd, rb, cD.IM, cD.JM, cD.KM, Lb, Mb);
                         std::map<std::pair<int, int>, long long> src;
                         for (auto &e : A) {
                             int l2, m2;
                             trans(pr.orient, e.l, e.m, La, Ma, l2, m2);
-                            src[{l2, m2}] = ix(v, e.ri, e.rj, e.rk);
+                            src[{l2, m2}] = ix(vs, e.ri, e.rj, e.rk);
                         }
+                        const int sign = rotate ? (dir == 0 ? 1 : -1) : 0;
                         for (auto &e : Bw) {
                             auto it = src.find({e.l, e.m});
-                            if (it == src.end()) throw std::runtime_error("periodic patches of different size");
-                            int sign = dir == 0 ? 1 : -1;
-                            long long dsts[2] = {ix(v, e.gi, e.gj, e.gk), -1};
+                            if (it == src.end()) throw std::runtime_error(rotate ? "periodic patches of different size" : "interface patches of different size");
+                            long long dsts[2] = {ix(vd, e.gi, e.gj, e.gk), -1};
                             if (nd == 1) {
                                 // the first layer also fills the ghost cell next to the face
                                 int gi = e.gi, gj = e.gj, gk = e.gk;
-                                if (gi < 0) gi = 0; else if (gi > c.IM) gi = c.IM;
-                                if (gj < 0) gj = 0; else if (gj > c.JM) gj = c.JM;
-                                if (gk < 0) gk = 0; else if (gk > c.KM) gk = c.KM;
-                                if (gi == c.IM + 1) gi = c.IM;
-                                dsts[1] = ix(v, gi, gj, gk);
+                                if (gi < 0) gi = 0; else if (gi > cD.IM) gi = cD.IM;
+                                if (gj < 0) gj = 0; else if (gj > cD.JM) gj = cD.JM;
+                                if (gk < 0) gk = 0; else if (gk > cD.KM) gk = cD.KM;
+                                if (gi == cD.IM + 1) gi = cD.IM;
+                                dsts[1] = ix(vd, gi, gj, gk);
                             }
                             for (long long dd : dsts) {
                                 if (dd < 0) continue;
+                                // the rotation angle is block 1's pitch
+                                const int meta = sa * 4 + sign + 1;
                                 auto f = last.find(dd);
-                                if (f != last.end()) { psrc[f->second] = it->second; pmeta[f->second] = s * 4 + sign + 1; }
-                                else { last[dd] = pdst.size(); pdst.push_back(dd); psrc.push_back(it->second); pmeta.push_back(s * 4 + sign + 1); }
+                                if (f != last.end()) { psrc[f->second] = it->second; pmeta[f->second] = meta; }
+                                else { last[dd] = pdst.size(); pdst.push_back(dd); psrc.push_back(it->second); pmeta.push_back(meta); }
                             }
                         }
                     }
@@ -793,24 +856,32 @@ public:
     // ---------------------------------------------------------------- reference call surface
     void init_uniform() override
     {
-        // source/Initialization.cpp:34-68 (nondimensional inlet totals; FP64 like the reference)
-        const CaseSpec &c = cases[0];
-        const double Gamma = P.gamma, Rgas = P.rgas, Ma0 = c.Ma0;
-        const double press = P.ptin * std::pow(1.0f + (Gamma - 1.0f) / 2.0f * Ma0 * Ma0, 0.0f - Gamma / (Gamma - 1.0f));
-        const double temp = P.ttin * std::pow(1.0f + (Gamma - 1.0f) / 2.0f * Ma0 * Ma0, 0.0f - 1.0f);
-        const double dens = press / (Rgas * temp);
-        const double Vel = std::pow(Gamma * Rgas * temp, 0.5f) * Ma0;
-        const double *a = c.inlet_dir;
-        const double n_m = std::pow(a[0] * a[0] + a[1] * a[1] + a[2] * a[2], 0.5);
-        const double u = Vel * a[0] / n_m, v = Vel * a[1] / n_m, w = Vel * a[2] / n_m;
-        const double V2 = u * u + v * v + w * w;
-        const double ener = press / (dens * (Gamma - 1.0f)) + V2 / 2.0f;
+        // source/Initialization.cpp:34-68 (nondimensional inlet totals; FP64 like the reference),
+        // with each case's initial Mach number
+        const double Gamma = P.gamma, Rgas = P.rgas;
+        std::vector<double> init((size_t)nsolve * 5);
+        for (int s = 0; s < nsolve; s++) {
+            const CaseSpec &c = cases[s];
+            const double Ma0 = c.Ma0;
+            const double press = P.ptin * std::pow(1.0f + (Gamma - 1.0f) / 2.0f * Ma0 * Ma0, 0.0f - Gamma / (Gamma - 1.0f));
+            const double temp = P.ttin * std::pow(1.0f + (Gamma - 1.0f) / 2.0f * Ma0 * Ma0, 0.0f - 1.0f);
+            const double dens = press / (Rgas * temp);
+            const double Vel = std::pow(Gamma * Rgas * temp, 0.5f) * Ma0;
+            const double *a = c.inlet_dir;
+            const double n_m = std::pow(a[0] * a[0] + a[1] * a[1] + a[2] * a[2], 0.5);
+            const double u = Vel * a[0] / n_m, v = Vel * a[1] / n_m, w = Vel * a[2] / n_m;
+            const double V2 = u * u + v * v + w * w;
+            const double ener = press / (dens * (Gamma - 1.0f)) + V2 / 2.0f;
+            const double q[5] = {dens, dens * u, dens * v, dens * w, dens * ener};
+            for (int m = 0; m < 5; m++) init[(size_t)s * 5 + m] = q[m];
+        }
         int l = ng == 1 ? 1 : 2;
         LaunchCtx cx = ctx(l);
         Flow<T> &W = lev[l].W;
-        k_fill_uniform<<<cx.grid_cells(256), 256, 0, stream>>>(cx.batch, W.cv[0], W.cv[1], W.cv[2], W.cv[3], W.cv[4], dens,
-                                                               dens * u, dens * v, dens * w, dens * ener);
+        CK(cudaMemcpyAsync(init_q, init.data(), sizeof(double) * init.size(), cudaMemcpyHostToDevice, stream));
+        k_fill_uniform<<<cx.grid_cells(256), 256, 0, stream>>>(cx.batch, W.cv[0], W.cv[1], W.cv[2], W.cv[3], W.cv[4], init_q);
         launch_primitive<T>(cx, P, W);
+        CK(cudaStreamSynchronize(stream));
         CK(cudaGetLastError());
     }
     void resflux(int l) override
@@ -830,7 +901,7 @@ public:
     void sweep_shape(int l, int out[2]) const override { out[0] = lev[l].planes.cpw; out[1] = lev[l].planes.wpb; }
     void res_calculate_static(int l, double *host_out) override
     {
-        launch_res_norm_static<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, host_out);
+        launch_res_norm_static<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, ncase, host_out);
     }
     void primitive_vars(int l) override { Mark m(this, "primitive"); launch_primitive<T>(ctx(l), P, lev[l].W); }
     void limit_vars(int l) override { Mark m(this, "limiter", 2); launch_limiter<T>(ctx(l), P, lev[l].W, l, bad_list, bad_cap, bad_count); }
@@ -859,9 +930,9 @@ public:
     }
     void outlet_pressure(double *out) override
     {
-        std::vector<SolveState> st(nsolve);
+        std::vector<SolveState> st(ncase);
         states(st.data());
-        for (int s = 0; s < nsolve; s++) out[s] = st[s].pout;
+        for (int c = 0; c < ncase; c++) out[c] = st[c].pout;
     }
 
     // CSolver::Solver (source/Solver.cpp:47-140) for the current iteration number
@@ -931,12 +1002,13 @@ public:
             if (hist) {
                 CK(cudaMemcpyAsync(st.data(), st_d, sizeof(SolveState) * nsolve, cudaMemcpyDeviceToHost, stream));
                 CK(cudaStreamSynchronize(stream));
-                for (int s = 0; s < nsolve; s++) {
-                    double *r = hist + ((size_t)q * nsolve + s) * 12;
-                    r[0] = st[s].iter;
-                    for (int c = 0; c < 5; c++) r[1 + c] = st[s].res[c];
-                    r[6] = st[s].m_in; r[7] = st[s].m_out; r[8] = st[s].pr; r[9] = st[s].eff; r[10] = st[s].m_ratio;
-                    r[11] = st[s].cfl;
+                for (int cix = 0; cix < ncase; cix++) {
+                    const SolveState &a = st[case_first[cix]];
+                    double *r = hist + ((size_t)q * ncase + cix) * 12;
+                    r[0] = a.iter;
+                    for (int c = 0; c < 5; c++) r[1 + c] = a.res[c];
+                    r[6] = a.m_in; r[7] = a.m_out; r[8] = a.pr; r[9] = a.eff; r[10] = a.m_ratio;
+                    r[11] = a.cfl;
                 }
             }
         }
@@ -945,8 +1017,16 @@ public:
 
     void states(SolveState *out) override
     {
-        CK(cudaMemcpyAsync(out, st_d, sizeof(SolveState) * nsolve, cudaMemcpyDeviceToHost, stream));
+        std::vector<SolveState> st(nsolve);
+        CK(cudaMemcpyAsync(st.data(), st_d, sizeof(SolveState) * nsolve, cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));
+        for (int c = 0; c < ncase; c++) {
+            out[c] = st[case_first[c]];
+            for (int b = 1; b < case_nblk[c]; b++) {
+                out[c].status |= st[case_first[c] + b].status;
+                out[c].limiter_hits += st[case_first[c] + b].limiter_hits;
+            }
+        }
     }
 
     void dims(int solve, int l, int out[4]) const override
@@ -1068,75 +1148,100 @@ public:
     }
 
     // ---- the reference's solution files (source/Ouput.cpp:109-259, source/UserInput.cpp:1118-1159)
-    std::string default_path(int solve, const std::string &path, const char *name) const
+    std::string default_path(int cix, const std::string &path, const char *name) const
     {
-        return path.empty() ? cases[solve].dir + "/" + name : path;
+        return path.empty() ? cases[case_first[cix]].dir + "/" + name : path;
     }
-    void fine_state(int solve, std::vector<double> &pv, std::vector<double> &cv, std::vector<double> *mut)
+    void check_case(int cix) const { if (cix < 0 || cix >= ncase) throw std::runtime_error("bad solve"); }
+    void fine_state(int slot, std::vector<double> &pv, std::vector<double> &cv, std::vector<double> *mut)
     {
-        const Lvl &v = lev[1].lv[solve];
+        const Lvl &v = lev[1].lv[slot];
         const size_t nb = (size_t)(v.IM + 1) * (v.JM + 1) * (v.KM + 1);
         pv.resize(nb * 6);
         cv.resize(nb * 5);
-        if (get_field(solve, 1, "pv", pv.data(), (long)pv.size()) < 0 || get_field(solve, 1, "cv", cv.data(), (long)cv.size()) < 0)
+        if (get_field(slot, 1, "pv", pv.data(), (long)pv.size()) < 0 || get_field(slot, 1, "cv", cv.data(), (long)cv.size()) < 0)
             throw std::runtime_error("state download failed");
         if (mut) {
             mut->resize(nb);
-            if (get_field(solve, 1, "mut", mut->data(), (long)mut->size()) < 0) throw std::runtime_error("state download failed");
+            if (get_field(slot, 1, "mut", mut->data(), (long)mut->size()) < 0) throw std::runtime_error("state download failed");
         }
     }
-    void write_restart(int solve, const std::string &path) override
+    // the fine-level fields of every block of a case
+    void case_fields(int cix, std::vector<std::vector<double>> &pv, std::vector<std::vector<double>> &cv,
+                     std::vector<std::vector<double>> *mut, std::vector<BlockField> &blocks)
     {
-        if (solve < 0 || solve >= nsolve) throw std::runtime_error("bad solve");
-        const Lvl &v = lev[1].lv[solve];
-        std::vector<double> pv, cv;
-        fine_state(solve, pv, cv, nullptr);
-        write_restart_file(default_path(solve, path, "RestartSolution.dat"), v.IM, v.JM, v.KM, pv.data(), cv.data());
+        const int nb = case_nblk[cix];
+        pv.resize(nb); cv.resize(nb);
+        if (mut) mut->resize(nb);
+        blocks.resize(nb);
+        for (int b = 0; b < nb; b++) {
+            const int s = case_first[cix] + b;
+            fine_state(s, pv[b], cv[b], mut ? &(*mut)[b] : nullptr);
+            const Lvl &v = lev[1].lv[s];
+            BlockField &f = blocks[b];
+            f.IM = v.IM; f.JM = v.JM; f.KM = v.KM;
+            f.pv = pv[b].data(); f.cv = cv[b].data(); f.mut = mut ? (*mut)[b].data() : nullptr;
+            f.x = cases[s].x.data(); f.y = cases[s].y.data(); f.z = cases[s].z.data();
+            f.w_rot = lev[1].sc[s].w_rot; f.delta_th = lev[1].sc[s].delta_th;
+        }
     }
-    void write_solution(int solve, const std::string &path) override
+    void write_restart(int cix, const std::string &path) override
     {
-        if (solve < 0 || solve >= nsolve) throw std::runtime_error("bad solve");
-        const Lvl &v = lev[1].lv[solve];
-        std::vector<double> pv, cv, mut;
-        fine_state(solve, pv, cv, &mut);
-        const CaseSpec &c = cases[solve];
+        check_case(cix);
+        std::vector<std::vector<double>> pv, cv;
+        std::vector<BlockField> blocks;
+        case_fields(cix, pv, cv, nullptr, blocks);
+        write_restart_file(default_path(cix, path, "RestartSolution.dat"), blocks);
+    }
+    void write_solution(int cix, const std::string &path) override
+    {
+        check_case(cix);
+        std::vector<std::vector<double>> pv, cv, mut;
+        std::vector<BlockField> blocks;
+        case_fields(cix, pv, cv, &mut, blocks);
+        const CaseSpec &c = cases[case_first[cix]];
         SolutionScales sc;
         sc.gamma = P.gamma; sc.rgas = P.rgas;
         sc.len_ref = c.Len_ref; sc.dens_ref = nd_ref.dens_ref; sc.vel_ref = nd_ref.vel_ref; sc.temp_ref = nd_ref.temp_ref;
         sc.mue_ref = nd_ref.mue_ref; sc.re_ref = nd_ref.re_ref;
-        sc.w_rot = lev[1].sc[solve].w_rot; sc.delta_th = lev[1].sc[solve].delta_th;
-        write_solution_file(default_path(solve, path, "RelativeSolution.plt"), v.IM, v.JM, v.KM, c.x.data(), c.y.data(),
-                            c.z.data(), pv.data(), mut.data(), sc);
+        write_solution_file(default_path(cix, path, "RelativeSolution.plt"), blocks, sc);
     }
-    void read_restart(int solve, const std::string &path) override
+    void read_restart(int cix, const std::string &path) override
     {
-        if (solve < 0 || solve >= nsolve) throw std::runtime_error("bad solve");
-        const Lvl &v = lev[1].lv[solve];
-        const size_t n = (size_t)(v.IM - 1) * (v.JM - 1) * (v.KM - 1);
-        std::vector<double> cv(n * 5), pv(n * 6);
-        read_restart_file(default_path(solve, path, "RestartSolution.dat"), v.IM, v.JM, v.KM, cv.data(), pv.data());
+        check_case(cix);
+        std::vector<BlockField> blocks(case_nblk[cix]);
+        for (int b = 0; b < case_nblk[cix]; b++) {
+            const Lvl &v = lev[1].lv[case_first[cix] + b];
+            blocks[b].IM = v.IM; blocks[b].JM = v.JM; blocks[b].KM = v.KM;
+        }
+        std::vector<std::vector<double>> cvs, pvs;
+        read_restart_file(default_path(cix, path, "RestartSolution.dat"), blocks, cvs, pvs);
         // Q and the primitive variables exactly as read (CUserInput::ReadSolution sets both)
         CK(cudaStreamSynchronize(stream));
-        const long long bn = box_size(v.IM, v.JM, v.KM);
-        Lvl z = v; z.base = 0;
         Flow<T> &W = lev[1].W;
-        for (int c = 0; c < 5; c++) {
-            std::vector<double> h((size_t)bn);
-            CK(cudaMemcpy(h.data(), W.cv[c] + v.base, sizeof(double) * bn, cudaMemcpyDeviceToHost));
-            size_t q = c;
-            for (int i = 1; i <= v.IM - 1; i++)
-                for (int j = 1; j <= v.JM - 1; j++)
-                    for (int k = 1; k <= v.KM - 1; k++, q += 5) h[(size_t)ix(z, i, j, k)] = cv[q];
-            CK(cudaMemcpy(W.cv[c] + v.base, h.data(), sizeof(double) * bn, cudaMemcpyHostToDevice));
-        }
-        for (int c = 0; c < 6; c++) {
-            std::vector<T> h((size_t)bn);
-            CK(cudaMemcpy(h.data(), W.pv[c] + v.base, sizeof(T) * bn, cudaMemcpyDeviceToHost));
-            size_t q = c;
-            for (int i = 1; i <= v.IM - 1; i++)
-                for (int j = 1; j <= v.JM - 1; j++)
-                    for (int k = 1; k <= v.KM - 1; k++, q += 6) h[(size_t)ix(z, i, j, k)] = (T)pv[q];
-            CK(cudaMemcpy(W.pv[c] + v.base, h.data(), sizeof(T) * bn, cudaMemcpyHostToDevice));
+        for (int b = 0; b < case_nblk[cix]; b++) {
+            const Lvl &v = lev[1].lv[case_first[cix] + b];
+            const std::vector<double> &cv = cvs[b], &pv = pvs[b];
+            const long long bn = box_size(v.IM, v.JM, v.KM);
+            Lvl z = v; z.base = 0;
+            for (int c = 0; c < 5; c++) {
+                std::vector<double> h((size_t)bn);
+                CK(cudaMemcpy(h.data(), W.cv[c] + v.base, sizeof(double) * bn, cudaMemcpyDeviceToHost));
+                size_t q = c;
+                for (int i = 1; i <= v.IM - 1; i++)
+                    for (int j = 1; j <= v.JM - 1; j++)
+                        for (int k = 1; k <= v.KM - 1; k++, q += 5) h[(size_t)ix(z, i, j, k)] = cv[q];
+                CK(cudaMemcpy(W.cv[c] + v.base, h.data(), sizeof(double) * bn, cudaMemcpyHostToDevice));
+            }
+            for (int c = 0; c < 6; c++) {
+                std::vector<T> h((size_t)bn);
+                CK(cudaMemcpy(h.data(), W.pv[c] + v.base, sizeof(T) * bn, cudaMemcpyDeviceToHost));
+                size_t q = c;
+                for (int i = 1; i <= v.IM - 1; i++)
+                    for (int j = 1; j <= v.JM - 1; j++)
+                        for (int k = 1; k <= v.KM - 1; k++, q += 6) h[(size_t)ix(z, i, j, k)] = (T)pv[q];
+                CK(cudaMemcpy(W.pv[c] + v.base, h.data(), sizeof(T) * bn, cudaMemcpyHostToDevice));
+            }
         }
     }
 

@@ -1,4 +1,6 @@
-// Host orchestration of a batch of operating points ("solves") on one GPU. The class keeps the
+// Host orchestration of a batch of operating points ("solves", one case directory each) on one GPU.
+// Every block of every case has its own box ("slot"): the blocks of case 0 come first, then those
+// of case 1, and so on; a single-block case has one slot, and then slot and case index agree. The class keeps the
 // reference's call surface (CSolver::Solver, CMesh::ResFlux / Time_Marching / Res_Calculate /
 // PrimitiveVars / Limit_Vars / CornerTreatment, CSolver::Prolong / Interpolate /
 // ComputeDeltConsVars, COutput::OutputGeneralParameters) as methods that enqueue kernels on the
@@ -22,8 +24,10 @@ struct DevBuf {
 class SolverBase {
 public:
     virtual ~SolverBase() = default;
-    int nsolve = 0, ng = 1, coarse_iter = 0, iter = 0, precision = 0;
-    std::vector<CaseSpec> cases;
+    int nsolve = 0, ng = 1, coarse_iter = 0, iter = 0, precision = 0;   // nsolve: slots (blocks of all cases)
+    int ncase = 0;
+    std::vector<int> case_first, case_nblk;      // per case: its first slot and its number of blocks
+    std::vector<CaseSpec> cases;                 // per slot: the options, patches and grid of that block
     Phys P{};
     cudaStream_t stream = nullptr;
     bool use_graphs = true;
@@ -32,7 +36,7 @@ public:
     virtual void resflux(int level) = 0;
     virtual void time_marching(int level) = 0;
     virtual void res_calculate(int level) = 0;
-    // res_calculate with static scratch and no allocation; norms to host_out (5 per solve) if given
+    // res_calculate with static scratch and no allocation; norms to host_out (5 per case) if given
     virtual void res_calculate_static(int level, double *host_out) = 0;
     virtual void primitive_vars(int level) = 0;
     virtual void limit_vars(int level) = 0;
@@ -44,18 +48,22 @@ public:
     virtual void solver_step() = 0;
     // one back-pressure update of the cases that impose their mass flow (after the integrals)
     virtual void mass_flow_imposed() = 0;
-    // current nondimensional back pressure of every solve
+    // current nondimensional back pressure of every case
     virtual void outlet_pressure(double *out) = 0;
-    // n driver iterations; hist (if not null) receives n * nsolve rows of 12 values
+    // n driver iterations; hist (if not null) receives n * ncase rows of 12 values
     virtual void iterate(int n, double *hist) = 0;
-    virtual void dims(int solve, int level, int out[4]) const = 0;
-    virtual long get_field(int solve, int level, const std::string &name, double *out, long cap) = 0;
-    virtual void set_cv(int solve, int level, const double *in, long n) = 0;
-    // the reference's solution files for one solve (fine level): RestartSolution.dat in and out,
-    // RelativeSolution.plt out; an empty path means the file of that name in the case directory
+    // box dimensions and field access address a slot (one block of one case)
+    virtual void dims(int slot, int level, int out[4]) const = 0;
+    virtual long get_field(int slot, int level, const std::string &name, double *out, long cap) = 0;
+    virtual void set_cv(int slot, int level, const double *in, long n) = 0;
+    // the reference's solution files for one case, all its blocks (fine level): RestartSolution.dat
+    // in and out, RelativeSolution.plt out; an empty path means the file of that name in the case
+    // directory
     virtual void read_restart(int solve, const std::string &path) = 0;
     virtual void write_restart(int solve, const std::string &path) = 0;
     virtual void write_solution(int solve, const std::string &path) = 0;
+    // per case: the state of its first slot, with the status bits of all its blocks combined and
+    // their limiter hits summed
     virtual void states(SolveState *out) = 0;
     virtual void set_use_force(int level, bool on) = 0;
     // block shape the sweep autotuner chose for a level: cells per warp, warps per block

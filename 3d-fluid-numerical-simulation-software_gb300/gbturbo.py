@@ -36,6 +36,8 @@ def load() -> ctypes.CDLL:
         "gb_solver_destroy": ([vp], ip),
         "gb_last_error": ([], ctypes.c_char_p),
         "gb_dims": ([vp, ip, ip, ctypes.POINTER(ip)], ip),
+        "gb_num_blocks": ([vp, ctypes.POINTER(ip), ctypes.POINTER(ip)], ip),
+        "gb_case_blocks": ([vp, ip, ctypes.POINTER(ip)], ip),
         "gb_init_uniform": ([vp], ip),
         "gb_resflux": ([vp, ip], ip),
         "gb_time_marching": ([vp, ip], ip),
@@ -81,7 +83,8 @@ EXPORTED = ["gb_solver_create", "gb_solver_destroy", "gb_last_error", "gb_dims",
             "gb_solver_step", "gb_integrals", "gb_iterate", "gb_get_status", "gb_get_field", "gb_set_cv",
             "gb_sync", "gb_set_graphs", "gb_timer_start", "gb_timer_stop", "gb_profile_begin", "gb_profile_end",
             "gb_res_calculate_noalloc", "gb_sweep_tuning", "gb_read_restart", "gb_write_restart",
-            "gb_write_solution", "gb_mass_flow_imposed", "gb_get_outlet_pressure"]
+            "gb_write_solution", "gb_mass_flow_imposed", "gb_get_outlet_pressure", "gb_num_blocks",
+            "gb_case_blocks"]
 
 
 class GBError(RuntimeError):
@@ -116,7 +119,9 @@ HIST_COLUMNS = ["iter", "res_dens", "res_xmom", "res_ymom", "res_zmom", "res_ene
 
 
 class Solver:
-    """A batch of operating points, each read from a reference case directory."""
+    """A batch of operating points, each read from a reference case directory. Per-solve results
+    (norms, integrals, history, status) have one entry per case directory; box access (dims, get,
+    set_cv) takes a slot: the blocks of case 0 come first, then those of case 1, ... (slots())."""
 
     def __init__(self, case_dirs: Union[str, Sequence[str]], precision: int = FP64):
         self._L = load()
@@ -130,6 +135,9 @@ class Solver:
             raise GBError(self._L.gb_last_error().decode())
         self.h = h
         self.n = len(self.case_dirs)
+        nc, nb = ctypes.c_int(), ctypes.c_int()
+        self._ck(self._L.gb_num_blocks(self.h, ctypes.byref(nc), ctypes.byref(nb)))
+        self.n_slots = nb.value
         self.precision = precision
         self.ng = self.dims(0, 1)[3]
 
@@ -153,6 +161,12 @@ class Solver:
 
     def __exit__(self, *a):
         self.close()
+
+    def slots(self, solve: int = 0) -> range:
+        """the slots holding the blocks of one case, in block order"""
+        v = (ctypes.c_int * 2)()
+        self._ck(self._L.gb_case_blocks(self.h, solve, v))
+        return range(v[0], v[0] + v[1])
 
     # ---- reference call surface
     def dims(self, solve: int = 0, level: int = 1):

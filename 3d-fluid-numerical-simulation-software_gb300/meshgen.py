@@ -391,3 +391,124 @@ def sample_operating_points(n: int, seed: int = 2024) -> List[Dict[str, float]]:
                     "IM": m[0], "JM": m[1], "KM": m[2],
                     "stagger_offset": float(rng.normal(0.0, 1.0))})
     return pts
+
+
+# ----------------------------------------------------------------------------------------
+# multi-block cases: blocks stacked along the axis, joined by interfaces
+# ----------------------------------------------------------------------------------------
+@dataclasses.dataclass
+class BlockPatch:
+    """A patch of a multi-block case: ``block`` (1-based) owns it; interfaces and periodic pairs
+    name the partner block in ``block2``."""
+    patch: Patch
+    block: int
+    block2: int = 0
+
+
+@dataclasses.dataclass
+class MultiBlockCase:
+    name: str
+    blocks: List[np.ndarray]       # per block (IM, JM, KM, 3) nodes
+    patches: List[BlockPatch]      # inlets, outlets, walls, periodic pairs and interfaces
+    nblade: int
+    rpm: float
+    options: Dict[str, str]
+
+    @property
+    def n_cells(self) -> int:
+        return sum((b.shape[0] - 1) * (b.shape[1] - 1) * (b.shape[2] - 1) for b in self.blocks)
+
+
+def split_axial(case: Case, cuts: Sequence[int], name: Optional[str] = None) -> MultiBlockCase:
+    """The single-block case cut into blocks at the node planes ``k = cuts`` (1-based), in the
+    H-H-H arrangement of the reference's rotor-67 example (``run_rotor67/BoundaryDefinition.dat``):
+    neighbouring blocks share their cut plane and are joined by an interface between the k+ face
+    of the upstream block and the k- face of the downstream one (orientation 2: the i index of one
+    face runs along the j index of the other's shadow order). Patches on i- and j-faces are split
+    at the cuts; the inlet goes to the first block, the outlet to the last."""
+    IM, JM, KM = case.dims
+    edges = [1] + list(cuts) + [KM]
+    if any(b <= a for a, b in zip(edges, edges[1:])):
+        raise ValueError("cuts must increase strictly inside (1, KM)")
+    blocks = [np.ascontiguousarray(case.nodes[:, :, k0 - 1:k1, :]) for k0, k1 in zip(edges, edges[1:])]
+    out: List[BlockPatch] = []
+    nb = len(blocks)
+    for p in case.patches:
+        if p.kind in ("inlet", "outlet") or p.face in (5, 6):
+            b = 1 if p.face == 5 else nb
+            k = 1 if p.face == 5 else blocks[-1].shape[2]
+            r = list(p.rng)
+            r[4] = r[5] = k
+            out.append(BlockPatch(dataclasses.replace(p, rng=tuple(r)), b))
+            continue
+        for b, (k0, k1) in enumerate(zip(edges, edges[1:]), 1):
+            # cells k0 .. k1-1 of the single block are cells 1 .. k1-k0 of block b
+            lo, hi = max(p.rng[4], k0), min(p.rng[5], k1 - 1)
+            if lo > hi:
+                continue
+            r = list(p.rng)
+            r[4], r[5] = lo - k0 + 1, hi - k0 + 1
+            q = dataclasses.replace(p, rng=tuple(r))
+            if p.kind == "periodic":
+                r2 = list(p.rng2)
+                r2[4], r2[5] = r[4], r[5]
+                q = dataclasses.replace(q, rng2=tuple(r2))
+                out.append(BlockPatch(q, b, b))
+            else:
+                out.append(BlockPatch(q, b))
+    for b in range(1, nb):
+        kb = blocks[b - 1].shape[2]
+        face = Patch("interior", 6, (1, IM - 1, 1, JM - 1, kb, kb), face2=5, rng2=(1, IM - 1, 1, JM - 1, 1, 1), orient=2)
+        out.append(BlockPatch(face, b, b + 1))
+    return MultiBlockCase(name or case.name + "_mb", blocks, out, case.nblade, case.rpm, dict(case.options))
+
+
+def _bc_text_multi(case: MultiBlockCase) -> str:
+    def sel(kind):
+        return [p for p in case.patches if p.patch.kind == kind]
+
+    def rng(t):
+        return "\t".join(str(v) for v in t)
+
+    inl, out, wal, per, itf = sel("inlet"), sel("outlet"), sel("wall"), sel("periodic"), sel("interior")
+    L = ["# Boundary definition", "#", "# inlet", "#---------------------------",
+         f" {len(inl)}\t\t# number of inlets", "#ID_BID FT_Ista_Iend_Jsta_Jend_Ksta_Kend"]
+    L += [f"{n}\t{p.block}\t{p.patch.face}\t{rng(p.patch.rng)}" for n, p in enumerate(inl, 1)]
+    L += ["#", "# outlet", "#---------------------------",
+          f" {len(out)}\t\t# number of outlets", "#ID_BID_FT_Ista_Iend_Jsta_Jend_Ksta_Kend"]
+    L += [f"{n}\t{p.block}\t{p.patch.face}\t{rng(p.patch.rng)}" for n, p in enumerate(out, 1)]
+    L += ["#", "# wall", "#---------------------------",
+          f" {len(wal)}\t\t# number of Walls", "#ID_BID_FT_wrot_Ista_Iend_Jsta_Jend_Ksta_Kend"]
+    L += [f"{n}\t{p.block}\t{p.patch.face}\t{p.patch.rotate}\t{rng(p.patch.rng)}" for n, p in enumerate(wal, 1)]
+    L += ["#", "# periodic", "#---------------------------", f"{len(per)}\t\t# number of Periodics",
+          "#ID_ori_BID1_FT1_Ista1_Iend1_Jsta1_Jend1_Ksta1_Kend1_BID2_FT2_..."]
+    L += [f"{n}\t{p.patch.orient}\t{p.block}\t{p.patch.face}\t{rng(p.patch.rng)}\t{p.block2}\t{p.patch.face2}\t"
+          f"{rng(p.patch.rng2)}" for n, p in enumerate(per, 1)]
+    L += ["#", "# interior", "#--------------------------", f" {len(itf)}\t\t# number of Interiors",
+          "#ID_ori_BID1_FT1_Ista1_Iend1_Jsta1_Jend1_Ksta1_Kend1_BID2_FT2_..."]
+    L += [f"{n}\t{p.patch.orient}\t{p.block}\t{p.patch.face}\t{rng(p.patch.rng)}\t{p.block2}\t{p.patch.face2}\t"
+          f"{rng(p.patch.rng2)}" for n, p in enumerate(itf, 1)]
+    L += ["#", "# mixing plane", "#--------------------------", " 0\t\t# number of MixingPlanes",
+          "#ID_ori_BID1_FT1_...", "#", "# Blocks", "#--------------------------",
+          f"{len(case.blocks)}\t\t# number of Blocks", "#BID_IM_JM_KM_Nblade_rpm"]
+    for b, nodes in enumerate(case.blocks, 1):
+        IM, JM, KM = nodes.shape[:3]
+        L.append(f"{b}    {IM} {JM} {KM}\t{case.nblade}  {case.rpm:.17g}")
+    L.append("")
+    return "\n".join(L)
+
+
+def write_multiblock_case(case: MultiBlockCase, directory: str, gridfile: str = "grid.dat") -> None:
+    """Grid file with every block (block count, then per block its id, ``IM JM KM`` and nodes),
+    BoundaryDefinition.dat with block ids, config.dat."""
+    os.makedirs(directory, exist_ok=True)
+    with open(os.path.join(directory, gridfile), "w") as f:
+        f.write("%d\n" % len(case.blocks))
+        for b, nodes in enumerate(case.blocks, 1):
+            IM, JM, KM = nodes.shape[:3]
+            f.write("%d\n%d %d %d\n" % (b, IM, JM, KM))
+            np.savetxt(f, np.ascontiguousarray(np.transpose(nodes, (2, 1, 0, 3)).reshape(-1, 3)), fmt="%.17g")
+    with open(os.path.join(directory, "BoundaryDefinition.dat"), "w") as f:
+        f.write(_bc_text_multi(case))
+    with open(os.path.join(directory, "config.dat"), "w") as f:
+        f.write(_config_text(case.options, gridfile, "BoundaryDefinition.dat"))

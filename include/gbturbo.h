@@ -3,7 +3,12 @@
  *
  * A handle owns one batch of operating points ("solves") on the current CUDA device; each solve
  * is configured from the reference's own case files (config.dat, BoundaryDefinition.dat and the
- * grid file named in config.dat) and all solves of a batch share the numerical options. The
+ * grid file named in config.dat) and all solves of a batch share the numerical options. A solve
+ * may have several blocks joined by interfaces (source/BndCondInteriorPeriodic.cpp:8-34); every
+ * block has its own slot in the handle, the blocks of solve 0 first, then those of solve 1, and
+ * so on (gb_case_blocks). Calls that report per solve (norms, integrals, history, status, back
+ * pressure, solution files) take or fill one entry per solve; calls that address one box (dims,
+ * field access) take a slot, which equals the solve index when every solve has one block. The
  * entry points replace the reference's C++ member-function surface one for one (file:line of the
  * reference in each comment). All calls are asynchronous on the handle's stream unless they
  * return data to host buffers; all return 0 on success and a negative code on failure, with
@@ -34,8 +39,12 @@ int gb_solver_destroy(gb_solver *h);
 /* message of the last failure on the calling thread */
 const char *gb_last_error(void);
 
-/* out[0..3] = IM, JM, KM (node counts) of a level of one solve, and the number of levels */
+/* out[0..3] = IM, JM, KM (node counts) of a level of one slot (block), and the number of levels */
 int gb_dims(gb_solver *h, int solve, int level, int out[4]);
+/* number of solves (case directories) and of slots (blocks of all solves); either may be NULL */
+int gb_num_blocks(gb_solver *h, int *n_cases, int *n_blocks);
+/* out[0] = first slot of a solve, out[1] = its number of blocks (CMesh::NB) */
+int gb_case_blocks(gb_solver *h, int solve, int out[2]);
 
 /* CMesh::Initial, uniform start (source/Initialization.cpp:17-76) on the coarsest used level */
 int gb_init_uniform(gb_solver *h);
@@ -74,17 +83,18 @@ int gb_iterate(gb_solver *h, int n, double *hist);
  * last step, bit 4: limiter list overflow); out[n_solves] */
 int gb_get_status(gb_solver *h, int *out);
 
-/* Copies a named array of one solve and level to out (row-major, components fastest):
+/* Copies a named array of one slot (block) and level to out (row-major, components fastest):
  * "cv" (IM+1,JM+1,KM+1,5) and "pv" (..,6), "mut" (..,1) including ghosts; "res","dq" and
  * "dt","omega","lamcI".."lamvK" over the cells; "FcI","FvI" (IM,JM-1,KM-1,5) and J, K;
- * "faceI" (IM,JM-1,KM-1,18), "faceJ", "faceK", "cell" (IM-1,JM-1,KM-1,13), "totalvol";
+ * "faceI" (IM,JM-1,KM-1,18), "faceJ", "faceK", "cell" (IM-1,JM-1,KM-1,13), "totalvol" (of the
+ * slot's whole solve, CMesh::TotalVol);
  * "dIS_cv".."dKP_pv" reconstruction layers. Returns the count written (>= 0) or < 0. */
 long gb_get_field(gb_solver *h, int solve, int level, const char *name, double *out, long cap);
 /* overwrites the interior conserved variables (IM-1,JM-1,KM-1,5) and the primitive variables */
 int gb_set_cv(gb_solver *h, int solve, int level, const double *cv, long n);
 
-/* The reference's solution files for one solve (fine level). A NULL path means the file of that
- * name in the solve's case directory.
+/* The reference's solution files for one solve, all its blocks in block order (fine level). A
+ * NULL path means the file of that name in the solve's case directory.
  * gb_read_restart: CUserInput::ReadSolution (source/UserInput.cpp:1118-1159): reads
  *   RestartSolution.dat and sets Q and the primitive variables as read; it takes the place of
  *   gb_init_uniform for cases whose config asks for the previous solution, for which the driver
@@ -127,7 +137,7 @@ int gb_timer_stop(gb_solver *h, float *ms);
  * inside the library. It has no counterpart in the reference; it exists for callers that may not
  * allocate between iterations (a convergence monitor of a batch whose device memory is committed
  * to the solve pools, a host thread under a no-heap rule). Batches of more than
- * GB_NOALLOC_MAX_SOLVES solves are rejected with GB_ERR_ARG. All calls on a device share the one
+ * GB_NOALLOC_MAX_SOLVES slots (blocks of all solves) are rejected with GB_ERR_ARG. All calls on a device share the one
  * array, so calls that overlap in time race and must be serialised by the caller. The first call
  * on a device looks the array up and zeroes it: make that call before any stream capture begins.
  * Call it with the handle's device current. */

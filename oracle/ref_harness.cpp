@@ -104,9 +104,9 @@ static double cell_c(const TCell &f, int c)
     }
 }
 
-static void dump_geometry(CMesh &M, const std::string &p)
+static void dump_geometry(CMesh &M, const std::string &p, int nb = 1)
 {
-    CGeometry &G = M.Block[1].Geometry;
+    CGeometry &G = M.Block[nb].Geometry;
     int IM = G.IM, JM = G.JM, KM = G.KM;
     dump_box(p + "faceI", G.FaceI, 1, IM, 1, JM - 1, 1, KM - 1, 18, face_c);
     dump_box(p + "faceJ", G.FaceJ, 1, IM - 1, 1, JM, 1, KM - 1, 18, face_c);
@@ -115,9 +115,9 @@ static void dump_geometry(CMesh &M, const std::string &p)
     npy_write(p + "totalvol", {(double)M.TotalVol}, {1});
 }
 
-static void dump_state(CMesh &M, const std::string &p)
+static void dump_state(CMesh &M, const std::string &p, int nb = 1)
 {
-    CBlocks &B = M.Block[1];
+    CBlocks &B = M.Block[nb];
     CFluidProps &F = B.FluidProp;
     int IM = B.Geometry.IM, JM = B.Geometry.JM, KM = B.Geometry.KM;
     dump_cells(p + "cv", F.Cell_cv, IM, JM, KM, 5, cv_c);
@@ -126,14 +126,14 @@ static void dump_state(CMesh &M, const std::string &p)
                [](const TVisVars &v, int) { return (double)v.mue; });
 }
 
-static void dump_resflux(CMesh &M, const std::string &p)
+static void dump_resflux(CMesh &M, const std::string &p, int nb = 1)
 {
-    CBlocks &B = M.Block[1];
+    CBlocks &B = M.Block[nb];
     CFluidProps &F = B.FluidProp;
     CSpaceDiscr &S = B.SpaceDiscr;
     CTimeDiscr &T = B.TimeDiscr;
     int IM = B.Geometry.IM, JM = B.Geometry.JM, KM = B.Geometry.KM;
-    dump_state(M, p);
+    dump_state(M, p, nb);
     auto cvg = cv_c;
     auto pvg = pv_c;
     // reconstruction dummies, stored as [layer 1..2] in the direction normal to the face
@@ -195,9 +195,15 @@ int main(int argc, char **argv)
     else if (Solver.NG == 1) Solver.Mesh[1].Initial();
     else Solver.Mesh[2].Initial();
 
-    dump_geometry(Solver.Mesh[1], "g1_");
-    if (Solver.NG == 2) dump_geometry(Solver.Mesh[2], "g2_");
+    // a case of several blocks gets every array once per block, prefixed "b<block>_"
+    const int NB = CMesh::NB;
+    auto bp = [&](int nb) { return NB > 1 ? "b" + std::to_string(nb) + "_" : std::string(); };
+    for (int nb = 1; nb <= NB; nb++) {
+        dump_geometry(Solver.Mesh[1], bp(nb) + "g1_", nb);
+        if (Solver.NG == 2) dump_geometry(Solver.Mesh[2], bp(nb) + "g2_", nb);
+    }
     npy_write("ng", {(double)Solver.NG}, {1});
+    npy_write("nb", {(double)NB}, {1});
 
     // history rows: iter, Res.dens, Res.xmom..ener, m_in, m_out, PR, eta, m_ratio, CFL
     std::vector<double> hist;
@@ -229,13 +235,15 @@ int main(int argc, char **argv)
         COutput::OutputSolution(Solver.Mesh[1]);
         COutput::OutputRestartSolution(Solver.Mesh[1]);
     }
-    dump_state(Solver.Mesh[1], "s1_");
-    if (Solver.NG == 2) dump_state(Solver.Mesh[2], "s2_");
+    for (int nb = 1; nb <= NB; nb++) {
+        dump_state(Solver.Mesh[1], bp(nb) + "s1_", nb);
+        if (Solver.NG == 2) dump_state(Solver.Mesh[2], bp(nb) + "s2_", nb);
+    }
     if (dump_rf) {
         // one more residual evaluation on the fine level at the final state, with every
         // intermediate array of the path
         Solver.Mesh[1].ResFlux();
-        dump_resflux(Solver.Mesh[1], "r1_");
+        for (int nb = 1; nb <= NB; nb++) dump_resflux(Solver.Mesh[1], bp(nb) + "r1_", nb);
     }
     // the reference's destructors crash on the two-level mesh arrays; the dumps are complete
     fflush(nullptr);

@@ -9,8 +9,8 @@ evaluation at that state (every intermediate array) in tests/golden/<name>.npz.
 Only runs where the reference sources and a C++ compiler exist; the fixtures it writes are
 committed so the tests need neither.
 
-    python tests/golden/make_golden.py [name ...]      (default: every short case and the restart case;
-                                                        long cases by name)
+    python tests/golden/make_golden.py [name ...]      (default: every short case, the restart case and
+                                                        the multi-block cases; long cases by name)
 """
 from __future__ import annotations
 
@@ -56,6 +56,14 @@ CASES = {
 # same generator call (its grid file is several MB)
 LONG = {
     "duct_33x33x65_2000": ("annular_duct", dict(IM=33, JM=33, KM=65), {}, 2000),
+}
+
+# multi-block: the rotor passage cut at the blade's leading- and trailing-edge planes into three
+# blocks joined by interfaces (meshgen.split_axial); every array per block ("b<block>_" prefix),
+# and the reference's solution and restart files written at the end
+MULTI = {
+    "rotor_9x9x33_3block": (dict(IM=9, JM=9, KM=33), [9, 25], {}, 12),
+    "rotor_9x9x33_3block_mg": (dict(IM=9, JM=9, KM=33), [9, 25], {"multigrid": "Y", "coarse_iter": "4"}, 12),
 }
 
 # restart round trip: the reference runs n1 iterations and writes its solution and restart files,
@@ -113,7 +121,39 @@ def make_restart(name: str) -> None:
     print(name, "iterations:", n1, "+", n2)
 
 
+def make_multi(name: str) -> None:
+    mg = _meshgen()
+    kw, cuts, opts, n_iter = MULTI[name]
+    case = mg.split_axial(mg.rotor_passage(**kw, options=dict(opts), name=name), cuts, name=name)
+    cdir = os.path.join(HERE, name)
+    if os.path.isdir(cdir):
+        shutil.rmtree(cdir)
+    mg.write_multiblock_case(case, cdir)
+    keep = ("cv", "pv", "mut", "omega", "lamcK", "lamvK", "dt", "FcK", "FvK", "FcJ", "res", "dKS_pv", "dKP_pv")
+    with tempfile.TemporaryDirectory() as tmp:
+        for f in os.listdir(cdir):
+            shutil.copy(os.path.join(cdir, f), tmp)
+        out = os.path.join(tmp, "out")
+        subprocess.run([HARNESS, str(n_iter), out, "1", "1"], cwd=tmp, check=True, stdout=subprocess.DEVNULL)
+        data = {"history": np.load(os.path.join(out, "history.npy"))}
+        for f in sorted(os.listdir(out)):
+            key = f[:-4]
+            parts = key.split("_", 2)
+            if not key.startswith("b") or len(parts) < 3:
+                continue
+            kind, field = parts[1], parts[2]
+            if (kind == "r1" and field in keep) or (kind == "g1" and field in ("faceK", "cell", "totalvol")):
+                data[key] = np.load(os.path.join(out, f))
+        for key, f in (("restart_file", "RestartSolution.dat"), ("solution_file", "RelativeSolution.plt")):
+            data[key] = np.frombuffer(open(os.path.join(tmp, f), "rb").read(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **data)
+    print(name, "iterations:", int(data["history"].shape[0]))
+
+
 def make(name: str) -> None:
+    if name in MULTI:
+        make_multi(name)
+        return
     if name in RESTART:
         make_restart(name)
         return
@@ -152,5 +192,5 @@ def make(name: str) -> None:
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: oracle/build_ref.sh")
-    for n in (sys.argv[1:] or list(CASES) + list(RESTART)):
+    for n in (sys.argv[1:] or list(CASES) + list(RESTART) + list(MULTI)):
         make(n)
