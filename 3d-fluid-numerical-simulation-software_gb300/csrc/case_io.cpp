@@ -308,8 +308,8 @@ void validate_block(const CaseSpec &c)
 
 void validate(const CaseSpec &c)
 {
-    if (c.scheme != 200 && c.scheme != 300)
-        throw std::runtime_error("space scheme " + std::to_string(c.scheme) + " is not on this path (Steger-Warming 200, Roe 300)");
+    if (c.scheme != 100 && c.scheme != 200 && c.scheme != 300)
+        throw std::runtime_error("space scheme " + std::to_string(c.scheme) + " is not on this path (JST 100, Steger-Warming 200, Roe 300)");
     if (c.recon_var != 100 && c.recon_var != 200)
         throw std::runtime_error("reconstruction variables " + std::to_string(c.recon_var) + " are not supported (100, 200)");
     if (c.time_scheme >= 100 && c.time_scheme <= 400)

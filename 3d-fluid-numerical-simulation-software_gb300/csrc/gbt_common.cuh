@@ -4,7 +4,7 @@
 // box i in [-3, IM+3] x j in [-3, JM+3] x k in [-3, KM+3] with k contiguous (the axial index is
 // the longest one on turbomachinery passages, so warps read along it). Cell (i,j,k) spans nodes
 // i..i+1; index 0 and IM hold the first ghost layer of the reference solver and the two
-// reconstruction layers ("dummies") sit at -1,-2 and IM+1, IM+2. Face family f (0=I, 1=J, 2=K)
+// reconstruction layers ("dummies") sit at -1,-2 and IM+1, IM+2 (a third at -3, IM+3 with JST). Face family f (0=I, 1=J, 2=K)
 // at (i,j,k) is the reference's FaceI/J/K[i][j][k]. All solves of a batch share one pool per
 // field; a solve's box starts at Lvl::base.
 #pragma once
@@ -57,6 +57,7 @@ struct Flow {
     T *mut, *omega, *dt;
     T *lamc[3], *lamv[3];
     T *Ff[3][NQ], *Vf[3][NQ];                        // face convective / viscous fluxes
+    T *Fd[3][NQ];                                    // face artificial dissipation (JST only, else null)
     T *res[NQ], *dq[NQ];
     double *cv2h[NQ];                                // multigrid (coarse level only)
     T *res2h[NQ], *dq2h[NQ];
@@ -101,6 +102,7 @@ struct Phys {
     double inlet_dir[3], inlet_vnm;
     double c_timestep, relax;
     double suth_c1, suth_c2;                         // (1 + 110.4/288.15) and 110.4/288.15 (float-rounded)
+    double k2, k4;                                   // JST coefficients (k4 as the reciprocal of the config value)
     int equation_ns, turb_bl, recon_var, recon, scheme, limiter, global_dt, ndummy;
 };
 

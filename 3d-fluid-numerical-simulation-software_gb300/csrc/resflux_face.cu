@@ -69,10 +69,11 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 4) k_face(Batch B, P
     const T Sx = G.S[F][0][p], Sy = G.S[F][1][p], Sz = G.S[F][2][p];
     const int wq = W.wallf[F][p];
     T f0, f1, f2, f3, f4;
-    if (wq) {
+    if (wq || (!MODE && scheme == 100)) {
         // wall face: flux from the face average of ghost and interior, in the wall's frame
-        const DevWall wl = walls[wq - 1];
-        const T rot = wl.rotate ? (T)B.sc[s].w_rot : (T)0;
+        // (source/WallFlux.cpp:70-175); the JST central flux has the same form in the block's
+        // frame (source/JST_Convective.cpp:53-95)
+        const T rot = wq ? (walls[wq - 1].rotate ? (T)B.sc[s].w_rot : (T)0) : (T)B.sc[s].w_rot;
         const long long m = p - sn;
         const P6<T> A = ld_pv(W, p), Bq = ld_pv(W, m);
         const T d = (T)0.5 * (A.d + Bq.d), u = (T)0.5 * (A.u + Bq.u), v = (T)0.5 * (A.v + Bq.v),
@@ -181,7 +182,62 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 4) k_face(Batch B, P
     W.Vf[F][4][p] = qx * Sx + qy * Sy + qz * Sz;
 }
 
-// face sums, rotation source, residual R = Fc - Fv
+// JST artificial dissipation of one face (source/JST_Dissip.cpp:193-413): pressure sensors of the
+// four cells around the face, blended second and fourth differences of Q scaled by the
+// anisotropy-weighted spectral radius. Positions along the face normal follow the reference's
+// switch between cells and reconstruction layers (position c <= 0 is dummy layer 1 - c, c >= N
+// dummy layer c - N + 1).
+template <typename T, int F>
+__global__ void __launch_bounds__(128) k_jst_dissip(Batch B, Phys P, Flow<T> W)
+{
+    const int s = blockIdx.y;
+    const Lvl L = B.lv[s];
+    int ni, nj, nk, i, j, k;
+    face_extent(L, F, ni, nj, nk);
+    if (!box_index(ni, nj, nk, i, j, k)) return;
+    const long long p = ix(L, i, j, k);
+    const long long sn = F == 0 ? (long long)L.NJ * L.NK : (F == 1 ? (long long)L.NK : 1LL);
+    const int NN = F == 0 ? L.IM : (F == 1 ? L.JM : L.KM);
+    const int a = F == 0 ? i : (F == 1 ? j : k);
+    const long long p0 = p - (long long)a * sn;
+    auto at = [&](int c) { return p0 + (long long)(c <= 0 ? c - 1 : (c >= NN ? c + 1 : c)) * sn; };
+    // pressure sensor of position c (sensorI/J/K, :5-190); the k-direction sensor's range check
+    // compares j with KM, as the reference's does
+    const bool out_of_range = F == 2 && j > L.KM;
+    auto sensor = [&](int c) -> T {
+        if (out_of_range) return (T)0;
+        const T pf = W.pv[PP][at(c + 1)], pc = W.pv[PP][at(c)], pb = W.pv[PP][at(c - 1)];
+        return fabs((pf - (T)2 * pc + pb) / (pf + (T)2 * pc + pb));
+    };
+    const T e2 = (T)P.k2 * fmax(fmax(sensor(a + 1), sensor(a)), fmax(sensor(a - 1), sensor(a - 2)));
+    const T e4 = fmax((T)0, (T)P.k4 - e2);
+    // anisotropy weight phi * lambda of the cell on each side (:198-216)
+    // the two other directions in the reference's order of the sum: I faces J, K; J faces I, K;
+    // K faces J, I
+    const int t1 = F == 1 ? 0 : 1, t2 = F == 2 ? 0 : 2;
+    const T ex = (T)(double)0.4f;
+    auto va = [&](long long q) -> T {
+        const T ln = W.lamc[F][q];
+        const T a1 = W.lamc[t1][q] / ln, a2 = W.lamc[t2][q] / ln;
+        const T phi = (T)1 + pow(a1, ex) + pow(a2, ex);
+        return phi * ln;
+    };
+    T alpha;
+    if (a == 1) alpha = va(p);
+    else if (a == NN) alpha = va(p - sn);
+    else alpha = (T)0.5 * (va(p) + va(p - sn));
+    const long long c1 = at(a + 1), c2 = at(a), c3 = at(a - 1), c4 = at(a - 2);
+    T d[NQ];
+#pragma unroll
+    for (int c = 0; c < NQ; c++) {
+        const T q1 = (T)W.cv[c][c1], q2 = (T)W.cv[c][c2], q3 = (T)W.cv[c][c3], q4 = (T)W.cv[c][c4];
+        d[c] = alpha * (e2 * (q2 - q3) - e4 * (q1 - (T)3 * q2 + (T)3 * q3 - q4));
+    }
+#pragma unroll
+    for (int c = 0; c < NQ; c++) W.Fd[F][c][p] = d[c];
+}
+
+// face sums, rotation source, residual R = Fc - Fv (- Fd with JST)
 template <typename T>
 __global__ void __launch_bounds__(256) k_cell_sum(Batch B, Phys P, GeoW<T> G, Flow<T> W)
 {
@@ -202,6 +258,8 @@ __global__ void __launch_bounds__(256) k_cell_sum(Batch B, Phys P, GeoW<T> G, Fl
         if (P.equation_ns)
             fv = W.Vf[0][c][pI] - W.Vf[0][c][p] + W.Vf[1][c][pJ] - W.Vf[1][c][p] + W.Vf[2][c][pK] - W.Vf[2][c][p];
         r[c] = fc - fv;
+        if (W.Fd[0][0])
+            r[c] = r[c] - (W.Fd[0][c][pI] - W.Fd[0][c][p] + W.Fd[1][c][pJ] - W.Fd[1][c][p] + W.Fd[2][c][pK] - W.Fd[2][c][p]);
     }
 #pragma unroll
     for (int c = 0; c < NQ; c++) W.res[c][p] = r[c];
@@ -232,6 +290,13 @@ void launch_resflux(const LaunchCtx &ctx, const Phys &P, const PhysW<T> &PC, con
         k_face<T, 2, 0><<<ctx.grid_faces(2, 128), 128, 0, ctx.stream>>>(B, P, PC, GW, W, bc.wall);
     }
     ctx.mark("face_flux", 0, 3);
+    if (P.scheme == 100) {
+        ctx.mark("jst_dissipation", 1, 3);
+        k_jst_dissip<T, 0><<<ctx.grid_faces(0, 128), 128, 0, ctx.stream>>>(B, P, W);
+        k_jst_dissip<T, 1><<<ctx.grid_faces(1, 128), 128, 0, ctx.stream>>>(B, P, W);
+        k_jst_dissip<T, 2><<<ctx.grid_faces(2, 128), 128, 0, ctx.stream>>>(B, P, W);
+        ctx.mark("jst_dissipation", 0, 3);
+    }
     ctx.mark("cell_sum", 1);
     k_cell_sum<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, GW, W);
     ctx.mark("cell_sum", 0);

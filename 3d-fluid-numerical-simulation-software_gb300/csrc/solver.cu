@@ -58,6 +58,7 @@ struct Level {
     Geo G{};
     GeoW<T> GW{};                         // working-precision geometry (aliases in FP64, FP32 copies in mixed)
     DevBuf geow_mem;
+    DevBuf fd_mem;                        // JST face dissipation
     DevBuf wdist_mem;                     // Baldwin-Lomax wall distances (fine level)
     Flow<T> W{};
     double *totalvol = nullptr, *blockvol = nullptr;
@@ -352,6 +353,7 @@ public:
             if (c.ng != c0.ng || c.coarse_iter != c0.coarse_iter || c.scheme != c0.scheme || c.recon != c0.recon ||
                 c.recon_var != c0.recon_var || c.turb != c0.turb || c.equation_ns != c0.equation_ns ||
                 c.limiter != c0.limiter || c.global_dt != c0.global_dt || c.Gamma != c0.Gamma || c.Rgas != c0.Rgas ||
+                c.k2 != c0.k2 || c.k4 != c0.k4 ||
                 c.restart != c0.restart ||
                 c.Pr_lam != c0.Pr_lam || c.Pr_tur != c0.Pr_tur || c.Ptin != c0.Ptin || c.Ttin != c0.Ttin ||
                 c.Len_ref != c0.Len_ref || c.relax != c0.relax || c.C_timestep != c0.C_timestep ||
@@ -373,7 +375,9 @@ public:
         P.suth_c2 = (double)(110.4f / 288.15f);
         P.equation_ns = c0.equation_ns; P.turb_bl = c0.turb == 100; P.recon_var = c0.recon_var; P.recon = c0.recon;
         P.scheme = c0.scheme; P.limiter = c0.limiter; P.global_dt = c0.global_dt;
-        P.ndummy = c0.recon == 0 ? 3 : 2;
+        P.k2 = c0.k2; P.k4 = c0.k4;
+        // dummy layers: three for no reconstruction and for JST (source/UserInput.cpp:131-163)
+        P.ndummy = (c0.recon == 0 || c0.scheme == 100) ? 3 : 2;
         PC = phys_working<T>(P);
 
         CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
@@ -482,6 +486,16 @@ public:
         W.mut = tk(); W.omega = tk(); W.dt = tk();
         for (int f = 0; f < 3; f++) { W.lamc[f] = tk(); W.lamv[f] = tk(); for (int c = 0; c < NQ; c++) { W.Ff[f][c] = tk(); W.Vf[f][c] = tk(); } }
         for (int c = 0; c < NQ; c++) { W.res[c] = tk(); W.dq[c] = tk(); W.res2h[c] = tk(); W.dq2h[c] = tk(); }
+        if (P.scheme == 100) {
+            // face dissipation of JST (source/SpaceDiscr.cpp:611-640)
+            Lv.fd_mem.bytes = sizeof(T) * N * 15;
+            CK(cudaMalloc(&Lv.fd_mem.p, Lv.fd_mem.bytes));
+            CK(cudaMemset(Lv.fd_mem.p, 0, Lv.fd_mem.bytes));
+            T *fd = (T *)Lv.fd_mem.p;
+            for (int f = 0; f < 3; f++) for (int c = 0; c < NQ; c++) { W.Fd[f][c] = fd; fd += N; }
+        } else {
+            for (int f = 0; f < 3; f++) for (int c = 0; c < NQ; c++) W.Fd[f][c] = nullptr;
+        }
         Lv.int_mem.bytes = sizeof(int) * N * 4;
         CK(cudaMalloc(&Lv.int_mem.p, Lv.int_mem.bytes));
         CK(cudaMemset(Lv.int_mem.p, 0, Lv.int_mem.bytes));

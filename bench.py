@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=1, help="operating points per GPU")
     ap.add_argument("--sampled", action="store_true",
                     help="draw the batch from the seeded operating-point sampler (three mesh sizes)")
+    ap.add_argument("--blocks", type=int, default=1, choices=[1, 3],
+                    help="3: the passage as three blocks joined by interfaces (reference's rotor-67 layout)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the secondary measurements of the mixed-precision and batched forms")
@@ -57,9 +59,10 @@ def parse():
     return ap.parse_args()
 
 
-def make_cases(root: str, n: int, seed_offset: int = 0, back_pressures=None):
+def make_cases(root: str, n: int, seed_offset: int = 0, back_pressures=None, blocks: int = 1):
     """the 129 x 49 x 49 rotor passage; in a batch the back pressure varies over [1.05, 1.30] x p_t
-    (or is given, as ratios to the inlet total pressure)"""
+    (or is given, as ratios to the inlet total pressure). blocks=3: the same passage cut at the
+    blade's leading- and trailing-edge planes (k = 41, 89) into three blocks joined by interfaces"""
     import meshgen as mg
     dirs = []
     for q in range(n):
@@ -69,7 +72,12 @@ def make_cases(root: str, n: int, seed_offset: int = 0, back_pressures=None):
         case = mg.rotor_passage(IM=49, JM=49, KM=129, options={
             "Pout": "%.1f" % (pb * 101325.0), "multigrid": "Y", "coarse_iter": "2", "Ma0": "0.45"})
         d = os.path.join(root, f"op{q}")
-        mg.write_case(case, d)
+        if blocks == 3:
+            mg.write_multiblock_case(mg.split_axial(case, [41, 89]), d)
+        elif blocks == 1:
+            mg.write_case(case, d)
+        else:
+            raise ValueError("--blocks takes 1 or 3")
         dirs.append(d)
     return dirs, case.n_cells
 
@@ -417,6 +425,8 @@ def run_study(args):
 def config_block(args, cells, nsolve):
     if getattr(args, "sampled", False):
         wl, mesh = "sampled_rotor_passages_2level_multigrid", "97x41x41 / 129x49x49 / 161x65x65 (seeded sampler)"
+    elif getattr(args, "blocks", 1) == 3:
+        wl, mesh = "rotor_passage_129x49x49_3block_2level_multigrid", "129x49x49 as blocks of 41/49/41 axial nodes"
     else:
         wl, mesh = "rotor_passage_129x49x49_2level_multigrid", "129x49x49 (axial x pitch x span)"
     return {"workload": wl, "mesh_nodes": mesh,
@@ -441,7 +451,7 @@ def run_gpu(args, rank, world, dist):
             dirs, cell_list = make_sampled_cases(tmp, args.batch, seed=2024 + rank)
             cells = sum(cell_list) / len(cell_list)     # mean per solve; totals below multiply by nsolve
         else:
-            dirs, cells = make_cases(tmp, args.batch, seed_offset=rank)
+            dirs, cells = make_cases(tmp, args.batch, seed_offset=rank, blocks=args.blocks)
         nsolve = len(dirs)
         grid_bytes = sum(os.path.getsize(os.path.join(d, "grid.dat")) for d in dirs)
 
@@ -467,7 +477,7 @@ def run_gpu(args, rank, world, dist):
         s.profile_begin()
         s.iterate(nprof, history=False)
         prof = s.profile_end()
-        level_dims = [s.dims(q, l)[:3] for q in range(nsolve) for l in range(1, s.ng + 1)]
+        level_dims = [s.dims(q, l)[:3] for q in range(s.n_slots) for l in range(1, s.ng + 1)]
         tuning = {f"level{l}": list(s.sweep_tuning(l)) for l in range(1, s.ng + 1)}
         total_prof = sum(v[0] for v in prof.values())
         launches_per_step = sum(v[1] for v in prof.values()) / nprof
@@ -493,7 +503,7 @@ def run_gpu(args, rank, world, dist):
         except FileNotFoundError:
             pass
         forms = None
-        if rank == 0 and world == 1 and not args.no_forms and prec == gbturbo.FP64 and nsolve == 1:
+        if rank == 0 and world == 1 and not args.no_forms and prec == gbturbo.FP64 and nsolve == 1 and args.blocks == 1:
             n_ref = max(args.warmup, 3) + args.steps + nprof
             forms = measure_forms(gbturbo, dirs, cells, n_ref, s.integrals(1)[0], min(args.steps, 50), tmp)
         s.close()
@@ -514,7 +524,8 @@ def run_gpu(args, rank, world, dist):
         e2e_value = cells * nsolve * world * n_e2e / t_e2e
 
         base = None
-        if rank == 0 and not args.no_cpu_baseline:
+        if rank == 0 and not args.no_cpu_baseline and args.blocks == 1:
+            # (the CPU oracle port is single-block)
             base = cpu_baseline(dirs[0], cells, warm=3, steps=2)
 
         if rank == 0:

@@ -47,6 +47,10 @@ CASES = {
                                    {"recon": "200", "timestep": "G", "limiter": "N"}, 10),
     "rotor_9x9x33": ("rotor_passage", dict(IM=9, JM=9, KM=33), {}, 20),
     "rotor_9x9x33_mg": ("rotor_passage", dict(IM=9, JM=9, KM=33), {"multigrid": "Y", "coarse_iter": "5"}, 14),
+    # JST central scheme with artificial dissipation (k2 0.6, k4 1/100), three dummy layers
+    "duct_9x9x17_jst": ("annular_duct", dict(IM=9, JM=9, KM=17), {"scheme": "100"}, 12),
+    "rotor_9x9x33_jst_mg": ("rotor_passage", dict(IM=9, JM=9, KM=33),
+                            {"scheme": "100", "k2": "0.5", "k4": "32.0", "multigrid": "Y", "coarse_iter": "4"}, 12),
     # imposed mass flow: 25 kg/s, relaxation 0.2, every 2 iterations, residual gate 1.0
     "rotor_9x9x33_massflow": ("rotor_passage", dict(IM=9, JM=9, KM=33),
                               {"mass_imposed": "Y", "mass_line": "25.0 0.2 2 1.0"}, 20),

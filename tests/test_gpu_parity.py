@@ -5,7 +5,7 @@ efficiency) -- the GPU reassociates sums and contracts multiply-adds, so it is n
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, golden_dir, load_golden, rel_err
+from conftest import GOLDEN_CASES, REFERENCE_ONLY_CASES, golden_dir, load_golden, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -22,7 +22,7 @@ def hist_err(a, b):
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
 
 
-@pytest.mark.parametrize("name", GOLDEN_CASES)
+@pytest.mark.parametrize("name", GOLDEN_CASES + REFERENCE_ONLY_CASES)
 def test_fp64_matches_reference(name, gpu_lib):
     g = load_golden(name)
     with gpu_lib.Solver(golden_dir(name), gpu_lib.FP64) as s:
@@ -128,7 +128,7 @@ def test_mixed_precision_tracks_fp64(gpu_lib):
 
 
 def test_bad_case_is_reported(gpu_lib, meshgen, tmp_path):
-    case = meshgen.annular_duct(IM=9, JM=9, KM=17, options={"scheme": "100"})
+    case = meshgen.annular_duct(IM=9, JM=9, KM=17, options={"scheme": "400"})
     meshgen.write_case(case, str(tmp_path))
     with pytest.raises(gpu_lib.GBError, match="not on this path"):
         gpu_lib.Solver(str(tmp_path))
@@ -175,3 +175,15 @@ def test_sweep_autotuner_picks_a_candidate(gpu_lib):
             s.sweep_tuning(3)
     with gpu_lib.Solver([golden_dir("rotor_9x9x33_mg")] * 4, gpu_lib.MIXED) as s:  # timed candidates
         assert s.sweep_tuning(1) in shapes and s.sweep_tuning(2) in shapes
+
+
+def test_mixed_precision_jst_tracks_fp64(gpu_lib):
+    name = "rotor_9x9x33_jst_mg"
+    res = {}
+    for prec in (gpu_lib.FP64, gpu_lib.MIXED):
+        with gpu_lib.Solver(golden_dir(name), prec) as s:
+            s.init_uniform()
+            res[prec] = s.iterate(12)[:, 0, :]
+    a, b = res[gpu_lib.MIXED], res[gpu_lib.FP64]
+    for col in (6, 7, 8):
+        assert float(np.max(np.abs(a[:, col] - b[:, col]) / np.abs(b[:, col]))) < 1e-4
