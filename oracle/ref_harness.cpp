@@ -189,6 +189,11 @@ int main(int argc, char **argv)
     for (int i = 1; i <= Solver.NG; i++) Solver.Mesh[i].AllocateMemory();
     if (Solver.NG == 2) Solver.Mesh[2].AllocateMemory_Pro_Inter_Vars();
     for (int i = 1; i <= Solver.NG; i++) Solver.Mesh[i].Geometry();
+    // Spalart-Allmaras wall distances of the fine mesh (source/Structured_FV3D.cpp:71-84)
+    if (CFluidProps::turbulenceType == TurbulenceTypes::SA) {
+        if (!Solver.reUseWallDistance) Solver.Mesh[1].WallDistanceSA();
+        else CUserInput::ReadWallDistance(Solver.Mesh[1]);
+    }
     // start: uniform field, or the reference's restart file when the case asks for it
     // (source/Structured_FV3D.cpp:86-102)
     if (Solver.reUseSolution) CUserInput::ReadSolution(Solver.Mesh[1]);
