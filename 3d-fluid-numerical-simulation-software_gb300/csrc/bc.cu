@@ -246,6 +246,7 @@ void launch_boundary(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> 
     if (bc.n_wall) k_bc_wall<T><<<dim3((bc.max_wall + 127) / 128, bc.n_wall), 128, 0, ctx.stream>>>(B, P, G, W, bc.wall);
     if (bc.n_per)
         k_bc_periodic<T><<<(unsigned)((bc.n_per + 255) / 256), 256, 0, ctx.stream>>>(B, W, bc.per_dst, bc.per_src, bc.per_meta, bc.n_per);
+    if (W.ev) launch_sa_boundary<T>(ctx, P, W, bc);
 }
 
 template void launch_boundary<double>(const LaunchCtx &, const Phys &, const Geo &, Flow<double>, const BcTables &);

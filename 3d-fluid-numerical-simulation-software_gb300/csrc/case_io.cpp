@@ -314,8 +314,12 @@ void validate(const CaseSpec &c)
         throw std::runtime_error("reconstruction variables " + std::to_string(c.recon_var) + " are not supported (100, 200)");
     if (c.time_scheme >= 100 && c.time_scheme <= 400)
         throw std::runtime_error("Runge-Kutta marching is not on this path (LU-SGS only)");
-    if (c.turb != 0 && c.turb != 100)
-        throw std::runtime_error("turbulence model " + std::to_string(c.turb) + " is not on this path (none 0, Baldwin-Lomax 100)");
+    if (c.turb != 0 && c.turb != 100 && c.turb != 200)
+        throw std::runtime_error("turbulence model " + std::to_string(c.turb) + " is not on this path (none 0, Baldwin-Lomax 100, Spalart-Allmaras 200)");
+    if (c.turb == 200 && c.use_mg)
+        throw std::runtime_error("Spalart-Allmaras runs on a single grid level here: under multigrid the reference starts on the coarse "
+                                 "level and never initialises or transfers the fine level's variable");
+    if (c.turb == 200 && c.walls.empty()) throw std::runtime_error("Spalart-Allmaras needs at least one wall (wall distances)");
     if (c.irs) throw std::runtime_error("implicit residual smoothing is not on this path");
     if (!c.turbo_axial) throw std::runtime_error("only the axial outlet is on this path");
     if (c.use_mg && c.coarse_iter < 1)

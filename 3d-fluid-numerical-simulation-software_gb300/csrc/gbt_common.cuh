@@ -63,6 +63,13 @@ struct Flow {
     T *res2h[NQ], *dq2h[NQ];
     int *flag;                                       // Baldwin-Lomax first-touch marks
     const int *wallf[3];                             // per face: wall patch (1-based) or 0
+    // Spalart-Allmaras (fine level of a case with turbulence model 200; null otherwise): the
+    // eddy-viscosity variable (FP64 like Q) and its copy before the model's clipping, its
+    // residual and update, face fluxes (convective, viscous, gradient) and the wall distance
+    double *ev, *evg;
+    T *res_ev, *dq_ev;
+    T *Fct[3], *Fvt[3], *Fv1t[3];
+    double *dwall;
 };
 
 // Per-solve scalars that evolve on the device (one record per solve).
@@ -103,7 +110,9 @@ struct Phys {
     double c_timestep, relax;
     double suth_c1, suth_c2;                         // (1 + 110.4/288.15) and 110.4/288.15 (float-rounded)
     double k2, k4;                                   // JST coefficients (k4 as the reciprocal of the config value)
+    double ev_ratio;                                 // Spalart-Allmaras inlet / initial value of the variable
     int equation_ns, turb_bl, recon_var, recon, scheme, limiter, global_dt, ndummy;
+    int turb_sa;
 };
 
 // Geometry in the working precision T, the copy the T-arithmetic kernels (face fluxes, spectral

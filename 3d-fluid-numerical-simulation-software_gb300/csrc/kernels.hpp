@@ -50,6 +50,9 @@ struct BcTables {
     void *wall_dist = nullptr;
     const long long *wall_dist_off = nullptr;
     const DevInOut *inlet_first = nullptr, *outlet_first = nullptr;   // per solve: Inlet[1], Outlet[1]
+    // Spalart-Allmaras: ghost cells of the variable filled by interfaces and periodic pairs
+    const long long *sa_dst = nullptr, *sa_src = nullptr;
+    long long n_sa_gather = 0;
 };
 
 constexpr int kIntegralBlocks = 16;             // blocks per inlet/outlet section in the integrals
@@ -89,8 +92,11 @@ template <typename T>
 void launch_resflux(const LaunchCtx &ctx, const Phys &P, const PhysW<T> &PC, const Geo &G, const GeoW<T> &GW, Flow<T> F,
                     const BcTables &bc, int level, T *scratch_dtmin);
 
+// the mean-flow sweeps; with the Spalart-Allmaras variable present (F.ev), its scalar sweep of each
+// direction follows the mean-flow sweep of that direction
 template <typename T>
-void launch_lusgs_sweeps(const LaunchCtx &ctx, const PhysW<T> &P, Flow<T> F, const PlaneTables &pt, const SweepData<T> &S);
+void launch_lusgs_sweeps(const LaunchCtx &ctx, const PhysW<T> &P, const Geo &G, Flow<T> F, const PlaneTables &pt,
+                         const SweepData<T> &S);
 
 // fastest block shape of the sweep kernels for this level, as cells_per_warp * 16 + warps_per_block
 // (times the plane chains on benign inputs in the plane-order scratch; synchronises the stream)
@@ -146,5 +152,21 @@ void launch_interpolate(const LaunchCtx &cf, const LaunchCtx &cc, Flow<T> Ff, Fl
 
 // per-solve scalar stages
 void launch_cfl_ramp(const LaunchCtx &ctx, int iter);
+
+// Spalart-Allmaras (sa.cu)
+void launch_sa_wall_distance(const LaunchCtx &ctx, const Geo &G, const long long *face_p, const int *face_f, long long n,
+                             double *scratch_xyz, const long long *case_off, double *dwall);
+void launch_sa_init(const LaunchCtx &ctx, double *ev, double ev_ratio);
+template <typename T>
+void launch_sa_boundary(const LaunchCtx &ctx, const Phys &P, Flow<T> W, const BcTables &bc);
+template <typename T>
+void launch_sa_model(const LaunchCtx &ctx, const Phys &P, const GeoW<T> &GW, Flow<T> W);
+template <typename T>
+void launch_sa_sweep(const LaunchCtx &ctx, const PhysW<T> &PC, const Geo &G, Flow<T> W, const PlaneTables &pt,
+                     const SweepData<T> &S, int dir);
+template <typename T>
+void launch_sa_update(const LaunchCtx &ctx, const Phys &P, Flow<T> W, int *bad_list, int bad_cap, int *bad_count);
+template <typename T>
+void launch_sa_limit(const LaunchCtx &ctx, Flow<T> W, int *bad_list, int bad_cap, int *bad_count);
 
 }  // namespace gbt

@@ -269,7 +269,8 @@ int tune_sweep_cpw(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneTables &p
 }
 
 template <typename T>
-void launch_lusgs_sweeps(const LaunchCtx &ctx, const PhysW<T> &P, Flow<T> W, const PlaneTables &pt, const SweepData<T> &S)
+void launch_lusgs_sweeps(const LaunchCtx &ctx, const PhysW<T> &P, const Geo &G, Flow<T> W, const PlaneTables &pt,
+                         const SweepData<T> &S)
 {
     const int np = pt.max_plane;
     const unsigned gq = (unsigned)((pt.nq + 255) / 256);
@@ -277,10 +278,22 @@ void launch_lusgs_sweeps(const LaunchCtx &ctx, const PhysW<T> &P, Flow<T> W, con
     k_sweep_gather<T><<<gq, 256, 0, ctx.stream>>>(W, S, pt.nq);
     for (int pl = 3; pl <= np; pl++) launch_plane<T, 1>(ctx, P, pt, S, pl, pl == 3);
     ctx.mark("sweep_forward", 0, np - 1);
+    if (W.ev) {
+        ctx.mark("sa_sweeps", 1, np - 2);
+        launch_sa_sweep<T>(ctx, P, G, W, pt, S, 1);
+        ctx.mark("sa_sweeps", 0, np - 2);
+    }
     ctx.mark("sweep_backward", 1, np - 1);
     for (int pl = np; pl >= 3; pl--) launch_plane<T, -1>(ctx, P, pt, S, pl, pl == np);
-    k_sweep_scatter<T><<<gq, 256, 0, ctx.stream>>>(W, S, pt.nq);
     ctx.mark("sweep_backward", 0, np - 1);
+    if (W.ev) {
+        ctx.mark("sa_sweeps", 1, np - 2);
+        launch_sa_sweep<T>(ctx, P, G, W, pt, S, -1);
+        ctx.mark("sa_sweeps", 0, np - 2);
+    }
+    ctx.mark("sweep_backward", 1, 1);
+    k_sweep_scatter<T><<<gq, 256, 0, ctx.stream>>>(W, S, pt.nq);
+    ctx.mark("sweep_backward", 0, 1);
 }
 
 template <typename T>
@@ -458,6 +471,12 @@ void launch_update(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W,
     cudaMemsetAsync(bad_count, 0, sizeof(int) * B.nsolve, ctx.stream);
     k_update<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, W, bad_list, bad_cap, bad_count);
     if (P.limiter) k_limiter<T><<<(B.nsolve + 31) / 32, 32, 0, ctx.stream>>>(B, P, W, level, bad_list, bad_cap, bad_count);
+    if (W.ev) {
+        // the variable's update and Limit_SA after the mean flow's (source/LU_SGS_Marching.cpp:275-277,
+        // source/ComputeAllBlockVars.cpp:257-266); the limiter list is reused
+        launch_sa_update<T>(ctx, P, W, bad_list, bad_cap, bad_count);
+        if (P.limiter) launch_sa_limit<T>(ctx, W, bad_list, bad_cap, bad_count);
+    }
     ctx.mark("update_limiter", 0, 2);
 }
 
@@ -640,7 +659,7 @@ void launch_cfl_ramp(const LaunchCtx &ctx, int iter)
 }
 
 #define GBT_INST(T)                                                                                                   \
-    template void launch_lusgs_sweeps<T>(const LaunchCtx &, const PhysW<T> &, Flow<T>, const PlaneTables &, const SweepData<T> &); \
+    template void launch_lusgs_sweeps<T>(const LaunchCtx &, const PhysW<T> &, const Geo &, Flow<T>, const PlaneTables &, const SweepData<T> &); \
     template void launch_sweep_geometry<T>(const LaunchCtx &, const Geo &, const PlaneTables &, const SweepData<T> &); \
     template int tune_sweep_cpw<T>(const LaunchCtx &, const PhysW<T> &, const PlaneTables &, const SweepData<T> &); \
     template void launch_update<T>(const LaunchCtx &, const Phys &, const Geo &, Flow<T>, int, int *, int, int *);     \

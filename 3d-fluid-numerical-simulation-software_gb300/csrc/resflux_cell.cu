@@ -347,6 +347,7 @@ void launch_cell_stages(const LaunchCtx &ctx, const Phys &P, const PhysW<T> &PC,
                                                          (const T *)bc.wall_dist);
         }
     }
+    if (level == 1 && P.turb_sa && W.ev) launch_sa_model<T>(ctx, P, GW, W);
     if (bc.n_wall > 0) {
         dim3 g((unsigned)((bc.max_wall + 127) / 128), bc.n_wall);
         k_wall_mut<T><<<g, 128, 0, ctx.stream>>>(B, W, bc.wall);

@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 4) k_face(Batch B, P
     const T mul = sutherland(PC, tf);
     const T gR = gamma * PC.rgas / g1;
     T mu = mul, cond = mul * gR / PC.pr_lam;
-    if (P.turb_bl) {
+    if (P.turb_bl || P.turb_sa) {
         const T mt = (W.mut[m] + W.mut[p]) / (T)2;
         mu = mul + mt;
         cond = cond + mt * gR / PC.pr_tur;

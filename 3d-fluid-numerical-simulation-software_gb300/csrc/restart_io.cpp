@@ -45,33 +45,42 @@ void write_restart_file(const std::string &path, const std::vector<BlockField> &
                 for (int i = 1; i <= IM - 1; i++) {
                     const double *q = B.pv + bx(i, j, k, JM, KM, 6);
                     const double e = B.cv[bx(i, j, k, JM, KM, 5) + 4];
-                    // p, u, v, w, T, rho, rhoE (pv holds rho u v w p T)
-                    std::fprintf(out.f, "%d %d %d %d %g %g %g %g %g %g %g\n", (int)nb + 1, i, j, k, q[4], q[1], q[2], q[3],
-                                 q[5], q[0], e);
+                    // p, u, v, w, T, rho, rhoE (pv holds rho u v w p T), and the SA variable if present
+                    if (B.ev)
+                        std::fprintf(out.f, "%d %d %d %d %g %g %g %g %g %g %g %g\n", (int)nb + 1, i, j, k, q[4], q[1], q[2],
+                                     q[3], q[5], q[0], e, B.ev[bx(i, j, k, JM, KM, 1)]);
+                    else
+                        std::fprintf(out.f, "%d %d %d %d %g %g %g %g %g %g %g\n", (int)nb + 1, i, j, k, q[4], q[1], q[2], q[3],
+                                     q[5], q[0], e);
                 }
     }
 }
 
 void read_restart_file(const std::string &path, const std::vector<BlockField> &blocks, std::vector<std::vector<double>> &cvs,
-                       std::vector<std::vector<double>> &pvs)
+                       std::vector<std::vector<double>> &pvs, bool with_ev, std::vector<std::vector<double>> *evs)
 {
     File in(path, "r");
     cvs.resize(blocks.size());
     pvs.resize(blocks.size());
+    if (with_ev) evs->resize(blocks.size());
     for (size_t nb = 0; nb < blocks.size(); nb++) {
         const int IM = blocks[nb].IM, JM = blocks[nb].JM, KM = blocks[nb].KM;
         // the reference reads the values in its own loop order and ignores the indices on each line
         const long n = (long)(IM - 1) * (JM - 1) * (KM - 1);
-        std::vector<double> rows((size_t)n * 7);
+        std::vector<double> rows((size_t)n * 8);
         for (long r = 0; r < n; r++) {
             int b, i, j, k;
-            double v[7];
-            if (std::fscanf(in.f, "%d %d %d %d %lf %lf %lf %lf %lf %lf %lf", &b, &i, &j, &k, &v[0], &v[1], &v[2], &v[3],
-                            &v[4], &v[5], &v[6]) != 11)
+            double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            const int got = std::fscanf(in.f, "%d %d %d %d %lf %lf %lf %lf %lf %lf %lf", &b, &i, &j, &k, &v[0], &v[1], &v[2],
+                                        &v[3], &v[4], &v[5], &v[6]);
+            const bool ok = got == 11 && (!with_ev || std::fscanf(in.f, "%lf", &v[7]) == 1);
+            if (!ok)
                 throw std::runtime_error(path + ": block " + std::to_string(nb + 1) + " expects " + std::to_string(n) +
-                                         " lines of 11 values (no SA variable); its line " + std::to_string(r + 1) + " is short");
-            std::memcpy(&rows[(size_t)r * 7], v, sizeof v);
+                                         (with_ev ? " lines of 12 values (with the SA variable)" : " lines of 11 values (no SA variable)") +
+                                         "; its line " + std::to_string(r + 1) + " is short");
+            std::memcpy(&rows[(size_t)r * 8], v, sizeof v);
         }
+        if (with_ev) (*evs)[nb].assign((size_t)n, 0.0);
         std::vector<double> &cv = cvs[nb], &pv = pvs[nb];
         cv.assign((size_t)n * 5, 0.0);
         pv.assign((size_t)n * 6, 0.0);
@@ -80,13 +89,14 @@ void read_restart_file(const std::string &path, const std::vector<BlockField> &b
         for (int k = 1; k <= KM - 1; k++)
             for (int j = 1; j <= JM - 1; j++)
                 for (int i = 1; i <= IM - 1; i++, r++) {
-                    const double *v = &rows[(size_t)r * 7];
+                    const double *v = &rows[(size_t)r * 8];
                     const double press = v[0], u = v[1], vv = v[2], w = v[3], temp = v[4], dens = v[5], ener = v[6];
                     const size_t o = ((size_t)(i - 1) * (JM - 1) + (j - 1)) * (KM - 1) + (k - 1);
                     cv[o * 5 + 0] = dens; cv[o * 5 + 1] = dens * u; cv[o * 5 + 2] = dens * vv; cv[o * 5 + 3] = dens * w;
                     cv[o * 5 + 4] = ener;
                     pv[o * 6 + 0] = dens; pv[o * 6 + 1] = u; pv[o * 6 + 2] = vv; pv[o * 6 + 3] = w; pv[o * 6 + 4] = press;
                     pv[o * 6 + 5] = temp;
+                    if (with_ev) (*evs)[nb][o] = v[7];
                 }
     }
 }

@@ -59,6 +59,7 @@ struct Level {
     GeoW<T> GW{};                         // working-precision geometry (aliases in FP64, FP32 copies in mixed)
     DevBuf geow_mem;
     DevBuf fd_mem;                        // JST face dissipation
+    DevBuf sa_mem, sa_tab_mem;            // Spalart-Allmaras fields; its tables
     DevBuf wdist_mem;                     // Baldwin-Lomax wall distances (fine level)
     Flow<T> W{};
     double *totalvol = nullptr, *blockvol = nullptr;
@@ -376,6 +377,8 @@ public:
         P.equation_ns = c0.equation_ns; P.turb_bl = c0.turb == 100; P.recon_var = c0.recon_var; P.recon = c0.recon;
         P.scheme = c0.scheme; P.limiter = c0.limiter; P.global_dt = c0.global_dt;
         P.k2 = c0.k2; P.k4 = c0.k4;
+        P.turb_sa = c0.turb == 200;
+        P.ev_ratio = c0.ev_ratio;
         // dummy layers: three for no reconstruction and for JST (source/UserInput.cpp:131-163)
         P.ndummy = (c0.recon == 0 || c0.scheme == 100) ? 3 : 2;
         PC = phys_working<T>(P);
@@ -486,6 +489,17 @@ public:
         W.mut = tk(); W.omega = tk(); W.dt = tk();
         for (int f = 0; f < 3; f++) { W.lamc[f] = tk(); W.lamv[f] = tk(); for (int c = 0; c < NQ; c++) { W.Ff[f][c] = tk(); W.Vf[f][c] = tk(); } }
         for (int c = 0; c < NQ; c++) { W.res[c] = tk(); W.dq[c] = tk(); W.res2h[c] = tk(); W.dq2h[c] = tk(); }
+        if (P.turb_sa && l == 1) {
+            // Spalart-Allmaras variable, its copy, residual, update, face fluxes and wall distance
+            Lv.sa_mem.bytes = sizeof(double) * N * 3 + sizeof(T) * N * 11;
+            CK(cudaMalloc(&Lv.sa_mem.p, Lv.sa_mem.bytes));
+            CK(cudaMemset(Lv.sa_mem.p, 0, Lv.sa_mem.bytes));
+            double *sd = (double *)Lv.sa_mem.p;
+            W.ev = sd; W.evg = sd + N; W.dwall = sd + 2 * N;
+            T *st = (T *)(sd + 3 * N);
+            W.res_ev = st; W.dq_ev = st + N;
+            for (int f = 0; f < 3; f++) { W.Fct[f] = st + (2 + f) * N; W.Fvt[f] = st + (5 + f) * N; W.Fv1t[f] = st + (8 + f) * N; }
+        }
         if (P.scheme == 100) {
             // face dissipation of JST (source/SpaceDiscr.cpp:611-640)
             Lv.fd_mem.bytes = sizeof(T) * N * 15;
@@ -525,6 +539,7 @@ public:
         build_planes(l);
         launch_geometry(ctx(l), G, Lv.blockvol);
         k_case_volume<<<(nsolve + 127) / 128, 128, 0, stream>>>(batch(l), Lv.blockvol, Lv.totalvol);
+        if (Lv.W.ev) build_sa_wall_distance(l);
         build_geometry_working(l);
         build_wall_distances(l);
         launch_sweep_geometry<T>(ctx(l), G, Lv.planes, Lv.sweep);
@@ -548,6 +563,49 @@ public:
         }
         CK(cudaStreamSynchronize(stream));
         CK(cudaGetLastError());
+    }
+
+    // Spalart-Allmaras wall distances (CMesh::WallDistanceSA, source/WallDistanceSA.cpp:6-160): every
+    // wall face of every block of a case, once
+    void build_sa_wall_distance(int l)
+    {
+        Level<T> &Lv = lev[l];
+        std::vector<long long> fp, off(1, 0);
+        std::vector<int> ff;
+        for (int c = 0; c < ncase; c++) {
+            for (int b = 0; b < case_nblk[c]; b++) {
+                const int s = case_first[c] + b;
+                const Lvl &v = Lv.lv[s];
+                for (const WallIO &w : cases[s].walls) {
+                    const int f = (w.face - 1) / 2;
+                    const bool hi = w.face % 2 == 0;
+                    int i0 = w.is, i1 = w.ie, j0 = w.js, j1 = w.je, k0 = w.ks, k1 = w.ke;
+                    if (f == 0) i0 = i1 = hi ? v.IM : 1;
+                    if (f == 1) j0 = j1 = hi ? v.JM : 1;
+                    if (f == 2) k0 = k1 = hi ? v.KM : 1;
+                    for (int i = i0; i <= i1; i++)
+                        for (int j = j0; j <= j1; j++)
+                            for (int k = k0; k <= k1; k++) { fp.push_back(ix(v, i, j, k)); ff.push_back(f); }
+                }
+            }
+            off.push_back((long long)fp.size());
+        }
+        const long long n = (long long)fp.size();
+        auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+        Lv.sa_tab_mem.bytes = al(sizeof(long long) * n) + al(sizeof(int) * n) + al(sizeof(long long) * off.size()) + al(sizeof(double) * 3 * n) + 256;
+        CK(cudaMalloc(&Lv.sa_tab_mem.p, Lv.sa_tab_mem.bytes));
+        char *q = (char *)Lv.sa_tab_mem.p;
+        long long *dp = (long long *)q; q += al(sizeof(long long) * n);
+        int *df = (int *)q; q += al(sizeof(int) * n);
+        long long *doff = (long long *)q; q += al(sizeof(long long) * off.size());
+        double *xyz = (double *)q;
+        if (n) {
+            CK(cudaMemcpy(dp, fp.data(), sizeof(long long) * n, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(df, ff.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+        }
+        CK(cudaMemcpy(doff, off.data(), sizeof(long long) * off.size(), cudaMemcpyHostToDevice));
+        launch_sa_wall_distance(ctx(l), Lv.G, dp, df, n, xyz, doff, Lv.W.dwall);
+        CK(cudaStreamSynchronize(stream));
     }
 
     // Baldwin-Lomax wall distances of the fine level (constant geometry, computed once)
@@ -713,7 +771,7 @@ public:
         BcTables &bc = Lv.bc;
         std::vector<DevInOut> inl, outl, inl1, outl1;
         std::vector<DevWall> walls;
-        std::vector<long long> pdst, psrc;
+        std::vector<long long> pdst, psrc, sa_dst_h, sa_src_h;
         std::vector<int> pmeta;
         std::vector<int> wallf[3];
         for (int f = 0; f < 3; f++) wallf[f].assign((size_t)Lv.pool_n, 0);
@@ -777,7 +835,7 @@ public:
         for (int cix = 0; cix < ncase; cix++) {
             const int s0 = case_first[cix];
             const CaseSpec &cs = cases[s0];
-            std::map<long long, size_t> last;
+            std::map<long long, size_t> last, last_sa;
             std::vector<std::pair<PeriodicIO, bool>> pairs;
             for (auto &p : cs.interiors) pairs.push_back({level_pair(p, l), false});
             for (auto &p : cs.periodics) pairs.push_back({level_pair(p, l), true});
@@ -832,6 +890,12 @@ public:
                                 if (f != last.end()) { psrc[f->second] = it->second; pmeta[f->second] = meta; }
                                 else { last[dd] = pdst.size(); pdst.push_back(dd); psrc.push_back(it->second); pmeta.push_back(meta); }
                             }
+                            if (dsts[1] >= 0) {
+                                // the Spalart-Allmaras variable goes to the first ghost layer only
+                                auto f = last_sa.find(dsts[1]);
+                                if (f != last_sa.end()) sa_src_h[f->second] = it->second;
+                                else { last_sa[dsts[1]] = sa_dst_h.size(); sa_dst_h.push_back(dsts[1]); sa_src_h.push_back(it->second); }
+                            }
                         }
                     }
                 }
@@ -842,7 +906,7 @@ public:
         size_t tot = bytes(inl.size(), sizeof(DevInOut)) + bytes(outl.size(), sizeof(DevInOut)) + bytes(inl1.size(), sizeof(DevInOut)) +
                      bytes(outl1.size(), sizeof(DevInOut)) + bytes(walls.size(), sizeof(DevWall)) + bytes(pdst.size(), 8) * 2 +
                      bytes(pmeta.size(), 4) + bytes(outl.size() * (size_t)(bc.max_outlet_im + 1), 8) +
-                     bytes((size_t)nsolve * 2 * kIntegralBlocks * 3, 8) + 256;
+                     bytes((size_t)nsolve * 2 * kIntegralBlocks * 3, 8) + bytes(sa_dst_h.size(), 8) * 2 + 256;
         CK(cudaMalloc(&Lv.tab_mem.p, tot));
         char *q = (char *)Lv.tab_mem.p;
         auto up = [&](const void *h, size_t n, size_t sz) {
@@ -860,6 +924,9 @@ public:
         bc.per_src = (const long long *)up(psrc.data(), psrc.size(), 8);
         bc.per_meta = (const int *)up(pmeta.data(), pmeta.size(), 4);
         bc.n_per = (long long)pdst.size();
+        bc.sa_dst = (const long long *)up(sa_dst_h.data(), sa_dst_h.size(), 8);
+        bc.sa_src = (const long long *)up(sa_src_h.data(), sa_src_h.size(), 8);
+        bc.n_sa_gather = (long long)sa_dst_h.size();
         bc.outlet_cu = (double *)up(nullptr, 0, 8); q += bytes(outl.size() * (size_t)(bc.max_outlet_im + 1), 8);
         bc.integ_part = (double *)up(nullptr, 0, 8); q += bytes((size_t)nsolve * 2 * kIntegralBlocks * 3, 8);
         for (int f = 0; f < 3; f++)
@@ -894,6 +961,7 @@ public:
         Flow<T> &W = lev[l].W;
         CK(cudaMemcpyAsync(init_q, init.data(), sizeof(double) * init.size(), cudaMemcpyHostToDevice, stream));
         k_fill_uniform<<<cx.grid_cells(256), 256, 0, stream>>>(cx.batch, W.cv[0], W.cv[1], W.cv[2], W.cv[3], W.cv[4], init_q);
+        if (W.ev) launch_sa_init(cx, W.ev, P.ev_ratio);        // Initialization.cpp:40,70-71
         launch_primitive<T>(cx, P, W);
         CK(cudaStreamSynchronize(stream));
         CK(cudaGetLastError());
@@ -908,7 +976,7 @@ public:
         Level<T> &Lv = lev[l];
         if (!Lv.use_force) resflux(l);
         else { Mark m(this, "mg_forcing"); launch_forcing<T>(cx, Lv.W); }
-        launch_lusgs_sweeps<T>(cx, PC, Lv.W, Lv.planes, Lv.sweep);
+        launch_lusgs_sweeps<T>(cx, PC, Lv.G, Lv.W, Lv.planes, Lv.sweep);
         launch_update<T>(cx, P, Lv.G, Lv.W, l, bad_list, bad_cap, bad_count);
     }
     void res_calculate(int l) override { launch_res_norm<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, norm_part, norm_blk); }
@@ -1097,6 +1165,12 @@ public:
         if (name == "cv") { for (int c = 0; c < 5; c++) cs.push_back(D(W.cv[c])); return box(v, cs, 0, IM, 0, JM, 0, KM, out, cap); }
         if (name == "pv") { for (int c = 0; c < 6; c++) cs.push_back(Tt(W.pv[c])); return box(v, cs, 0, IM, 0, JM, 0, KM, out, cap); }
         if (name == "mut") return box(v, {Tt(W.mut)}, 0, IM, 0, JM, 0, KM, out, cap);
+        if (name == "ev" || name == "res_ev" || name == "dwall") {
+            if (!W.ev) return -1;                  // Spalart-Allmaras cases, fine level
+            if (name == "ev") return box(v, {D(W.ev)}, 0, IM, 0, JM, 0, KM, out, cap);
+            if (name == "res_ev") return box(v, {Tt(W.res_ev)}, 1, IM - 1, 1, JM - 1, 1, KM - 1, out, cap);
+            return box(v, {D(W.dwall)}, 1, IM - 1, 1, JM - 1, 1, KM - 1, out, cap);
+        }
         if (name == "res") { for (int c = 0; c < 5; c++) cs.push_back(Tt(W.res[c])); return box(v, cs, 1, IM - 1, 1, JM - 1, 1, KM - 1, out, cap); }
         if (name == "dq") { for (int c = 0; c < 5; c++) cs.push_back(Tt(W.dq[c])); return box(v, cs, 1, IM - 1, 1, JM - 1, 1, KM - 1, out, cap); }
         if (name == "dt") return box(v, {Tt(W.dt)}, 1, IM - 1, 1, JM - 1, 1, KM - 1, out, cap);
@@ -1182,10 +1256,12 @@ public:
     }
     // the fine-level fields of every block of a case
     void case_fields(int cix, std::vector<std::vector<double>> &pv, std::vector<std::vector<double>> &cv,
-                     std::vector<std::vector<double>> *mut, std::vector<BlockField> &blocks)
+                     std::vector<std::vector<double>> *mut, std::vector<BlockField> &blocks,
+                     std::vector<std::vector<double>> *ev = nullptr)
     {
         const int nb = case_nblk[cix];
         pv.resize(nb); cv.resize(nb);
+        if (ev) ev->resize(nb);
         if (mut) mut->resize(nb);
         blocks.resize(nb);
         for (int b = 0; b < nb; b++) {
@@ -1197,14 +1273,19 @@ public:
             f.pv = pv[b].data(); f.cv = cv[b].data(); f.mut = mut ? (*mut)[b].data() : nullptr;
             f.x = cases[s].x.data(); f.y = cases[s].y.data(); f.z = cases[s].z.data();
             f.w_rot = lev[1].sc[s].w_rot; f.delta_th = lev[1].sc[s].delta_th;
+            if (ev && lev[1].W.ev) {
+                (*ev)[b].resize((size_t)(v.IM + 1) * (v.JM + 1) * (v.KM + 1));
+                if (get_field(s, 1, "ev", (*ev)[b].data(), (long)(*ev)[b].size()) < 0) throw std::runtime_error("state download failed");
+                f.ev = (*ev)[b].data();
+            }
         }
     }
     void write_restart(int cix, const std::string &path) override
     {
         check_case(cix);
-        std::vector<std::vector<double>> pv, cv;
+        std::vector<std::vector<double>> pv, cv, ev;
         std::vector<BlockField> blocks;
-        case_fields(cix, pv, cv, nullptr, blocks);
+        case_fields(cix, pv, cv, nullptr, blocks, &ev);
         write_restart_file(default_path(cix, path, "RestartSolution.dat"), blocks);
     }
     void write_solution(int cix, const std::string &path) override
@@ -1228,11 +1309,11 @@ public:
             const Lvl &v = lev[1].lv[case_first[cix] + b];
             blocks[b].IM = v.IM; blocks[b].JM = v.JM; blocks[b].KM = v.KM;
         }
-        std::vector<std::vector<double>> cvs, pvs;
-        read_restart_file(default_path(cix, path, "RestartSolution.dat"), blocks, cvs, pvs);
-        // Q and the primitive variables exactly as read (CUserInput::ReadSolution sets both)
-        CK(cudaStreamSynchronize(stream));
+        std::vector<std::vector<double>> cvs, pvs, evs;
         Flow<T> &W = lev[1].W;
+        read_restart_file(default_path(cix, path, "RestartSolution.dat"), blocks, cvs, pvs, W.ev != nullptr, &evs);
+        // Q, the primitive variables (and the SA variable) exactly as read (CUserInput::ReadSolution)
+        CK(cudaStreamSynchronize(stream));
         for (int b = 0; b < case_nblk[cix]; b++) {
             const Lvl &v = lev[1].lv[case_first[cix] + b];
             const std::vector<double> &cv = cvs[b], &pv = pvs[b];
@@ -1255,6 +1336,15 @@ public:
                     for (int j = 1; j <= v.JM - 1; j++)
                         for (int k = 1; k <= v.KM - 1; k++, q += 6) h[(size_t)ix(z, i, j, k)] = (T)pv[q];
                 CK(cudaMemcpy(W.pv[c] + v.base, h.data(), sizeof(T) * bn, cudaMemcpyHostToDevice));
+            }
+            if (W.ev) {
+                std::vector<double> h((size_t)bn);
+                CK(cudaMemcpy(h.data(), W.ev + v.base, sizeof(double) * bn, cudaMemcpyDeviceToHost));
+                size_t q = 0;
+                for (int i = 1; i <= v.IM - 1; i++)
+                    for (int j = 1; j <= v.JM - 1; j++)
+                        for (int k = 1; k <= v.KM - 1; k++, q++) h[(size_t)ix(z, i, j, k)] = evs[b][q];
+                CK(cudaMemcpy(W.ev + v.base, h.data(), sizeof(double) * bn, cudaMemcpyHostToDevice));
             }
         }
     }

@@ -106,7 +106,8 @@ FIELD_SHAPES = {
     "faceK": lambda I, J, K: (I - 1, J - 1, K, 18), "cell": lambda I, J, K: (I - 1, J - 1, K - 1, 13),
     "totalvol": lambda I, J, K: (1,),
 }
-for _n in ("dt", "omega", "lamcI", "lamcJ", "lamcK", "lamvI", "lamvJ", "lamvK"):
+FIELD_SHAPES["ev"] = lambda I, J, K: (I + 1, J + 1, K + 1, 1)        # Spalart-Allmaras cases
+for _n in ("dt", "omega", "lamcI", "lamcJ", "lamcK", "lamvI", "lamvJ", "lamvK", "res_ev", "dwall"):
     FIELD_SHAPES[_n] = lambda I, J, K: (I - 1, J - 1, K - 1, 1)
 for _d, _f in (("I", lambda I, J, K: (2, J - 1, K - 1)), ("J", lambda I, J, K: (I - 1, 2, K - 1)),
                ("K", lambda I, J, K: (I - 1, J - 1, 2))):

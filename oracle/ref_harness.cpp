@@ -112,6 +112,8 @@ static void dump_geometry(CMesh &M, const std::string &p, int nb = 1)
     dump_box(p + "faceJ", G.FaceJ, 1, IM - 1, 1, JM, 1, KM - 1, 18, face_c);
     dump_box(p + "faceK", G.FaceK, 1, IM - 1, 1, JM - 1, 1, KM, 18, face_c);
     dump_box(p + "cell", G.Cell, 1, IM - 1, 1, JM - 1, 1, KM - 1, 13, cell_c);
+    if (CFluidProps::turbulenceType == TurbulenceTypes::SA && M.Mesh_ID == 1)
+        dump_box(p + "dwall", G.Cell, 1, IM - 1, 1, JM - 1, 1, KM - 1, 1, [](const TCell &c, int) { return (double)c.dis_Wall; });
     npy_write(p + "totalvol", {(double)M.TotalVol}, {1});
 }
 
@@ -124,6 +126,8 @@ static void dump_state(CMesh &M, const std::string &p, int nb = 1)
     dump_cells(p + "pv", F.Cell_pv, IM, JM, KM, 6, pv_c);
     dump_cells(p + "mut", F.Cell_tur, IM, JM, KM, 1,
                [](const TVisVars &v, int) { return (double)v.mue; });
+    if (CFluidProps::turbulenceType == TurbulenceTypes::SA)
+        dump_cells(p + "ev", F.Cell_ev, IM, JM, KM, 1, [](const TEddyVars &v, int) { return (double)v.ev; });
 }
 
 static void dump_resflux(CMesh &M, const std::string &p, int nb = 1)
@@ -169,6 +173,8 @@ static void dump_resflux(CMesh &M, const std::string &p, int nb = 1)
     dump_box(p + "Fc", S.Cell_Fc, 1, IM - 1, 1, JM - 1, 1, KM - 1, 5, cvg);
     dump_box(p + "Fv", S.Cell_Fv, 1, IM - 1, 1, JM - 1, 1, KM - 1, 5, cvg);
     dump_box(p + "res", S.Res_cv, 1, IM - 1, 1, JM - 1, 1, KM - 1, 5, cvg);
+    if (CFluidProps::turbulenceType == TurbulenceTypes::SA)
+        dump_box(p + "res_ev", S.Res_ev, 1, IM - 1, 1, JM - 1, 1, KM - 1, 1, [](const TEddyVars &v, int) { return (double)v.ev; });
 }
 
 int main(int argc, char **argv)

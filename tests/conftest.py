@@ -14,9 +14,9 @@ for p in (PKG, os.path.join(ROOT, "oracle")):
 
 GOLDEN_CASES = ["duct_9x9x17", "duct_9x9x17_sw_nnd", "duct_9x9x17_laminar_cons", "duct_9x9x17_muscl2u_global",
                 "rotor_9x9x33", "rotor_9x9x33_mg"]
-# fixtures of options the CPU oracle port does not restate (JST): the GPU path is checked against
+# fixtures of options the CPU oracle port does not restate (JST, Spalart-Allmaras): the GPU path is checked against
 # the reference's own outputs only
-REFERENCE_ONLY_CASES = ["duct_9x9x17_jst", "rotor_9x9x33_jst_mg"]
+REFERENCE_ONLY_CASES = ["duct_9x9x17_jst", "rotor_9x9x33_jst_mg", "duct_9x9x17_sa", "rotor_9x9x33_sa"]
 
 
 def pytest_configure(config):

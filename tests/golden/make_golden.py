@@ -51,6 +51,10 @@ CASES = {
     "duct_9x9x17_jst": ("annular_duct", dict(IM=9, JM=9, KM=17), {"scheme": "100"}, 12),
     "rotor_9x9x33_jst_mg": ("rotor_passage", dict(IM=9, JM=9, KM=33),
                             {"scheme": "100", "k2": "0.5", "k4": "32.0", "multigrid": "Y", "coarse_iter": "4"}, 12),
+    # Spalart-Allmaras (wall distances, the eddy-viscosity equation in the residual and the
+    # LU-SGS sweeps), single grid
+    "duct_9x9x17_sa": ("annular_duct", dict(IM=9, JM=9, KM=17), {"turb": "200"}, 12),
+    "rotor_9x9x33_sa": ("rotor_passage", dict(IM=9, JM=9, KM=33), {"turb": "200"}, 12),
     # imposed mass flow: 25 kg/s, relaxation 0.2, every 2 iterations, residual gate 1.0
     "rotor_9x9x33_massflow": ("rotor_passage", dict(IM=9, JM=9, KM=33),
                               {"mass_imposed": "Y", "mass_line": "25.0 0.2 2 1.0"}, 20),
@@ -77,7 +81,7 @@ RESTART = {
     "rotor_9x9x33_restart": ("rotor_passage", dict(IM=9, JM=9, KM=33), {}, 10, 10),
 }
 
-KEEP_R = ["cv", "pv", "mut", "omega", "lamcI", "lamcJ", "lamcK", "lamvI", "lamvJ", "lamvK", "dt", "FcI", "FcJ",
+KEEP_R = ["cv", "pv", "mut", "ev", "res_ev", "omega", "lamcI", "lamcJ", "lamcK", "lamvI", "lamvJ", "lamvK", "dt", "FcI", "FcJ",
           "FcK", "FvI", "FvJ", "FvK", "res", "dIS_pv", "dIP_pv", "dJS_pv", "dJP_pv", "dKS_pv", "dKP_pv", "dIS_cv",
           "dKP_cv"]
 
@@ -184,7 +188,7 @@ def make(name: str) -> None:
                 continue
             if key.startswith("s") or key.startswith("g2_"):
                 continue                       # state after the loop is r1_cv's interior
-            if key.startswith("g1_") and not base_case:
+            if key.startswith("g1_") and not base_case and key != "g1_dwall":
                 continue                       # geometry is pinned on the two base cases
             if not base_case and key.startswith("r1_d"):
                 continue

@@ -9,7 +9,7 @@ from conftest import GOLDEN_CASES, REFERENCE_ONLY_CASES, golden_dir, load_golden
 
 pytestmark = pytest.mark.gpu
 
-R1_KEYS = ["cv", "pv", "mut", "omega", "lamcI", "lamcJ", "lamcK", "lamvI", "lamvJ", "lamvK", "dt", "FcI", "FcJ",
+R1_KEYS = ["cv", "pv", "mut", "ev", "res_ev", "omega", "lamcI", "lamcJ", "lamcK", "lamvI", "lamvJ", "lamvK", "dt", "FcI", "FcJ",
            "FcK", "FvI", "FvJ", "FvK", "res", "dIS_pv", "dIP_pv", "dJS_pv", "dJP_pv", "dKS_pv", "dKP_pv", "dIS_cv",
            "dKP_cv"]
 HIST_COLS = [0, 1, 6, 7, 8, 9, 11]     # iter, Res.dens, m_in, m_out, PR, eta, CFL (others divide by zero momenta)
@@ -26,7 +26,7 @@ def hist_err(a, b):
 def test_fp64_matches_reference(name, gpu_lib):
     g = load_golden(name)
     with gpu_lib.Solver(golden_dir(name), gpu_lib.FP64) as s:
-        for key in ("faceI", "faceJ", "faceK", "cell", "totalvol"):
+        for key in ("faceI", "faceJ", "faceK", "cell", "totalvol", "dwall"):
             if "g1_" + key in g:
                 assert rel_err(s.get(key), g["g1_" + key]) < 1e-11, key
         s.init_uniform()
@@ -187,3 +187,39 @@ def test_mixed_precision_jst_tracks_fp64(gpu_lib):
     a, b = res[gpu_lib.MIXED], res[gpu_lib.FP64]
     for col in (6, 7, 8):
         assert float(np.max(np.abs(a[:, col] - b[:, col]) / np.abs(b[:, col]))) < 1e-4
+
+
+def test_spalart_allmaras_restart_round_trip(gpu_lib, tmp_path):
+    """the restart file of a Spalart-Allmaras case carries the variable as a twelfth column and
+    reads back into the same state (to the six printed digits)"""
+    name = "rotor_9x9x33_sa"
+    with gpu_lib.Solver(golden_dir(name), gpu_lib.FP64) as s:
+        s.init_uniform()
+        s.iterate(4, history=False)
+        s.write_restart(0, str(tmp_path / "r.dat"))
+        ev = s.get("ev")[1:-1, 1:-1, 1:-1]
+        s.read_restart(0, str(tmp_path / "r.dat"))
+        ev2 = s.get("ev")[1:-1, 1:-1, 1:-1]
+        h = s.iterate(3)[:, 0, :]
+    assert all(len(l.split()) == 12 for l in open(tmp_path / "r.dat").read().splitlines()[:50])
+    assert rel_err(ev2, ev) < 1e-5
+    assert np.all(np.isfinite(h[:, HIST_COLS]))
+
+
+def test_mixed_precision_spalart_allmaras_tracks_fp64(gpu_lib):
+    name = "rotor_9x9x33_sa"
+    res = {}
+    for prec in (gpu_lib.FP64, gpu_lib.MIXED):
+        with gpu_lib.Solver(golden_dir(name), prec) as s:
+            s.init_uniform()
+            res[prec] = s.iterate(12)[:, 0, :]
+    a, b = res[gpu_lib.MIXED], res[gpu_lib.FP64]
+    for col in (6, 7, 8):
+        assert float(np.max(np.abs(a[:, col] - b[:, col]) / np.abs(b[:, col]))) < 1e-4
+
+
+def test_spalart_allmaras_with_multigrid_is_refused(gpu_lib, meshgen, tmp_path):
+    case = meshgen.annular_duct(IM=9, JM=9, KM=17, options={"turb": "200", "multigrid": "Y", "coarse_iter": "2"})
+    meshgen.write_case(case, str(tmp_path))
+    with pytest.raises(gpu_lib.GBError, match="single grid"):
+        gpu_lib.Solver(str(tmp_path))
