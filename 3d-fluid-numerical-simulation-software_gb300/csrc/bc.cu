@@ -231,6 +231,106 @@ __global__ void k_bc_periodic(Batch B, Flow<T> W, const long long *dst, const lo
     st_state(W, b, c, q);
 }
 
+// mixing plane (CMesh::BndCondMixingPlane, source/BndCondMixingPlane.cpp:287-520), one thread per
+// radial row: flux averages over the pitch of the last cell layer upstream (block 1, k = KM - 1,
+// normals of the k = KM faces) and of the first layer downstream (block 2, k = 1), each turned into
+// a mixed-out state by the quadratic for the pressure
+template <typename T>
+__global__ void k_mix_average(Batch B, Phys P, Geo G, Flow<T> W, const DevMix *mix, int max_rows, double *avg)
+{
+    const DevMix m = mix[blockIdx.y];
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r > m.ie - m.is) return;
+    const int i = m.is + r;
+    const double g = P.gamma, R = P.rgas;
+    double *o = avg + ((long long)blockIdx.y * max_rows + r) * kMixVals;
+    for (int side = 0; side < 2; side++) {
+        const int s = side ? m.s2 : m.s1;
+        const Lvl L = B.lv[s];
+        const int kf = side ? 1 : L.KM, kc = side ? 1 : L.KM - 1;
+        const int j0 = side ? m.js2 : m.js1, j1 = side ? m.je2 : m.je1;
+        double I1 = 0.0, I2 = 0.0, I3 = 0.0, I4 = 0.0, I5 = 0.0, I6 = 0.0, nsx = 0.0, nsy = 0.0, nsz = 0.0, ss = 0.0;
+        for (int j = j0; j <= j1; j++) {
+            const long long f = ix(L, i, j, kf), c = ix(L, i, j, kc);
+            const double sa = G.s[2][f];
+            const double nx = G.S[2][0][f] / sa, ny = G.S[2][1][f] / sa, nz = G.S[2][2][f] / sa;
+            nsx = nsx + nx * sa; nsy = nsy + ny * sa; nsz = nsz + nz * sa;
+            ss = ss + sa;
+            const double u = W.pv[PU][c], v = W.pv[PV][c], w = W.pv[PW][c], pr = W.pv[PP][c];
+            const double Vn = u * nx + v * ny + w * nz;
+            I1 = I1 + W.cv[0][c] * Vn * sa;
+            I2 = I2 + (W.cv[1][c] * Vn + nx * pr) * sa;
+            I3 = I3 + (W.cv[2][c] * Vn + ny * pr) * sa;
+            I4 = I4 + (W.cv[3][c] * Vn + nz * pr) * sa;
+            I5 = I5 + (W.cv[4][c] + pr) * Vn * sa;
+            if (W.ev) I6 = I6 + W.cv[0][c] * W.ev[c] * Vn * sa;
+        }
+        I1 = I1 / ss; I2 = I2 / ss; I3 = I3 / ss; I4 = I4 / ss; I5 = I5 / ss;
+        if (side == 0) o[12] = W.ev ? (I6 / ss) / I1 : 0.0;
+        const double nux = nsx / ss, nuy = nsy / ss, nuz = nsz / ss;
+        const double A = I2 * nux + I3 * nuy + I4 * nuz;
+        const double Bq = (double)2.0f * I1 * I5 - (I2 * I2 + I3 * I3 + I4 * I4);
+        const double C = nux * nux + nuy * nuy + nuz * nuz;
+        const double pr = (A / C + sqrt(A * A / C / C - (g * g - 1.0) * Bq / C)) / (g + 1.0);
+        const double u = (I2 - pr * nux) / I1, v = (I3 - pr * nuy) / I1, w = (I4 - pr * nuz) / I1;
+        const double d = I1 / (u * nux + v * nuy + w * nuz);
+        const double t = pr / R / d;
+        double *q = o + 6 * side;
+        q[0] = d; q[1] = u; q[2] = v; q[3] = w; q[4] = pr; q[5] = sqrt(g * R * t);
+    }
+}
+
+// ghost and reconstruction layers of both sides from the other side's mixed-out state and the
+// outgoing characteristics (:431-518); the SA variable of both ghosts is the upstream average
+template <typename T>
+__global__ void k_mix_fill(Batch B, Phys P, Flow<T> W, const DevMix *mix, int max_rows, int max_j, const double *avg)
+{
+    const DevMix m = mix[blockIdx.y];
+    const int side = blockIdx.z;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j0 = side ? m.js2 : m.js1, nj = (side ? m.je2 : m.je1) - j0 + 1;
+    const int nr = m.ie - m.is + 1;
+    if (t >= nr * nj) return;
+    const int r = t / nj, i = m.is + r, j = j0 + t % nj;
+    const double *o = avg + ((long long)blockIdx.y * max_rows + r) * kMixVals;
+    const double *pu = o, *pd = o + 6;                         // d u v w p c of the upstream / downstream average
+    const double g = P.gamma, R = P.rgas;
+    const Lvl L = B.lv[side ? m.s2 : m.s1];
+    double d, u, v, w, pr;
+    long long gp, step;
+    if (side == 0) {
+        const long long c = ix(L, i, j, L.KM - 1);
+        const double cu = pu[5], cd = pd[5];
+        const double C1 = -cu * cu * ((double)W.pv[PD][c] - pu[0]) + ((double)W.pv[PP][c] - pu[4]);
+        const double C2 = pu[0] * cu * ((double)W.pv[PW][c] - pu[3]) + ((double)W.pv[PP][c] - pu[4]);
+        const double C5 = 0.0;
+        d = pd[0] + (-C1 + (C2 + C5) / 2.0) / (cd * cd);
+        w = pd[3] + (C2 - C5) / (2.0 * pd[0] * cd);
+        v = W.pv[PV][c];
+        u = W.pv[PU][c];
+        pr = pd[4] + (C2 + C5) / 2.0;
+        gp = ix(L, i, j, L.KM);
+        step = 1;
+    } else {
+        const long long c = ix(L, i, j, 1);
+        const double cu = pu[5], cd = pd[5];
+        const double C5 = (0.0 - pd[0] * cd * ((double)W.pv[PW][c] - pd[3]) + ((double)W.pv[PP][c] - pd[4]));
+        d = pu[0] + (-0.0 + (0.0 + C5) / 2.0) / (cu * cu);
+        w = pu[3] - C5 / (2.0 * pu[0] * cu);
+        v = pu[2] + 0.0 / (pu[0] * cu);
+        u = pu[1] + 0.0 / (pu[0] * cu);
+        pr = pu[4] + (0.0 + C5) / 2.0;
+        gp = ix(L, i, j, 0);
+        step = -1;
+    }
+    const double V2 = pow(u, 2.0) + pow(v, 2.0) + pow(w, 2.0);
+    const double c[5] = {d, d * u, d * v, d * w, pr / (g - 1.0) + d * V2 / 2.0};
+    const T q[6] = {(T)d, (T)u, (T)v, (T)w, (T)pr, (T)(pr / R / d)};
+    st_state(W, gp, c, q);
+    if (W.ev) W.ev[gp] = o[12];
+    for (int nd = 1; nd <= P.ndummy; nd++) st_state(W, gp + step * nd, c, q);
+}
+
 template <typename T>
 void launch_boundary(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> W, const BcTables &bc)
 {
@@ -247,6 +347,11 @@ void launch_boundary(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> 
     if (bc.n_per)
         k_bc_periodic<T><<<(unsigned)((bc.n_per + 255) / 256), 256, 0, ctx.stream>>>(B, W, bc.per_dst, bc.per_src, bc.per_meta, bc.n_per);
     if (W.ev) launch_sa_boundary<T>(ctx, P, W, bc);
+    if (bc.n_mix) {
+        k_mix_average<T><<<dim3((bc.max_mix_rows + 31) / 32, bc.n_mix), 32, 0, ctx.stream>>>(B, P, G, W, bc.mix, bc.max_mix_rows, bc.mix_avg);
+        k_mix_fill<T><<<dim3((bc.max_mix_rows * bc.max_mix_j + 127) / 128, bc.n_mix, 2), 128, 0, ctx.stream>>>(
+            B, P, W, bc.mix, bc.max_mix_rows, bc.max_mix_j, bc.mix_avg);
+    }
 }
 
 template void launch_boundary<double>(const LaunchCtx &, const Phys &, const Geo &, Flow<double>, const BcTables &);

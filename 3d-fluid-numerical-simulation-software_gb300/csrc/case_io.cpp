@@ -212,8 +212,9 @@ void read_bc(CaseSpec &c, std::vector<BlockRow> &blocks)
     r.next();
     for (int q = 0; q < n; q++) c.interiors.push_back(pair_line("interior"));
     r.skip(3);
-    if (count("mixing-plane count") != 0) throw std::runtime_error("mixing planes are not supported");
+    n = count("mixing-plane count");
     r.next();
+    for (int q = 0; q < n; q++) c.mixing.push_back(pair_line("mixing plane"));
     r.skip(3);
     const int nb = count("block count");
     if (nb < 1) throw std::runtime_error(c.bc_file + ": the case needs at least one block");
@@ -249,6 +250,13 @@ void read_bc(CaseSpec &c, std::vector<BlockRow> &blocks)
     for (auto &w : c.walls) in_range(w.block, "a wall");
     for (auto &p : c.periodics) { in_range(p.b1, "a periodic pair"); in_range(p.b2, "a periodic pair"); }
     for (auto &p : c.interiors) { in_range(p.b1, "an interface"); in_range(p.b2, "an interface"); }
+    for (auto &p : c.mixing) {
+        in_range(p.b1, "a mixing plane"); in_range(p.b2, "a mixing plane");
+        // CMesh::BndCondMixingPlane averages the k = KM cells of block 1 and the k = 1 cells of
+        // block 2 over the pitch, row by row of block 1's i range (source/BndCondMixingPlane.cpp:287-520)
+        if (p.f1 != 6 || p.f2 != 5)
+            throw std::runtime_error(c.bc_file + ": a mixing plane joins the k+ face (6) of its first block to the k- face (5) of its second");
+    }
 }
 
 // the grid file: block count, then per block its id line, "IM JM KM" and the nodes, i fastest

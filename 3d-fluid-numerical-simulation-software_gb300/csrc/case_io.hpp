@@ -45,7 +45,7 @@ struct CaseSpec {
     // pairs and block interfaces (which join two blocks) are the case's full lists, in file order
     std::vector<PatchIO> inlets, outlets;
     std::vector<WallIO> walls;
-    std::vector<PeriodicIO> periodics, interiors;
+    std::vector<PeriodicIO> periodics, interiors, mixing;     // mixing: mixing planes (same line format)
     PatchIO first_inlet{}, first_outlet{};       // the case's Inlet[1] and Outlet[1] (the reported sections)
     int nblade = 1;
     double rpm = 0;

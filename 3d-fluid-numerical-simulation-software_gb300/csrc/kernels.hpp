@@ -29,6 +29,9 @@ struct LaunchCtx {
 // boundary patches in device form; every record names its solve
 struct DevInOut { int solve, face, is, ie, js, je, ks, ke; };
 struct DevWall { int solve, face, rotate, is, ie, js, je, ks, ke; };
+// mixing plane: k+ face of slot s1 (rows is..ie, pitch range js1..je1) against the k- face of slot s2
+struct DevMix { int s1, s2, is, ie, js1, je1, js2, je2; };
+constexpr int kMixVals = 14;                    // per row: both sides' averaged d, u, v, w, p, c; the SA value
 struct BcTables {
     const DevInOut *inlet = nullptr; int n_inlet = 0, max_inlet = 0;     // max cells of a patch
     const DevInOut *outlet = nullptr; int n_outlet = 0;
@@ -50,6 +53,10 @@ struct BcTables {
     void *wall_dist = nullptr;
     const long long *wall_dist_off = nullptr;
     const DevInOut *inlet_first = nullptr, *outlet_first = nullptr;   // per solve: Inlet[1], Outlet[1]
+    // mixing planes (applied after every other boundary) and their per-row averages
+    const DevMix *mix = nullptr;
+    int n_mix = 0, max_mix_rows = 0, max_mix_j = 0;
+    double *mix_avg = nullptr;
     // Spalart-Allmaras: ghost cells of the variable filled by interfaces and periodic pairs
     const long long *sa_dst = nullptr, *sa_src = nullptr;
     long long n_sa_gather = 0;

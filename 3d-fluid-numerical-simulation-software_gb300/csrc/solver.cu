@@ -901,12 +901,28 @@ public:
                 }
             }
         }
+        // mixing planes of every case (applied last, source/BoundaryCondition.cpp:59-62)
+        std::vector<DevMix> mixes;
+        for (int cix = 0; cix < ncase; cix++) {
+            const int s0 = case_first[cix];
+            for (auto mp : cases[s0].mixing) {
+                const PeriodicIO q = level_pair(mp, l);
+                DevMix m{s0 + q.b1 - 1, s0 + q.b2 - 1, q.r1[0], q.r1[1], q.r1[2], q.r1[3], q.r2[2], q.r2[3]};
+                const Lvl &v1 = Lv.lv[m.s1], &v2 = Lv.lv[m.s2];
+                if (m.is < 1 || m.ie > v1.IM - 1 || m.ie > v2.IM - 1 || m.js1 < 1 || m.je1 > v1.JM - 1 || m.js2 < 1 || m.je2 > v2.JM - 1)
+                    throw std::runtime_error("mixing plane range outside its blocks (rows of the first block are used on both sides)");
+                mixes.push_back(m);
+                bc.max_mix_rows = std::max(bc.max_mix_rows, m.ie - m.is + 1);
+                bc.max_mix_j = std::max(bc.max_mix_j, std::max(m.je1 - m.js1 + 1, m.je2 - m.js2 + 1));
+            }
+        }
         // upload everything into one table buffer
         auto bytes = [](size_t n, size_t sz) { return (n * sz + 255) & ~(size_t)255; };
         size_t tot = bytes(inl.size(), sizeof(DevInOut)) + bytes(outl.size(), sizeof(DevInOut)) + bytes(inl1.size(), sizeof(DevInOut)) +
                      bytes(outl1.size(), sizeof(DevInOut)) + bytes(walls.size(), sizeof(DevWall)) + bytes(pdst.size(), 8) * 2 +
                      bytes(pmeta.size(), 4) + bytes(outl.size() * (size_t)(bc.max_outlet_im + 1), 8) +
-                     bytes((size_t)nsolve * 2 * kIntegralBlocks * 3, 8) + bytes(sa_dst_h.size(), 8) * 2 + 256;
+                     bytes((size_t)nsolve * 2 * kIntegralBlocks * 3, 8) + bytes(sa_dst_h.size(), 8) * 2 +
+                     bytes(mixes.size(), sizeof(DevMix)) + bytes(mixes.size() * (size_t)bc.max_mix_rows * kMixVals, 8) + 256;
         CK(cudaMalloc(&Lv.tab_mem.p, tot));
         char *q = (char *)Lv.tab_mem.p;
         auto up = [&](const void *h, size_t n, size_t sz) {
@@ -927,6 +943,9 @@ public:
         bc.sa_dst = (const long long *)up(sa_dst_h.data(), sa_dst_h.size(), 8);
         bc.sa_src = (const long long *)up(sa_src_h.data(), sa_src_h.size(), 8);
         bc.n_sa_gather = (long long)sa_dst_h.size();
+        bc.mix = (const DevMix *)up(mixes.data(), mixes.size(), sizeof(DevMix));
+        bc.n_mix = (int)mixes.size();
+        bc.mix_avg = (double *)up(nullptr, 0, 8); q += bytes(mixes.size() * (size_t)bc.max_mix_rows * kMixVals, 8);
         bc.outlet_cu = (double *)up(nullptr, 0, 8); q += bytes(outl.size() * (size_t)(bc.max_outlet_im + 1), 8);
         bc.integ_part = (double *)up(nullptr, 0, 8); q += bytes((size_t)nsolve * 2 * kIntegralBlocks * 3, 8);
         for (int f = 0; f < 3; f++)

@@ -413,6 +413,8 @@ class MultiBlockCase:
     nblade: int
     rpm: float
     options: Dict[str, str]
+    block_nblade: Optional[List[int]] = None     # per block, when the blocks differ (stages)
+    block_rpm: Optional[List[float]] = None
 
     @property
     def n_cells(self) -> int:
@@ -471,6 +473,7 @@ def _bc_text_multi(case: MultiBlockCase) -> str:
         return "\t".join(str(v) for v in t)
 
     inl, out, wal, per, itf = sel("inlet"), sel("outlet"), sel("wall"), sel("periodic"), sel("interior")
+    mix = sel("mixing")
     L = ["# Boundary definition", "#", "# inlet", "#---------------------------",
          f" {len(inl)}\t\t# number of inlets", "#ID_BID FT_Ista_Iend_Jsta_Jend_Ksta_Kend"]
     L += [f"{n}\t{p.block}\t{p.patch.face}\t{rng(p.patch.rng)}" for n, p in enumerate(inl, 1)]
@@ -488,12 +491,17 @@ def _bc_text_multi(case: MultiBlockCase) -> str:
           "#ID_ori_BID1_FT1_Ista1_Iend1_Jsta1_Jend1_Ksta1_Kend1_BID2_FT2_..."]
     L += [f"{n}\t{p.patch.orient}\t{p.block}\t{p.patch.face}\t{rng(p.patch.rng)}\t{p.block2}\t{p.patch.face2}\t"
           f"{rng(p.patch.rng2)}" for n, p in enumerate(itf, 1)]
-    L += ["#", "# mixing plane", "#--------------------------", " 0\t\t# number of MixingPlanes",
-          "#ID_ori_BID1_FT1_...", "#", "# Blocks", "#--------------------------",
+    L += ["#", "# mixing plane", "#--------------------------", f" {len(mix)}\t\t# number of MixingPlanes",
+          "#ID_ori_BID1_FT1_..."]
+    L += [f"{n}\t{p.patch.orient}\t{p.block}\t{p.patch.face}\t{rng(p.patch.rng)}\t{p.block2}\t{p.patch.face2}\t"
+          f"{rng(p.patch.rng2)}" for n, p in enumerate(mix, 1)]
+    L += ["#", "# Blocks", "#--------------------------",
           f"{len(case.blocks)}\t\t# number of Blocks", "#BID_IM_JM_KM_Nblade_rpm"]
     for b, nodes in enumerate(case.blocks, 1):
         IM, JM, KM = nodes.shape[:3]
-        L.append(f"{b}    {IM} {JM} {KM}\t{case.nblade}  {case.rpm:.17g}")
+        nbl = case.block_nblade[b - 1] if case.block_nblade else case.nblade
+        rpm = case.block_rpm[b - 1] if case.block_rpm else case.rpm
+        L.append(f"{b}    {IM} {JM} {KM}\t{nbl}  {rpm:.17g}")
     L.append("")
     return "\n".join(L)
 
@@ -512,3 +520,35 @@ def write_multiblock_case(case: MultiBlockCase, directory: str, gridfile: str = 
         f.write(_bc_text_multi(case))
     with open(os.path.join(directory, "config.dat"), "w") as f:
         f.write(_config_text(case.options, gridfile, "BoundaryDefinition.dat"))
+
+
+def stage_passage(IM: int = 9, JM1: int = 9, KM1: int = 17, JM2: int = 9, KM2: int = 17, nblade1: int = 22,
+                  nblade2: int = 30, rpm: float = 16000.0, options: Optional[Dict[str, str]] = None,
+                  name: str = "stage") -> MultiBlockCase:
+    """A rotor passage followed by a stator passage, joined by a mixing plane (the reference's
+    CMesh::BndCondMixingPlane between the k+ face of block 1 and the k- face of block 2): block 1 is
+    ``rotor_passage`` with ``nblade1`` blades at ``rpm``, block 2 a stationary blade row of
+    ``nblade2`` blades (the same generator with its stagger mirrored and no rotation) placed
+    downstream, with the same radial node distribution so that the rows of the mixing plane match.
+    The rotor's outlet face and the stator's inlet face become the mixing plane."""
+    opts = dict(options or {})
+    rot = rotor_passage(IM=IM, JM=JM1, KM=KM1, nblade=nblade1, rpm=rpm, options=opts, name=name)
+    sta = rotor_passage(IM=IM, JM=JM2, KM=KM2, nblade=nblade2, rpm=0.0, stagger_hub=-30.0, stagger_tip=-20.0,
+                        camber_hub=-30.0, camber_tip=-20.0, options=opts, name=name)
+    n2 = sta.nodes.copy()
+    n2[..., 2] += rot.nodes[..., 2].max() - n2[..., 2].min()
+    patches: List[BlockPatch] = []
+    for p in rot.patches:
+        if p.kind == "outlet":
+            continue
+        patches.append(BlockPatch(p, 1, 1 if p.kind == "periodic" else 0))
+    for p in sta.patches:
+        if p.kind == "inlet":
+            continue
+        if p.kind == "wall" and p.face in (1, 2):
+            p = dataclasses.replace(p, rotate=0)           # stator hub and casing do not rotate
+        patches.append(BlockPatch(p, 2, 2 if p.kind == "periodic" else 0))
+    mp = Patch("mixing", 6, (1, IM - 1, 1, JM1 - 1, KM1, KM1), face2=5, rng2=(1, IM - 1, 1, JM2 - 1, 1, 1), orient=2)
+    patches.append(BlockPatch(mp, 1, 2))
+    return MultiBlockCase(name, [rot.nodes, n2], patches, nblade1, rpm, opts, block_nblade=[nblade1, nblade2],
+                          block_rpm=[rpm, 0.0])

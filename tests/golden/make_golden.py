@@ -10,7 +10,7 @@ Only runs where the reference sources and a C++ compiler exist; the fixtures it 
 committed so the tests need neither.
 
     python tests/golden/make_golden.py [name ...]      (default: every short case, the restart case and
-                                                        the multi-block cases; long cases by name)
+                                                        the multi-block and stage cases; long cases by name)
 """
 from __future__ import annotations
 
@@ -74,6 +74,13 @@ MULTI = {
     "rotor_9x9x33_3block_mg": (dict(IM=9, JM=9, KM=33), [9, 25], {"multigrid": "Y", "coarse_iter": "4"}, 12),
 }
 
+# rotor-stator stage: a rotor passage of 22 blades at 16000 rpm and a stationary row of 30 blades,
+# joined by a mixing plane (meshgen.stage_passage)
+STAGE = {
+    "stage_9x9x17": (dict(), {}, 12),
+    "stage_9x9x17_mg": (dict(), {"multigrid": "Y", "coarse_iter": "4"}, 12),
+}
+
 # restart round trip: the reference runs n1 iterations and writes its solution and restart files,
 # then a second run of the same case with "use previous solution" reads the restart file and runs
 # n2 more; both case directories are kept (the second holds the restart file it starts from)
@@ -131,8 +138,12 @@ def make_restart(name: str) -> None:
 
 def make_multi(name: str) -> None:
     mg = _meshgen()
-    kw, cuts, opts, n_iter = MULTI[name]
-    case = mg.split_axial(mg.rotor_passage(**kw, options=dict(opts), name=name), cuts, name=name)
+    if name in STAGE:
+        kw, opts, n_iter = STAGE[name]
+        case = mg.stage_passage(**kw, options=dict(opts), name=name)
+    else:
+        kw, cuts, opts, n_iter = MULTI[name]
+        case = mg.split_axial(mg.rotor_passage(**kw, options=dict(opts), name=name), cuts, name=name)
     cdir = os.path.join(HERE, name)
     if os.path.isdir(cdir):
         shutil.rmtree(cdir)
@@ -159,7 +170,7 @@ def make_multi(name: str) -> None:
 
 
 def make(name: str) -> None:
-    if name in MULTI:
+    if name in MULTI or name in STAGE:
         make_multi(name)
         return
     if name in RESTART:
@@ -200,5 +211,5 @@ def make(name: str) -> None:
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: oracle/build_ref.sh")
-    for n in (sys.argv[1:] or list(CASES) + list(RESTART) + list(MULTI)):
+    for n in (sys.argv[1:] or list(CASES) + list(RESTART) + list(MULTI) + list(STAGE)):
         make(n)

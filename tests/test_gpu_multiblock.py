@@ -1,9 +1,11 @@
 """Multi-block cases (several blocks per solve, joined by interfaces: CMesh::BndCondInterior,
 source/BndCondInteriorPeriodic.cpp:8-34, applied before the periodic pairs,
-source/BoundaryCondition.cpp:46-58) through the C-ABI, against the reference's own run of the
-same three-block rotor passage (fixtures rotor_9x9x33_3block and rotor_9x9x33_3block_mg, made by
-tests/golden/make_golden.py: the 9x9x33 passage cut at its blade's leading- and trailing-edge
-planes, in the arrangement of the reference's rotor-67 example). Tolerances as the single-block
+source/BoundaryCondition.cpp:46-58, or by a mixing plane: CMesh::BndCondMixingPlane,
+source/BndCondMixingPlane.cpp:287-520, applied last) through the C-ABI, against the reference's
+own runs of the same cases (made by tests/golden/make_golden.py): rotor_9x9x33_3block and
+rotor_9x9x33_3block_mg, the 9x9x33 passage cut at its blade's leading- and trailing-edge planes
+in the arrangement of the reference's rotor-67 example; stage_9x9x17 and stage_9x9x17_mg, a
+22-blade rotor at 16000 rpm and a stationary 30-blade row joined by a mixing plane. Tolerances as the single-block
 parity tests: 1e-11 on geometry, 1e-10 normwise on a residual evaluation and its intermediates,
 1e-9 on the driver history; the solution files as the restart tests (six printed digits)."""
 import numpy as np
@@ -16,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 HIST_COLS = [0, 1, 6, 7, 8, 9, 11]
 R1_KEYS = ["cv", "pv", "mut", "omega", "lamcK", "lamvK", "dt", "FcK", "FvK", "FcJ", "res", "dKS_pv", "dKP_pv"]
-CASES = ["rotor_9x9x33_3block", "rotor_9x9x33_3block_mg"]
+CASES = ["rotor_9x9x33_3block", "rotor_9x9x33_3block_mg", "stage_9x9x17", "stage_9x9x17_mg"]
 
 
 def _hist_err(a, b):
@@ -25,10 +27,11 @@ def _hist_err(a, b):
 
 
 @pytest.mark.parametrize("name", CASES)
-def test_three_blocks_match_the_reference(name, gpu_lib, tmp_path):
+def test_blocks_match_the_reference(name, gpu_lib, tmp_path):
     g = load_golden(name)
+    nb = sum(1 for k in g if k.endswith("_g1_cell"))
     with gpu_lib.Solver(golden_dir(name), gpu_lib.FP64) as s:
-        assert s.n == 1 and s.n_slots == 3 and list(s.slots(0)) == [0, 1, 2]
+        assert s.n == 1 and s.n_slots == nb and list(s.slots(0)) == list(range(nb))
         for b, slot in enumerate(s.slots(0), 1):
             for key in ("faceK", "cell", "totalvol"):
                 assert rel_err(s.get(key, solve=slot), g[f"b{b}_g1_{key}"]) < 1e-11, (b, key)
