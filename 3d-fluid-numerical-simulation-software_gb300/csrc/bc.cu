@@ -231,53 +231,57 @@ __global__ void k_bc_periodic(Batch B, Flow<T> W, const long long *dst, const lo
     st_state(W, b, c, q);
 }
 
-// mixing plane (CMesh::BndCondMixingPlane, source/BndCondMixingPlane.cpp:287-520), one thread per
-// radial row: flux averages over the pitch of the last cell layer upstream (block 1, k = KM - 1,
-// normals of the k = KM faces) and of the first layer downstream (block 2, k = 1), each turned into
-// a mixed-out state by the quadratic for the pressure
+// mixing plane (CMesh::BndCondMixingPlane, source/BndCondMixingPlane.cpp:287-520), one warp per
+// radial row and side: flux averages over the pitch of the last cell layer upstream (block 1,
+// k = KM - 1, normals of the k = KM faces) and of the first layer downstream (block 2, k = 1), each
+// turned into a mixed-out state by the quadratic for the pressure (the pitch sums are formed as a
+// warp reduction, not in the reference's sequential order)
 template <typename T>
-__global__ void k_mix_average(Batch B, Phys P, Geo G, Flow<T> W, const DevMix *mix, int max_rows, double *avg)
+__global__ void __launch_bounds__(32) k_mix_average(Batch B, Phys P, Geo G, Flow<T> W, const DevMix *mix, int max_rows, double *avg)
 {
     const DevMix m = mix[blockIdx.y];
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.x, side = blockIdx.z;
     if (r > m.ie - m.is) return;
     const int i = m.is + r;
     const double g = P.gamma, R = P.rgas;
     double *o = avg + ((long long)blockIdx.y * max_rows + r) * kMixVals;
-    for (int side = 0; side < 2; side++) {
-        const int s = side ? m.s2 : m.s1;
-        const Lvl L = B.lv[s];
-        const int kf = side ? 1 : L.KM, kc = side ? 1 : L.KM - 1;
-        const int j0 = side ? m.js2 : m.js1, j1 = side ? m.je2 : m.je1;
-        double I1 = 0.0, I2 = 0.0, I3 = 0.0, I4 = 0.0, I5 = 0.0, I6 = 0.0, nsx = 0.0, nsy = 0.0, nsz = 0.0, ss = 0.0;
-        for (int j = j0; j <= j1; j++) {
-            const long long f = ix(L, i, j, kf), c = ix(L, i, j, kc);
-            const double sa = G.s[2][f];
-            const double nx = G.S[2][0][f] / sa, ny = G.S[2][1][f] / sa, nz = G.S[2][2][f] / sa;
-            nsx = nsx + nx * sa; nsy = nsy + ny * sa; nsz = nsz + nz * sa;
-            ss = ss + sa;
-            const double u = W.pv[PU][c], v = W.pv[PV][c], w = W.pv[PW][c], pr = W.pv[PP][c];
-            const double Vn = u * nx + v * ny + w * nz;
-            I1 = I1 + W.cv[0][c] * Vn * sa;
-            I2 = I2 + (W.cv[1][c] * Vn + nx * pr) * sa;
-            I3 = I3 + (W.cv[2][c] * Vn + ny * pr) * sa;
-            I4 = I4 + (W.cv[3][c] * Vn + nz * pr) * sa;
-            I5 = I5 + (W.cv[4][c] + pr) * Vn * sa;
-            if (W.ev) I6 = I6 + W.cv[0][c] * W.ev[c] * Vn * sa;
-        }
-        I1 = I1 / ss; I2 = I2 / ss; I3 = I3 / ss; I4 = I4 / ss; I5 = I5 / ss;
-        if (side == 0) o[12] = W.ev ? (I6 / ss) / I1 : 0.0;
-        const double nux = nsx / ss, nuy = nsy / ss, nuz = nsz / ss;
-        const double A = I2 * nux + I3 * nuy + I4 * nuz;
-        const double Bq = (double)2.0f * I1 * I5 - (I2 * I2 + I3 * I3 + I4 * I4);
-        const double C = nux * nux + nuy * nuy + nuz * nuz;
-        const double pr = (A / C + sqrt(A * A / C / C - (g * g - 1.0) * Bq / C)) / (g + 1.0);
-        const double u = (I2 - pr * nux) / I1, v = (I3 - pr * nuy) / I1, w = (I4 - pr * nuz) / I1;
-        const double d = I1 / (u * nux + v * nuy + w * nuz);
-        const double t = pr / R / d;
-        double *q = o + 6 * side;
-        q[0] = d; q[1] = u; q[2] = v; q[3] = w; q[4] = pr; q[5] = sqrt(g * R * t);
+    const int s = side ? m.s2 : m.s1;
+    const Lvl L = B.lv[s];
+    const int kf = side ? 1 : L.KM, kc = side ? 1 : L.KM - 1;
+    const int j0 = side ? m.js2 : m.js1, j1 = side ? m.je2 : m.je1;
+    double acc[10] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};   // I1..I6, n*s (3), s
+    for (int j = j0 + (int)threadIdx.x; j <= j1; j += 32) {
+        const long long f = ix(L, i, j, kf), c = ix(L, i, j, kc);
+        const double sa = G.s[2][f];
+        const double nx = G.S[2][0][f] / sa, ny = G.S[2][1][f] / sa, nz = G.S[2][2][f] / sa;
+        const double u = W.pv[PU][c], v = W.pv[PV][c], w = W.pv[PW][c], pr = W.pv[PP][c];
+        const double Vn = u * nx + v * ny + w * nz;
+        acc[0] += W.cv[0][c] * Vn * sa;
+        acc[1] += (W.cv[1][c] * Vn + nx * pr) * sa;
+        acc[2] += (W.cv[2][c] * Vn + ny * pr) * sa;
+        acc[3] += (W.cv[3][c] * Vn + nz * pr) * sa;
+        acc[4] += (W.cv[4][c] + pr) * Vn * sa;
+        if (W.ev) acc[5] += W.cv[0][c] * W.ev[c] * Vn * sa;
+        acc[6] += nx * sa; acc[7] += ny * sa; acc[8] += nz * sa;
+        acc[9] += sa;
     }
+#pragma unroll
+    for (int q = 0; q < 10; q++)
+        for (int off = 16; off > 0; off >>= 1) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], off);
+    if (threadIdx.x != 0) return;
+    const double ss = acc[9];
+    const double I1 = acc[0] / ss, I2 = acc[1] / ss, I3 = acc[2] / ss, I4 = acc[3] / ss, I5 = acc[4] / ss;
+    if (side == 0) o[12] = W.ev ? (acc[5] / ss) / I1 : 0.0;
+    const double nux = acc[6] / ss, nuy = acc[7] / ss, nuz = acc[8] / ss;
+    const double A = I2 * nux + I3 * nuy + I4 * nuz;
+    const double Bq = 2.0 * I1 * I5 - (I2 * I2 + I3 * I3 + I4 * I4);
+    const double C = nux * nux + nuy * nuy + nuz * nuz;
+    const double pr = (A / C + sqrt(A * A / C / C - (g * g - 1.0) * Bq / C)) / (g + 1.0);
+    const double u = (I2 - pr * nux) / I1, v = (I3 - pr * nuy) / I1, w = (I4 - pr * nuz) / I1;
+    const double d = I1 / (u * nux + v * nuy + w * nuz);
+    const double t = pr / R / d;
+    double *q = o + 6 * side;
+    q[0] = d; q[1] = u; q[2] = v; q[3] = w; q[4] = pr; q[5] = sqrt(g * R * t);
 }
 
 // ghost and reconstruction layers of both sides from the other side's mixed-out state and the
@@ -348,7 +352,7 @@ void launch_boundary(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> 
         k_bc_periodic<T><<<(unsigned)((bc.n_per + 255) / 256), 256, 0, ctx.stream>>>(B, W, bc.per_dst, bc.per_src, bc.per_meta, bc.n_per);
     if (W.ev) launch_sa_boundary<T>(ctx, P, W, bc);
     if (bc.n_mix) {
-        k_mix_average<T><<<dim3((bc.max_mix_rows + 31) / 32, bc.n_mix), 32, 0, ctx.stream>>>(B, P, G, W, bc.mix, bc.max_mix_rows, bc.mix_avg);
+        k_mix_average<T><<<dim3(bc.max_mix_rows, bc.n_mix, 2), 32, 0, ctx.stream>>>(B, P, G, W, bc.mix, bc.max_mix_rows, bc.mix_avg);
         k_mix_fill<T><<<dim3((bc.max_mix_rows * bc.max_mix_j + 127) / 128, bc.n_mix, 2), 128, 0, ctx.stream>>>(
             B, P, W, bc.mix, bc.max_mix_rows, bc.max_mix_j, bc.mix_avg);
     }

@@ -58,6 +58,7 @@ struct Flow {
     T *lamc[3], *lamv[3];
     T *Ff[3][NQ], *Vf[3][NQ];                        // face convective / viscous fluxes
     T *Fd[3][NQ];                                    // face artificial dissipation (JST only, else null)
+    T *jsens[3], *jva[3];                            // JST per cell and direction: pressure sensor, phi * lambda
     T *res[NQ], *dq[NQ];
     double *cv2h[NQ];                                // multigrid (coarse level only)
     T *res2h[NQ], *dq2h[NQ];

@@ -87,6 +87,11 @@ struct SweepData {
     T *gn[3][3] = {}, *gs[3] = {}, *gve[3] = {}, *gvol = nullptr;   // per direction: mean normal, |S|, entrainment
     T *cv[NQ] = {}, *pp = nullptr, *lamc[3] = {}, *lamv[3] = {}, *dt = nullptr, *res[NQ] = {};
     T *dq[NQ] = {};
+    // Spalart-Allmaras sweep (null without it), per cell as a neighbour in direction d: normal
+    // velocity with the mean flow's dQ added, old variable times old normal velocity, mean |S|,
+    // relax * lambda_c, lambda_v; per cell: old variable, diagonal, residual, update
+    T *sa_vn[3] = {}, *sa_eb[3] = {}, *sa_s[3] = {}, *sa_rl[3] = {}, *sa_lv[3] = {};
+    T *sa_ev0 = nullptr, *sa_alpha = nullptr, *sa_res = nullptr, *sa_dq = nullptr;
 };
 
 void launch_geometry(const LaunchCtx &ctx, const Geo &G, double *totalvol);

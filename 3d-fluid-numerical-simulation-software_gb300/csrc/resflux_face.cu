@@ -182,11 +182,57 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 4) k_face(Batch B, P
     W.Vf[F][4][p] = qx * Sx + qy * Sy + qz * Sz;
 }
 
-// JST artificial dissipation of one face (source/JST_Dissip.cpp:193-413): pressure sensors of the
-// four cells around the face, blended second and fourth differences of Q scaled by the
-// anisotropy-weighted spectral radius. Positions along the face normal follow the reference's
-// switch between cells and reconstruction layers (position c <= 0 is dummy layer 1 - c, c >= N
-// dummy layer c - N + 1).
+// JST artificial dissipation (source/JST_Dissip.cpp:5-431). Positions along a grid line follow
+// the reference's switch between cells and reconstruction layers (position c <= 0 is dummy layer
+// 1 - c, c >= N dummy layer c - N + 1), which in the padded box is index c - 1 / c + 1.
+__device__ __forceinline__ int jst_pos(int c, int NN) { return c <= 0 ? c - 1 : (c >= NN ? c + 1 : c); }
+
+// pressure sensor of every position -1 .. N + 1 of every line of direction F (sensorI/J/K, :5-190);
+// the k-direction sensor's range check compares j with KM, as the reference's does
+template <typename T, int F>
+__global__ void __launch_bounds__(256) k_jst_sensor(Batch B, Flow<T> W)
+{
+    const Lvl L = B.lv[blockIdx.y];
+    const int NN = F == 0 ? L.IM : (F == 1 ? L.JM : L.KM);
+    const int n1 = F == 0 ? L.JM - 1 : L.IM - 1, n2 = F == 2 ? L.JM - 1 : L.KM - 1;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned np = (unsigned)(NN + 3);
+    if (t >= np * (unsigned)n1 * (unsigned)n2) return;
+    const int c = (int)(t % np) - 1;
+    const unsigned r = t / np;
+    const int a1 = 1 + (int)(r % (unsigned)n1), a2 = 1 + (int)(r / (unsigned)n1);
+    int i, j, k;
+    if (F == 0) { j = a1; k = a2; i = 0; }
+    else if (F == 1) { i = a1; k = a2; j = 0; }
+    else { i = a1; j = a2; k = 0; }
+    const long long sn = F == 0 ? (long long)L.NJ * L.NK : (F == 1 ? (long long)L.NK : 1LL);
+    const long long p0 = ix(L, i, j, k);
+    T v = (T)0;
+    if (!(F == 2 && j > L.KM)) {
+        const T pf = W.pv[PP][p0 + jst_pos(c + 1, NN) * sn], pc = W.pv[PP][p0 + jst_pos(c, NN) * sn],
+                pb = W.pv[PP][p0 + jst_pos(c - 1, NN) * sn];
+        v = fabs((pf - (T)2 * pc + pb) / (pf + (T)2 * pc + pb));
+    }
+    W.jsens[F][p0 + jst_pos(c, NN) * sn] = v;
+}
+
+// anisotropy-weighted spectral radius phi * lambda of every cell and direction (:198-216); the
+// two other directions in the reference's order of the sum: I faces J, K; J faces I, K; K faces J, I
+template <typename T>
+__global__ void __launch_bounds__(256) k_jst_weights(Batch B, Flow<T> W)
+{
+    const Lvl L = B.lv[blockIdx.y];
+    int i, j, k;
+    if (!box_index(L.IM - 1, L.JM - 1, L.KM - 1, i, j, k)) return;
+    const long long p = ix(L, i, j, k);
+    const T ex = (T)(double)0.4f;
+    const T l0 = W.lamc[0][p], l1 = W.lamc[1][p], l2 = W.lamc[2][p];
+    W.jva[0][p] = ((T)1 + pow(l1 / l0, ex) + pow(l2 / l0, ex)) * l0;
+    W.jva[1][p] = ((T)1 + pow(l0 / l1, ex) + pow(l2 / l1, ex)) * l1;
+    W.jva[2][p] = ((T)1 + pow(l1 / l2, ex) + pow(l0 / l2, ex)) * l2;
+}
+
+// dissipation of one face: blended second and fourth differences of Q (:193-413)
 template <typename T, int F>
 __global__ void __launch_bounds__(128) k_jst_dissip(Batch B, Phys P, Flow<T> W)
 {
@@ -200,33 +246,15 @@ __global__ void __launch_bounds__(128) k_jst_dissip(Batch B, Phys P, Flow<T> W)
     const int NN = F == 0 ? L.IM : (F == 1 ? L.JM : L.KM);
     const int a = F == 0 ? i : (F == 1 ? j : k);
     const long long p0 = p - (long long)a * sn;
-    auto at = [&](int c) { return p0 + (long long)(c <= 0 ? c - 1 : (c >= NN ? c + 1 : c)) * sn; };
-    // pressure sensor of position c (sensorI/J/K, :5-190); the k-direction sensor's range check
-    // compares j with KM, as the reference's does
-    const bool out_of_range = F == 2 && j > L.KM;
-    auto sensor = [&](int c) -> T {
-        if (out_of_range) return (T)0;
-        const T pf = W.pv[PP][at(c + 1)], pc = W.pv[PP][at(c)], pb = W.pv[PP][at(c - 1)];
-        return fabs((pf - (T)2 * pc + pb) / (pf + (T)2 * pc + pb));
-    };
-    const T e2 = (T)P.k2 * fmax(fmax(sensor(a + 1), sensor(a)), fmax(sensor(a - 1), sensor(a - 2)));
+    const long long c1 = p0 + jst_pos(a + 1, NN) * sn, c2 = p0 + jst_pos(a, NN) * sn, c3 = p0 + jst_pos(a - 1, NN) * sn,
+                    c4 = p0 + jst_pos(a - 2, NN) * sn;
+    const T *sen = W.jsens[F];
+    const T e2 = (T)P.k2 * fmax(fmax(sen[c1], sen[c2]), fmax(sen[c3], sen[c4]));
     const T e4 = fmax((T)0, (T)P.k4 - e2);
-    // anisotropy weight phi * lambda of the cell on each side (:198-216)
-    // the two other directions in the reference's order of the sum: I faces J, K; J faces I, K;
-    // K faces J, I
-    const int t1 = F == 1 ? 0 : 1, t2 = F == 2 ? 0 : 2;
-    const T ex = (T)(double)0.4f;
-    auto va = [&](long long q) -> T {
-        const T ln = W.lamc[F][q];
-        const T a1 = W.lamc[t1][q] / ln, a2 = W.lamc[t2][q] / ln;
-        const T phi = (T)1 + pow(a1, ex) + pow(a2, ex);
-        return phi * ln;
-    };
     T alpha;
-    if (a == 1) alpha = va(p);
-    else if (a == NN) alpha = va(p - sn);
-    else alpha = (T)0.5 * (va(p) + va(p - sn));
-    const long long c1 = at(a + 1), c2 = at(a), c3 = at(a - 1), c4 = at(a - 2);
+    if (a == 1) alpha = W.jva[F][p];
+    else if (a == NN) alpha = W.jva[F][p - sn];
+    else alpha = (T)0.5 * (W.jva[F][p] + W.jva[F][p - sn]);
     T d[NQ];
 #pragma unroll
     for (int c = 0; c < NQ; c++) {
@@ -291,11 +319,18 @@ void launch_resflux(const LaunchCtx &ctx, const Phys &P, const PhysW<T> &PC, con
     }
     ctx.mark("face_flux", 0, 3);
     if (P.scheme == 100) {
-        ctx.mark("jst_dissipation", 1, 3);
+        ctx.mark("jst_dissipation", 1, 7);
+        const long long ls0 = (long long)(ctx.maxIM + 3) * (ctx.maxJM - 1) * (ctx.maxKM - 1);
+        const long long ls1 = (long long)(ctx.maxJM + 3) * (ctx.maxIM - 1) * (ctx.maxKM - 1);
+        const long long ls2 = (long long)(ctx.maxKM + 3) * (ctx.maxIM - 1) * (ctx.maxJM - 1);
+        k_jst_sensor<T, 0><<<ctx.grid_n(ls0, 256), 256, 0, ctx.stream>>>(B, W);
+        k_jst_sensor<T, 1><<<ctx.grid_n(ls1, 256), 256, 0, ctx.stream>>>(B, W);
+        k_jst_sensor<T, 2><<<ctx.grid_n(ls2, 256), 256, 0, ctx.stream>>>(B, W);
+        k_jst_weights<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, W);
         k_jst_dissip<T, 0><<<ctx.grid_faces(0, 128), 128, 0, ctx.stream>>>(B, P, W);
         k_jst_dissip<T, 1><<<ctx.grid_faces(1, 128), 128, 0, ctx.stream>>>(B, P, W);
         k_jst_dissip<T, 2><<<ctx.grid_faces(2, 128), 128, 0, ctx.stream>>>(B, P, W);
-        ctx.mark("jst_dissipation", 0, 3);
+        ctx.mark("jst_dissipation", 0, 7);
     }
     ctx.mark("cell_sum", 1);
     k_cell_sum<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, GW, W);

@@ -357,47 +357,102 @@ void launch_sa_model(const LaunchCtx &ctx, const Phys &P, const GeoW<T> &GW, Flo
 }
 
 // ---------------------------------------------------------------------------------------------
-// LU-SGS sweeps of the variable: one launch per hyperplane after the mean-flow chain of the same
-// direction, reading the mean flow's dQ of the neighbours in plane order
+// LU-SGS sweeps of the variable (source/LU_SGS_Marching.cpp:76-258, delt_Fn_up/down :293-419). They
+// run after the mean-flow chain of the same direction, so every neighbour's mean-flow dQ is final:
+// a parallel pass first forms, for every cell as somebody's neighbour, the parts of
+// delt_Fn_ev = ev_new * Vn_new - ev_old * Vn_old that do not depend on the variable's own update
+// (Vn_new, ev_old * Vn_old) and the diagonal; the hyperplane chain then only adds the neighbours'
+// updates. One launch per plane, chained by programmatic dependent launch like the mean flow.
 // ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ void sa_wait_previous() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void sa_release_next() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 template <typename T, int DIR>
-__global__ void __launch_bounds__(128) k_sa_sweep(Batch B, PhysW<T> PC, Geo G, Flow<T> W, const int *start, int stride,
-                                                  int plane, SweepData<T> S)
+__global__ void __launch_bounds__(256) k_sa_sweep_prep(PhysW<T> PC, Geo G, Flow<T> W, SweepData<T> S, long long nq)
 {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const long long p = S.cell[q];
+    const double o0 = W.cv[0][p], o1 = W.cv[1][p], o2 = W.cv[2][p], o3 = W.cv[3][p];
+    const T dn0 = (T)(o0 + (double)S.dq[0][q]), dn1 = (T)(o1 + (double)S.dq[1][q]), dn2 = (T)(o2 + (double)S.dq[2][q]),
+            dn3 = (T)(o3 + (double)S.dq[3][q]);
+    const T evo = (T)W.ev[p];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const T nx = (T)G.cn[d][0][p], ny = (T)G.cn[d][1][p], nz = (T)G.cn[d][2][p];
+        S.sa_vn[d][q] = dn1 / dn0 * nx + dn2 / dn0 * ny + dn3 / dn0 * nz;
+        if (DIR > 0) {
+            const T Vold = (T)o1 / (T)o0 * nx + (T)o2 / (T)o0 * ny + (T)o3 / (T)o0 * nz;
+            S.sa_eb[d][q] = evo * Vold;
+            S.sa_s[d][q] = (T)G.cs[d][p];
+            S.sa_rl[d][q] = PC.relax * W.lamc[d][p];
+            S.sa_lv[d][q] = W.lamv[d][p];
+        }
+    }
+    if (DIR > 0) {
+        const T lc = W.lamc[0][p] + W.lamc[1][p] + W.lamc[2][p];
+        const T lv = W.lamv[0][p] + W.lamv[1][p] + W.lamv[2][p];
+        S.sa_alpha[q] = (T)G.vol[p] / W.dt[p] + PC.relax * lc + (T)3 * lv;
+        S.sa_ev0[q] = evo;
+        S.sa_res[q] = W.res_ev[p];
+    }
+}
+
+template <typename T, int DIR>
+__global__ void __launch_bounds__(32) k_sa_sweep(SweepData<T> S, const int *start, int stride, int plane)
+{
+    sa_release_next();
     const int s = blockIdx.y;
     const int q0 = start[(long long)s * stride + plane], q1 = start[(long long)s * stride + plane + 1];
     const int q = q0 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= q1) return;
-    const long long p = S.cell[q];
-    const T relax = PC.relax;
-    const T lc = W.lamc[0][p] + W.lamc[1][p] + W.lamc[2][p];
-    const T lv = W.lamv[0][p] + W.lamv[1][p] + W.lamv[2][p];
-    const T alpha = (T)G.vol[p] / W.dt[p] + relax * lc + (T)3 * lv;
+    const bool in = q < q1;
+    T alpha = (T)1, own = (T)0;
+    int qn[3] = {-1, -1, -1};
+    if (in) {
+        alpha = S.sa_alpha[q];
+        own = DIR > 0 ? -S.sa_res[q] : alpha * S.sa_dq[q];
+#pragma unroll
+        for (int d = 0; d < 3; d++) qn[d] = S.nb[DIR > 0 ? 0 : 1][d][q];
+    }
+    sa_wait_previous();
+    if (!in) return;
     T aws[3], vws[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
         aws[d] = (T)0; vws[d] = (T)0;
-        const int qn = S.nb[DIR > 0 ? 0 : 1][d][q];
-        if (qn < 0) continue;
-        const long long pn = S.cell[qn];
-        // F_n(Q + dQ) - F_n(Q) of the variable for the neighbour, with its mean unit normal
-        const T nx = (T)G.cn[d][0][pn], ny = (T)G.cn[d][1][pn], nz = (T)G.cn[d][2][pn];
-        const double o0 = W.cv[0][pn], o1 = W.cv[1][pn], o2 = W.cv[2][pn], o3 = W.cv[3][pn];
-        const T dn0 = (T)(o0 + (double)S.dq[0][qn]), dn1 = (T)(o1 + (double)S.dq[1][qn]), dn2 = (T)(o2 + (double)S.dq[2][qn]),
-                dn3 = (T)(o3 + (double)S.dq[3][qn]);
-        const T Vold = (T)o1 / (T)o0 * nx + (T)o2 / (T)o0 * ny + (T)o3 / (T)o0 * nz;
-        const T Vnew = dn1 / dn0 * nx + dn2 / dn0 * ny + dn3 / dn0 * nz;
-        const T evo = (T)W.ev[pn], dqn = W.dq_ev[pn];
-        const T evn = evo + dqn;
-        const T dF = evn * Vnew - evo * Vold;
-        const T sm = (T)G.cs[d][pn];
-        aws[d] = (T)0.5 * (dF * sm + (DIR > 0 ? relax : -relax) * W.lamc[d][pn] * dqn);
-        vws[d] = W.lamv[d][pn] * dqn;
+        const int n = qn[d];
+        if (n < 0) continue;
+        const T dqn = S.sa_dq[n];
+        const T dF = (S.sa_ev0[n] + dqn) * S.sa_vn[d][n] - S.sa_eb[d][n];
+        aws[d] = (T)0.5 * (dF * S.sa_s[d][n] + (DIR > 0 ? S.sa_rl[d][n] : -S.sa_rl[d][n]) * dqn);
+        vws[d] = S.sa_lv[d][n] * dqn;
     }
     if (DIR > 0)
-        W.dq_ev[p] = (-W.res_ev[p] + aws[0] + aws[1] + aws[2] + vws[0] + vws[1] + vws[2]) / alpha;
+        S.sa_dq[q] = (own + aws[0] + aws[1] + aws[2] + vws[0] + vws[1] + vws[2]) / alpha;
     else
-        W.dq_ev[p] = (alpha * W.dq_ev[p] - aws[0] - aws[1] - aws[2] + vws[0] + vws[1] + vws[2]) / alpha;
+        S.sa_dq[q] = (own - aws[0] - aws[1] - aws[2] + vws[0] + vws[1] + vws[2]) / alpha;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_sa_sweep_scatter(Flow<T> W, SweepData<T> S, long long nq)
+{
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < nq) W.dq_ev[S.cell[q]] = S.sa_dq[q];
+}
+
+template <typename T, int DIR>
+static void launch_sa_plane(const LaunchCtx &ctx, const SweepData<T> &S, const PlaneTables &pt, int pl, bool first)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(max(1, (pt.max_count[pl] + 31) / 32), ctx.batch.nsolve);
+    cfg.blockDim = dim3(32);
+    cfg.stream = ctx.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = first ? 0 : 1;
+    cudaLaunchKernelEx(&cfg, k_sa_sweep<T, DIR>, S, pt.start, pt.stride, pl);
 }
 
 template <typename T>
@@ -405,12 +460,14 @@ void launch_sa_sweep(const LaunchCtx &ctx, const PhysW<T> &PC, const Geo &G, Flo
                      const SweepData<T> &S, int dir)
 {
     const int np = pt.max_plane;
+    const unsigned gq = (unsigned)((pt.nq + 255) / 256);
     if (dir > 0) {
-        for (int pl = 3; pl <= np; pl++)
-            k_sa_sweep<T, 1><<<ctx.grid_n(pt.max_count[pl], 128), 128, 0, ctx.stream>>>(ctx.batch, PC, G, W, pt.start, pt.stride, pl, S);
+        k_sa_sweep_prep<T, 1><<<gq, 256, 0, ctx.stream>>>(PC, G, W, S, pt.nq);
+        for (int pl = 3; pl <= np; pl++) launch_sa_plane<T, 1>(ctx, S, pt, pl, pl == 3);
     } else {
-        for (int pl = np; pl >= 3; pl--)
-            k_sa_sweep<T, -1><<<ctx.grid_n(pt.max_count[pl], 128), 128, 0, ctx.stream>>>(ctx.batch, PC, G, W, pt.start, pt.stride, pl, S);
+        k_sa_sweep_prep<T, -1><<<gq, 256, 0, ctx.stream>>>(PC, G, W, S, pt.nq);
+        for (int pl = np; pl >= 3; pl--) launch_sa_plane<T, -1>(ctx, S, pt, pl, pl == np);
+        k_sa_sweep_scatter<T><<<gq, 256, 0, ctx.stream>>>(W, S, pt.nq);
     }
 }
 

@@ -502,11 +502,12 @@ public:
         }
         if (P.scheme == 100) {
             // face dissipation of JST (source/SpaceDiscr.cpp:611-640)
-            Lv.fd_mem.bytes = sizeof(T) * N * 15;
+            Lv.fd_mem.bytes = sizeof(T) * N * 21;
             CK(cudaMalloc(&Lv.fd_mem.p, Lv.fd_mem.bytes));
             CK(cudaMemset(Lv.fd_mem.p, 0, Lv.fd_mem.bytes));
             T *fd = (T *)Lv.fd_mem.p;
             for (int f = 0; f < 3; f++) for (int c = 0; c < NQ; c++) { W.Fd[f][c] = fd; fd += N; }
+            for (int f = 0; f < 3; f++) { W.jsens[f] = fd; fd += N; W.jva[f] = fd; fd += N; }
         } else {
             for (int f = 0; f < 3; f++) for (int c = 0; c < NQ; c++) W.Fd[f][c] = nullptr;
         }
@@ -731,7 +732,8 @@ public:
         const size_t nq = cell.size();
         pt.nq = (long long)nq;
         auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-        const size_t n_t = 16 + 18 + NQ;                   // geometry, flow inputs, dQ
+        const bool sa = P.turb_sa && l == 1;
+        const size_t n_t = 16 + 18 + NQ + (sa ? 19 : 0);   // geometry, flow inputs, dQ (and the SA sweep's)
         Lv.plane_mem.bytes = al(sizeof(int) * start.size()) + al(sizeof(long long) * nq) + 6 * al(sizeof(int) * nq) +
                              n_t * al(sizeof(T) * nq) + 256;
         CK(cudaMalloc(&Lv.plane_mem.p, Lv.plane_mem.bytes));
@@ -763,6 +765,10 @@ public:
         S.dt = arr();
         for (int c = 0; c < NQ; c++) S.res[c] = arr();
         for (int c = 0; c < NQ; c++) S.dq[c] = arr();
+        if (sa) {
+            for (int d = 0; d < 3; d++) { S.sa_vn[d] = arr(); S.sa_eb[d] = arr(); S.sa_s[d] = arr(); S.sa_rl[d] = arr(); S.sa_lv[d] = arr(); }
+            S.sa_ev0 = arr(); S.sa_alpha = arr(); S.sa_res = arr(); S.sa_dq = arr();
+        }
     }
 
     void build_tables(int l, const std::vector<LevelCase> &lc, const std::vector<double> &hx, const std::vector<double> &hy)

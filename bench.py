@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=1, help="operating points per GPU")
     ap.add_argument("--sampled", action="store_true",
                     help="draw the batch from the seeded operating-point sampler (three mesh sizes)")
+    ap.add_argument("--variant", default="default", choices=["default", "jst", "sa", "stage"],
+                    help="numerical variant of the passage: JST, Spalart-Allmaras (single grid), rotor-stator stage")
     ap.add_argument("--blocks", type=int, default=1, choices=[1, 3],
                     help="3: the passage as three blocks joined by interfaces (reference's rotor-67 layout)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -59,19 +61,37 @@ def parse():
     return ap.parse_args()
 
 
-def make_cases(root: str, n: int, seed_offset: int = 0, back_pressures=None, blocks: int = 1):
+# numerical variants of the passage (config values): the default Roe + MUSCL3 + Baldwin-Lomax
+# two-level case, JST, Spalart-Allmaras (single grid, the reference's only SA form), and the
+# rotor-stator stage joined by a mixing plane
+VARIANTS = {
+    "default": {},
+    "jst": {"scheme": "100", "k2": "0.5", "k4": "32.0"},
+    "sa": {"turb": "200", "multigrid": "N", "coarse_iter": "0"},
+}
+
+
+def make_cases(root: str, n: int, seed_offset: int = 0, back_pressures=None, blocks: int = 1, variant: str = "default"):
     """the 129 x 49 x 49 rotor passage; in a batch the back pressure varies over [1.05, 1.30] x p_t
     (or is given, as ratios to the inlet total pressure). blocks=3: the same passage cut at the
-    blade's leading- and trailing-edge planes (k = 41, 89) into three blocks joined by interfaces"""
+    blade's leading- and trailing-edge planes (k = 41, 89) into three blocks joined by interfaces.
+    variant "stage": a rotor of 129 x 49 x 49 nodes and a stationary row of 65 x 49 x 49 behind it,
+    joined by a mixing plane"""
     import meshgen as mg
     dirs = []
     for q in range(n):
         pb = 1.20 if n == 1 else 1.05 + 0.25 * ((q + seed_offset) % n) / max(n - 1, 1)
         if back_pressures is not None:
             pb = back_pressures[q]
-        case = mg.rotor_passage(IM=49, JM=49, KM=129, options={
-            "Pout": "%.1f" % (pb * 101325.0), "multigrid": "Y", "coarse_iter": "2", "Ma0": "0.45"})
+        opts = {"Pout": "%.1f" % (pb * 101325.0), "multigrid": "Y", "coarse_iter": "2", "Ma0": "0.45"}
         d = os.path.join(root, f"op{q}")
+        if variant == "stage":
+            case = mg.stage_passage(IM=49, JM1=49, KM1=129, JM2=49, KM2=65, options=opts)
+            mg.write_multiblock_case(case, d)
+            dirs.append(d)
+            continue
+        opts.update(VARIANTS[variant])
+        case = mg.rotor_passage(IM=49, JM=49, KM=129, options=opts)
         if blocks == 3:
             mg.write_multiblock_case(mg.split_axial(case, [41, 89]), d)
         elif blocks == 1:
@@ -425,13 +445,21 @@ def run_study(args):
 def config_block(args, cells, nsolve):
     if getattr(args, "sampled", False):
         wl, mesh = "sampled_rotor_passages_2level_multigrid", "97x41x41 / 129x49x49 / 161x65x65 (seeded sampler)"
+    elif getattr(args, "variant", "default") != "default":
+        wl = {"jst": "rotor_passage_129x49x49_jst_2level_multigrid", "sa": "rotor_passage_129x49x49_spalart_allmaras_single_grid",
+              "stage": "rotor_stator_stage_129x49x49_65x49x49_mixing_plane_2level"}[args.variant]
+        mesh = "129x49x49 rotor + 65x49x49 stator" if args.variant == "stage" else "129x49x49 (axial x pitch x span)"
     elif getattr(args, "blocks", 1) == 3:
         wl, mesh = "rotor_passage_129x49x49_3block_2level_multigrid", "129x49x49 as blocks of 41/49/41 axial nodes"
     else:
         wl, mesh = "rotor_passage_129x49x49_2level_multigrid", "129x49x49 (axial x pitch x span)"
     return {"workload": wl, "mesh_nodes": mesh,
             "cells_per_solve": cells, "solves_per_gpu": nsolve, "precision": args.precision,
-            "scheme": "Roe + MUSCL3 (primitive), Baldwin-Lomax, LU-SGS, 2-level FAS (reference maximum)",
+            "scheme": {"default": "Roe + MUSCL3 (primitive), Baldwin-Lomax, LU-SGS, 2-level FAS (reference maximum)",
+                       "jst": "JST (k2 0.5, k4 1/32), Baldwin-Lomax, LU-SGS, 2-level FAS",
+                       "sa": "Roe + MUSCL3 (primitive), Spalart-Allmaras, LU-SGS, single grid",
+                       "stage": "Roe + MUSCL3 (primitive), Baldwin-Lomax, LU-SGS, 2-level FAS, mixing plane"}[
+                           getattr(args, "variant", "default")],
             "l2": "inputs larger than L2 (FP64 working set well above 129 MB), no flush",
             "parallelism": "replicas"}
 
@@ -451,7 +479,7 @@ def run_gpu(args, rank, world, dist):
             dirs, cell_list = make_sampled_cases(tmp, args.batch, seed=2024 + rank)
             cells = sum(cell_list) / len(cell_list)     # mean per solve; totals below multiply by nsolve
         else:
-            dirs, cells = make_cases(tmp, args.batch, seed_offset=rank, blocks=args.blocks)
+            dirs, cells = make_cases(tmp, args.batch, seed_offset=rank, blocks=args.blocks, variant=args.variant)
         nsolve = len(dirs)
         grid_bytes = sum(os.path.getsize(os.path.join(d, "grid.dat")) for d in dirs)
 
@@ -503,7 +531,8 @@ def run_gpu(args, rank, world, dist):
         except FileNotFoundError:
             pass
         forms = None
-        if rank == 0 and world == 1 and not args.no_forms and prec == gbturbo.FP64 and nsolve == 1 and args.blocks == 1:
+        if (rank == 0 and world == 1 and not args.no_forms and prec == gbturbo.FP64 and nsolve == 1 and args.blocks == 1
+                and args.variant == "default"):
             n_ref = max(args.warmup, 3) + args.steps + nprof
             forms = measure_forms(gbturbo, dirs, cells, n_ref, s.integrals(1)[0], min(args.steps, 50), tmp)
         s.close()
@@ -524,7 +553,7 @@ def run_gpu(args, rank, world, dist):
         e2e_value = cells * nsolve * world * n_e2e / t_e2e
 
         base = None
-        if rank == 0 and not args.no_cpu_baseline and args.blocks == 1:
+        if rank == 0 and not args.no_cpu_baseline and args.blocks == 1 and args.variant == "default":
             # (the CPU oracle port is single-block)
             base = cpu_baseline(dirs[0], cells, warm=3, steps=2)
 
