@@ -5,6 +5,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <sstream>
+#include <charconv>
+#include <system_error>
 #include <algorithm>
 
 namespace gbt {
@@ -259,20 +261,80 @@ void read_bc(CaseSpec &c, std::vector<BlockRow> &blocks)
     }
 }
 
+// The grid file in memory, line by line, with the reference's line rule (ReadLine: '#' starts a
+// comment, surrounding blanks dropped, a trailing carriage return dropped). Text grids of large
+// cases hold millions of numbers, so the file is read with one fread and the numbers are parsed
+// in place (std::from_chars, correctly rounded like the stream the reference reads with).
+struct GridText {
+    std::string buf;
+    size_t pos = 0;
+    int lineno = 0;
+    std::string name;
+    GridText(const std::string &path, const std::string &nm) : name(nm)
+    {
+        std::FILE *f = std::fopen(path.c_str(), "rb");
+        if (!f) throw std::runtime_error("cannot open " + path);
+        std::fseek(f, 0, SEEK_END);
+        const long n = std::ftell(f);
+        std::fseek(f, 0, SEEK_SET);
+        buf.resize(n > 0 ? (size_t)n : 0);
+        const size_t got = n > 0 ? std::fread(&buf[0], 1, (size_t)n, f) : 0;
+        std::fclose(f);
+        if (got != buf.size()) throw std::runtime_error("cannot read " + path);
+    }
+    // [b, e) of the next line's content
+    void next(const char *&b, const char *&e)
+    {
+        if (pos >= buf.size()) throw std::runtime_error(name + ": file ended at line " + std::to_string(lineno + 1));
+        const char *s0 = buf.data() + pos, *end = buf.data() + buf.size();
+        const char *nl = (const char *)std::memchr(s0, '\n', (size_t)(end - s0));
+        const char *le = nl ? nl : end;
+        pos = (size_t)(le - buf.data()) + (nl ? 1 : 0);
+        lineno++;
+        if (le > s0 && le[-1] == '\r') le--;
+        const char *h = (const char *)std::memchr(s0, '#', (size_t)(le - s0));
+        if (h) le = h;
+        while (s0 < le && *s0 == ' ') s0++;
+        while (le > s0 && le[-1] == ' ') le--;
+        b = s0;
+        e = le;
+    }
+    std::string next_string()
+    {
+        const char *b, *e;
+        next(b, e);
+        return std::string(b, e);
+    }
+};
+
+// three numbers of a node line
+inline bool parse3(const char *b, const char *e, double &x, double &y, double &z)
+{
+    double *v[3] = {&x, &y, &z};
+    for (int q = 0; q < 3; q++) {
+        while (b < e && (*b == ' ' || *b == '\t')) b++;
+        if (b < e && *b == '+') b++;
+        auto r = std::from_chars(b, e, *v[q]);
+        if (r.ec != std::errc()) return false;
+        b = r.ptr;
+    }
+    return true;
+}
+
 // the grid file: block count, then per block its id line, "IM JM KM" and the nodes, i fastest
 // (source/UserInput.cpp:241-290)
 void read_grid(const CaseSpec &c, const std::vector<BlockRow> &rows, std::vector<CaseSpec> &out)
 {
     std::string path = c.dir + "/" + c.grid_file;
-    LineReader r(path, c.grid_file);
-    const int nb = as_int(r.next(), "block count");
+    GridText r(path, c.grid_file);
+    const int nb = as_int(r.next_string(), "block count");
     if (nb != (int)rows.size()) throw std::runtime_error("grid and boundary file disagree on the number of blocks");
     for (int b = 1; b <= nb; b++) {
-        if (as_int(r.next(), "block id") != b)
+        if (as_int(r.next_string(), "block id") != b)
             throw std::runtime_error(c.grid_file + ": blocks must be numbered 1, 2, ... in file order");
         int IM, JM, KM;
         {
-            std::istringstream is(r.next());
+            std::istringstream is(r.next_string());
             if (!(is >> IM >> JM >> KM)) throw std::runtime_error(c.grid_file + ": bad block size line");
         }
         const BlockRow &br = rows[b - 1];
@@ -290,12 +352,10 @@ void read_grid(const CaseSpec &c, const std::vector<BlockRow> &rows, std::vector
         size_t n = (size_t)IM * JM * KM;
         bs.x.resize(n); bs.y.resize(n); bs.z.resize(n);
         for (size_t q = 0; q < n; q++) {
-            std::string s = r.next();
-            const char *p = s.c_str();
-            char *e;
-            bs.x[q] = std::strtod(p, &e); if (e == p) throw std::runtime_error(c.grid_file + ": bad node line"); p = e;
-            bs.y[q] = std::strtod(p, &e); if (e == p) throw std::runtime_error(c.grid_file + ": bad node line"); p = e;
-            bs.z[q] = std::strtod(p, &e); if (e == p) throw std::runtime_error(c.grid_file + ": bad node line");
+            const char *lb, *le;
+            r.next(lb, le);
+            if (!parse3(lb, le, bs.x[q], bs.y[q], bs.z[q]))
+                throw std::runtime_error(c.grid_file + ": bad node line " + std::to_string(r.lineno));
         }
         out.push_back(std::move(bs));
     }

@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <atomic>
+#include <chrono>
 #include <exception>
 #include <thread>
 #include <map>
@@ -223,6 +224,21 @@ __global__ void k_iter_begin(Batch B)
     }
 }
 
+// set-up phase times on stderr when GBTURBO_TIMING is set (the stream is synchronised at each mark
+// then, so that device work is charged to its phase)
+struct PhaseTimer {
+    bool on = std::getenv("GBTURBO_TIMING") != nullptr;
+    std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+    void mark(const char *what, cudaStream_t st)
+    {
+        if (!on) return;
+        if (st) cudaStreamSynchronize(st);
+        const auto n = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "[gbturbo set-up] %-28s %8.1f ms\n", what, std::chrono::duration<double, std::milli>(n - t).count());
+        t = n;
+    }
+};
+
 template <typename T>
 class SolverT : public SolverBase {
 public:
@@ -320,6 +336,7 @@ public:
         return c;
     }
 
+    PhaseTimer timer;
     explicit SolverT(const std::vector<std::string> &dirs, int prec)
     {
         precision = prec;
@@ -349,6 +366,7 @@ public:
             }
         }
         nsolve = (int)cases.size();
+        timer.mark("read case files", nullptr);
         const CaseSpec &c0 = cases[0];
         for (auto &c : cases) {
             if (c.ng != c0.ng || c.coarse_iter != c0.coarse_iter || c.scheme != c0.scheme || c.recon != c0.recon ||
@@ -407,6 +425,7 @@ public:
         bad_list = (int *)q; q += sizeof(int) * (size_t)nsolve * bad_cap;
         bad_count = (int *)q; q += sizeof(int) * nsolve;
         dtmin = (T *)(((uintptr_t)q + 15) & ~(uintptr_t)15);
+        timer.mark("solve state and scratch", stream);
         for (int l = 1; l <= ng; l++) build_level(l);
     }
 
@@ -446,6 +465,7 @@ public:
         }
         Lv.pool_n = base;
         const size_t N = (size_t)base;
+        timer.mark("level boxes", nullptr);
         // device descriptors
         CK(cudaMalloc(&Lv.meta_mem.p, sizeof(Lvl) * nsolve + sizeof(SolveConst) * nsolve + 16));
         Lv.lv_d = (Lvl *)Lv.meta_mem.p;
@@ -537,13 +557,17 @@ public:
             CK(cudaMemcpy(G.z, hz.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
             build_tables(l, lc, hx, hy);
         }
+        timer.mark("pools, nodes, patch tables", stream);
         build_planes(l);
+        timer.mark("hyperplane tables", stream);
         launch_geometry(ctx(l), G, Lv.blockvol);
         k_case_volume<<<(nsolve + 127) / 128, 128, 0, stream>>>(batch(l), Lv.blockvol, Lv.totalvol);
         if (Lv.W.ev) build_sa_wall_distance(l);
+        timer.mark("geometry", stream);
         build_geometry_working(l);
         build_wall_distances(l);
         launch_sweep_geometry<T>(ctx(l), G, Lv.planes, Lv.sweep);
+        timer.mark("working geometry, wall lines", stream);
         {
             // block shape of the sweep kernels: GBTURBO_SWEEP_SHAPE="cpw,wpb" pins it; batches of
             // four or more solves time the candidates; smaller ones, where the candidates are within
@@ -563,6 +587,7 @@ public:
             Lv.planes.wpb = wpb;
         }
         CK(cudaStreamSynchronize(stream));
+        timer.mark("sweep shape", stream);
         CK(cudaGetLastError());
     }
 
