@@ -34,6 +34,31 @@ extern "C" {
 
 const char *gb_last_error(void) { return g_err.c_str(); }
 
+int gb_case_info(const char *case_dir, long long info[9], double *nodes_out, long long cap)
+{
+    if (!case_dir || !info) { g_err = "bad arguments"; return GB_ERR_ARG; }
+    return guard([&] {
+        std::vector<gbt::CaseSpec> b = gbt::read_case(case_dir);
+        const gbt::CaseSpec &c = b[0];
+        long long nodes = 0, nin = 0, nout = 0, nwall = 0;
+        for (auto &s : b) {
+            nodes += (long long)s.IM * s.JM * s.KM;
+            nin += (long long)s.inlets.size(); nout += (long long)s.outlets.size(); nwall += (long long)s.walls.size();
+        }
+        const long long v[9] = {(long long)b.size(), c.ng, nin, nout, nwall, (long long)c.periodics.size(),
+                                (long long)c.interiors.size(), (long long)c.mixing.size(), nodes};
+        for (int q = 0; q < 9; q++) info[q] = v[q];
+        if (nodes_out) {
+            if (cap < 3 * nodes) throw std::invalid_argument("node buffer too short");
+            long long o = 0;
+            for (auto &s : b)
+                for (size_t q = 0; q < s.x.size(); q++) {
+                    nodes_out[o++] = s.x[q]; nodes_out[o++] = s.y[q]; nodes_out[o++] = s.z[q];
+                }
+        }
+    });
+}
+
 int gb_solver_create(const char *const *case_dirs, int n_solves, int precision, gb_solver **out)
 {
     if (!case_dirs || n_solves < 1 || !out) { g_err = "bad arguments"; return GB_ERR_ARG; }

@@ -38,6 +38,7 @@ def load() -> ctypes.CDLL:
         "gb_dims": ([vp, ip, ip, ctypes.POINTER(ip)], ip),
         "gb_num_blocks": ([vp, ctypes.POINTER(ip), ctypes.POINTER(ip)], ip),
         "gb_case_blocks": ([vp, ip, ctypes.POINTER(ip)], ip),
+        "gb_case_info": ([ctypes.c_char_p, ctypes.POINTER(ctypes.c_longlong), dp, ctypes.c_longlong], ip),
         "gb_init_uniform": ([vp], ip),
         "gb_resflux": ([vp, ip], ip),
         "gb_time_marching": ([vp, ip], ip),
@@ -84,11 +85,32 @@ EXPORTED = ["gb_solver_create", "gb_solver_destroy", "gb_last_error", "gb_dims",
             "gb_sync", "gb_set_graphs", "gb_timer_start", "gb_timer_stop", "gb_profile_begin", "gb_profile_end",
             "gb_res_calculate_noalloc", "gb_sweep_tuning", "gb_read_restart", "gb_write_restart",
             "gb_write_solution", "gb_mass_flow_imposed", "gb_get_outlet_pressure", "gb_num_blocks",
-            "gb_case_blocks"]
+            "gb_case_blocks", "gb_case_info"]
 
 
 class GBError(RuntimeError):
     pass
+
+
+CASE_INFO_KEYS = ["blocks", "levels", "inlets", "outlets", "walls", "periodic_pairs", "interfaces", "mixing_planes", "nodes"]
+
+
+def case_info(case_dir: str, nodes: bool = False):
+    """Reads a case directory on the host only (the solver's reader and checks, no GPU): a dict of
+    CASE_INFO_KEYS, and with nodes=True also the (n, 3) node coordinates, block after block."""
+    L = load()
+    info = (ctypes.c_longlong * 9)()
+    rc = L.gb_case_info(os.path.abspath(case_dir).encode(), info, None, 0)
+    if rc != 0:
+        raise GBError(L.gb_last_error().decode())
+    d = dict(zip(CASE_INFO_KEYS, [int(v) for v in info]))
+    if not nodes:
+        return d
+    xyz = np.zeros(3 * d["nodes"])
+    rc = L.gb_case_info(os.path.abspath(case_dir).encode(), info, _dp(xyz), xyz.size)
+    if rc != 0:
+        raise GBError(L.gb_last_error().decode())
+    return d, xyz.reshape(-1, 3)
 
 
 def _dp(a: np.ndarray):

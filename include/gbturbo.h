@@ -144,6 +144,14 @@ int gb_timer_stop(gb_solver *h, float *ms);
 #define GB_NOALLOC_MAX_SOLVES 128
 int gb_res_calculate_noalloc(gb_solver *h, int level, double *out);
 
+/* Reads one case directory on the host only (no device, no handle): the reader of
+ * gb_solver_create with its checks. info[0..8] = blocks, grid levels, inlets, outlets, walls,
+ * periodic pairs, block interfaces, mixing planes, nodes of all blocks; nodes_out (may be NULL)
+ * receives x, y, z of every node, block after block, i fastest (3 * info[8] doubles, cap the
+ * buffer's length). It has no counterpart in the reference; it lets a caller (and the CPU tests)
+ * check a case without a GPU. */
+int gb_case_info(const char *case_dir, long long info[9], double *nodes_out, long long cap);
+
 #ifdef __cplusplus
 }
 #endif
