@@ -24,8 +24,8 @@ __device__ __forceinline__ void release_next_plane() { asm volatile("griddepcont
 // in the reference's order (-R + A_I + A_J + A_K + V_I + V_J + V_K). A plane's cells and their
 // neighbours are read from the plane-order copy (SweepData), so a warp's loads are dense. The
 // neighbour's old flux F_n(Q) and the diagonal 1/alpha do not depend on dQ and are formed before
-// the wait, so only the new flux F_n(Q + dQ) and the combination sit on the plane-to-plane
-// critical path.
+// the wait (in the mixed form the gather forms them for all cells at once), so only the new flux
+// F_n(Q + dQ) and the combination sit on the plane-to-plane critical path.
 template <typename T, int DIR, int CPW, int WPB>   // DIR = +1 forward, -1 backward; CPW cells per warp, WPB warps per block
 __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, const int *__restrict__ pstart,
                                                     int pstride, int plane)
@@ -47,23 +47,37 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
             nx = S.gn[d][0][nb]; ny = S.gn[d][1][nb]; nz = S.gn[d][2][nb];
             ve = S.gve[d][nb];
             od = S.cv[0][nb]; omx = S.cv[1][nb]; omy = S.cv[2][nb]; omz = S.cv[3][nb]; oe = S.cv[4][nb];
-            const T po = S.pp[nb];
-            const T oinv = (T)1 / od;
-            const T Vo = omx * oinv * nx + omy * oinv * ny + omz * oinv * nz;
-            const T dov = Vo - ve;
-            fo[0] = od * dov;
-            fo[1] = omx * dov + po * nx;
-            fo[2] = omy * dov + po * ny;
-            fo[3] = omz * dov + po * nz;
-            fo[4] = (oe + po) * dov + po * ve;
+            if constexpr (sizeof(T) == 8) {
+                // FP64 (parity) form: formed here, in the reference's sequence, as every other
+                // evaluation of the path is; the 2000-iteration efficiency is sensitive to how the
+                // compiler contracts these products, so the expressions stay where they were pinned
+                const T po = S.pp[nb];
+                const T oinv = (T)1 / od;
+                const T Vo = omx * oinv * nx + omy * oinv * ny + omz * oinv * nz;
+                const T dov = Vo - ve;
+                fo[0] = od * dov;
+                fo[1] = omx * dov + po * nx;
+                fo[2] = omy * dov + po * ny;
+                fo[3] = omz * dov + po * nz;
+                fo[4] = (oe + po) * dov + po * ve;
+            } else {
+#pragma unroll
+                for (int c = 0; c < 5; c++) fo[c] = S.fo[d][c][nb];
+            }
             sd = S.gs[d][nb];
-            rl = P.relax * S.lamc[d][nb];
+            if constexpr (sizeof(T) == 8) rl = P.relax * S.lamc[d][nb];
+            else rl = S.lamc[d][nb];                   // relax * lambda_c, formed by the gather
             lv = S.lamv[d][nb];
         }
         if (d == 0) {
-            alpha = S.gvol[q] / S.dt[q] + P.relax * (S.lamc[0][q] + S.lamc[1][q] + S.lamc[2][q]) +
-                    (T)2 * (S.lamv[0][q] + S.lamv[1][q] + S.lamv[2][q]);
-            inva = (T)1 / alpha;
+            if constexpr (sizeof(T) == 8) {
+                alpha = S.gvol[q] / S.dt[q] + P.relax * (S.lamc[0][q] + S.lamc[1][q] + S.lamc[2][q]) +
+                        (T)2 * (S.lamv[0][q] + S.lamv[1][q] + S.lamv[2][q]);
+                inva = (T)1 / alpha;
+            } else {
+                inva = S.ainv[q];
+                alpha = S.alpha[q];
+            }
             if (DIR > 0) {
 #pragma unroll
                 for (int c = 0; c < 5; c++) rhs[c] = -S.res[c][q];
@@ -132,18 +146,46 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
 }
 
 // flow inputs of the sweeps into plane order (before every forward sweep)
+// and, in the mixed form, the parts of the sweeps that do not depend on dQ, for all cells at once:
+// every cell's old flux F_n(Q) as the neighbour in each direction (across its mean normal, in the
+// rotating frame), its diagonal alpha = Vol/dt + relax sum lambda_c + 2 sum lambda_v and 1/alpha,
+// relax * lambda_c (the FP64 form forms them in the sweep kernel, where its parity was pinned)
 template <typename T>
-__global__ void __launch_bounds__(256) k_sweep_gather(Flow<T> W, SweepData<T> S, long long nq)
+__global__ void __launch_bounds__(256) k_sweep_gather(PhysW<T> P, Flow<T> W, SweepData<T> S, long long nq)
 {
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nq) return;
     const long long p = S.cell[q];
+    T cv[5], lc[3], lv[3];
 #pragma unroll
-    for (int c = 0; c < 5; c++) { S.cv[c][q] = (T)W.cv[c][p]; S.res[c][q] = W.res[c][p]; }
+    for (int c = 0; c < 5; c++) { cv[c] = (T)W.cv[c][p]; S.cv[c][q] = cv[c]; S.res[c][q] = W.res[c][p]; }
 #pragma unroll
-    for (int d = 0; d < 3; d++) { S.lamc[d][q] = W.lamc[d][p]; S.lamv[d][q] = W.lamv[d][p]; }
-    S.pp[q] = W.pv[PP][p];
-    S.dt[q] = W.dt[p];
+    for (int d = 0; d < 3; d++) {
+        lc[d] = W.lamc[d][p]; lv[d] = W.lamv[d][p];
+        // the FP64 form keeps lambda_c and forms relax * lambda_c and the diagonal in the sweep
+        S.lamc[d][q] = sizeof(T) == 8 ? lc[d] : P.relax * lc[d];
+        S.lamv[d][q] = lv[d];
+    }
+    const T po = W.pv[PP][p], dt = W.dt[p];
+    S.pp[q] = po;
+    S.dt[q] = dt;
+    if constexpr (sizeof(T) == 8) return;
+    const T alpha = S.gvol[q] / dt + P.relax * (lc[0] + lc[1] + lc[2]) + (T)2 * (lv[0] + lv[1] + lv[2]);
+    S.alpha[q] = alpha;
+    S.ainv[q] = (T)1 / alpha;
+    const T od = cv[0], omx = cv[1], omy = cv[2], omz = cv[3], oe = cv[4];
+    const T oinv = (T)1 / od;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const T nx = S.gn[d][0][q], ny = S.gn[d][1][q], nz = S.gn[d][2][q], ve = S.gve[d][q];
+        const T Vo = omx * oinv * nx + omy * oinv * ny + omz * oinv * nz;
+        const T dov = Vo - ve;
+        S.fo[d][0][q] = od * dov;
+        S.fo[d][1][q] = omx * dov + po * nx;
+        S.fo[d][2][q] = omy * dov + po * ny;
+        S.fo[d][3][q] = omz * dov + po * nz;
+        S.fo[d][4][q] = (oe + po) * dov + po * ve;
+    }
 }
 
 // dQ back into the box (after the backward sweep)
@@ -229,6 +271,11 @@ __global__ void __launch_bounds__(256) k_sweep_fill(SweepData<T> S, long long nq
     for (int d = 0; d < 3; d++) { S.lamc[d][q] = (T)1; S.lamv[d][q] = (T)0.1; }
     S.dt[q] = (T)1;
     for (int c = 0; c < NQ; c++) { S.res[c][q] = (T)1e-3; S.dq[c][q] = (T)0; }
+    if (S.alpha) {
+        for (int d = 0; d < 3; d++)
+            for (int c = 0; c < NQ; c++) S.fo[d][c][q] = (T)0;
+        S.alpha[q] = (T)2; S.ainv[q] = (T)0.5;
+    }
 }
 
 // Autotuner of the sweep's block shape (cells per warp, warps per block): times the forward and
@@ -275,7 +322,7 @@ void launch_lusgs_sweeps(const LaunchCtx &ctx, const PhysW<T> &P, const Geo &G, 
     const int np = pt.max_plane;
     const unsigned gq = (unsigned)((pt.nq + 255) / 256);
     ctx.mark("sweep_forward", 1, np - 1);
-    k_sweep_gather<T><<<gq, 256, 0, ctx.stream>>>(W, S, pt.nq);
+    k_sweep_gather<T><<<gq, 256, 0, ctx.stream>>>(P, W, S, pt.nq);
     for (int pl = 3; pl <= np; pl++) launch_plane<T, 1>(ctx, P, pt, S, pl, pl == 3);
     ctx.mark("sweep_forward", 0, np - 1);
     if (W.ev) {
