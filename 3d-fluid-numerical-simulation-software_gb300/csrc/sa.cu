@@ -72,7 +72,9 @@ __global__ void __launch_bounds__(256) k_sa_wall_dist(Batch B, Geo G, const doub
     const int c = B.sc[s].cix;
     const long long a = case_off[c], b = case_off[c + 1];
     __shared__ double sx[256], sy[256], sz[256];
-    double dmin = 10000.0;
+    // the nearest point by squared distance, one root at the end: the root is monotone and
+    // correctly rounded, so this is the reference's minimum of the roots
+    double d2min = 1.0e8;                      // (the reference's initial 10000)^2
     for (long long t0 = a; t0 < b; t0 += 256) {
         const long long t = t0 + threadIdx.x;
         __syncthreads();
@@ -82,11 +84,11 @@ __global__ void __launch_bounds__(256) k_sa_wall_dist(Batch B, Geo G, const doub
         if (in)
             for (int q = 0; q < m; q++) {
                 const double dx = cx - sx[q], dy = cy - sy[q], dz = cz - sz[q];
-                const double d = sqrt(dx * dx + dy * dy + dz * dz);
-                if (dmin >= d) dmin = d;
+                const double d2 = dx * dx + dy * dy + dz * dz;
+                if (d2min >= d2) d2min = d2;
             }
     }
-    if (in) dwall[p] = dmin;
+    if (in) dwall[p] = sqrt(d2min);
 }
 
 void launch_sa_wall_distance(const LaunchCtx &ctx, const Geo &G, const long long *face_p, const int *face_f, long long n,
