@@ -59,7 +59,7 @@ int gb_case_info(const char *case_dir, long long info[9], double *nodes_out, lon
     });
 }
 
-int gb_solver_create(const char *const *case_dirs, int n_solves, int precision, gb_solver **out)
+int gb_solver_create_levels(const char *const *case_dirs, int n_solves, int precision, int max_levels, gb_solver **out)
 {
     if (!case_dirs || n_solves < 1 || !out) { g_err = "bad arguments"; return GB_ERR_ARG; }
     *out = nullptr;
@@ -68,13 +68,18 @@ int gb_solver_create(const char *const *case_dirs, int n_solves, int precision, 
         for (int i = 0; i < n_solves; i++) d.push_back(case_dirs[i] ? case_dirs[i] : "");
         auto h = new gb_solver;
         try {
-            h->s = gbt::make_solver(d, precision);
+            h->s = gbt::make_solver(d, precision, max_levels);
         } catch (...) {
             delete h;
             throw;
         }
         *out = h;
     });
+}
+
+int gb_solver_create(const char *const *case_dirs, int n_solves, int precision, gb_solver **out)
+{
+    return gb_solver_create_levels(case_dirs, n_solves, precision, 2, out);
 }
 
 int gb_solver_destroy(gb_solver *h)

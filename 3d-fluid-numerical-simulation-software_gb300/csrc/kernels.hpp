@@ -162,6 +162,10 @@ void launch_forcing(const LaunchCtx &cc, Flow<T> Fc);
 template <typename T>
 void launch_delta(const LaunchCtx &cc, Flow<T> Fc);
 template <typename T>
+void launch_forcing_keep(const LaunchCtx &cc, Flow<T> Fc);
+template <typename T>
+void launch_add_forcing(const LaunchCtx &cc, Flow<T> Fc);
+template <typename T>
 void launch_corner(const LaunchCtx &cc, Flow<T> Fc);
 template <typename T>
 void launch_interpolate(const LaunchCtx &cf, const LaunchCtx &cc, Flow<T> Ff, Flow<T> Fc, int init_from_coarse);

@@ -49,6 +49,34 @@ __global__ void __launch_bounds__(256) k_forcing(Batch B, Flow<T> W)
     }
 }
 
+// three-level V-cycle extension (proper FAS on the coarse levels): the forcing Qf = R_2h - R_c at
+// the restricted state replaces the residual by the restricted one and is kept (in res2h) for the
+// level's own FAS residual R_c(Q') + Qf after its smoothing, which is restricted further
+template <typename T>
+__global__ void __launch_bounds__(256) k_forcing_keep(Batch B, Flow<T> W)
+{
+    const Lvl L = B.lv[blockIdx.y];
+    int i, j, k;
+    if (!box_index(L.IM - 1, L.JM - 1, L.KM - 1, i, j, k)) return;
+    const long long p = ix(L, i, j, k);
+#pragma unroll
+    for (int c = 0; c < NQ; c++) {
+        const T qf = W.res2h[c][p] - W.res[c][p];
+        W.res[c][p] = W.res[c][p] + qf;
+        W.res2h[c][p] = qf;
+    }
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_add_forcing(Batch B, Flow<T> W)
+{
+    const Lvl L = B.lv[blockIdx.y];
+    int i, j, k;
+    if (!box_index(L.IM - 1, L.JM - 1, L.KM - 1, i, j, k)) return;
+    const long long p = ix(L, i, j, k);
+#pragma unroll
+    for (int c = 0; c < NQ; c++) W.res[c][p] = W.res[c][p] + W.res2h[c][p];
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_delta(Batch B, Flow<T> W)
 {
@@ -169,6 +197,16 @@ void launch_forcing(const LaunchCtx &cc, Flow<T> Fc)
     k_forcing<T><<<cc.grid_cells(256), 256, 0, cc.stream>>>(cc.batch, Fc);
 }
 template <typename T>
+void launch_forcing_keep(const LaunchCtx &cc, Flow<T> Fc)
+{
+    k_forcing_keep<T><<<cc.grid_cells(256), 256, 0, cc.stream>>>(cc.batch, Fc);
+}
+template <typename T>
+void launch_add_forcing(const LaunchCtx &cc, Flow<T> Fc)
+{
+    k_add_forcing<T><<<cc.grid_cells(256), 256, 0, cc.stream>>>(cc.batch, Fc);
+}
+template <typename T>
 void launch_delta(const LaunchCtx &cc, Flow<T> Fc)
 {
     k_delta<T><<<cc.grid_cells(256), 256, 0, cc.stream>>>(cc.batch, Fc);
@@ -189,6 +227,8 @@ void launch_interpolate(const LaunchCtx &cf, const LaunchCtx &cc, Flow<T> Ff, Fl
 #define GBT_INST(T)                                                                                                       \
     template void launch_restrict<T>(const LaunchCtx &, const LaunchCtx &, const Geo &, const Geo &, Flow<T>, Flow<T>); \
     template void launch_forcing<T>(const LaunchCtx &, Flow<T>);                                                         \
+    template void launch_forcing_keep<T>(const LaunchCtx &, Flow<T>);                                                    \
+    template void launch_add_forcing<T>(const LaunchCtx &, Flow<T>);                                                     \
     template void launch_delta<T>(const LaunchCtx &, Flow<T>);                                                           \
     template void launch_corner<T>(const LaunchCtx &, Flow<T>);                                                          \
     template void launch_interpolate<T>(const LaunchCtx &, const LaunchCtx &, Flow<T>, Flow<T>, int);

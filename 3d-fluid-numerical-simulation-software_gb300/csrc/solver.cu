@@ -94,28 +94,23 @@ struct LevelCase {
     std::vector<double> x, y, z;          // nodes, ((k-1)*JM + (j-1))*IM + (i-1)
 };
 
-// a periodic pair or block interface on a level
+// a periodic pair or block interface on a level (each coarser level re-indexes the previous one's)
 static PeriodicIO level_pair(PeriodicIO p, int level)
 {
-    if (level > 1)
+    for (int l = 2; l <= level; l++)
         for (int d = 0; d < 3; d++) { coarse_patch(p.r1[2 * d], p.r1[2 * d + 1]); coarse_patch(p.r2[2 * d], p.r2[2 * d + 1]); }
     return p;
 }
 static PatchIO level_patch(PatchIO p, int level)
 {
-    if (level > 1) { coarse_patch(p.is, p.ie); coarse_patch(p.js, p.je); coarse_patch(p.ks, p.ke); }
+    for (int l = 2; l <= level; l++) { coarse_patch(p.is, p.ie); coarse_patch(p.js, p.je); coarse_patch(p.ks, p.ke); }
     return p;
 }
 
-static LevelCase level_case(const CaseSpec &c, int level)
+// every second node and the re-indexed patches of a level
+static LevelCase coarsen(const LevelCase &c)
 {
     LevelCase L;
-    if (level == 1) {
-        L.IM = c.IM; L.JM = c.JM; L.KM = c.KM;
-        L.in = c.inlets; L.out = c.outlets; L.walls = c.walls;
-        L.x = c.x; L.y = c.y; L.z = c.z;
-        return L;
-    }
     L.IM = (c.IM + 1) / 2; L.JM = (c.JM + 1) / 2; L.KM = (c.KM + 1) / 2;
     size_t n = (size_t)L.IM * L.JM * L.KM;
     L.x.resize(n); L.y.resize(n); L.z.resize(n);
@@ -126,10 +121,43 @@ static LevelCase level_case(const CaseSpec &c, int level)
                 size_t f = ((size_t)(2 * k - 2) * c.JM + (2 * j - 2)) * c.IM + (2 * i - 2);
                 L.x[q] = c.x[f]; L.y[q] = c.y[f]; L.z[q] = c.z[f];
             }
-    for (auto p : c.inlets) { coarse_patch(p.is, p.ie); coarse_patch(p.js, p.je); coarse_patch(p.ks, p.ke); L.in.push_back(p); }
-    for (auto p : c.outlets) { coarse_patch(p.is, p.ie); coarse_patch(p.js, p.je); coarse_patch(p.ks, p.ke); L.out.push_back(p); }
+    for (auto p : c.in) { coarse_patch(p.is, p.ie); coarse_patch(p.js, p.je); coarse_patch(p.ks, p.ke); L.in.push_back(p); }
+    for (auto p : c.out) { coarse_patch(p.is, p.ie); coarse_patch(p.js, p.je); coarse_patch(p.ks, p.ke); L.out.push_back(p); }
     for (auto w : c.walls) { coarse_patch(w.is, w.ie); coarse_patch(w.js, w.je); coarse_patch(w.ks, w.ke); L.walls.push_back(w); }
     return L;
+}
+
+static LevelCase level_case(const CaseSpec &c, int level)
+{
+    if (level > 1) return coarsen(level_case(c, level - 1));
+    LevelCase L;
+    L.IM = c.IM; L.JM = c.JM; L.KM = c.KM;
+    L.in = c.inlets; L.out = c.outlets; L.walls = c.walls;
+    L.x = c.x; L.y = c.y; L.z = c.z;
+    return L;
+}
+
+// whether a block and all its patches coarsen a second time: node counts with (N-1) a multiple of
+// 4 and (N-1)/4 > 2, and every patch range odd-aligned on the second level as well (the
+// reference's own check allows at most two levels: source/UserInput.cpp:799-1068)
+static bool coarsens_twice(const CaseSpec &c)
+{
+    auto dim_ok = [](int N) { return (N - 1) % 4 == 0 && (N - 1) / 4 > 2; };
+    if (!dim_ok(c.IM) || !dim_ok(c.JM) || !dim_ok(c.KM)) return false;
+    auto rng_ok = [](int s, int e) {
+        if (s != e) e = e + 1;
+        return (s - 1) % 4 == 0 && (e - 1) % 4 == 0;
+    };
+    auto patch_ok = [&](int is, int ie, int js, int je, int ks, int ke) { return rng_ok(is, ie) && rng_ok(js, je) && rng_ok(ks, ke); };
+    for (auto &p : c.inlets) if (!patch_ok(p.is, p.ie, p.js, p.je, p.ks, p.ke)) return false;
+    for (auto &p : c.outlets) if (!patch_ok(p.is, p.ie, p.js, p.je, p.ks, p.ke)) return false;
+    for (auto &w : c.walls) if (!patch_ok(w.is, w.ie, w.js, w.je, w.ks, w.ke)) return false;
+    for (const auto *lst : {&c.periodics, &c.interiors, &c.mixing})
+        for (auto &p : *lst)
+            if (!patch_ok(p.r1[0], p.r1[1], p.r1[2], p.r1[3], p.r1[4], p.r1[5]) ||
+                !patch_ok(p.r2[0], p.r2[1], p.r2[2], p.r2[3], p.r2[4], p.r2[5]))
+                return false;
+    return true;
 }
 
 // Face-local traversal of a periodic patch in the order of the reference's shadow buffers
@@ -242,7 +270,7 @@ struct PhaseTimer {
 template <typename T>
 class SolverT : public SolverBase {
 public:
-    Level<T> lev[3];
+    Level<T> lev[4];                      // levels 1..ng (ng <= 3)
     DevBuf st_mem, scratch_mem;
     PhysW<T> PC{};                        // physical constants in the working precision
     NonDim nd_ref{};                      // reference scales of the batch (shared gas and inlet options)
@@ -337,7 +365,7 @@ public:
     }
 
     PhaseTimer timer;
-    explicit SolverT(const std::vector<std::string> &dirs, int prec)
+    explicit SolverT(const std::vector<std::string> &dirs, int prec, int max_levels)
     {
         precision = prec;
         ncase = (int)dirs.size();
@@ -380,6 +408,17 @@ public:
                 throw std::runtime_error("the cases of one batch must share numerics, gas and inlet options (only grid, back pressure, speed and blade count may differ)");
         }
         ng = c0.ng;
+        if (max_levels == 3 && ng == 2) {
+            // the three-level V-cycle extension (the reference stops at two levels)
+            for (auto &c : cases)
+                if (!coarsens_twice(c))
+                    throw std::runtime_error("three grid levels need node counts N with (N-1) a multiple of 4 and "
+                                             "(N-1)/4 > 2 and patch ranges that stay odd-aligned on the second level");
+            ng = 3;
+        } else if (max_levels != 2) {
+            if (max_levels != 3) throw std::runtime_error("grid levels must be 2 (the reference's maximum) or 3");
+            throw std::runtime_error("three grid levels need a multigrid case (config \"use multigrid\" Y)");
+        }
         coarse_iter = c0.coarse_iter;
         reuse = c0.restart;
         for (auto &c : cases) any_mass = any_mass || c.mass_imposed;
@@ -1032,8 +1071,34 @@ public:
         Level<T> &Lv = lev[l];
         if (!Lv.use_force) resflux(l);
         else { Mark m(this, "mg_forcing"); launch_forcing<T>(cx, Lv.W); }
+        sweep_update(l);
+    }
+    void sweep_update(int l)
+    {
+        LaunchCtx cx = ctx(l);
+        Level<T> &Lv = lev[l];
         launch_lusgs_sweeps<T>(cx, PC, Lv.G, Lv.W, Lv.planes, Lv.sweep);
         launch_update<T>(cx, P, Lv.G, Lv.W, l, bad_list, bad_cap, bad_count);
+    }
+    // transfers between level lf and the next coarser one
+    void restrict_lv(int lf)
+    {
+        Mark m(this, "mg_restrict");
+        launch_restrict<T>(ctx(lf), ctx(lf + 1), lev[lf].G, lev[lf + 1].G, lev[lf].W, lev[lf + 1].W);
+    }
+    void interpolate_lv(int lf, int init)
+    {
+        Mark m(this, "mg_prolong");
+        launch_interpolate<T>(ctx(lf), ctx(lf + 1), lev[lf].W, lev[lf + 1].W, init);
+    }
+    void delta_lv(int lc) { Mark m(this, "mg_delta"); launch_delta<T>(ctx(lc), lev[lc].W); }
+    // FAS smoothing of coarse level l (three-level extension): residual at the restricted state,
+    // forcing kept, sweeps and update
+    void smooth_fas(int l)
+    {
+        resflux(l);
+        { Mark m(this, "mg_forcing"); launch_forcing_keep<T>(ctx(l), lev[l].W); }
+        sweep_update(l);
     }
     void res_calculate(int l) override { launch_res_norm<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, norm_part, norm_blk); }
     void sweep_shape(int l, int out[2]) const override { out[0] = lev[l].planes.cpw; out[1] = lev[l].planes.wpb; }
@@ -1081,7 +1146,7 @@ public:
         else if (!reuse && iter == coarse_iter) {
             time_marching(2); res_calculate(2); corner_treatment(2);
             interpolate(1); primitive_vars(1); limit_vars(1);
-        } else {
+        } else if (ng == 2) {
             lev[2].use_force = true;
             time_marching(1); res_calculate(1);
             resflux(1);
@@ -1091,6 +1156,27 @@ public:
             delta_cons();
             corner_treatment(2);
             interpolate(0);
+            primitive_vars(1); limit_vars(1);
+        } else {
+            // three-level V-cycle (extension): the fine step as in the two-level cycle, then FAS
+            // on levels 2 and 3 with the coarse residuals evaluated at the restricted states
+            time_marching(1); res_calculate(1);
+            resflux(1);
+            restrict_lv(1);
+            primitive_vars(2); limit_vars(2);
+            smooth_fas(2);
+            resflux(2);
+            { Mark m(this, "mg_forcing"); launch_add_forcing<T>(ctx(2), lev[2].W); }
+            restrict_lv(2);
+            primitive_vars(3); limit_vars(3);
+            smooth_fas(3);
+            delta_lv(3);
+            corner_treatment(3);
+            interpolate_lv(2, 0);
+            primitive_vars(2); limit_vars(2);
+            delta_lv(2);
+            corner_treatment(2);
+            interpolate_lv(1, 0);
             primitive_vars(1); limit_vars(1);
         }
     }
@@ -1428,10 +1514,10 @@ public:
     }
 };
 
-std::unique_ptr<SolverBase> make_solver(const std::vector<std::string> &dirs, int precision)
+std::unique_ptr<SolverBase> make_solver(const std::vector<std::string> &dirs, int precision, int max_levels)
 {
-    if (precision == 0) return std::unique_ptr<SolverBase>(new SolverT<double>(dirs, 0));
-    if (precision == 1) return std::unique_ptr<SolverBase>(new SolverT<float>(dirs, 1));
+    if (precision == 0) return std::unique_ptr<SolverBase>(new SolverT<double>(dirs, 0, max_levels));
+    if (precision == 1) return std::unique_ptr<SolverBase>(new SolverT<float>(dirs, 1, max_levels));
     throw std::runtime_error("precision must be 0 (FP64) or 1 (mixed FP32/FP64)");
 }
 

@@ -74,7 +74,9 @@ public:
     virtual std::string profile_end() = 0;
 };
 
-std::unique_ptr<SolverBase> make_solver(const std::vector<std::string> &dirs, int precision);
+// max_levels: 2 follows the reference (at most two grid levels); 3 enables the three-level
+// V-cycle extension for multigrid cases whose grids coarsen twice
+std::unique_ptr<SolverBase> make_solver(const std::vector<std::string> &dirs, int precision, int max_levels = 2);
 
 // nondimensional constants exactly as the reference derives them (source/UserInput.cpp:1070-1092)
 struct NonDim {

@@ -33,6 +33,7 @@ def load() -> ctypes.CDLL:
     vp, ip, dp = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)
     sig = {
         "gb_solver_create": ([ctypes.POINTER(ctypes.c_char_p), ip, ip, ctypes.POINTER(vp)], ip),
+        "gb_solver_create_levels": ([ctypes.POINTER(ctypes.c_char_p), ip, ip, ip, ctypes.POINTER(vp)], ip),
         "gb_solver_destroy": ([vp], ip),
         "gb_last_error": ([], ctypes.c_char_p),
         "gb_dims": ([vp, ip, ip, ctypes.POINTER(ip)], ip),
@@ -85,7 +86,7 @@ EXPORTED = ["gb_solver_create", "gb_solver_destroy", "gb_last_error", "gb_dims",
             "gb_sync", "gb_set_graphs", "gb_timer_start", "gb_timer_stop", "gb_profile_begin", "gb_profile_end",
             "gb_res_calculate_noalloc", "gb_sweep_tuning", "gb_read_restart", "gb_write_restart",
             "gb_write_solution", "gb_mass_flow_imposed", "gb_get_outlet_pressure", "gb_num_blocks",
-            "gb_case_blocks", "gb_case_info"]
+            "gb_case_blocks", "gb_case_info", "gb_solver_create_levels"]
 
 
 class GBError(RuntimeError):
@@ -146,14 +147,17 @@ class Solver:
     (norms, integrals, history, status) have one entry per case directory; box access (dims, get,
     set_cv) takes a slot: the blocks of case 0 come first, then those of case 1, ... (slots())."""
 
-    def __init__(self, case_dirs: Union[str, Sequence[str]], precision: int = FP64):
+    def __init__(self, case_dirs: Union[str, Sequence[str]], precision: int = FP64, levels: int = 2):
         self._L = load()
         if isinstance(case_dirs, str):
             case_dirs = [case_dirs]
         self.case_dirs = [os.path.abspath(d) for d in case_dirs]
         arr = (ctypes.c_char_p * len(self.case_dirs))(*[d.encode() for d in self.case_dirs])
         h = ctypes.c_void_p()
-        rc = self._L.gb_solver_create(arr, len(self.case_dirs), precision, ctypes.byref(h))
+        if levels == 2:
+            rc = self._L.gb_solver_create(arr, len(self.case_dirs), precision, ctypes.byref(h))
+        else:       # the three-level V-cycle extension
+            rc = self._L.gb_solver_create_levels(arr, len(self.case_dirs), precision, levels, ctypes.byref(h))
         if rc != 0:
             raise GBError(self._L.gb_last_error().decode())
         self.h = h

@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=1, help="operating points per GPU")
     ap.add_argument("--sampled", action="store_true",
                     help="draw the batch from the seeded operating-point sampler (three mesh sizes)")
+    ap.add_argument("--levels", type=int, default=2, choices=[2, 3],
+                    help="3: the three-level V-cycle extension (the reference stops at two levels)")
     ap.add_argument("--variant", default="default", choices=["default", "jst", "sa", "stage"],
                     help="numerical variant of the passage: JST, Spalart-Allmaras (single grid), rotor-stator stage")
     ap.add_argument("--blocks", type=int, default=1, choices=[1, 3],
@@ -52,7 +54,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the secondary measurements of the mixed-precision and batched forms")
-    ap.add_argument("--study", choices=["precision", "solves"],
+    ap.add_argument("--study", choices=["precision", "solves", "multigrid"],
                     help="long runs instead of the benchmark line: 'precision' = the mixed form's integrals "
                          "against the FP64 solve after 3000 cycles at three back pressures; 'solves' = "
                          "converged solves per hour of the plain FP64 path and the batched mixed form")
@@ -426,6 +428,28 @@ def study_solves(gbturbo, tmp, cycles, npoints):
     return out
 
 
+def study_multigrid(gbturbo, tmp, cycles):
+    """the 129 x 49 x 49 passage at 1.10 x p_t with two levels (the reference's cycle) and with the
+    three-level V-cycle extension, both forms: density residual and mass-flow imbalance at
+    checkpoints, device time per cycle"""
+    dirs, cells = make_cases(os.path.join(tmp, "mg"), 1, back_pressures=[1.10])
+    out = {"study": "multigrid", "cycles": cycles, "cells": cells, "runs": {}}
+    for levels in (2, 3):
+        for name, prec in (("fp64", gbturbo.FP64), ("mixed", gbturbo.MIXED)):
+            with gbturbo.Solver(dirs, prec, levels=levels) as s:
+                s.init_uniform()
+                s.timer_start()
+                h = s.iterate(cycles)[:, 0, :]
+                ms = s.timer_stop()
+            marks = [c for c in (50, 100, 200, 300, 500, 1000, 1500, 2000, 3000) if c <= cycles]
+            out["runs"][f"{levels}_levels_{name}"] = {
+                "ms_per_cycle": ms / cycles,
+                "res_dens": {str(c): float(h[c - 1, 1]) for c in marks},
+                "mass_ratio": {str(c): float(h[c - 1, 10]) for c in marks},
+                "min_res_dens": float(h[:, 1].min()), "first_below_1e-4": int(np.argmax(h[:, 1] < 1e-4)) + 1 if (h[:, 1] < 1e-4).any() else None}
+    return out
+
+
 def run_study(args):
     import build as pkg_build
     pkg_build.build()
@@ -434,6 +458,8 @@ def run_study(args):
     try:
         if args.study == "precision":
             res = study_precision(gbturbo, tmp, args.cycles or 3000)
+        elif args.study == "multigrid":
+            res = study_multigrid(gbturbo, tmp, args.cycles or 1000)
         else:
             res = study_solves(gbturbo, tmp, args.cycles or 4000, args.points)
         print(json.dumps(res), flush=True)
@@ -453,8 +479,11 @@ def config_block(args, cells, nsolve):
         wl, mesh = "rotor_passage_129x49x49_3block_2level_multigrid", "129x49x49 as blocks of 41/49/41 axial nodes"
     else:
         wl, mesh = "rotor_passage_129x49x49_2level_multigrid", "129x49x49 (axial x pitch x span)"
+    if getattr(args, "levels", 2) == 3:
+        wl = wl.replace("2level_multigrid", "3level_vcycle")
     return {"workload": wl, "mesh_nodes": mesh,
             "cells_per_solve": cells, "solves_per_gpu": nsolve, "precision": args.precision,
+            "levels": getattr(args, "levels", 2),
             "scheme": {"default": "Roe + MUSCL3 (primitive), Baldwin-Lomax, LU-SGS, 2-level FAS (reference maximum)",
                        "jst": "JST (k2 0.5, k4 1/32), Baldwin-Lomax, LU-SGS, 2-level FAS",
                        "sa": "Roe + MUSCL3 (primitive), Spalart-Allmaras, LU-SGS, single grid",
@@ -484,7 +513,7 @@ def run_gpu(args, rank, world, dist):
         grid_bytes = sum(os.path.getsize(os.path.join(d, "grid.dat")) for d in dirs)
 
         # --- device-resident throughput (value)
-        s = gbturbo.Solver(dirs, prec)
+        s = gbturbo.Solver(dirs, prec, levels=args.levels)
         s.init_uniform()
         s.iterate(max(args.warmup, 3), history=False)
         s.sync()
@@ -532,7 +561,7 @@ def run_gpu(args, rank, world, dist):
             pass
         forms = None
         if (rank == 0 and world == 1 and not args.no_forms and prec == gbturbo.FP64 and nsolve == 1 and args.blocks == 1
-                and args.variant == "default"):
+                and args.variant == "default" and args.levels == 2):
             n_ref = max(args.warmup, 3) + args.steps + nprof
             forms = measure_forms(gbturbo, dirs, cells, n_ref, s.integrals(1)[0], min(args.steps, 50), tmp)
         s.close()
@@ -541,7 +570,7 @@ def run_gpu(args, rank, world, dist):
         # -> iterations with the history row read back every step
         barrier(dist)
         t0 = time.perf_counter()
-        e = gbturbo.Solver(dirs, prec)
+        e = gbturbo.Solver(dirs, prec, levels=args.levels)
         e.init_uniform()
         e.iterate(max(args.warmup, 3), history=True)
         for _ in range(args.steps):
@@ -553,7 +582,7 @@ def run_gpu(args, rank, world, dist):
         e2e_value = cells * nsolve * world * n_e2e / t_e2e
 
         base = None
-        if rank == 0 and not args.no_cpu_baseline and args.blocks == 1 and args.variant == "default":
+        if rank == 0 and not args.no_cpu_baseline and args.blocks == 1 and args.variant == "default" and args.levels == 2:
             # (the CPU oracle port is single-block)
             base = cpu_baseline(dirs[0], cells, warm=3, steps=2)
 

@@ -35,6 +35,13 @@ typedef struct gb_solver gb_solver;
  * (CUserInput::ReadConfig, NumberOfMultigrid, ReadGrids, ReadBndGrid, NonDimensionalization),
  * memory and geometry of :59-69 (CMesh::AllocateMemory, CMesh::Geometry). */
 int gb_solver_create(const char *const *case_dirs, int n_solves, int precision, gb_solver **out);
+/* gb_solver_create with the number of grid levels of multigrid cases: 2 follows the reference
+ * (at most two levels, source/UserInput.cpp:1062); 3 selects the three-level V-cycle extension
+ * (no counterpart in the reference): the fine step as in the two-level cycle, then FAS smoothing
+ * on levels 2 and 3 with their residuals evaluated at the restricted states. Three levels need
+ * node counts N with (N-1) a multiple of 4 and (N-1)/4 > 2 and patch ranges that stay odd-aligned
+ * on the second level. */
+int gb_solver_create_levels(const char *const *case_dirs, int n_solves, int precision, int max_levels, gb_solver **out);
 int gb_solver_destroy(gb_solver *h);
 /* message of the last failure on the calling thread */
 const char *gb_last_error(void);
