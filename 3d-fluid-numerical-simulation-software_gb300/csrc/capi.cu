@@ -1,12 +1,16 @@
 // extern "C" boundary: forwards to gbt::SolverBase and turns exceptions into error codes.
 #include "../../include/gbturbo.h"
 #include "solver.hpp"
+#include "warmstart.hpp"
 #include <cstring>
 #include <string>
 
 struct gb_solver {
     std::unique_ptr<gbt::SolverBase> s;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
+};
+struct gb_warmstart {
+    std::unique_ptr<gbt::WarmStart> w;
 };
 
 static thread_local std::string g_err;
@@ -276,6 +280,93 @@ int gb_timer_stop(gb_solver *h, float *ms)
         gbt::check_cuda(cudaEventRecord(h->t1, h->s->stream), "cudaEventRecord");
         gbt::check_cuda(cudaEventSynchronize(h->t1), "cudaEventSynchronize");
         gbt::check_cuda(cudaEventElapsedTime(ms, h->t0, h->t1), "cudaEventElapsedTime");
+    });
+}
+
+int gb_start_from_fine_state(gb_solver *h)
+{
+    NEED(h);
+    return guard([&] { h->s->start_from_fine_state(); });
+}
+
+#define NEEDW(x) do { if (!(x) || !(x)->w) { g_err = "null warm-start handle"; return GB_ERR_ARG; } } while (0)
+
+int gb_ws_create(unsigned seed, gb_warmstart **out)
+{
+    if (!out) { g_err = "null out"; return GB_ERR_ARG; }
+    *out = nullptr;
+    return guard([&] {
+        std::unique_ptr<gb_warmstart> p(new gb_warmstart);
+        p->w.reset(new gbt::WarmStart(seed));
+        *out = p.release();
+    });
+}
+int gb_ws_destroy(gb_warmstart *w)
+{
+    delete w;
+    return GB_OK;
+}
+long gb_ws_num_params(void) { return (long)gbt::WarmStart::n_params(); }
+int gb_ws_add_solves(gb_warmstart *w, gb_solver *h, const float *params)
+{
+    NEEDW(w); NEED(h);
+    if (!params) { g_err = "null parameters"; return GB_ERR_ARG; }
+    return guard([&] { w->w->add_solves(*h->s, params); });
+}
+long long gb_ws_samples(gb_warmstart *w) { return (w && w->w) ? w->w->samples() : -1; }
+int gb_ws_train(gb_warmstart *w, int steps, int batch, float lr, float *loss)
+{
+    NEEDW(w);
+    if (steps < 0 || batch <= 0) { g_err = "bad steps or batch"; return GB_ERR_ARG; }
+    return guard([&] {
+        const float l = w->w->train(steps, batch, lr);
+        if (loss) *loss = l;
+    });
+}
+int gb_ws_apply(gb_warmstart *w, gb_solver *h, const float *params, int *used, double *res_warm, double *res_uniform)
+{
+    NEEDW(w); NEED(h);
+    if (!params || !used) { g_err = "null buffer"; return GB_ERR_ARG; }
+    return guard([&] { w->w->apply(*h->s, params, used, res_warm, res_uniform); });
+}
+int gb_ws_get_params(gb_warmstart *w, float *out)
+{
+    NEEDW(w);
+    if (!out) { g_err = "null buffer"; return GB_ERR_ARG; }
+    return guard([&] { w->w->get_params(out); });
+}
+int gb_ws_set_params(gb_warmstart *w, const float *in)
+{
+    NEEDW(w);
+    if (!in) { g_err = "null buffer"; return GB_ERR_ARG; }
+    return guard([&] { w->w->set_params(in); });
+}
+int gb_ws_get_norm(gb_warmstart *w, float *out)
+{
+    NEEDW(w);
+    if (!out) { g_err = "null buffer"; return GB_ERR_ARG; }
+    w->w->get_norm(out);
+    return GB_OK;
+}
+int gb_ws_set_norm(gb_warmstart *w, const float *in)
+{
+    NEEDW(w);
+    if (!in) { g_err = "null buffer"; return GB_ERR_ARG; }
+    return guard([&] { w->w->set_norm(in); });
+}
+int gb_ws_forward(gb_warmstart *w, const float *feat, int n, float *y)
+{
+    NEEDW(w);
+    if (!feat || !y || n <= 0) { g_err = "bad arguments"; return GB_ERR_ARG; }
+    return guard([&] { w->w->forward(feat, n, y); });
+}
+int gb_ws_forward_backward(gb_warmstart *w, const float *feat, const float *target, int n, float *loss, float *grad)
+{
+    NEEDW(w);
+    if (!feat || !target || !grad || n <= 0) { g_err = "bad arguments"; return GB_ERR_ARG; }
+    return guard([&] {
+        const float l = w->w->forward_backward(feat, target, n, grad);
+        if (loss) *loss = l;
     });
 }
 

@@ -211,6 +211,42 @@ __global__ void k_fill_uniform(Batch B, double *cv0, double *cv1, double *cv2, d
     cv0[p] = c[0]; cv1[p] = c[1]; cv2[p] = c[2]; cv3[p] = c[3]; cv4[p] = c[4];
 }
 
+// the uniform start of one slot (init_q) on its level's interior cells
+__global__ void k_fill_uniform_slot(Batch B, int slot, double *cv0, double *cv1, double *cv2, double *cv3, double *cv4,
+                                    const double *init)
+{
+    const Lvl L = B.lv[slot];
+    int i, j, k;
+    if (!box_index(L.IM - 1, L.JM - 1, L.KM - 1, i, j, k)) return;
+    const long long p = ix(L, i, j, k);
+    const double *c = init + 5 * slot;
+    cv0[p] = c[0]; cv1[p] = c[1]; cv2[p] = c[2]; cv3[p] = c[3]; cv4[p] = c[4];
+}
+
+// per slot, kAbsResBlocks partial sums of |R_rho| over the interior cells (fixed order)
+constexpr int kAbsResBlocks = 64;
+template <typename T>
+__global__ void __launch_bounds__(256) k_abs_res_partial(Batch B, const T *res0, double *part)
+{
+    const Lvl L = B.lv[blockIdx.y];
+    const long long n = (long long)(L.IM - 1) * (L.JM - 1) * (L.KM - 1);
+    double a = 0.0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(t % (L.KM - 1)) + 1;
+        const long long r = t / (L.KM - 1);
+        const int j = (int)(r % (L.JM - 1)) + 1, i = (int)(r / (L.JM - 1)) + 1;
+        a += fabs((double)res0[ix(L, i, j, k)]);
+    }
+    __shared__ double sh[256];
+    sh[threadIdx.x] = a;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = sh[0];
+}
+
 // volume of a case: its blocks' volumes summed in block order (source/ComputeAllBlockVars.cpp:32)
 __global__ void k_case_volume(Batch B, const double *blockvol, double *casevol)
 {
@@ -1180,7 +1216,10 @@ public:
             primitive_vars(1); limit_vars(1);
         }
     }
-    int report_level() const { return (ng != 1 && iter <= coarse_iter) ? 2 : 1; }
+    // the level whose integrals an iteration reports (source/Structured_FV3D.cpp:150-156: the coarse
+    // one up to the start-up's last iteration); a start from a given fine field has no start-up
+    bool fine_start = false;
+    int report_level() const { return (ng != 1 && !fine_start && iter <= coarse_iter) ? 2 : 1; }
     // driver phase: single grid; coarse-only start-up; the start-up's last cycle (eager); FAS. A
     // restarted multigrid run goes straight to FAS cycles (source/Solver.cpp:67-140)
     int phase() const
@@ -1204,7 +1243,10 @@ public:
         for (int q = 0; q < n; q++) {
             iter++;
             int ph = phase();
-            if (use_graphs && ph >= 0 && !profiling) {
+            // a phase graph fixes the reporting level it was captured with: a restarted multigrid
+            // case reports the coarse level for its first iterations, which therefore run eagerly
+            const bool level_moves = reuse && report_level() != 1;
+            if (use_graphs && ph >= 0 && !profiling && !level_moves) {
                 if (!graphs[ph]) {
                     cudaGraph_t g;
                     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
@@ -1489,6 +1531,105 @@ public:
                 CK(cudaMemcpy(W.ev + v.base, h.data(), sizeof(double) * bn, cudaMemcpyHostToDevice));
             }
         }
+    }
+
+    FineView fine_view() override
+    {
+        FineView v;
+        v.nslot = nsolve;
+        v.lv = lev[1].lv;
+        v.lv_dev = lev[1].lv_d;
+        for (int c = 0; c < NQ; c++) v.cv[c] = lev[1].W.cv[c];
+        for (int c = 0; c < 3; c++) v.cc[c] = lev[1].G.cc[c];
+        v.mut = lev[1].W.mut;
+        v.fp32 = sizeof(T) == 4;
+        return v;
+    }
+    void fill_uniform_fine(const std::vector<int> &slots) override
+    {
+        LaunchCtx cx = ctx(1);
+        Flow<T> &W = lev[1].W;
+        std::vector<int> all;
+        const std::vector<int> *list = &slots;
+        if (slots.empty()) {
+            for (int s = 0; s < nsolve; s++) all.push_back(s);
+            list = &all;
+        }
+        for (int s : *list) {
+            if (s < 0 || s >= nsolve) throw std::runtime_error("slot out of range");
+            const Lvl &v = lev[1].lv[s];
+            const long long n = (long long)(v.IM - 1) * (v.JM - 1) * (v.KM - 1);
+            k_fill_uniform_slot<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(cx.batch, s, W.cv[0], W.cv[1], W.cv[2],
+                                                                                W.cv[3], W.cv[4], init_q);
+        }
+        CK(cudaGetLastError());
+    }
+    void fine_primitive() override { launch_primitive<T>(ctx(1), P, lev[1].W); }
+    void fine_residual(std::vector<double> &per_case) override
+    {
+        resflux(1);
+        std::vector<double> part((size_t)nsolve * kAbsResBlocks);
+        DevBuf d;
+        d.bytes = sizeof(double) * part.size();
+        CK(cudaMalloc(&d.p, d.bytes));
+        k_abs_res_partial<T><<<dim3(kAbsResBlocks, nsolve), 256, 0, stream>>>(batch(1), lev[1].W.res[0], (double *)d.p);
+        CK(cudaMemcpyAsync(part.data(), d.p, d.bytes, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        per_case.assign(ncase, 0.0);
+        for (int c = 0; c < ncase; c++)
+            for (int b = 0; b < case_nblk[c]; b++)
+                for (int q = 0; q < kAbsResBlocks; q++) per_case[c] += part[(size_t)(case_first[c] + b) * kAbsResBlocks + q];
+    }
+    void start_from_fine_state() override
+    {
+        if (iter != 0) throw std::runtime_error("a start field is set before the first iteration");
+        if (ng >= 2) {
+            // the two-level cycle keeps the coarse level's time steps and spectral radii from its
+            // start-up (the coarse residual is not evaluated again, source/Solver.cpp:88-110); without
+            // a start-up they are evaluated once here, at the fine field restricted to the coarse
+            // level (and, with three levels, to the coarsest)
+            resflux(1);
+            restrict_to_coarse();
+            primitive_vars(2); limit_vars(2);
+            resflux(2);
+            if (ng == 3) {
+                restrict_lv(2);
+                primitive_vars(3); limit_vars(3);
+                resflux(3);
+            }
+            CK(cudaStreamSynchronize(stream));
+            CK(cudaGetLastError());
+        }
+        reuse = true;
+        fine_start = true;
+    }
+    DevBuf snap;
+    void save_fine_state() override
+    {
+        Level<T> &L = lev[1];
+        if (snap.p) { cudaFree(snap.p); snap.p = nullptr; snap.bytes = 0; }
+        snap.bytes = L.flow_d_mem.bytes + L.flow_t_mem.bytes + L.sa_mem.bytes + sizeof(SolveState) * nsolve;
+        CK(cudaMalloc(&snap.p, snap.bytes));
+        char *q = (char *)snap.p;
+        CK(cudaMemcpyAsync(q, L.flow_d_mem.p, L.flow_d_mem.bytes, cudaMemcpyDeviceToDevice, stream)); q += L.flow_d_mem.bytes;
+        CK(cudaMemcpyAsync(q, L.flow_t_mem.p, L.flow_t_mem.bytes, cudaMemcpyDeviceToDevice, stream)); q += L.flow_t_mem.bytes;
+        if (L.sa_mem.bytes) { CK(cudaMemcpyAsync(q, L.sa_mem.p, L.sa_mem.bytes, cudaMemcpyDeviceToDevice, stream)); q += L.sa_mem.bytes; }
+        CK(cudaMemcpyAsync(q, st_d, sizeof(SolveState) * nsolve, cudaMemcpyDeviceToDevice, stream));
+        CK(cudaStreamSynchronize(stream));
+    }
+    void restore_fine_state(bool put_back) override
+    {
+        if (!snap.p) throw std::runtime_error("no saved state");
+        if (put_back) {
+            Level<T> &L = lev[1];
+            const char *q = (const char *)snap.p;
+            CK(cudaMemcpyAsync(L.flow_d_mem.p, q, L.flow_d_mem.bytes, cudaMemcpyDeviceToDevice, stream)); q += L.flow_d_mem.bytes;
+            CK(cudaMemcpyAsync(L.flow_t_mem.p, q, L.flow_t_mem.bytes, cudaMemcpyDeviceToDevice, stream)); q += L.flow_t_mem.bytes;
+            if (L.sa_mem.bytes) { CK(cudaMemcpyAsync(L.sa_mem.p, q, L.sa_mem.bytes, cudaMemcpyDeviceToDevice, stream)); q += L.sa_mem.bytes; }
+            CK(cudaMemcpyAsync(st_d, q, sizeof(SolveState) * nsolve, cudaMemcpyDeviceToDevice, stream));
+            CK(cudaStreamSynchronize(stream));
+        }
+        if (snap.p) { cudaFree(snap.p); snap.p = nullptr; snap.bytes = 0; }
     }
 
     void set_cv(int solve, int l, const double *in, long n) override

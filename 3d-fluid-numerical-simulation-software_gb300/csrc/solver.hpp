@@ -21,6 +21,18 @@ struct DevBuf {
     ~DevBuf() { if (p) cudaFree(p); }
 };
 
+// Fine-level arrays of a batch as the warm start reads and writes them (device pointers into the
+// level's pools, box layout of gbt_common.cuh)
+struct FineView {
+    int nslot = 0;
+    std::vector<Lvl> lv;                         // per slot
+    const Lvl *lv_dev = nullptr;
+    double *cv[NQ] = {};
+    const double *cc[3] = {};                    // cell centres
+    const void *mut = nullptr;                   // eddy viscosity, in the working type
+    bool fp32 = false;                           // working type float (mixed form)
+};
+
 class SolverBase {
 public:
     virtual ~SolverBase() = default;
@@ -72,6 +84,21 @@ public:
     virtual void profile_begin() = 0;
     // "stage:milliseconds:launches;..." totals since profile_begin
     virtual std::string profile_end() = 0;
+
+    // start from a given fine-level field (the warm start): the arrays it writes, the uniform
+    // inlet state of init_uniform on the fine level's interior cells of the listed slots (every
+    // slot for an empty list), the primitive variables from Q, per case the sum over its cells of
+    // |R_rho| after one residual evaluation of the fine level, and the switch that makes the
+    // following iterations run full cycles from the fine state (as a restarted case does)
+    virtual FineView fine_view() = 0;
+    virtual void fill_uniform_fine(const std::vector<int> &slots) = 0;
+    virtual void fine_primitive() = 0;
+    virtual void fine_residual(std::vector<double> &per_case) = 0;
+    virtual void start_from_fine_state() = 0;
+    // a device copy of the fine level's flow arrays and of the solve states, put back (or dropped)
+    // after residual evaluations that must leave no trace
+    virtual void save_fine_state() = 0;
+    virtual void restore_fine_state(bool put_back) = 0;
 };
 
 // max_levels: 2 follows the reference (at most two grid levels); 3 enables the three-level

@@ -41,6 +41,21 @@ def load() -> ctypes.CDLL:
         "gb_case_blocks": ([vp, ip, ctypes.POINTER(ip)], ip),
         "gb_case_info": ([ctypes.c_char_p, ctypes.POINTER(ctypes.c_longlong), dp, ctypes.c_longlong], ip),
         "gb_init_uniform": ([vp], ip),
+        "gb_start_from_fine_state": ([vp], ip),
+        "gb_ws_create": ([ctypes.c_uint, ctypes.POINTER(vp)], ip),
+        "gb_ws_destroy": ([vp], ip),
+        "gb_ws_num_params": ([], ctypes.c_long),
+        "gb_ws_add_solves": ([vp, vp, ctypes.POINTER(ctypes.c_float)], ip),
+        "gb_ws_samples": ([vp], ctypes.c_longlong),
+        "gb_ws_train": ([vp, ip, ip, ctypes.c_float, ctypes.POINTER(ctypes.c_float)], ip),
+        "gb_ws_apply": ([vp, vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ip), dp, dp], ip),
+        "gb_ws_get_params": ([vp, ctypes.POINTER(ctypes.c_float)], ip),
+        "gb_ws_set_params": ([vp, ctypes.POINTER(ctypes.c_float)], ip),
+        "gb_ws_get_norm": ([vp, ctypes.POINTER(ctypes.c_float)], ip),
+        "gb_ws_set_norm": ([vp, ctypes.POINTER(ctypes.c_float)], ip),
+        "gb_ws_forward": ([vp, ctypes.POINTER(ctypes.c_float), ip, ctypes.POINTER(ctypes.c_float)], ip),
+        "gb_ws_forward_backward": ([vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), ip,
+                                    ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)], ip),
         "gb_resflux": ([vp, ip], ip),
         "gb_time_marching": ([vp, ip], ip),
         "gb_res_calculate": ([vp, ip, dp], ip),
@@ -86,7 +101,9 @@ EXPORTED = ["gb_solver_create", "gb_solver_destroy", "gb_last_error", "gb_dims",
             "gb_sync", "gb_set_graphs", "gb_timer_start", "gb_timer_stop", "gb_profile_begin", "gb_profile_end",
             "gb_res_calculate_noalloc", "gb_sweep_tuning", "gb_read_restart", "gb_write_restart",
             "gb_write_solution", "gb_mass_flow_imposed", "gb_get_outlet_pressure", "gb_num_blocks",
-            "gb_case_blocks", "gb_case_info", "gb_solver_create_levels"]
+            "gb_case_blocks", "gb_case_info", "gb_solver_create_levels", "gb_start_from_fine_state", "gb_ws_create", "gb_ws_destroy",
+            "gb_ws_num_params", "gb_ws_add_solves", "gb_ws_samples", "gb_ws_train", "gb_ws_apply", "gb_ws_get_params",
+            "gb_ws_set_params", "gb_ws_get_norm", "gb_ws_set_norm", "gb_ws_forward", "gb_ws_forward_backward"]
 
 
 class GBError(RuntimeError):
@@ -277,6 +294,11 @@ class Solver:
         a = np.ascontiguousarray(cv, dtype=np.float64).ravel()
         self._ck(self._L.gb_set_cv(self.h, solve, level, _dp(a), a.size))
 
+    def start_from_fine_state(self) -> None:
+        """after init_uniform and set_cv of the fine level of every slot: the iterations run full
+        cycles from that field"""
+        self._ck(self._L.gb_start_from_fine_state(self.h))
+
     # ---- the reference's solution files (a None path: the file in the solve's case directory)
     def read_restart(self, solve: int = 0, path: Optional[str] = None) -> None:
         self._ck(self._L.gb_read_restart(self.h, solve, path.encode() if path else None))
@@ -328,3 +350,100 @@ class Solver:
         ms = ctypes.c_float()
         self._ck(self._L.gb_timer_stop(self.h, ctypes.byref(ms)))
         return float(ms.value)
+
+
+WS_IN, WS_OUT, WS_OUT_USED, WS_PARAMS, WS_NORM = 64, 16, 6, 3, 24
+
+
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class WarmStart:
+    """The learned warm start (gb_ws_*): a coordinate MLP trained on fine-level fields of solves
+    this library ran, giving new cases their starting field, with the uniform start as the
+    fallback. Case parameters: WS_PARAMS floats per case (operating-point descriptors)."""
+
+    def __init__(self, seed: int = 0):
+        self._L = load()
+        h = ctypes.c_void_p()
+        if self._L.gb_ws_create(int(seed), ctypes.byref(h)) != 0:
+            raise GBError(self._L.gb_last_error().decode())
+        self.h = h
+        self.n_params = int(self._L.gb_ws_num_params())
+
+    def close(self):
+        if self.h:
+            self._L.gb_ws_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != 0:
+            raise GBError(self._L.gb_last_error().decode())
+
+    @staticmethod
+    def _params(params, n):
+        p = np.ascontiguousarray(np.asarray(params, dtype=np.float32).reshape(n, WS_PARAMS))
+        return p
+
+    def add_solves(self, solver: "Solver", params) -> None:
+        p = self._params(params, solver.n)
+        self._check(self._L.gb_ws_add_solves(self.h, solver.h, _fptr(p)))
+
+    @property
+    def samples(self) -> int:
+        return int(self._L.gb_ws_samples(self.h))
+
+    def train(self, steps: int, batch: int = 32768, lr: float = 1e-3) -> float:
+        loss = ctypes.c_float()
+        self._check(self._L.gb_ws_train(self.h, int(steps), int(batch), float(lr), ctypes.byref(loss)))
+        return float(loss.value)
+
+    def apply(self, solver: "Solver", params):
+        """per case: (used, residual sum of the network's field, of the uniform start)"""
+        p = self._params(params, solver.n)
+        used = (ctypes.c_int * solver.n)()
+        rw = np.zeros(solver.n)
+        ru = np.zeros(solver.n)
+        dp = ctypes.POINTER(ctypes.c_double)
+        self._check(self._L.gb_ws_apply(self.h, solver.h, _fptr(p), used, rw.ctypes.data_as(dp), ru.ctypes.data_as(dp)))
+        return np.array(list(used), dtype=np.int32), rw, ru
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.n_params, dtype=np.float32)
+        self._check(self._L.gb_ws_get_params(self.h, _fptr(out)))
+        return out
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(np.asarray(p, dtype=np.float32).reshape(self.n_params))
+        self._check(self._L.gb_ws_set_params(self.h, _fptr(p)))
+
+    def get_norm(self) -> np.ndarray:
+        out = np.zeros(WS_NORM, dtype=np.float32)
+        self._check(self._L.gb_ws_get_norm(self.h, _fptr(out)))
+        return out
+
+    def set_norm(self, v) -> None:
+        v = np.ascontiguousarray(np.asarray(v, dtype=np.float32).reshape(WS_NORM))
+        self._check(self._L.gb_ws_set_norm(self.h, _fptr(v)))
+
+    def forward(self, feat) -> np.ndarray:
+        f = np.ascontiguousarray(np.asarray(feat, dtype=np.float32))
+        n = f.shape[0]
+        y = np.zeros((n, WS_OUT), dtype=np.float32)
+        self._check(self._L.gb_ws_forward(self.h, _fptr(f), n, _fptr(y)))
+        return y
+
+    def forward_backward(self, feat, target):
+        f = np.ascontiguousarray(np.asarray(feat, dtype=np.float32))
+        t = np.ascontiguousarray(np.asarray(target, dtype=np.float32).reshape(f.shape[0], WS_OUT_USED))
+        g = np.zeros(self.n_params, dtype=np.float32)
+        loss = ctypes.c_float()
+        self._check(self._L.gb_ws_forward_backward(self.h, _fptr(f), _fptr(t), f.shape[0], ctypes.byref(loss), _fptr(g)))
+        return float(loss.value), g

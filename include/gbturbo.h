@@ -159,6 +159,54 @@ int gb_res_calculate_noalloc(gb_solver *h, int level, double *out);
  * check a case without a GPU. */
 int gb_case_info(const char *case_dir, long long info[9], double *nodes_out, long long cap);
 
+/* ---- Learned warm start. No counterpart in the reference: its solves start from the uniform
+ * inlet state of CBlocks::Initialization (source/Initialization.cpp:34-68), which stays the
+ * fallback here. A coordinate MLP (64 Fourier / parameter features, five hidden layers of 256
+ * with SiLU, 16 outputs of which the first six are rho, rho u, rho v, rho w, rho E, mu_t,
+ * normalised) is trained on fine-level fields of solves this library ran, in BF16 with FP32
+ * accumulation on the tensor cores (tcgen05), and gives new cases their starting field.
+ * Case parameters: GB_WS_PARAMS floats per case (the caller's operating-point descriptors, e.g.
+ * back-pressure ratio, rotation-speed ratio, stagger offset), normalised by the training set.
+ * gb_ws_add_solves: appends every fine interior cell of every case of h (its current state).
+ * gb_ws_train: Adam steps on random minibatches of `batch` samples; *loss = mean loss of the last
+ *   (up to) 20 steps. The first call fixes the normalisation from the training set.
+ * gb_ws_apply: before the first iteration of h: evaluates the network on every fine cell, keeps
+ *   it for a case when the case's sum of |R_rho| over its cells (one residual evaluation) is below
+ *   the uniform start's (used[case] = 1), else puts the uniform start back (used = 0); the
+ *   following iterations run full cycles from the fine field, as a restarted case does; when no
+ *   case keeps the network's field, the plain start-up of gb_init_uniform runs. res_warm and
+ *   res_uniform (may be NULL) receive the two residual sums per case.
+ * gb_ws_get/set_params: the flat FP32 parameters, layer after layer the weights [N][K] (row-major)
+ *   and the biases [N]; gb_ws_num_params() values. gb_ws_get/set_norm: GB_WS_NORM constants
+ *   (coordinate min[3], max[3] of axial position, radius, pitch angle; parameter mean[3], std[3];
+ *   target mean[6], std[6]).
+ * gb_ws_forward / gb_ws_forward_backward: the network on given features (n x 64, FP32, rounded to
+ *   BF16 on upload): outputs (n x 16); with targets (n x 6, normalised) the mean-squared loss and
+ *   the gradient of every parameter (the layout of gb_ws_get_params). */
+/* After gb_init_uniform and gb_set_cv of the fine level (level 1) of every slot, before the first
+ * iteration: the iterations run full multigrid cycles from that fine field, as a restarted case
+ * does, with the coarse levels' time steps and spectral radii evaluated once at the fine field
+ * restricted to them. No counterpart in the reference (its start-up always begins on the coarse
+ * level unless the config asks for the previous solution); gb_ws_apply uses it. */
+int gb_start_from_fine_state(gb_solver *h);
+
+#define GB_WS_PARAMS 3
+#define GB_WS_NORM 24
+typedef struct gb_warmstart gb_warmstart;
+int gb_ws_create(unsigned seed, gb_warmstart **out);
+int gb_ws_destroy(gb_warmstart *w);
+long gb_ws_num_params(void);
+int gb_ws_add_solves(gb_warmstart *w, gb_solver *h, const float *params);
+long long gb_ws_samples(gb_warmstart *w);
+int gb_ws_train(gb_warmstart *w, int steps, int batch, float lr, float *loss);
+int gb_ws_apply(gb_warmstart *w, gb_solver *h, const float *params, int *used, double *res_warm, double *res_uniform);
+int gb_ws_get_params(gb_warmstart *w, float *out);
+int gb_ws_set_params(gb_warmstart *w, const float *in);
+int gb_ws_get_norm(gb_warmstart *w, float *out);
+int gb_ws_set_norm(gb_warmstart *w, const float *in);
+int gb_ws_forward(gb_warmstart *w, const float *feat, int n, float *y);
+int gb_ws_forward_backward(gb_warmstart *w, const float *feat, const float *target, int n, float *loss, float *grad);
+
 #ifdef __cplusplus
 }
 #endif
