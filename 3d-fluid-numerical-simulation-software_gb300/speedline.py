@@ -81,10 +81,11 @@ def make_points(template: str, back_pressures: Sequence[float], root: str, ratio
 
 
 def run(dirs: Sequence[str], precision: int = gbturbo.MIXED, max_iter: Optional[int] = None, chunk: int = 50,
-        tol: Optional[float] = None) -> List[Dict]:
+        tol: Optional[float] = None, start=None) -> List[Dict]:
     """Runs the points as one batch until every point met the reference's convergence rule or the
     iteration cap (default: the template's maxiter), and reports each point at its first
-    converged iteration (its last iteration if it never converged)."""
+    converged iteration (its last iteration if it never converged). start(solver), if given, sets
+    the starting field in place of the uniform start (e.g. a WarmStart's apply)."""
     cfg = _lines(os.path.join(dirs[0], "config.dat"))
     tol = float(_value(cfg[LINE_CONVTOL])) if tol is None else tol
     max_iter = int(_value(cfg[LINE_MAXITER])) if max_iter is None else max_iter
@@ -93,7 +94,10 @@ def run(dirs: Sequence[str], precision: int = gbturbo.MIXED, max_iter: Optional[
     done = [None] * n                      # history row at convergence
     last = None
     with gbturbo.Solver(list(dirs), precision) as s:
-        s.init_uniform()
+        if start is None:
+            s.init_uniform()
+        else:
+            start(s)
         it = 0
         while it < max_iter and any(r is None for r in done):
             h = s.iterate(min(chunk, max_iter - it))          # (chunk, n, 12)

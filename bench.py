@@ -54,10 +54,12 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the secondary measurements of the mixed-precision and batched forms")
-    ap.add_argument("--study", choices=["precision", "solves", "multigrid"],
+    ap.add_argument("--study", choices=["precision", "solves", "multigrid", "warmstart"],
                     help="long runs instead of the benchmark line: 'precision' = the mixed form's integrals "
                          "against the FP64 solve after 3000 cycles at three back pressures; 'solves' = "
-                         "converged solves per hour of the plain FP64 path and the batched mixed form")
+                         "converged solves per hour of the plain FP64 path and the batched mixed form; "
+                         "'multigrid' = two- and three-level cycles; 'warmstart' = the learned warm start "
+                         "trained on 256 sampled points and evaluated on --points held-out ones")
     ap.add_argument("--cycles", type=int, default=None, help="cycle cap of a study (3000 / 4000 by default)")
     ap.add_argument("--points", type=int, default=64, help="operating points of the batched form in the solves study")
     return ap.parse_args()
@@ -428,6 +430,143 @@ def study_solves(gbturbo, tmp, cycles, npoints):
     return out
 
 
+def study_warmstart(gbturbo, tmp, cycles, n_test, n_train=256, mesh=(25, 25, 65), seed=2024, train_cycles=1000,
+                    steps=8000, batch=32768):
+    """The learned warm start on the seeded operating-point sampler (back pressure U[1.05, 1.30] x
+    p_t, speed {0.8, 0.9, 1.0} x 16000 rpm, stagger offset N(0, 1 deg)) on one mesh of the blade
+    family (the full-size passages stall before converging, see the precision study):
+      training data: n_train points as one mixed batch, uniform start, train_cycles cycles, every
+        fine cell a sample; training: Adam steps on minibatches (BF16, FP32 accumulation);
+      held out: n_test further points from the same sampler, the cycle cap run as one batch per
+        form with every cycle's history: mixed from the uniform start, mixed from the network's
+        field (with the residual-gated fallback), plain FP64 from the uniform start (the judge:
+        its integrals at the cap for the points it converged by the reference's rule, density
+        residual <= 1e-6 and mass ratio <= 0.003);
+      per point: the first cycle meeting the reference's rule, and the first cycle from which the
+        inlet mass flow stays within 1e-3 and the pressure ratio within 1e-4 of the judge's;
+      solves per hour: plain FP64 one solve at a time (a subsample, wall clock through the
+        speedline driver), and a batch that retires each point when it reaches the judge's
+        integrals, from the measured device time per batch cycle."""
+    import meshgen as mg
+    import speedline
+    ops = mg.sample_operating_points(n_train + n_test, seed)
+    for op in ops:
+        op["IM"], op["JM"], op["KM"] = mesh
+    jobs = [(os.path.join(tmp, f"ws{q}"), op) for q, op in enumerate(ops)]
+    with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
+        cells = pool.map(_write_sampled_case, jobs)
+    dirs = [d for d, _ in jobs]
+    prm = [[op["pb"], op["rpm"] / 16000.0, op["stagger_offset"]] for op in ops]
+    tr, te = slice(0, n_train), slice(n_train, n_train + n_test)
+    out = {"study": "warmstart", "mesh": list(mesh), "fine_cells_per_point": int(cells[0]), "train_points": n_train,
+           "held_out_points": n_test, "train_cycles": train_cycles, "cycle_cap": cycles, "tol": 1e-6,
+           "mass_ratio_limit": speedline.MASS_RATIO_LIMIT, "steps": steps, "batch": batch}
+    w = gbturbo.WarmStart(seed=7)
+    t0 = time.perf_counter()
+    with gbturbo.Solver(dirs[tr], gbturbo.MIXED) as s:
+        s.init_uniform()
+        h = s.iterate(train_cycles)
+        w.add_solves(s, prm[tr])
+    out["data_s"] = time.perf_counter() - t0
+    out["train_res_dens_final"] = [float(v) for v in np.percentile(h[-1, :, 1], [10, 50, 90])]
+    out["samples"] = w.samples
+    t0 = time.perf_counter()
+    losses = []
+    for k in range(steps // 500):
+        losses.append(w.train(500, batch=batch, lr=1e-3 if k < (steps // 500) * 3 // 4 else 3e-4))
+    out["train_s"] = time.perf_counter() - t0
+    out["loss_every_500_steps"] = losses
+    used_all = []
+
+    def warm(s):
+        used, rw, ru = w.apply(s, prm[te])
+        used_all.append(used.tolist())
+
+    # the held-out points as one batch per form, every cycle's history kept
+    hist = {}
+    for name, prec, start in (("mixed_batch_uniform", gbturbo.MIXED, None), ("mixed_batch_warm", gbturbo.MIXED, warm),
+                              ("fp64_batch_uniform", gbturbo.FP64, None)):
+        t0 = time.perf_counter()
+        with gbturbo.Solver(dirs[te], prec) as s:
+            t_create = time.perf_counter() - t0
+            t1 = time.perf_counter()
+            if start is None:
+                s.init_uniform()
+            else:
+                start(s)
+            t_start = time.perf_counter() - t1
+            s.timer_start()
+            H = s.iterate(cycles)
+            ms = s.timer_stop()
+        hist[name] = H
+        out[name] = {"create_s": t_create, "start_s": t_start, "ms_per_cycle": ms / cycles,
+                     "wall_s": time.perf_counter() - t0}
+    out["mixed_batch_warm"]["network_field_kept"] = int(sum(used_all[0]))
+    tol_m, tol_pr = 1e-3, 1e-4
+
+    def first_rule(H, q):
+        ok = np.nonzero((H[:, q, 1] <= 1e-6) & (H[:, q, 10] <= speedline.MASS_RATIO_LIMIT))[0]
+        return int(ok[0]) + 1 if ok.size else None
+
+    # the judge: the plain FP64 solve's integrals at the cap, for points it converged
+    ref = {q: hist["fp64_batch_uniform"][-1, q] for q in range(n_test) if first_rule(hist["fp64_batch_uniform"], q)}
+    out["fp64_batch_uniform"]["converged"] = len(ref)
+
+    def first_within(H, q):
+        r = ref[q]
+        bad = np.nonzero((np.abs(H[:, q, 6] - r[6]) > tol_m * abs(r[6])) | (np.abs(H[:, q, 8] - r[8]) > tol_pr * abs(r[8])))[0]
+        return 0 if bad.size == 0 else (int(bad[-1]) + 2 if bad[-1] + 1 < H.shape[0] else None)
+
+    per = {}
+    for name in ("mixed_batch_uniform", "mixed_batch_warm"):
+        H = hist[name]
+        rule = [first_rule(H, q) for q in range(n_test)]
+        within = [first_within(H, q) if q in ref else None for q in range(n_test)]
+        per[name] = (rule, within)
+        err_at_rule = [max(abs(H[c - 1, q, 6] - ref[q][6]) / abs(ref[q][6]), 0.0) for q, c in enumerate(rule) if c and q in ref]
+        pr_at_rule = [abs(H[c - 1, q, 8] - ref[q][8]) / abs(ref[q][8]) for q, c in enumerate(rule) if c and q in ref]
+        out[name].update({
+            "converged_by_rule": sum(1 for c in rule if c), "cycles_to_rule": rule,
+            "within_tol_of_fp64": sum(1 for c in within if c is not None), "cycles_to_fp64_integrals": within,
+            "at_rule_mass_flow_rel_err_max": max(err_at_rule) if err_at_rule else None,
+            "at_rule_pressure_ratio_rel_err_max": max(pr_at_rule) if pr_at_rule else None})
+    both = [q for q in range(n_test) if per["mixed_batch_uniform"][1][q] is not None and per["mixed_batch_warm"][1][q] is not None]
+    out["points_both_reach_fp64_integrals"] = len(both)
+    if both:
+        cu = [per["mixed_batch_uniform"][1][q] for q in both]
+        cw = [per["mixed_batch_warm"][1][q] for q in both]
+        out["median_cycles_to_fp64_integrals"] = {"uniform": float(np.median(cu)), "warm": float(np.median(cw))}
+        out["sum_cycles_to_fp64_integrals"] = {"uniform": int(sum(cu)), "warm": int(sum(cw))}
+    both_r = [q for q in range(n_test) if per["mixed_batch_uniform"][0][q] and per["mixed_batch_warm"][0][q]]
+    if both_r:
+        out["median_cycles_to_rule"] = {"uniform": float(np.median([per["mixed_batch_uniform"][0][q] for q in both_r])),
+                                        "warm": float(np.median([per["mixed_batch_warm"][0][q] for q in both_r]))}
+    # solves per hour of a batch that retires each point when it reaches the FP64 integrals (the
+    # points that never do count at the cap), from the measured time per cycle of the batch: one
+    # point-cycle costs ms_per_cycle / n_test
+    for name in ("mixed_batch_uniform", "mixed_batch_warm"):
+        pc = sum(c if c is not None else cycles for c in per[name][1])
+        t = pc * out[name]["ms_per_cycle"] / n_test / 1000.0 + out[name]["start_s"]
+        out[name]["point_cycles"] = pc
+        out[name]["retiring_batch_solves_per_hour"] = 3600.0 * n_test / t
+    # plain FP64 one solve at a time from the uniform start (a subsample of the held-out points)
+    sub = list(range(n_train, n_train + n_test))[:4]
+    t_sub = 0.0
+    for q in sub:
+        t0 = time.perf_counter()
+        speedline.run([dirs[q]], gbturbo.FP64, max_iter=cycles, chunk=50, tol=1e-6)
+        t_sub += time.perf_counter() - t0
+    out["fp64_single_uniform"] = {"subsample": len(sub), "wall_s": t_sub, "solves_per_hour": 3600.0 * len(sub) / t_sub}
+    base = out["fp64_single_uniform"]["solves_per_hour"]
+    for name in ("mixed_batch_uniform", "mixed_batch_warm"):
+        out[name]["retiring_over_plain_fp64_single"] = out[name]["retiring_batch_solves_per_hour"] / base
+    amort = out["mixed_batch_warm"]["point_cycles"] * out["mixed_batch_warm"]["ms_per_cycle"] / n_test / 1000.0 + \
+        out["mixed_batch_warm"]["start_s"] + out["data_s"] + out["train_s"]
+    out["warm_retiring_including_training_solves_per_hour"] = 3600.0 * n_test / amort
+    w.close()
+    return out
+
+
 def study_multigrid(gbturbo, tmp, cycles):
     """the 129 x 49 x 49 passage at 1.10 x p_t with two levels (the reference's cycle) and with the
     three-level V-cycle extension, both forms: density residual and mass-flow imbalance at
@@ -460,6 +599,8 @@ def run_study(args):
             res = study_precision(gbturbo, tmp, args.cycles or 3000)
         elif args.study == "multigrid":
             res = study_multigrid(gbturbo, tmp, args.cycles or 1000)
+        elif args.study == "warmstart":
+            res = study_warmstart(gbturbo, tmp, args.cycles or 2000, args.points)
         else:
             res = study_solves(gbturbo, tmp, args.cycles or 4000, args.points)
         print(json.dumps(res), flush=True)
