@@ -369,5 +369,11 @@ int gb_ws_forward_backward(gb_warmstart *w, const float *feat, const float *targ
         if (loss) *loss = l;
     });
 }
+int gb_ws_benchmark(gb_warmstart *w, long long n, int iters, float *ms_forward, float *ms_step)
+{
+    NEEDW(w);
+    if (!ms_forward || !ms_step) { g_err = "null buffer"; return GB_ERR_ARG; }
+    return guard([&] { w->w->benchmark(n, iters, ms_forward, ms_step); });
+}
 
 }  // extern "C"

@@ -12,6 +12,8 @@
 // tcgen05.ld (warp w owns TMEM lanes 32w..32w+31, i.e. rows 32w..32w+31 of the tile).
 #include "warmstart.hpp"
 #include "gbt_common.cuh"
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <algorithm>
 #include <cmath>
@@ -106,24 +108,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16])
 }
 
 // ---------------------------------------------------------------- operand staging
-// rows x K (K a multiple of 16) of a row-major BF16 matrix (row stride ld elements) into the
-// K-major core-matrix layout: core matrix (row/8, k/8) at ((row/8) * K/8 + k/8) * 128 bytes,
-// row%8 at 16 bytes each. Rows at or past rows_valid are zero.
-__device__ __forceinline__ void stage_rows(unsigned char *dst, const bf16 *src, long long ld, int rows, int K,
-                                           long long rows_valid)
-{
-    const int kc = K >> 3;
-    const int n = rows * kc;
-    for (int c = threadIdx.x; c < n; c += blockDim.x) {
-        const int r8 = c & 7, rest = c >> 3;
-        const int k8 = rest % kc, g = rest / kc;
-        const int row = g * 8 + r8;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (row < rows_valid) v = __ldg(reinterpret_cast<const uint4 *>(src + (long long)row * ld + k8 * 8));
-        *reinterpret_cast<uint4 *>(dst + ((size_t)(g * kc + k8) * 128 + r8 * 16)) = v;
-    }
-}
-
 // the transpose: cols x 64 cells, the cells of a row-major matrix X[cells x width] (row stride
 // ld) becoming the K dimension: core matrix (col/8, cell/8); each thread moves 8 x 8 blocks
 // through registers. Cells at or past cells_valid are zero.
@@ -154,17 +138,27 @@ __device__ __forceinline__ void stage_cols_t(unsigned char *dst, const bf16 *src
     }
 }
 
-__device__ __forceinline__ float sigmoidf_(float z) { return 1.0f / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float sigmoidf_(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
 
 // ---------------------------------------------------------------- the row product
 // D[128 x N] = A[128 x K] . B[N x K]^T per tile of 128 rows (cells); N, K multiples of 16, N <= 256,
-// K <= 256. Persistent: B is staged once, the CTA walks the row tiles. Epilogues:
+// K <= 256. Warp-specialised and persistent over the row tiles:
+//   warp 16: TMA producer. For every K chunk of up to 64 elements it loads, into one stage of a
+//     4-deep shared-memory ring, the A chunk (128 rows) and the B chunk (N rows) as boxes of
+//     8 elements x rows from 2D tensor maps; a box lands as rows x 16 bytes, i.e. a column of core
+//     matrices of the K-major layout (M/N neighbours 128 bytes apart, K neighbours one box apart).
+//     Rows past M read as zeros.
+//   warp 17: MMA issuer. Waits for a stage, issues its tcgen05.mma (K = 16 each) into one of two TMEM
+//     accumulators (256 columns each), and tcgen05.commit frees the stage when they complete;
+//     after a tile's last chunk a commit marks the accumulator full.
+//   warps 0-15: epilogue. Read the full accumulator (warp w: TMEM lanes 32(w%4)..32(w%4)+31, the
+//     (w/4)-th quarter of the columns), apply the epilogue, store, and hand the accumulator back,
+//     while the next tile accumulates in the other.
+// Epilogues:
 //   0: z = D + bias -> Z (BF16), H = SiLU(z) (BF16)
 //   1: y = D + bias -> Y (FP32)
 //   2: dZ = D * SiLU'(Zp) (BF16)
 struct GemmArgs {
-    const bf16 *A; long long lda;
-    const bf16 *B; long long ldb;
     long long M; int N, K;
     const float *bias;
     bf16 *Z, *H; float *Y; long long ldo;
@@ -172,99 +166,159 @@ struct GemmArgs {
     int *err;
 };
 
-constexpr int kTcSmem = 200 * 1024;              // one CTA per SM (and so at most 256 TMEM columns in use)
+constexpr int kTcSmem = 200 * 1024;              // one CTA per SM (and so at most 512 TMEM columns in use)
+constexpr int kStages = 4, kChunk = 64;
+constexpr int kEpiWarps = 16;                    // four per TMEM lane quadrant
+constexpr int kStageA = 128 * kChunk * 2, kStageB = 256 * kChunk * 2;
 
 __host__ __device__ inline int tmem_cols(int n) { int c = 32; while (c < n) c <<= 1; return c; }
 
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
 template <int EPI>
-__global__ void __launch_bounds__(128, 1) k_mlp_gemm(GemmArgs g)
+__global__ void __launch_bounds__(32 * (kEpiWarps + 2), 1) k_mlp_gemm(const __grid_constant__ CUtensorMap tmA,
+                                                     const __grid_constant__ CUtensorMap tmB, GemmArgs g)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
-    unsigned char *Bs = sm;
-    unsigned char *As = sm + (((size_t)g.N * g.K * 2 + 1023) & ~(size_t)1023);
-    unsigned char *tail = As + (size_t)128 * g.K * 2;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(tail);
-    uint32_t *slot = reinterpret_cast<uint32_t *>(tail + 8);
+    unsigned char *ring = sm;                                           // kStages x (A | B)
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sm + kStages * (kStageA + kStageB));
+    // bars: full[kStages], empty[kStages], acc_full[2], acc_empty[2]
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 2 * kStages + 4);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t ncols = (uint32_t)tmem_cols(g.N);
-    if (warp == 0) tmem_alloc(smem_u32(slot), ncols);
-    if (threadIdx.x == 0) mbar_init(smem_u32(bar), 1);
-    stage_rows(Bs, g.B, g.ldb, g.N, g.K, g.N);
+    const uint32_t bar0 = smem_u32(bars);
+    auto full = [&](int s) { return bar0 + 8u * (uint32_t)s; };
+    auto empty = [&](int s) { return bar0 + 8u * (uint32_t)(kStages + s); };
+    auto accf = [&](int a) { return bar0 + 8u * (uint32_t)(2 * kStages + a); };
+    auto acce = [&](int a) { return bar0 + 8u * (uint32_t)(2 * kStages + 2 + a); };
+    if (warp == kEpiWarps) tmem_alloc(smem_u32(slot), 512);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; s++) { mbar_init(full(s), 1); mbar_init(empty(s), 1); }
+        for (int a = 0; a < 2; a++) { mbar_init(accf(a), 1); mbar_init(acce(a), kEpiWarps); }
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *slot;
-    const uint32_t idesc = idesc_bf16(128, g.N);
-    const uint32_t sbo = (uint32_t)g.K * 16;
+    const int chunk = g.K < kChunk ? g.K : kChunk, nchunk = g.K / chunk, nk8 = chunk / 8;
     const long long tiles = (g.M + 127) / 128;
-    uint32_t phase = 0;
     bool failed = false;
-    for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {
-        const long long row0 = t * 128;
-        stage_rows(As, g.A + row0 * g.lda, g.lda, 128, g.K, g.M - row0);
-        fence_proxy_async();
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            tc_fence_after();
-            for (int ks = 0; ks < g.K / 16; ks++)
-                mma_bf16(tmem, smem_desc(smem_u32(As) + ks * 256, 128, sbo), smem_desc(smem_u32(Bs) + ks * 256, 128, sbo),
-                         idesc, ks > 0);
-            mma_commit(smem_u32(bar));
+    if (warp == kEpiWarps) {
+        if (lane == 0) {
+            const uint32_t bytes = (uint32_t)nk8 * (128u + (uint32_t)g.N) * 16u;
+            long long it = 0;
+            for (long long t = blockIdx.x; t < tiles && !failed; t += gridDim.x)
+                for (int kc = 0; kc < nchunk; kc++, it++) {
+                    const int s = (int)(it % kStages);
+                    const uint32_t ph = (uint32_t)((it / kStages) & 1);
+                    if (!mbar_wait_bounded(empty(s), ph ^ 1u)) { failed = true; break; }
+                    mbar_expect_tx(full(s), bytes);
+                    const uint32_t a_s = smem_u32(ring + (size_t)s * (kStageA + kStageB));
+                    const uint32_t b_s = a_s + kStageA;
+                    for (int k8 = 0; k8 < nk8; k8++) {
+                        const int x = kc * chunk + k8 * 8;
+                        tma_load_2d(a_s + (uint32_t)k8 * 128u * 16u, &tmA, x, (int)(t * 128), full(s));
+                        tma_load_2d(b_s + (uint32_t)k8 * (uint32_t)g.N * 16u, &tmB, x, 0, full(s));
+                    }
+                }
         }
-        const bool ok = mbar_wait_bounded(smem_u32(bar), phase);
-        phase ^= 1u;
-        tc_fence_after();
-        if (__syncthreads_or(!ok)) { failed = true; break; }
-        const long long row = row0 + warp * 32 + lane;
-        const bool live = row < g.M;
-        for (int c0 = 0; c0 < g.N; c0 += 16) {
-            float v[16];
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-            if (!live) continue;
-            if constexpr (EPI == 0) {
-                alignas(16) bf16 zo[16], ho[16];
-#pragma unroll
-                for (int i = 0; i < 16; i++) {
-                    const float z = v[i] + g.bias[c0 + i];
-                    zo[i] = __float2bfloat16_rn(z);
-                    ho[i] = __float2bfloat16_rn(z * sigmoidf_(z));
+    } else if (warp == kEpiWarps + 1) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16(128, g.N);
+            long long it = 0, ai = 0;
+            for (long long t = blockIdx.x; t < tiles && !failed; t += gridDim.x, ai++) {
+                const int a = (int)(ai & 1);
+                if (!mbar_wait_bounded(acce(a), (uint32_t)(((ai >> 1) & 1) ^ 1))) { failed = true; break; }
+                tc_fence_after();
+                for (int kc = 0; kc < nchunk; kc++, it++) {
+                    const int s = (int)(it % kStages);
+                    if (!mbar_wait_bounded(full(s), (uint32_t)((it / kStages) & 1))) { failed = true; break; }
+                    tc_fence_after();
+                    const uint32_t a_s = smem_u32(ring + (size_t)s * (kStageA + kStageB));
+                    const uint32_t b_s = a_s + kStageA;
+                    for (int ks = 0; ks < chunk / 16; ks++)
+                        mma_bf16(tmem + (uint32_t)(a * 256), smem_desc(a_s + (uint32_t)ks * 2u * 2048u, 2048u, 128u),
+                                 smem_desc(b_s + (uint32_t)ks * 2u * (uint32_t)g.N * 16u, (uint32_t)g.N * 16u, 128u), idesc,
+                                 (kc > 0 || ks > 0) ? 1u : 0u);
+                    mma_commit(empty(s));
                 }
-                uint4 *zp = reinterpret_cast<uint4 *>(g.Z + row * g.ldo + c0);
-                uint4 *hp = reinterpret_cast<uint4 *>(g.H + row * g.ldo + c0);
-                zp[0] = reinterpret_cast<uint4 *>(zo)[0]; zp[1] = reinterpret_cast<uint4 *>(zo)[1];
-                hp[0] = reinterpret_cast<uint4 *>(ho)[0]; hp[1] = reinterpret_cast<uint4 *>(ho)[1];
-            } else if constexpr (EPI == 1) {
-                float4 *yp = reinterpret_cast<float4 *>(g.Y + row * g.ldo + c0);
-#pragma unroll
-                for (int i = 0; i < 4; i++)
-                    yp[i] = make_float4(v[4 * i] + g.bias[c0 + 4 * i], v[4 * i + 1] + g.bias[c0 + 4 * i + 1],
-                                        v[4 * i + 2] + g.bias[c0 + 4 * i + 2], v[4 * i + 3] + g.bias[c0 + 4 * i + 3]);
-            } else {
-                alignas(16) bf16 zi[16], dz[16];
-                const uint4 *zs = reinterpret_cast<const uint4 *>(g.Zp + row * g.ldo + c0);
-                reinterpret_cast<uint4 *>(zi)[0] = zs[0];
-                reinterpret_cast<uint4 *>(zi)[1] = zs[1];
-#pragma unroll
-                for (int i = 0; i < 16; i++) {
-                    const float z = __bfloat162float(zi[i]);
-                    const float s = sigmoidf_(z);
-                    dz[i] = __float2bfloat16_rn(v[i] * (s * (1.0f + z * (1.0f - s))));
-                }
-                uint4 *dp = reinterpret_cast<uint4 *>(g.dZ + row * g.ldo + c0);
-                dp[0] = reinterpret_cast<uint4 *>(dz)[0]; dp[1] = reinterpret_cast<uint4 *>(dz)[1];
+                if (failed) break;
+                mma_commit(accf(a));
             }
         }
-        tc_fence_before();
-        __syncthreads();
+    } else {
+        long long ai = 0;
+        for (long long t = blockIdx.x; t < tiles; t += gridDim.x, ai++) {
+            const int a = (int)(ai & 1);
+            const bool ok = mbar_wait_bounded(accf(a), (uint32_t)((ai >> 1) & 1));
+            tc_fence_after();
+            if (!ok) { failed = true; break; }
+            const int quad = warp & 3;
+            const int cols = g.N >= 64 ? g.N / 4 : 16;        // a quarter of the columns, at least 16
+            const int cbeg = (warp >> 2) * cols, cend = cbeg + cols < g.N ? cbeg + cols : g.N;
+            const long long row = t * 128 + quad * 32 + lane;
+            const bool live = row < g.M;
+            for (int c0 = cbeg; c0 < cend; c0 += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(a * 256 + c0), v);
+                if (!live) continue;
+                if constexpr (EPI == 0) {
+                    alignas(16) bf16 zo[16], ho[16];
+#pragma unroll
+                    for (int i = 0; i < 16; i++) {
+                        const float z = v[i] + g.bias[c0 + i];
+                        zo[i] = __float2bfloat16_rn(z);
+                        ho[i] = __float2bfloat16_rn(z * sigmoidf_(z));
+                    }
+                    uint4 *zp = reinterpret_cast<uint4 *>(g.Z + row * g.ldo + c0);
+                    uint4 *hp = reinterpret_cast<uint4 *>(g.H + row * g.ldo + c0);
+                    zp[0] = reinterpret_cast<uint4 *>(zo)[0]; zp[1] = reinterpret_cast<uint4 *>(zo)[1];
+                    hp[0] = reinterpret_cast<uint4 *>(ho)[0]; hp[1] = reinterpret_cast<uint4 *>(ho)[1];
+                } else if constexpr (EPI == 1) {
+                    float4 *yp = reinterpret_cast<float4 *>(g.Y + row * g.ldo + c0);
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+                        yp[i] = make_float4(v[4 * i] + g.bias[c0 + 4 * i], v[4 * i + 1] + g.bias[c0 + 4 * i + 1],
+                                            v[4 * i + 2] + g.bias[c0 + 4 * i + 2], v[4 * i + 3] + g.bias[c0 + 4 * i + 3]);
+                } else {
+                    alignas(16) bf16 zi[16], dz[16];
+                    const uint4 *zs = reinterpret_cast<const uint4 *>(g.Zp + row * g.ldo + c0);
+                    reinterpret_cast<uint4 *>(zi)[0] = zs[0];
+                    reinterpret_cast<uint4 *>(zi)[1] = zs[1];
+#pragma unroll
+                    for (int i = 0; i < 16; i++) {
+                        const float z = __bfloat162float(zi[i]);
+                        const float sg = sigmoidf_(z);
+                        dz[i] = __float2bfloat16_rn(v[i] * (sg * (1.0f + z * (1.0f - sg))));
+                    }
+                    uint4 *dp = reinterpret_cast<uint4 *>(g.dZ + row * g.ldo + c0);
+                    dp[0] = reinterpret_cast<uint4 *>(dz)[0]; dp[1] = reinterpret_cast<uint4 *>(dz)[1];
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acce(a));
+        }
     }
-    if (failed) {
-        if (threadIdx.x == 0) atomicOr(g.err, 1);
-        mbar_wait_bounded(smem_u32(bar), phase ^ 1u);   // the product still in flight, if any
-    }
+    if (failed) atomicOr(g.err, 1);
+    __syncwarp();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 0) tmem_dealloc(tmem, ncols);
+    if (warp == kEpiWarps) tmem_dealloc(tmem, 512);
 }
 
 // ---------------------------------------------------------------- the weight gradient
@@ -581,6 +635,32 @@ __global__ void __launch_bounds__(256) k_ws_stats(const float *set, long long n,
 }
 
 // ---------------------------------------------------------------- host side
+// 2D tensor map of a row-major BF16 matrix [rows x cols] (row stride ld elements) read in boxes
+// of 8 columns (16 bytes) x box_rows rows; rows past the end read as zeros
+static CUtensorMap tensor_map_rows(const bf16 *base, long long rows, int cols, long long ld, int box_rows)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        WCK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q));
+        if (!f || q != cudaDriverEntryPointSuccess) throw std::runtime_error("cuTensorMapEncodeTiled is not available");
+        encode = (PFN_cuTensorMapEncodeTiled_v12000)f;
+    }
+    if (((uintptr_t)base & 15) || ((ld * 2) & 15) || (cols & 7) || box_rows < 1 || box_rows > 256)
+        throw std::runtime_error("tensor map: misaligned matrix or box");
+    CUtensorMap m;
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {8u, (cuuint32_t)box_rows};
+    const cuuint32_t es[2] = {1u, 1u};
+    const CUresult r = encode(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)base, dims, strides, box, es,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed");
+    return m;
+}
+
 static const int kN[kWsLayers] = {kWsHidden, kWsHidden, kWsHidden, kWsHidden, kWsHidden, kWsOut};
 static const int kK[kWsLayers] = {kWsIn, kWsHidden, kWsHidden, kWsHidden, kWsHidden, kWsHidden};
 
@@ -643,13 +723,13 @@ struct WarmStart::Impl {
     {
         if (M <= 0) return;
         GemmArgs g{};
-        g.A = A; g.lda = lda;
-        g.B = transposed ? Wt[l_w] : Wb[l_w]; g.ldb = K;
         g.M = M; g.N = N; g.K = K;
         g.bias = bias; g.Z = Zo; g.H = Ho; g.Y = Yo; g.ldo = ldo; g.Zp = Zp; g.dZ = dZ; g.err = err;
+        const CUtensorMap ta = tensor_map_rows(A, M, K, lda, 128);
+        const CUtensorMap tb = tensor_map_rows(transposed ? Wt[l_w] : Wb[l_w], N, K, K, N);
         const long long tiles = (M + 127) / 128;
         const int grid = (int)std::min<long long>(tiles, n_sm);
-        k_mlp_gemm<EPI><<<grid, 128, kTcSmem, st>>>(g);
+        k_mlp_gemm<EPI><<<grid, 32 * (kEpiWarps + 2), kTcSmem, st>>>(ta, tb, g);
         WCK(cudaGetLastError());
     }
 
@@ -1020,6 +1100,53 @@ float WarmStart::forward_backward(const float *feat, const float *target, int M,
     WCK(cudaStreamSynchronize(m.st));
     if (error_flag()) throw std::runtime_error("a tensor-core wait of the warm-start network ran out");
     return l;
+}
+
+__global__ void k_ws_random_rows(long long M, unsigned long long seed, bf16 *X0, float *T)
+{
+    const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    for (int c = 0; c < kWsIn; c++) {
+        const unsigned long long h = mix64(seed ^ ((unsigned long long)m * kWsIn + c));
+        X0[m * kWsIn + c] = __float2bfloat16_rn((float)(h >> 40) * (2.0f / 16777216.0f) - 1.0f);
+    }
+    for (int o = 0; o < 8; o++) {
+        const unsigned long long h = mix64(~seed ^ ((unsigned long long)m * 8 + o));
+        T[m * 8 + o] = o < kWsOutUsed ? (float)(h >> 40) * (2.0f / 16777216.0f) - 1.0f : 0.0f;
+    }
+}
+
+void WarmStart::benchmark(long long M, int iters, float *ms_forward, float *ms_step)
+{
+    if (M < 128 || iters < 1) throw std::invalid_argument("benchmark: at least 128 rows and one iteration");
+    Impl &m = *d;
+    m.ensure(M);
+    k_ws_random_rows<<<(unsigned)((M + 255) / 256), 256, 0, m.st>>>(M, 12345ull, m.X0, m.T);
+    cudaEvent_t e0, e1;
+    WCK(cudaEventCreate(&e0));
+    WCK(cudaEventCreate(&e1));
+    m.forward(M);                                        // warm-up
+    WCK(cudaEventRecord(e0, m.st));
+    for (int i = 0; i < iters; i++) m.forward(M);
+    WCK(cudaEventRecord(e1, m.st));
+    WCK(cudaEventSynchronize(e1));
+    float t = 0.f;
+    WCK(cudaEventElapsedTime(&t, e0, e1));
+    *ms_forward = t / iters;
+    const int nb = (int)((M + 255) / 256);
+    WCK(cudaEventRecord(e0, m.st));
+    for (int i = 0; i < iters; i++) {
+        m.forward(M);
+        k_ws_loss<<<nb, 256, 0, m.st>>>(m.Y, m.T, M, m.dY, m.lpart);
+        m.backward(M);
+    }
+    WCK(cudaEventRecord(e1, m.st));
+    WCK(cudaEventSynchronize(e1));
+    WCK(cudaEventElapsedTime(&t, e0, e1));
+    *ms_step = t / iters;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (error_flag()) throw std::runtime_error("a tensor-core wait of the warm-start network ran out");
 }
 
 }  // namespace gbt

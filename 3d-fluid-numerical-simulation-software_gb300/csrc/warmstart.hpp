@@ -48,6 +48,9 @@ public:
     // normalised), the loss and the gradient of every parameter (n_params values)
     void forward(const float *feat, int M, float *y);
     float forward_backward(const float *feat, const float *target, int M, float *grad);
+    // device time (CUDA events on the network's stream) per forward pass and per forward and
+    // backward pass over M rows of device-resident random features and targets, mean of iters
+    void benchmark(long long M, int iters, float *ms_forward, float *ms_step);
     int error_flag();
 
 private:

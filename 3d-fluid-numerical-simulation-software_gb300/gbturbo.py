@@ -56,6 +56,7 @@ def load() -> ctypes.CDLL:
         "gb_ws_forward": ([vp, ctypes.POINTER(ctypes.c_float), ip, ctypes.POINTER(ctypes.c_float)], ip),
         "gb_ws_forward_backward": ([vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), ip,
                                     ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)], ip),
+        "gb_ws_benchmark": ([vp, ctypes.c_longlong, ip, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)], ip),
         "gb_resflux": ([vp, ip], ip),
         "gb_time_marching": ([vp, ip], ip),
         "gb_res_calculate": ([vp, ip, dp], ip),
@@ -103,7 +104,8 @@ EXPORTED = ["gb_solver_create", "gb_solver_destroy", "gb_last_error", "gb_dims",
             "gb_write_solution", "gb_mass_flow_imposed", "gb_get_outlet_pressure", "gb_num_blocks",
             "gb_case_blocks", "gb_case_info", "gb_solver_create_levels", "gb_start_from_fine_state", "gb_ws_create", "gb_ws_destroy",
             "gb_ws_num_params", "gb_ws_add_solves", "gb_ws_samples", "gb_ws_train", "gb_ws_apply", "gb_ws_get_params",
-            "gb_ws_set_params", "gb_ws_get_norm", "gb_ws_set_norm", "gb_ws_forward", "gb_ws_forward_backward"]
+            "gb_ws_set_params", "gb_ws_get_norm", "gb_ws_set_norm", "gb_ws_forward", "gb_ws_forward_backward",
+            "gb_ws_benchmark"]
 
 
 class GBError(RuntimeError):
@@ -447,3 +449,9 @@ class WarmStart:
         loss = ctypes.c_float()
         self._check(self._L.gb_ws_forward_backward(self.h, _fptr(f), _fptr(t), f.shape[0], ctypes.byref(loss), _fptr(g)))
         return float(loss.value), g
+
+    def benchmark(self, rows: int, iters: int = 20):
+        """device ms per forward pass and per forward-and-backward pass over rows random rows"""
+        f, b = ctypes.c_float(), ctypes.c_float()
+        self._check(self._L.gb_ws_benchmark(self.h, int(rows), int(iters), ctypes.byref(f), ctypes.byref(b)))
+        return float(f.value), float(b.value)

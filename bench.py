@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the secondary measurements of the mixed-precision and batched forms")
-    ap.add_argument("--study", choices=["precision", "solves", "multigrid", "warmstart"],
+    ap.add_argument("--study", choices=["precision", "solves", "multigrid", "warmstart", "network"],
                     help="long runs instead of the benchmark line: 'precision' = the mixed form's integrals "
                          "against the FP64 solve after 3000 cycles at three back pressures; 'solves' = "
                          "converged solves per hour of the plain FP64 path and the batched mixed form; "
@@ -567,6 +567,31 @@ def study_warmstart(gbturbo, tmp, cycles, n_test, n_train=256, mesh=(25, 25, 65)
     return out
 
 
+def study_network(gbturbo):
+    """the warm-start network's tensor-core kernels alone: device time per forward pass and per
+    training pass (forward, loss, backward) at several row counts, and the dense BF16 rate they
+    reach (FLOPs per row: 2 x (64x256 + 4 x 256x256 + 256x16) forward; backward the same again for
+    the weight gradients and again less the first layer's 2 x 64x256 for the data gradients)"""
+    fwd_flop = 2 * (64 * 256 + 4 * 256 * 256 + 256 * 16)
+    step_flop = 3 * fwd_flop - 2 * 64 * 256
+    out = {"study": "network", "rows": {}}
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    with gbturbo.WarmStart(seed=1) as w:
+        for rows in (32768, 262144, 1048576):
+            ms_f, ms_s = w.benchmark(rows, iters=20)
+            tf_f = fwd_flop * rows / (ms_f / 1000.0) / 1e12
+            tf_s = step_flop * rows / (ms_s / 1000.0) / 1e12
+            out["rows"][str(rows)] = {"ms_forward": ms_f, "ms_train_step": ms_s, "tflops_forward": tf_f,
+                                      "tflops_train_step": tf_s, "frac_of_bf16_peak_forward": tf_f / peak}
+    out["bf16_peak_tflops"] = peak
+    return out
+
+
 def study_multigrid(gbturbo, tmp, cycles):
     """the 129 x 49 x 49 passage at 1.10 x p_t with two levels (the reference's cycle) and with the
     three-level V-cycle extension, both forms: density residual and mass-flow imbalance at
@@ -599,6 +624,8 @@ def run_study(args):
             res = study_precision(gbturbo, tmp, args.cycles or 3000)
         elif args.study == "multigrid":
             res = study_multigrid(gbturbo, tmp, args.cycles or 1000)
+        elif args.study == "network":
+            res = study_network(gbturbo)
         elif args.study == "warmstart":
             res = study_warmstart(gbturbo, tmp, args.cycles or 2000, args.points)
         else:

@@ -206,6 +206,9 @@ int gb_ws_get_norm(gb_warmstart *w, float *out);
 int gb_ws_set_norm(gb_warmstart *w, const float *in);
 int gb_ws_forward(gb_warmstart *w, const float *feat, int n, float *y);
 int gb_ws_forward_backward(gb_warmstart *w, const float *feat, const float *target, int n, float *loss, float *grad);
+/* device time per forward pass and per forward-and-backward pass (loss and every gradient) over
+ * n rows of device-resident random inputs, mean of iters after one warm-up (CUDA events) */
+int gb_ws_benchmark(gb_warmstart *w, long long n, int iters, float *ms_forward, float *ms_step);
 
 #ifdef __cplusplus
 }
