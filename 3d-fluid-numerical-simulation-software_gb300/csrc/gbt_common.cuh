@@ -173,6 +173,18 @@ __device__ __forceinline__ double rel_change(double o, double c)
     const double r1 = r0 * fma(-o, r0, 2.0);
     return fabs((o - c) * r1);
 }
+// the mixed form's term: the exact FP64 difference over o to FP32 accuracy (relative error of the
+// term, and so of the norm, below 2e-7), four FP64-pipe instructions in place of seven
+__device__ __forceinline__ double rel_change_mixed(double o, double c)
+{
+    return (double)fabsf((float)(o - c) * (1.0f / (float)o));
+}
+template <typename T>
+__device__ __forceinline__ double rel_change_t(double o, double c)
+{
+    if constexpr (sizeof(T) == 8) return rel_change(o, c);
+    else return rel_change_mixed(o, c);
+}
 
 template <typename T>
 __device__ __forceinline__ T sutherland(const PhysW<T> &P, T temp)

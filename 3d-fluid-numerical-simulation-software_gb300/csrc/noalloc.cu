@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(256) k_norm_onepass(Batch B, Geo G, Flow<T> W,
 #pragma unroll
         for (int c = 0; c < 5; c++) {
             const double o = W.cvold[c][p];
-            acc[c] += rel_change(o, W.cv[c][p]) * vol;
+            acc[c] += rel_change_t<T>(o, W.cv[c][p]) * vol;
         }
     }
     __shared__ double sh[8][5];
