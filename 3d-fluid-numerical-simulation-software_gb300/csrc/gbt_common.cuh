@@ -62,7 +62,9 @@ struct Flow {
     T *res[NQ], *dq[NQ];
     double *cv2h[NQ];                                // multigrid (coarse level only)
     T *res2h[NQ], *dq2h[NQ];
-    int *flag;                                       // Baldwin-Lomax first-touch marks
+    // Baldwin-Lomax merge over the walls: per cell the bit pattern of the smallest mu_t of the
+    // lines that reach it (mu_t >= 0 orders as an unsigned integer; all ones = not reached)
+    unsigned long long *blmin;
     const int *wallf[3];                             // per face: wall patch (1-based) or 0
     // Spalart-Allmaras (fine level of a case with turbulence model 200; null otherwise): the
     // eddy-viscosity variable (FP64 like Q) and its copy before the model's clipping, its

@@ -118,6 +118,13 @@ void launch_wall_distances(const LaunchCtx &ctx, const Geo &G, const BcTables &b
 template void launch_wall_distances<double>(const LaunchCtx &, const Geo &, const BcTables &);
 template void launch_wall_distances<float>(const LaunchCtx &, const Geo &, const BcTables &);
 
+// mu_t as an unsigned integer that orders like the value for mu_t >= 0, and back
+__device__ __forceinline__ unsigned long long bl_bits(double v) { return (unsigned long long)__double_as_longlong(v); }
+__device__ __forceinline__ unsigned long long bl_bits(float v) { return (unsigned long long)__float_as_uint(v); }
+template <typename T> __device__ __forceinline__ T bl_value(unsigned long long b);
+template <> __device__ __forceinline__ double bl_value<double>(unsigned long long b) { return __longlong_as_double((long long)b); }
+template <> __device__ __forceinline__ float bl_value<float>(unsigned long long b) { return __uint_as_float((unsigned)b); }
+
 template <typename T>
 __global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, PhysW<T> PC, Flow<T> W, const DevWall *walls, int off,
                                                       const long long *dist_off, const T *dist_all)
@@ -222,16 +229,27 @@ __global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, PhysW<T> PC, Flow
         const T m_out = aCcp * rho * Fwake * Fk;
         const T mt = (tabs(m_in) > tabs(m_out)) ? m_out : m_in;
         if (n0 == 1) {
-            W.mut[p] = (T)0;                                   // wall-adjacent cell
+            atomicMin(&W.blmin[p], 0ull);                      // wall-adjacent cell: mu_t = 0
             W.mut[p0 + (long long)(lo ? 0 : N) * sn] = (T)0;   // its ghost
-            W.flag[p] = 1;
             continue;
         }
-        if (W.flag[p] == 0) { W.flag[p] = 1; W.mut[p] = mt; }
-        else { const T old = W.mut[p]; W.mut[p] = (old < mt) ? old : mt; }
+        // the smallest mu_t over the walls whose lines reach the cell (the reference's merge,
+        // BL_Model.cpp:88-96,163-171,239-247: the first wall sets it, later walls keep the minimum; mu_t >= 0, so
+        // the minimum of the bit patterns is the minimum of the values and the walls' order is moot)
+        atomicMin(&W.blmin[p], bl_bits(mt));
     }
 #undef CELL
 #undef DIST
+}
+
+// mu_t of every cell a wall line reached: the merged minimum (other cells keep their mu_t)
+template <typename T>
+__global__ void __launch_bounds__(256) k_bl_merge(Flow<T> W, long long n)
+{
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const unsigned long long b = W.blmin[p];
+    if (b != ~0ull) W.mut[p] = bl_value<T>(b);
 }
 
 // ghost mu_t mirrored across every wall face (source/WallFlux.cpp:106-109,137-140,168-171)
@@ -334,25 +352,21 @@ void launch_cell_stages(const LaunchCtx &ctx, const Phys &P, const PhysW<T> &PC,
     ctx.mark("spectral_curl", 1);
     k_cell_a<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, PC, GW, W);
     ctx.mark("spectral_curl", 0);
-    ctx.mark("baldwin_lomax", 1, bc.n_wall_slot + 2);
+    ctx.mark("baldwin_lomax", 1, 4);
     if (level == 1 && P.turb_bl && bc.n_wall > 0) {
-        // first-touch marks of the minimum merge, reset every evaluation
-        cudaMemsetAsync(W.flag, 0, (size_t)ctx.pool_n * sizeof(int), ctx.stream);
-        for (int q = 0; q < bc.n_wall_slot; q++) {
-            int n = bc.wall_slot_off[q + 1] - bc.wall_slot_off[q];
-            if (n <= 0) continue;
-            // 32 lines per block, the points of each line split over BL_WARPS warps
-            dim3 g((unsigned)((bc.wall_slot_lines[q] + 31) / 32), n);
-            k_bl<T><<<g, 32 * BL_WARPS, 0, ctx.stream>>>(B, PC, W, bc.wall, bc.wall_slot_off[q], bc.wall_dist_off,
-                                                         (const T *)bc.wall_dist);
-        }
+        // every wall of every solve in one launch (32 lines per block, the points of each line split
+        // over BL_WARPS warps), merged through the per-cell minimum, reset every evaluation
+        cudaMemsetAsync(W.blmin, 0xFF, (size_t)ctx.pool_n * sizeof(unsigned long long), ctx.stream);
+        dim3 g((unsigned)((bc.max_wall + 31) / 32), bc.n_wall);
+        k_bl<T><<<g, 32 * BL_WARPS, 0, ctx.stream>>>(B, PC, W, bc.wall, 0, bc.wall_dist_off, (const T *)bc.wall_dist);
+        k_bl_merge<T><<<(unsigned)((ctx.pool_n + 255) / 256), 256, 0, ctx.stream>>>(W, ctx.pool_n);
     }
     if (level == 1 && P.turb_sa && W.ev) launch_sa_model<T>(ctx, P, GW, W);
     if (bc.n_wall > 0) {
         dim3 g((unsigned)((bc.max_wall + 127) / 128), bc.n_wall);
         k_wall_mut<T><<<g, 128, 0, ctx.stream>>>(B, W, bc.wall);
     }
-    ctx.mark("baldwin_lomax", 0, bc.n_wall_slot + 2);
+    ctx.mark("baldwin_lomax", 0, 4);
     ctx.mark("time_step", 1, 2);
     k_cell_b<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, PC, GW, W, level);
     if (P.global_dt) {

@@ -606,12 +606,12 @@ public:
         } else {
             for (int f = 0; f < 3; f++) for (int c = 0; c < NQ; c++) W.Fd[f][c] = nullptr;
         }
-        Lv.int_mem.bytes = sizeof(int) * N * 4;
+        Lv.int_mem.bytes = sizeof(unsigned long long) * N + sizeof(int) * N * 3;
         CK(cudaMalloc(&Lv.int_mem.p, Lv.int_mem.bytes));
         CK(cudaMemset(Lv.int_mem.p, 0, Lv.int_mem.bytes));
-        int *ip = (int *)Lv.int_mem.p;
-        W.flag = ip;
-        int *wallf[3] = {ip + N, ip + 2 * N, ip + 3 * N};
+        W.blmin = (unsigned long long *)Lv.int_mem.p;
+        int *ip = (int *)(W.blmin + N);
+        int *wallf[3] = {ip, ip + N, ip + 2 * N};
         for (int f = 0; f < 3; f++) W.wallf[f] = wallf[f];
         // nodes
         {
