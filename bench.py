@@ -437,11 +437,11 @@ def study_warmstart(gbturbo, tmp, cycles, n_test, n_train=256, mesh=(25, 25, 65)
     family (the full-size passages stall before converging, see the precision study):
       training data: n_train points as one mixed batch, uniform start, train_cycles cycles, every
         fine cell a sample; training: Adam steps on minibatches (BF16, FP32 accumulation);
-      held out: n_test further points from the same sampler, the cycle cap run as one batch per
-        form with every cycle's history: mixed from the uniform start, mixed from the network's
-        field (with the residual-gated fallback), plain FP64 from the uniform start (the judge:
-        its integrals at the cap for the points it converged by the reference's rule, density
-        residual <= 1e-6 and mass ratio <= 0.003);
+      held out: n_test further points from the same sampler, run as one batch per form with every
+        cycle's history: mixed from the uniform start and mixed from the network's field (with the
+        residual-gated fallback) to the cycle cap; plain FP64 from the uniform start to twice the
+        cap (the judge: its integrals at the end, for the points it converged within the cap by
+        the reference's rule, density residual <= 1e-6 and mass ratio <= 0.003);
       per point: the first cycle meeting the reference's rule, and the first cycle from which the
         inlet mass flow stays within 1e-3 and the pressure ratio within 1e-4 of the judge's;
       solves per hour: plain FP64 one solve at a time (a subsample, wall clock through the
@@ -484,8 +484,11 @@ def study_warmstart(gbturbo, tmp, cycles, n_test, n_train=256, mesh=(25, 25, 65)
 
     # the held-out points as one batch per form, every cycle's history kept
     hist = {}
-    for name, prec, start in (("mixed_batch_uniform", gbturbo.MIXED, None), ("mixed_batch_warm", gbturbo.MIXED, warm),
-                              ("fp64_batch_uniform", gbturbo.FP64, None)):
+    judge_cycles = 2 * cycles
+    out["judge_cycles"] = judge_cycles
+    for name, prec, start, n_cyc in (("mixed_batch_uniform", gbturbo.MIXED, None, cycles),
+                                     ("mixed_batch_warm", gbturbo.MIXED, warm, cycles),
+                                     ("fp64_batch_uniform", gbturbo.FP64, None, judge_cycles)):
         t0 = time.perf_counter()
         with gbturbo.Solver(dirs[te], prec) as s:
             t_create = time.perf_counter() - t0
@@ -496,10 +499,10 @@ def study_warmstart(gbturbo, tmp, cycles, n_test, n_train=256, mesh=(25, 25, 65)
                 start(s)
             t_start = time.perf_counter() - t1
             s.timer_start()
-            H = s.iterate(cycles)
+            H = s.iterate(n_cyc)
             ms = s.timer_stop()
         hist[name] = H
-        out[name] = {"create_s": t_create, "start_s": t_start, "ms_per_cycle": ms / cycles,
+        out[name] = {"create_s": t_create, "start_s": t_start, "ms_per_cycle": ms / n_cyc,
                      "wall_s": time.perf_counter() - t0}
     out["mixed_batch_warm"]["network_field_kept"] = int(sum(used_all[0]))
     tol_m, tol_pr = 1e-3, 1e-4
@@ -508,8 +511,10 @@ def study_warmstart(gbturbo, tmp, cycles, n_test, n_train=256, mesh=(25, 25, 65)
         ok = np.nonzero((H[:, q, 1] <= 1e-6) & (H[:, q, 10] <= speedline.MASS_RATIO_LIMIT))[0]
         return int(ok[0]) + 1 if ok.size else None
 
-    # the judge: the plain FP64 solve's integrals at the cap, for points it converged
-    ref = {q: hist["fp64_batch_uniform"][-1, q] for q in range(n_test) if first_rule(hist["fp64_batch_uniform"], q)}
+    # the judge: the plain FP64 solve's integrals after twice the cap, for points it converged
+    # within the cap (so that they had as long again to settle)
+    ref = {q: hist["fp64_batch_uniform"][-1, q] for q in range(n_test)
+           if (first_rule(hist["fp64_batch_uniform"], q) or cycles + 1) <= cycles}
     out["fp64_batch_uniform"]["converged"] = len(ref)
 
     def first_within(H, q):
