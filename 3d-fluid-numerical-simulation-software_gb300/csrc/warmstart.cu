@@ -108,36 +108,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16])
 }
 
 // ---------------------------------------------------------------- operand staging
-// the transpose: cols x 64 cells, the cells of a row-major matrix X[cells x width] (row stride
-// ld) becoming the K dimension: core matrix (col/8, cell/8); each thread moves 8 x 8 blocks
-// through registers. Cells at or past cells_valid are zero.
-__device__ __forceinline__ void stage_cols_t(unsigned char *dst, const bf16 *src, long long ld, int col0, int cols,
-                                             long long cell0, long long cells_valid)
-{
-    const int nblk = (cols >> 3) * 8;                  // (col8, cell8) blocks, 64 cells = 8 cell groups
-    for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
-        const int a8 = b % (cols >> 3), c8 = b / (cols >> 3);
-        uint32_t x[8][4];
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-            const long long cell = cell0 + c8 * 8 + i;
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (cell < cells_valid) v = __ldg(reinterpret_cast<const uint4 *>(src + cell * ld + col0 + a8 * 8));
-            x[i][0] = v.x; x[i][1] = v.y; x[i][2] = v.z; x[i][3] = v.w;
-        }
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            const uint32_t sel = (j & 1) ? 0x7632u : 0x5410u;
-            uint4 w;
-            w.x = __byte_perm(x[0][j >> 1], x[1][j >> 1], sel);
-            w.y = __byte_perm(x[2][j >> 1], x[3][j >> 1], sel);
-            w.z = __byte_perm(x[4][j >> 1], x[5][j >> 1], sel);
-            w.w = __byte_perm(x[6][j >> 1], x[7][j >> 1], sel);
-            *reinterpret_cast<uint4 *>(dst + ((size_t)(a8 * 8 + c8) * 128 + j * 16)) = w;
-        }
-    }
-}
-
 __device__ __forceinline__ float sigmoidf_(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
 
 // ---------------------------------------------------------------- the row product
@@ -323,71 +293,101 @@ __global__ void __launch_bounds__(32 * (kEpiWarps + 2), 1) k_mlp_gemm(const __gr
 
 // ---------------------------------------------------------------- the weight gradient
 // part[(ay * gridDim.x + bx)][a][b] = sum over the CTA's cells of Xa[cell][128 ay + a] Xb[cell][b]
-// (a < 128, b < Nb); the cells (the product's K) in steps of 64.
+// (a < 128, b < Nb): the cells are the product's K. Both operands are MN-major: a TMA box of 8
+// features x 64 cells lands as 64 rows of 16 bytes, i.e. eight core matrices of the MN-major
+// no-swizzle layout stacked along K (128 bytes apart), the next 8 features one box (1024 bytes)
+// further. Warp 4 loads (4-stage ring), warp 5 issues the MMAs into one accumulator, warps 0-3
+// write it out once the CTA's cells are done.
 struct WgradArgs {
-    const bf16 *Xa; long long lda;
-    const bf16 *Xb; long long ldb;
     long long M; int Nb; long long chunk;
     float *part;
     int *err;
 };
 
-__global__ void __launch_bounds__(128, 1) k_mlp_wgrad(WgradArgs g)
+constexpr int kWgCells = 64;
+constexpr int kWgStageA = 128 * kWgCells * 2, kWgStageB = 256 * kWgCells * 2;
+
+__global__ void __launch_bounds__(192, 1) k_mlp_wgrad(const __grid_constant__ CUtensorMap tmA,
+                                                      const __grid_constant__ CUtensorMap tmB, WgradArgs g)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
-    unsigned char *As = sm;                                  // 128 x 64 cells
-    unsigned char *Bs = sm + 128 * 64 * 2;                   // Nb x 64 cells
-    unsigned char *tail = Bs + (size_t)g.Nb * 64 * 2;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(tail);
-    uint32_t *slot = reinterpret_cast<uint32_t *>(tail + 8);
+    unsigned char *ring = sm;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sm + kStages * (kWgStageA + kWgStageB));
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 2 * kStages + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t bar0 = smem_u32(bars);
+    auto full = [&](int s) { return bar0 + 8u * (uint32_t)s; };
+    auto empty = [&](int s) { return bar0 + 8u * (uint32_t)(kStages + s); };
+    const uint32_t accf = bar0 + 8u * (uint32_t)(2 * kStages);
     const uint32_t ncols = (uint32_t)tmem_cols(g.Nb);
-    if (warp == 0) tmem_alloc(smem_u32(slot), ncols);
-    if (threadIdx.x == 0) mbar_init(smem_u32(bar), 1);
+    if (warp == 4) tmem_alloc(smem_u32(slot), ncols);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; s++) { mbar_init(full(s), 1); mbar_init(empty(s), 1); }
+        mbar_init(accf, 1);
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *slot;
-    const uint32_t idesc = idesc_bf16(128, g.Nb);
     const long long c_begin = (long long)blockIdx.x * g.chunk;
-    const long long c_end = std::min(g.M, c_begin + g.chunk);
-    uint32_t phase = 0;
-    bool failed = false, any = false;
-    for (long long c0 = c_begin; c0 < c_end; c0 += 64) {
-        stage_cols_t(As, g.Xa, g.lda, blockIdx.y * 128, 128, c0, c_end);
-        stage_cols_t(Bs, g.Xb, g.ldb, 0, g.Nb, c0, c_end);
-        fence_proxy_async();
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            tc_fence_after();
-            for (int ks = 0; ks < 4; ks++)
-                mma_bf16(tmem, smem_desc(smem_u32(As) + ks * 256, 128, 1024), smem_desc(smem_u32(Bs) + ks * 256, 128, 1024),
-                         idesc, (any || ks > 0) ? 1u : 0u);
-            mma_commit(smem_u32(bar));
+    const long long c_end = c_begin + g.chunk < g.M ? c_begin + g.chunk : g.M;
+    const int nch = c_end > c_begin ? (int)((c_end - c_begin + kWgCells - 1) / kWgCells) : 0;
+    const int a0 = (int)blockIdx.y * 128;
+    bool failed = false;
+    if (warp == 4) {
+        if (lane == 0) {
+            const uint32_t bytes = (uint32_t)(16 + g.Nb / 8) * 1024u;
+            for (int it = 0; it < nch; it++) {
+                const int s = it % kStages;
+                if (!mbar_wait_bounded(empty(s), (uint32_t)(((it / kStages) & 1) ^ 1))) { failed = true; break; }
+                mbar_expect_tx(full(s), bytes);
+                const uint32_t a_s = smem_u32(ring + (size_t)s * (kWgStageA + kWgStageB));
+                const uint32_t b_s = a_s + kWgStageA;
+                const int y = (int)(c_begin + (long long)it * kWgCells);
+                for (int a8 = 0; a8 < 16; a8++) tma_load_2d(a_s + (uint32_t)a8 * 1024u, &tmA, a0 + a8 * 8, y, full(s));
+                for (int b8 = 0; b8 < g.Nb / 8; b8++) tma_load_2d(b_s + (uint32_t)b8 * 1024u, &tmB, b8 * 8, y, full(s));
+            }
         }
-        any = true;
-        const bool ok = mbar_wait_bounded(smem_u32(bar), phase);
-        phase ^= 1u;
-        tc_fence_after();
-        if (__syncthreads_or(!ok)) { failed = true; break; }
-    }
-    float *out = g.part + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * 128 * g.Nb;
-    const int a = warp * 32 + lane;
-    if (failed) {
-        if (threadIdx.x == 0) atomicOr(g.err, 1);
-        mbar_wait_bounded(smem_u32(bar), phase ^ 1u);
+    } else if (warp == 5) {
+        if (lane == 0 && nch > 0) {
+            // MN-major A and B (bits 15 and 16); in 16-byte units LBO = K step (128 B), SBO = MN step (1024 B)
+            const uint32_t idesc = idesc_bf16(128, g.Nb) | (1u << 15) | (1u << 16);
+            for (int it = 0; it < nch && !failed; it++) {
+                const int s = it % kStages;
+                if (!mbar_wait_bounded(full(s), (uint32_t)((it / kStages) & 1))) { failed = true; break; }
+                tc_fence_after();
+                const uint32_t a_s = smem_u32(ring + (size_t)s * (kWgStageA + kWgStageB));
+                const uint32_t b_s = a_s + kWgStageA;
+                for (int ks = 0; ks < kWgCells / 16; ks++)
+                    mma_bf16(tmem, smem_desc(a_s + (uint32_t)ks * 256u, 128u, 1024u), smem_desc(b_s + (uint32_t)ks * 256u, 128u, 1024u),
+                             idesc, (it > 0 || ks > 0) ? 1u : 0u);
+                mma_commit(empty(s));
+            }
+            if (!failed) mma_commit(accf);
+        }
     } else {
-        for (int c0 = 0; c0 < g.Nb; c0 += 16) {
-            float v[16];
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-#pragma unroll
-            for (int i = 0; i < 16; i++) out[(size_t)a * g.Nb + c0 + i] = any ? v[i] : 0.0f;
+        float *out = g.part + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * 128 * g.Nb;
+        const int a = warp * 32 + lane;
+        bool ok = true;
+        if (nch > 0) {
+            ok = mbar_wait_bounded(accf, 0u);
+            tc_fence_after();
         }
+        if (!ok) failed = true;
+        else
+            for (int c0 = 0; c0 < g.Nb; c0 += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+#pragma unroll
+                for (int i = 0; i < 16; i++) out[(size_t)a * g.Nb + c0 + i] = nch > 0 ? v[i] : 0.0f;
+            }
     }
+    if (failed) atomicOr(g.err, 1);
+    __syncwarp();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 0) tmem_dealloc(tmem, ncols);
+    if (warp == 4) tmem_dealloc(tmem, ncols);
 }
 
 // dst = scale * sum over the CTAs (fixed order); trans stores element (a, b) at b * Wa + a
@@ -747,8 +747,10 @@ struct WarmStart::Impl {
             part_n = need;
         }
         WgradArgs g{};
-        g.Xa = Xa; g.lda = lda; g.Xb = Xb; g.ldb = Nb; g.M = M; g.Nb = Nb; g.chunk = chunk; g.part = part; g.err = err;
-        k_mlp_wgrad<<<dim3(gx, gy), 128, kTcSmem, st>>>(g);
+        g.M = M; g.Nb = Nb; g.chunk = chunk; g.part = part; g.err = err;
+        const CUtensorMap ta = tensor_map_rows(Xa, M, Wa, lda, kWgCells);
+        const CUtensorMap tb = tensor_map_rows(Xb, M, Nb, Nb, kWgCells);
+        k_mlp_wgrad<<<dim3(gx, gy), 192, kTcSmem, st>>>(ta, tb, g);
         WCK(cudaGetLastError());
         k_wgrad_reduce<<<(Wa * Nb + 255) / 256, 256, 0, st>>>(part, gx, Wa, Nb, scale, trans, dst);
     }
