@@ -46,3 +46,23 @@ def test_case_reader_parity_with_oracle_options(meshgen, tmp_path, oracle_mod):
     o = oracle_mod.Oracle(str(tmp_path))
     assert o.dims(1)[3] == 2
     assert o.dims(2)[:3] == (9, 9, 33)
+
+
+def test_warm_start_entry_points_check_their_arguments_without_gpu(gbturbo):
+    """the gb_ws_* group and gb_start_from_fine_state reject null handles and buffers before any
+    CUDA call"""
+    L = gbturbo.load()
+    f = ctypes.POINTER(ctypes.c_float)
+    assert L.gb_ws_create(0, None) == -1
+    assert L.gb_ws_add_solves(None, None, None) == -1
+    assert L.gb_ws_train(None, 10, 1024, ctypes.c_float(1e-3), None) == -1
+    assert L.gb_ws_apply(None, None, None, None, None, None) == -1
+    assert L.gb_ws_get_params(None, None) == -1
+    assert L.gb_ws_set_norm(None, None) == -1
+    assert L.gb_ws_forward(None, None, 0, None) == -1
+    assert L.gb_ws_forward_backward(None, None, None, 0, None, None) == -1
+    assert L.gb_ws_benchmark(None, 1024, 1, None, None) == -1
+    assert L.gb_ws_samples(None) == -1
+    assert L.gb_start_from_fine_state(None) == -1
+    assert L.gb_ws_destroy(None) == 0
+    assert b"null" in L.gb_last_error()
