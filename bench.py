@@ -775,7 +775,10 @@ def run_gpu(args, rank, world, dist):
                 "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "alg_bytes_per_launch": bytes_per_launch,
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800 GB/s",
-                             "note": "FP64 on GB300 is bound by the FP64 pipe, not HBM" if prec == gbturbo.FP64 else ""},
+                             "note": ("FP64 on GB300 is bound by the FP64 pipe, not HBM: ncu sm__pipe_fp64_cycles_active "
+                                      "87% for the FP64 face flux (profiles/k_face_rotor129x49x49_fp64.md)")
+                                     if prec == gbturbo.FP64 and dom == "face_flux" else
+                                     ("FP64 on GB300 is bound by the FP64 pipe, not HBM" if prec == gbturbo.FP64 else "")},
                 "sweep_shape_cells_per_warp_warps_per_block": tuning,
                 "stages": stages,
                 "forms": forms,
