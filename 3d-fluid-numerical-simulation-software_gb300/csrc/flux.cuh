@@ -122,8 +122,22 @@ __device__ __forceinline__ C5<T> roe(T gamma, const C5<T> &QL, const C5<T> &QR, 
     const T delta = (T)0.5;
     T l1 = entropy_corr(tabs(una - ca), delta), l2 = entropy_corr(tabs(una), delta), l5 = entropy_corr(tabs(una + ca), delta);
     T dd = dR - dL, dmx = QR.mx - QL.mx, dmy = QR.my - QL.my, dmz = QR.mz - QL.mz, de = QR.e - QL.e;
-    T a2 = dmy / (va + (T)(double)1E-8f) - dd;
-    T a3 = dmz / (wa + (T)(double)1E-8f) - dd;
+    T a2, a3;
+    if constexpr (sizeof(T) == 8) {
+        a2 = dmy / (va + (T)(double)1E-8f) - dd;
+        a3 = dmz / (wa + (T)(double)1E-8f) - dd;
+    } else {
+        // mixed form: the FP32 round-off of a near-zero tangential velocity (about 1e-8 of the
+        // speed) is as large as the reference's 1e-8 regularisation, so v + 1e-8 can reach 0 and the
+        // wave strength infinity where FP64 round-off (1e-16) stays far from it; below half the
+        // regularisation the denominator is held there, sign kept (|v / den| <= 3 in that band)
+        const T eps = (T)(double)1E-8f, h = (T)0.5 * eps;
+        T d2 = va + eps, d3 = wa + eps;
+        if (tabs(d2) < h) d2 = d2 < (T)0 ? -h : h;
+        if (tabs(d3) < h) d3 = d3 < (T)0 ? -h : h;
+        a2 = dmy / d2 - dd;
+        a3 = dmz / d3 - dd;
+    }
     const T rca = (T)1 / ca;
     T a4 = g1 * (dd * (Ha - ua * ua - va * va - wa * wa) + ua * dmx + va * dmy + wa * dmz - de) * (rca * rca);
     T a1 = ((ua + ca) * dd - dmx - ca * a4) * ((T)0.5 * rca);
