@@ -440,12 +440,12 @@ def study_warmstart(gbturbo, tmp, cycles, n_test, n_train=256, mesh=(25, 25, 65)
       held out: n_test further points from the same sampler, run as one batch per form with every
         cycle's history: mixed from the uniform start and mixed from the network's field (with the
         residual-gated fallback) to the cycle cap; plain FP64 from the uniform start to twice the
-        cap (the judge: its integrals at the end, for the points it converged within the cap by
+        cap (the FP64 reference solve: its integrals at the end, for the points it converged within the cap by
         the reference's rule, density residual <= 1e-6 and mass ratio <= 0.003);
       per point: the first cycle meeting the reference's rule, and the first cycle from which the
-        inlet mass flow stays within 1e-3 and the pressure ratio within 1e-4 of the judge's;
+        inlet mass flow stays within 1e-3 and the pressure ratio within 1e-4 of the FP64 reference's;
       solves per hour: plain FP64 one solve at a time (a subsample, wall clock through the
-        speedline driver), and a batch that retires each point when it reaches the judge's
+        speedline driver), and a batch that retires each point when it reaches the FP64 reference's
         integrals, from the measured device time per batch cycle."""
     import meshgen as mg
     import speedline
@@ -484,11 +484,11 @@ def study_warmstart(gbturbo, tmp, cycles, n_test, n_train=256, mesh=(25, 25, 65)
 
     # the held-out points as one batch per form, every cycle's history kept
     hist = {}
-    judge_cycles = 2 * cycles
-    out["judge_cycles"] = judge_cycles
+    fp64_reference_cycles = 2 * cycles
+    out["fp64_reference_cycles"] = fp64_reference_cycles
     for name, prec, start, n_cyc in (("mixed_batch_uniform", gbturbo.MIXED, None, cycles),
                                      ("mixed_batch_warm", gbturbo.MIXED, warm, cycles),
-                                     ("fp64_batch_uniform", gbturbo.FP64, None, judge_cycles)):
+                                     ("fp64_batch_uniform", gbturbo.FP64, None, fp64_reference_cycles)):
         t0 = time.perf_counter()
         with gbturbo.Solver(dirs[te], prec) as s:
             t_create = time.perf_counter() - t0
@@ -511,7 +511,7 @@ def study_warmstart(gbturbo, tmp, cycles, n_test, n_train=256, mesh=(25, 25, 65)
         ok = np.nonzero((H[:, q, 1] <= 1e-6) & (H[:, q, 10] <= speedline.MASS_RATIO_LIMIT))[0]
         return int(ok[0]) + 1 if ok.size else None
 
-    # the judge: the plain FP64 solve's integrals after twice the cap, for points it converged
+    # the FP64 reference: the plain FP64 solve's integrals after twice the cap, for points it converged
     # within the cap (so that they had as long again to settle)
     ref = {q: hist["fp64_batch_uniform"][-1, q] for q in range(n_test)
            if (first_rule(hist["fp64_batch_uniform"], q) or cycles + 1) <= cycles}
