@@ -42,6 +42,7 @@ typedef struct {
     REAL totalvol;
     REAL *cv[NQ], *pv[NP], *mut, *omega, *lamc[3], *lamv[3], *dt;
     REAL *Ff[3][NQ], *Vf[3][NQ], *Fc[NQ], *Fv[NQ], *res[NQ];
+    REAL *Fdf[3][NQ], *Fd[NQ];                /* JST artificial dissipation: faces, cells */
     REAL *cvold[NQ], *dq[NQ];
     REAL *cv2h[NQ], *dq2h[NQ], *res2h[NQ], *qf2h[NQ];
     int *flag;
@@ -167,9 +168,10 @@ static int alloc_level(level_t *L, int IM, int JM, int KM)
         for (int c = 0; c < 3; c++) { L->fS[f][c] = alloc_arr(L); L->fc[f][c] = alloc_arr(L); }
         L->fs[f] = alloc_arr(L); L->fr[f] = alloc_arr(L); L->fth[f] = alloc_arr(L);
         for (int c = 0; c < 9; c++) L->fm[f][c] = alloc_arr(L);
-        for (int c = 0; c < NQ; c++) { L->Ff[f][c] = alloc_arr(L); L->Vf[f][c] = alloc_arr(L); }
+        for (int c = 0; c < NQ; c++) { L->Ff[f][c] = alloc_arr(L); L->Vf[f][c] = alloc_arr(L); L->Fdf[f][c] = alloc_arr(L); }
         L->lamc[f] = alloc_arr(L); L->lamv[f] = alloc_arr(L);
     }
+    for (int c = 0; c < NQ; c++) L->Fd[c] = alloc_arr(L);
     L->vol = alloc_arr(L);
     for (int c = 0; c < 3; c++) L->cc[c] = alloc_arr(L);
     for (int c = 0; c < 9; c++) L->cm[c] = alloc_arr(L);
@@ -193,9 +195,10 @@ static void free_level(level_t *L)
         for (int c = 0; c < 3; c++) { free(L->fS[f][c]); free(L->fc[f][c]); }
         free(L->fs[f]); free(L->fr[f]); free(L->fth[f]);
         for (int c = 0; c < 9; c++) free(L->fm[f][c]);
-        for (int c = 0; c < NQ; c++) { free(L->Ff[f][c]); free(L->Vf[f][c]); }
+        for (int c = 0; c < NQ; c++) { free(L->Ff[f][c]); free(L->Vf[f][c]); free(L->Fdf[f][c]); }
         free(L->lamc[f]); free(L->lamv[f]);
     }
+    for (int c = 0; c < NQ; c++) free(L->Fd[c]);
     free(L->vol);
     for (int c = 0; c < 3; c++) free(L->cc[c]);
     for (int c = 0; c < 9; c++) free(L->cm[c]);
@@ -271,7 +274,8 @@ static int read_config(orc_solver *s, const char *dir, char *grid, char *bcf, ch
 #undef RL
     fclose(r.f);
     s->ndummy = (s->recon == 0) ? 3 : 2;
-    if (s->scheme != 200 && s->scheme != 300) { seterr(err, el, "space scheme %d is not on this path (Roe 300, Steger-Warming 200)", s->scheme); return -1; }
+    if (s->scheme == 100) s->ndummy = 3;                            /* JST: UserInput.cpp:158-161 */
+    if (s->scheme != 100 && s->scheme != 200 && s->scheme != 300) { seterr(err, el, "space scheme %d is not on this path (JST 100, Roe 300, Steger-Warming 200)", s->scheme); return -1; }
     if (s->time_scheme >= 100 && s->time_scheme <= 400) { seterr(err, el, "Runge-Kutta marching is not on this path (LU-SGS only)"); return -1; }
     if (s->use_mg && s->coarse_iter < 1) { seterr(err, el, "multigrid needs at least one coarse-grid iteration (the fine level is initialised from it)"); return -1; }
     if (s->recon_var != 100 && s->recon_var != 200) { seterr(err, el, "reconstruction variables %d not supported", s->recon_var); return -1; }
@@ -1549,10 +1553,131 @@ static void wall_flux(orc_solver *s, level_t *L, const wall_t *w)
             }
 }
 
+/* source/JST_Convective.cpp:5-95: the central flux of every face from the average of the two
+ * cells' primitive variables (the first ghost layer at the block faces), in the block's frame */
+static void jst_convective(orc_solver *s, level_t *L)
+{
+    REAL Gamma = s->Gamma;
+    int IM = L->IM, JM = L->JM, KM = L->KM;
+    for (int f = 0; f < 3; f++) {
+        int ie = f == 0 ? IM : IM - 1, je = f == 1 ? JM : JM - 1, ke = f == 2 ? KM : KM - 1;
+        for (int i = 1; i <= ie; i++)
+            for (int j = 1; j <= je; j++)
+                for (int k = 1; k <= ke; k++) {
+                    size_t p = IX(L, i, j, k);
+                    size_t m = f == 0 ? IX(L, i - 1, j, k) : (f == 1 ? IX(L, i, j - 1, k) : IX(L, i, j, k - 1));
+                    vec_t S = fS(L, f, p);
+                    prim_t fp = p_scl(0.5f, p_add(ld_pv(L->pv, p), ld_pv(L->pv, m)));
+                    REAL fue = -1.0f * L->fc[f][1][p] * L->w_rot;
+                    REAL fve = L->fc[f][0][p] * L->w_rot;
+                    cons_t fc = {fp.d, fp.d * fp.u, fp.d * fp.v, fp.d * fp.w, 0.0};
+                    REAL Vn_a = fp.u * S.x + fp.v * S.y + fp.w * S.z;
+                    REAL Vn_e = fue * S.x + fve * S.y + 0.0f * S.z;
+                    fc.e = fp.p / (Gamma - 1.0f) + fp.d * (fp.u * fp.u + fp.v * fp.v + fp.w * fp.w) / 2.0f;
+                    L->Ff[f][0][p] = fc.d * (Vn_a - Vn_e);
+                    L->Ff[f][1][p] = fc.mx * (Vn_a - Vn_e) + fp.p * S.x;
+                    L->Ff[f][2][p] = fc.my * (Vn_a - Vn_e) + fp.p * S.y;
+                    L->Ff[f][3][p] = fc.mz * (Vn_a - Vn_e) + fp.p * S.z;
+                    L->Ff[f][4][p] = (fc.e + fp.p) * (Vn_a - Vn_e) + fp.p * Vn_e;
+                }
+    }
+}
+
+/* the JST pressure sensor |p(c+1) - 2 p(c) + p(c-1)| / (p(c+1) + 2 p(c) + p(c-1)) at position c
+ * along direction f of the line through (i, j, k) (source/JST_Dissip.cpp:5-194): positions at or
+ * below 0 and at or above N lie in the dummy layers (the remap of the reconstruction stencil). The
+ * range checks are the reference's, including its k-direction test of j against KM. */
+static REAL jst_sensor(const level_t *L, int f, int i, int j, int k)
+{
+    int IM = L->IM, JM = L->JM, KM = L->KM;
+    if (f == 0 && (j < 1 || j > JM || k < 1 || k > KM)) return 0.0;
+    if (f == 1 && (i < 1 || i > IM || k < 1 || k > KM)) return 0.0;
+    if (f == 2 && (i < 1 || i > IM || j < 1 || j > KM)) return 0.0;
+    int c = f == 0 ? i : (f == 1 ? j : k), N = f == 0 ? IM : (f == 1 ? JM : KM);
+    size_t q[3];
+    for (int o = -1; o <= 1; o++) {
+        int r = rmap(c + o, N);
+        q[o + 1] = f == 0 ? IX(L, r, j, k) : (f == 1 ? IX(L, i, r, k) : IX(L, i, j, r));
+    }
+    REAL PF = L->pv[PP][q[2]], PC = L->pv[PP][q[1]], PB = L->pv[PP][q[0]];
+    return fabs((PF - 2.0f * PC + PB) / (PF + 2.0f * PC + PB));
+}
+
+static REAL max4(REAL a, REAL b, REAL c, REAL d)
+{
+    REAL m = a;
+    if (b > m) m = b;
+    if (c > m) m = c;
+    if (d > m) m = d;
+    return m;
+}
+
+/* 1 + (lam_a / lam_n)^0.4 + (lam_b / lam_n)^0.4, the anisotropy weight of direction f; the two
+ * other directions in the reference's order (I: J, K; J: I, K; K: J, I) */
+static REAL jst_phi(const level_t *L, int f, size_t p)
+{
+    int a = f == 0 ? 1 : (f == 1 ? 0 : 1), b = f == 0 ? 2 : (f == 1 ? 2 : 0);
+    return 1.0f + pow_rt(L->lamc[a][p] / L->lamc[f][p], (double)0.4f) + pow_rt(L->lamc[b][p] / L->lamc[f][p], (double)0.4f);
+}
+
+/* source/JST_Dissip.cpp:196-423 and the cell sum :425-431 */
+static void jst_dissip(orc_solver *s, level_t *L)
+{
+    int IM = L->IM, JM = L->JM, KM = L->KM;
+    for (int f = 0; f < 3; f++) {
+        int ie = f == 0 ? IM : IM - 1, je = f == 1 ? JM : JM - 1, ke = f == 2 ? KM : KM - 1;
+        int N = f == 0 ? IM : (f == 1 ? JM : KM);
+        for (int i = 1; i <= ie; i++)
+            for (int j = 1; j <= je; j++)
+                for (int k = 1; k <= ke; k++) {
+                    int c = f == 0 ? i : (f == 1 ? j : k);
+                    size_t p = IX(L, i, j, k);
+                    size_t m = f == 0 ? IX(L, i - 1, j, k) : (f == 1 ? IX(L, i, j - 1, k) : IX(L, i, j, k - 1));
+                    REAL alpha;
+                    if (c == 1) alpha = jst_phi(L, f, p) * L->lamc[f][p];
+                    else if (c == N) alpha = jst_phi(L, f, m) * L->lamc[f][m];
+                    else {
+                        REAL VA_1 = jst_phi(L, f, p) * L->lamc[f][p];
+                        REAL VA_2 = jst_phi(L, f, m) * L->lamc[f][m];
+                        alpha = 0.5f * (VA_1 + VA_2);
+                    }
+                    REAL sn[4];
+                    for (int o = 1; o >= -2; o--) {
+                        int ii = f == 0 ? i + o : i, jj = f == 1 ? j + o : j, kk = f == 2 ? k + o : k;
+                        sn[1 - o] = jst_sensor(L, f, ii, jj, kk);
+                    }
+                    REAL eps2 = s->k2 * max4(sn[0], sn[1], sn[2], sn[3]);
+                    REAL eps4 = (0.0f > s->k4 - eps2) ? 0.0f : s->k4 - eps2;
+                    size_t q[4];                                  /* cv_1 .. cv_4: c+1, c, c-1, c-2 */
+                    for (int o = 1; o >= -2; o--) {
+                        int r = rmap(c + o, N);
+                        q[1 - o] = f == 0 ? IX(L, r, j, k) : (f == 1 ? IX(L, i, r, k) : IX(L, i, j, r));
+                    }
+                    cons_t c1 = ld_cv(L->cv, q[0]), c2 = ld_cv(L->cv, q[1]), c3 = ld_cv(L->cv, q[2]), c4 = ld_cv(L->cv, q[3]);
+                    cons_t d4 = c_sub(c_add(c_sub(c1, c_scl(c2, 3.0)), c_scl(c3, 3.0)), c4);
+                    cons_t fd = c_scl(c_sub(c_scl(c_sub(c2, c3), eps2), c_scl(d4, eps4)), alpha);
+                    st_cv(L->Fdf[f], p, fd);
+                }
+    }
+    for (int i = 1; i <= IM - 1; i++)
+        for (int j = 1; j <= JM - 1; j++)
+            for (int k = 1; k <= KM - 1; k++) {
+                size_t p = IX(L, i, j, k);
+                size_t q[3] = {IX(L, i + 1, j, k), IX(L, i, j + 1, k), IX(L, i, j, k + 1)};
+                cons_t a = c_sub(ld_cv(L->Fdf[0], q[0]), ld_cv(L->Fdf[0], p));
+                a = c_add(a, ld_cv(L->Fdf[1], q[1]));
+                a = c_sub(a, ld_cv(L->Fdf[1], p));
+                a = c_add(a, ld_cv(L->Fdf[2], q[2]));
+                a = c_sub(a, ld_cv(L->Fdf[2], p));
+                st_cv(L->Fd, p, a);
+            }
+}
+
 /* source/ComputeAllBlockVars.cpp:73-119 */
 static void convective_flux(orc_solver *s, level_t *L)
 {
-    upwind_convective(s, L);
+    if (s->scheme == 100) jst_convective(s, L);
+    else upwind_convective(s, L);
     for (int q = 1; q <= L->n_wall; q++) wall_flux(s, L, &L->wall[q]);
     REAL w_rot = L->w_rot;
     for (int i = 1; i <= L->IM - 1; i++)
@@ -1641,12 +1766,15 @@ static void resflux(orc_solver *s, level_t *L)
     if (s->equation_ns) viscous_flux(s, L);
     else
         for (int c = 0; c < NQ; c++) memset(L->Fv[c], 0, L->n * sizeof(REAL));
+    /* CMesh::Dissipation (:162-191): the JST dissipation, zero for the upwind schemes */
+    if (s->scheme == 100) jst_dissip(s, L);
+    else
+        for (int c = 0; c < NQ; c++) memset(L->Fd[c], 0, L->n * sizeof(REAL));
     for (int i = 1; i <= L->IM - 1; i++)
         for (int j = 1; j <= L->JM - 1; j++)
             for (int k = 1; k <= L->KM - 1; k++) {
                 size_t p = IX(L, i, j, k);
-                cons_t zero = {0.0, 0.0, 0.0, 0.0, 0.0};
-                st_cv(L->res, p, c_sub(c_sub(ld_cv(L->Fc, p), ld_cv(L->Fv, p)), zero));
+                st_cv(L->res, p, c_sub(c_sub(ld_cv(L->Fc, p), ld_cv(L->Fv, p)), ld_cv(L->Fd, p)));
             }
 }
 

@@ -15,7 +15,12 @@ def same(a, b):
     return np.array_equal(a, b, equal_nan=True)
 
 
-@pytest.mark.parametrize("name", GOLDEN_CASES)
+# the JST fixtures are checked here against the oracle's restatement of JST_Convective /
+# JST_Dissip; the GPU parity tests take them from the reference-only list
+JST_CASES = ["duct_9x9x17_jst", "rotor_9x9x33_jst_mg"]
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES + JST_CASES)
 def test_oracle_bitwise_against_reference(name, oracle_mod):
     g = load_golden(name)
     o = oracle_mod.Oracle(golden_dir(name))
@@ -32,7 +37,7 @@ def test_oracle_bitwise_against_reference(name, oracle_mod):
 
 
 def test_oracle_reports_bad_case(tmp_path, oracle_mod, meshgen):
-    case = meshgen.annular_duct(IM=9, JM=9, KM=17, options={"scheme": "100"})
+    case = meshgen.annular_duct(IM=9, JM=9, KM=17, options={"scheme": "400"})
     meshgen.write_case(case, str(tmp_path))
     with pytest.raises(RuntimeError, match="not on this path"):
         oracle_mod.Oracle(str(tmp_path))
