@@ -14,8 +14,8 @@ for p in (PKG, os.path.join(ROOT, "oracle")):
 
 GOLDEN_CASES = ["duct_9x9x17", "duct_9x9x17_sw_nnd", "duct_9x9x17_laminar_cons", "duct_9x9x17_muscl2u_global",
                 "rotor_9x9x33", "rotor_9x9x33_mg"]
-# fixtures of options the CPU oracle port does not restate (JST, Spalart-Allmaras): the GPU path is checked against
-# the reference's own outputs only
+# fixtures the GPU parity tests check against the reference's own outputs only: Spalart-Allmaras (not restated by the
+# CPU oracle) and JST (restated by the oracle, which test_oracle_golden checks against the same fixtures)
 REFERENCE_ONLY_CASES = ["duct_9x9x17_jst", "rotor_9x9x33_jst_mg", "duct_9x9x17_sa", "rotor_9x9x33_sa"]
 
 
