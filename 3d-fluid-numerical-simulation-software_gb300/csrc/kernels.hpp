@@ -13,10 +13,11 @@ struct LaunchCtx {
     int maxIM = 0, maxJM = 0, maxKM = 0;     // maxima over the solves of this level
     long long pool_n = 0;                     // elements of one field pool of this level
     // optional stage profiler: called before (begin = 1) and after (begin = 0) a group of
-    // launches with the group's name and the number of kernel launches in it
-    void (*hook)(void *user, const char *stage, int begin, int launches) = nullptr;
+    // launches with the group's name, the number of kernel launches in it and the grid level
+    void (*hook)(void *user, const char *stage, int begin, int launches, int level) = nullptr;
     void *hook_user = nullptr;
-    void mark(const char *stage, int begin, int launches = 1) const { if (hook) hook(hook_user, stage, begin, launches); }
+    int level = 0;                            // grid level of these launches (1 = fine)
+    void mark(const char *stage, int begin, int launches = 1) const { if (hook) hook(hook_user, stage, begin, launches, level); }
     dim3 grid_n(long long n, int bs) const { return dim3((unsigned)((n + bs - 1) / bs), batch.nsolve); }
     dim3 grid_cells(int bs) const { return grid_n((long long)(maxIM - 1) * (maxJM - 1) * (maxKM - 1), bs); }
     dim3 grid_faces(int f, int bs) const

@@ -338,9 +338,9 @@ void launch_lusgs_sweeps(const LaunchCtx &ctx, const PhysW<T> &P, const Geo &G, 
         launch_sa_sweep<T>(ctx, P, G, W, pt, S, -1);
         ctx.mark("sa_sweeps", 0, np - 2);
     }
-    ctx.mark("sweep_backward", 1, 1);
+    ctx.mark("sweep_scatter", 1, 1);
     k_sweep_scatter<T><<<gq, 256, 0, ctx.stream>>>(W, S, pt.nq);
-    ctx.mark("sweep_backward", 0, 1);
+    ctx.mark("sweep_scatter", 0, 1);
 }
 
 template <typename T>

@@ -15,7 +15,11 @@
 //    (two host threads, or two streams in flight at once) race on it and must be serialised by
 //    the caller;
 //  - the first call on a device looks the array's address up (cudaGetSymbolAddress, with that
-//    device current) and zeroes it; make that first call before any stream capture begins.
+//    device current) and zeroes it on the calling handle's stream; make that first call before any
+//    stream capture begins;
+//  - the address is kept per device for the life of the process: after cudaDeviceReset the kept
+//    address belongs to a context that no longer exists, so do not call this entry point again in a
+//    process that has reset the device.
 #include "../../include/gbturbo.h"
 #include "kernels.hpp"
 #include "solver.hpp"
@@ -38,8 +42,9 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 double *g_scratch_addr[kMaxDevices] = {};
 
-// Device address of g_norm_scratch on the current device, looked up (and zeroed) once per device.
-cudaError_t scratch_for_current_device(double **out)
+// Device address of g_norm_scratch on the current device, looked up (and zeroed on `stream`) once
+// per device.
+cudaError_t scratch_for_current_device(cudaStream_t stream, double **out)
 {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
@@ -50,7 +55,7 @@ cudaError_t scratch_for_current_device(double **out)
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_norm_scratch);
         if (e != cudaSuccess) return e;
-        e = cudaMemset(p, 0, sizeof(double) * kScratchDoubles);
+        e = cudaMemsetAsync(p, 0, sizeof(double) * kScratchDoubles, stream);
         if (e != cudaSuccess) return e;
         g_scratch_addr[dev] = (double *)p;
     }
@@ -125,12 +130,14 @@ void launch_res_norm_static(const LaunchCtx &ctx, const Geo &G, Flow<T> W, const
     const Batch &B = ctx.batch;
     if (B.nsolve > kMaxSolves) throw std::invalid_argument("batch larger than the static norm scratch");
     double *base = nullptr;
-    check_cuda(scratch_for_current_device(&base), "cudaGetSymbolAddress(g_norm_scratch)");
+    check_cuda(scratch_for_current_device(ctx.stream, &base), "cudaGetSymbolAddress(g_norm_scratch)");
     double *partials = base, *norms = base + kPartials;
     unsigned *arrivals = reinterpret_cast<unsigned *>(base + kPartials + kOut);
+    ctx.mark("res_norm_static", 1, 1);
     check_cuda(cudaMemsetAsync(arrivals, 0, sizeof(unsigned) * B.nsolve, ctx.stream), "cudaMemsetAsync");
     k_norm_onepass<T><<<dim3(kBlocks, B.nsolve), 256, 0, ctx.stream>>>(B, G, W, totalvol, partials, norms, arrivals);
     check_cuda(cudaGetLastError(), "k_norm_onepass launch");
+    ctx.mark("res_norm_static", 0, 1);
     if (host_out) {
         check_cuda(cudaMemcpyAsync(host_out, norms, sizeof(double) * 5 * ncase, cudaMemcpyDeviceToHost, ctx.stream),
                    "cudaMemcpyAsync");

@@ -8,11 +8,13 @@
 #include <cstring>
 #include <cstdio>
 #include <cstdlib>
+#include <array>
 #include <atomic>
 #include <chrono>
 #include <exception>
 #include <thread>
 #include <map>
+#include <array>
 #include <stdexcept>
 #include <algorithm>
 
@@ -322,7 +324,7 @@ public:
     cudaGraphExec_t graphs[3] = {nullptr, nullptr, nullptr};
 
     // ---- stage profiler
-    struct ProfRec { std::string stage; cudaEvent_t a, b; int launches; };
+    struct ProfRec { std::string stage; cudaEvent_t a, b; int launches, level; };
     bool profiling = false;
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_used = 0;
@@ -337,7 +339,7 @@ public:
         }
         return ev_pool[ev_used++];
     }
-    static void hook_fn(void *user, const char *stage, int begin, int launches)
+    static void hook_fn(void *user, const char *stage, int begin, int launches, int level)
     {
         SolverT *self = (SolverT *)user;
         cudaEvent_t e = self->next_event();
@@ -346,7 +348,7 @@ public:
         else {
             for (size_t q = self->open_marks.size(); q-- > 0;)
                 if (self->open_marks[q].first == stage) {
-                    self->prof.push_back({stage, self->open_marks[q].second, e, launches});
+                    self->prof.push_back({stage, self->open_marks[q].second, e, launches, level});
                     self->open_marks.erase(self->open_marks.begin() + q);
                     break;
                 }
@@ -366,25 +368,30 @@ public:
         profiling = false;
         std::vector<std::string> order;
         std::map<std::string, std::pair<double, long long>> tot;
+        // evaluations of the stage (bracketed groups of launches) on levels 1..3 (0: not level-bound)
+        std::map<std::string, std::array<long long, 4>> per_level;
         for (auto &r : prof) {
             float ms = 0;
             CK(cudaEventElapsedTime(&ms, r.a, r.b));
-            if (!tot.count(r.stage)) order.push_back(r.stage);
+            if (!tot.count(r.stage)) { order.push_back(r.stage); per_level[r.stage] = {0, 0, 0, 0}; }
             tot[r.stage].first += ms;
             tot[r.stage].second += r.launches;
+            per_level[r.stage][(r.level >= 0 && r.level <= 3) ? r.level : 0] += 1;
         }
         std::string out;
-        char buf[256];
+        char buf[320];
         for (auto &n : order) {
-            snprintf(buf, sizeof buf, "%s:%.6f:%lld;", n.c_str(), tot[n].first, tot[n].second);
+            const auto &pl = per_level[n];
+            snprintf(buf, sizeof buf, "%s:%.6f:%lld:%lld,%lld,%lld;", n.c_str(), tot[n].first, tot[n].second, pl[1], pl[2],
+                     pl[3]);
             out += buf;
         }
         return out;
     }
     struct Mark {
         const SolverT *s; const char *n; int l;
-        Mark(const SolverT *s_, const char *n_, int l_ = 1) : s(s_), n(n_), l(l_) { if (s->profiling) hook_fn((void *)s, n, 1, l); }
-        ~Mark() { if (s->profiling) hook_fn((void *)s, n, 0, l); }
+        Mark(const SolverT *s_, const char *n_, int l_ = 1) : s(s_), n(n_), l(l_) { if (s->profiling) hook_fn((void *)s, n, 1, l, 0); }
+        ~Mark() { if (s->profiling) hook_fn((void *)s, n, 0, l, 0); }
     };
 
     Batch batch(int l) const
@@ -397,6 +404,7 @@ public:
     {
         LaunchCtx c = lev[l].ctx(batch(l), stream);
         if (profiling) { c.hook = &SolverT::hook_fn; c.hook_user = (void *)this; }
+        c.level = l;
         return c;
     }
 

@@ -86,6 +86,7 @@ def load() -> ctypes.CDLL:
         "gb_profile_end": ([vp, ctypes.c_char_p, ip], ip),
         "gb_timer_start": ([vp], ip),
         "gb_timer_stop": ([vp, ctypes.POINTER(ctypes.c_float)], ip),
+        "gb_fp64_rate": ([dp], ip),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -105,7 +106,7 @@ EXPORTED = ["gb_solver_create", "gb_solver_destroy", "gb_last_error", "gb_dims",
             "gb_case_blocks", "gb_case_info", "gb_solver_create_levels", "gb_start_from_fine_state", "gb_ws_create", "gb_ws_destroy",
             "gb_ws_num_params", "gb_ws_add_solves", "gb_ws_samples", "gb_ws_train", "gb_ws_apply", "gb_ws_get_params",
             "gb_ws_set_params", "gb_ws_get_norm", "gb_ws_set_norm", "gb_ws_forward", "gb_ws_forward_backward",
-            "gb_ws_benchmark"]
+            "gb_ws_benchmark", "gb_fp64_rate"]
 
 
 class GBError(RuntimeError):
@@ -135,6 +136,17 @@ def case_info(case_dir: str, nodes: bool = False):
 
 def _dp(a: np.ndarray):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def fp64_rate() -> float:
+    """FP64 arithmetic rate of the current device in FLOP/s (two per FMA), measured by a device-timed
+    loop of independent FMA chains over every SM: the roof of the FP64 form's compute-bound kernels."""
+    L = load()
+    v = ctypes.c_double(0.0)
+    rc = L.gb_fp64_rate(ctypes.byref(v))
+    if rc != 0:
+        raise GBError(f"gb_fp64_rate failed ({rc})")
+    return float(v.value)
 
 
 FIELD_SHAPES = {
@@ -336,13 +348,14 @@ class Solver:
         self._ck(self._L.gb_profile_begin(self.h))
 
     def profile_end(self) -> dict:
+        """stage -> (device milliseconds, kernel launches, [evaluations on level 1, 2, 3])"""
         buf = ctypes.create_string_buffer(8192)
         self._ck(self._L.gb_profile_end(self.h, buf, 8192))
         out = {}
         for item in buf.value.decode().split(";"):
             if item:
-                name, ms, n = item.split(":")
-                out[name] = (float(ms), int(n))
+                name, ms, n, per_level = item.split(":")
+                out[name] = (float(ms), int(n), [int(v) for v in per_level.split(",")])
         return out
 
     def timer_start(self) -> None:

@@ -144,16 +144,35 @@ ALG = {
 }
 
 
-def alg_units_per_step(stage, level_dims):
-    """units of ALG[stage] processed in one multigrid cycle: each level's residual and sweeps run
-    once per cycle; level_dims holds the (IM, JM, KM) node counts of every level of every solve"""
+def alg_units_per_step(stage, slot_dims, evals, nprof):
+    """units of ALG[stage] processed per multigrid cycle: the stage profiler counts the stage's
+    evaluations on every level (a residual's three face families, one sweep over a level), and one
+    evaluation covers every slot of that level; slot_dims[l] holds the (IM, JM, KM) node counts of
+    level l + 1 of every slot"""
     n = 0
-    for I, J, K in level_dims:
-        if ALG[stage]["unit"] == "face":
-            n += I * (J - 1) * (K - 1) + (I - 1) * J * (K - 1) + (I - 1) * (J - 1) * K
-        else:
-            n += (I - 1) * (J - 1) * (K - 1)
-    return n
+    for l, dims in enumerate(slot_dims):
+        per_eval = 0
+        for I, J, K in dims:
+            if ALG[stage]["unit"] == "face":
+                per_eval += I * (J - 1) * (K - 1) + (I - 1) * J * (K - 1) + (I - 1) * (J - 1) * K
+            else:
+                per_eval += (I - 1) * (J - 1) * (K - 1)
+        n += per_eval * evals[l]
+    return n / nprof
+
+
+def fp64_ops_per_unit():
+    """FP64 operations (2 x DFMA + DMUL + DADD thread instructions, counted by ncu) per unit of a
+    stage of the FP64 form, from profiles/fp64_ops_per_unit.txt"""
+    out = {}
+    try:
+        for line in open(os.path.join(ROOT, "profiles", "fp64_ops_per_unit.txt")):
+            f = line.split()
+            if len(f) >= 3 and not line.startswith("#"):
+                out[f[0]] = float(f[2])
+    except FileNotFoundError:
+        pass
+    return out
 
 
 def alg_bytes_per_unit(stage, wsize):
@@ -234,9 +253,9 @@ def allmax(dist, x):
 # CPU arms
 # ---------------------------------------------------------------------------------------------
 def _oracle_worker(args):
-    case_dir, warm, steps = args
+    case_dir, warm, steps, fp32 = args
     import pyoracle
-    o = pyoracle.Oracle(case_dir)
+    o = pyoracle.Oracle(case_dir, fp32=fp32)
     for _ in range(warm):
         o.iterate()
     t0 = time.perf_counter()
@@ -245,14 +264,15 @@ def _oracle_worker(args):
     return time.perf_counter() - t0
 
 
-def cpu_baseline(case_dir, cells, warm, steps):
-    """the oracle port, one thread, bounded sample of the same workload"""
+def cpu_baseline(case_dir, cells, warm, steps, fp32=False):
+    """the oracle port, one thread, bounded sample of the same workload; fp32: the reference's
+    default FP32 build of the path (REAL = float), beside the GPU's mixed form"""
     import pyoracle
     pyoracle.build()
-    t = _oracle_worker((case_dir, warm, steps))
+    t = _oracle_worker((case_dir, warm, steps, fp32))
     return {"value": cells * steps / t, "unit": "cell-updates/s", "cores": 1, "kind": "port",
             "sample": f"{steps} multigrid cycles of one {cells}-cell passage after {warm} untimed iterations, "
-                      f"CPU oracle (single thread, FP64)"}
+                      f"CPU oracle (single thread, {'FP32: the reference FP32 build' if fp32 else 'FP64'})"}
 
 
 def run_reference(args, rank, world, dist):
@@ -261,6 +281,7 @@ def run_reference(args, rank, world, dist):
     import pyoracle
     pyoracle.build()
     cores = os.cpu_count() or 1
+    fp32 = args.precision == "mixed"             # the reference's default FP32 build beside the mixed form
     tmp = tempfile.mkdtemp(prefix="gbt_ref_")
     try:
         dirs, cells = make_cases(tmp, 1)
@@ -268,17 +289,18 @@ def run_reference(args, rank, world, dist):
         warm = max(args.warmup, 3)
         ctx = mp.get_context("spawn")
         with ctx.Pool(cores) as pool:
-            times = pool.map(_oracle_worker, [(dirs[0], warm, steps)] * cores)
+            times = pool.map(_oracle_worker, [(dirs[0], warm, steps, fp32)] * cores)
         t = max(times)
         value = cores * cells * steps / t
         line = {
             "impl": "reference", "metric": "cell_updates_per_s", "value": value, "unit": "cell-updates/s",
             "n_gpus": args.gpus, "steps": steps, "warmup": warm, "ms_per_step": 1000.0 * t / steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_block(args, cells, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32" if fp32 else "f64",
+            "data": "synthetic", "config": config_block(args, cells, 1),
             "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": cores, "kind": "port",
                              "sample": f"{cores} independent single-thread CPU solves (the reference's CPU path "
-                                       f"restated in C), {steps} multigrid cycles each after {warm} untimed"},
+                                       f"restated in C, {'FP32 build' if fp32 else 'FP64 build'}), {steps} multigrid "
+                                       f"cycles each after {warm} untimed"},
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
         print(json.dumps(line), flush=True)
@@ -707,15 +729,16 @@ def run_gpu(args, rank, world, dist):
         s.profile_begin()
         s.iterate(nprof, history=False)
         prof = s.profile_end()
-        level_dims = [s.dims(q, l)[:3] for q in range(s.n_slots) for l in range(1, s.ng + 1)]
+        slot_dims = [[s.dims(q, l)[:3] for q in range(s.n_slots)] for l in range(1, s.ng + 1)]
         tuning = {f"level{l}": list(s.sweep_tuning(l)) for l in range(1, s.ng + 1)}
         total_prof = sum(v[0] for v in prof.values())
         launches_per_step = sum(v[1] for v in prof.values()) / nprof
         dom = max((k for k in prof if k in ALG), key=lambda k: prof[k][0])
-        dom_ms, dom_launches = prof[dom]
+        dom_ms, dom_launches, dom_evals = prof[dom]
+        units_step = alg_units_per_step(dom, slot_dims, dom_evals, nprof)
         # algorithmic bytes of the stage per cycle / its device time per cycle (events around the
         # stage's launches, eager); per launch = per cycle / launches per cycle
-        bytes_per_step = alg_units_per_step(dom, level_dims) * alg_bytes_per_unit(dom, wsize)
+        bytes_per_step = units_step * alg_bytes_per_unit(dom, wsize)
         achieved = bytes_per_step / (dom_ms / nprof / 1000.0) / 1e9
         bytes_per_launch = bytes_per_step / (dom_launches / nprof)
         peaks = {}
@@ -732,6 +755,23 @@ def run_gpu(args, rank, world, dist):
                     traffic = float(f[3])        # DRAM read + write bytes per launch (ncu), same averaging
         except FileNotFoundError:
             pass
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "traffic": traffic, "alg_bytes_per_launch": bytes_per_launch,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800 GB/s"}
+        flops_unit = fp64_ops_per_unit().get(dom) if prec == gbturbo.FP64 else None
+        if flops_unit is not None:
+            # the FP64 form is bound by the FP64 pipe: counted FP64 operations of the stage (ncu, per
+            # face or plane cell) over its device time, against the FP64 rate measured in this run
+            rate = gbturbo.fp64_rate() / 1e12
+            flop_step = units_step * flops_unit
+            tf = flop_step / (dom_ms / nprof / 1000.0) / 1e12
+            roofline = {"bound": "fp64", "kernel": dom, "achieved": tf, "peak": rate, "unit": "TFLOP/s",
+                        "frac": tf / rate, "traffic": traffic, "flop_per_launch": flop_step / (dom_launches / nprof),
+                        "flop_per_unit": flops_unit,
+                        "peak_source": "FP64 FMA-chain loop timed in this run (gb_fp64_rate); "
+                                       "MEASURED_PEAKS.json holds no FP64 figure",
+                        "hbm": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                                "alg_bytes_per_launch": bytes_per_launch}}
         forms = None
         if (rank == 0 and world == 1 and not args.no_forms and prec == gbturbo.FP64 and nsolve == 1 and args.blocks == 1
                 and args.variant == "default" and args.levels == 2):
@@ -757,7 +797,7 @@ def run_gpu(args, rank, world, dist):
         base = None
         if rank == 0 and not args.no_cpu_baseline and args.blocks == 1 and args.variant == "default" and args.levels == 2:
             # (the CPU oracle port is single-block)
-            base = cpu_baseline(dirs[0], cells, warm=3, steps=2)
+            base = cpu_baseline(dirs[0], cells, warm=3, steps=2, fp32=prec == gbturbo.MIXED)
 
         if rank == 0:
             stages = {k: {"ms_per_step": round(v[0] / nprof, 4), "launches_per_step": round(v[1] / nprof, 1),
@@ -772,13 +812,7 @@ def run_gpu(args, rank, world, dist):
                 "e2e": {"value": e2e_value, "unit": "cell-updates/s",
                         "h2d_bytes_per_step": int(grid_bytes / n_e2e), "d2h_bytes_per_step": 96 * nsolve},
                 "gpu_launches": int(round(launches_per_step * args.steps)),
-                "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": traffic, "alg_bytes_per_launch": bytes_per_launch,
-                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800 GB/s",
-                             "note": ("FP64 on GB300 is bound by the FP64 pipe, not HBM: ncu sm__pipe_fp64_cycles_active "
-                                      "87% for the FP64 face flux (profiles/k_face_rotor129x49x49_fp64.md)")
-                                     if prec == gbturbo.FP64 and dom == "face_flux" else
-                                     ("FP64 on GB300 is bound by the FP64 pipe, not HBM" if prec == gbturbo.FP64 else "")},
+                "roofline": roofline,
                 "sweep_shape_cells_per_warp_warps_per_block": tuning,
                 "stages": stages,
                 "forms": forms,

@@ -131,13 +131,20 @@ int gb_sweep_tuning(gb_solver *h, int level, int out[2]);
 int gb_set_graphs(gb_solver *h, int enable);
 /* stage profiler: between the two calls iterations run without graphs and every stage of the
  * path is bracketed by CUDA events on the handle's stream; gb_profile_end writes
- * "stage:milliseconds:kernel launches;..." totals into buf */
+ * "stage:milliseconds:kernel launches:evaluations on level 1,2,3;..." totals into buf (an
+ * evaluation is one bracketed group of the stage's launches, e.g. the three face families of one
+ * residual, or one sweep over every plane of a level) */
 int gb_profile_begin(gb_solver *h);
 int gb_profile_end(gb_solver *h, char *buf, int buflen);
 /* device time of everything enqueued between the two calls, in milliseconds (events on the
  * handle's stream) */
 int gb_timer_start(gb_solver *h);
 int gb_timer_stop(gb_solver *h, float *ms);
+/* FP64 arithmetic rate of the current device in FLOP/s (two per FMA), from a device-timed loop of
+ * independent FMA chains over every SM (best of five launches, about 0.1 s). No counterpart in the
+ * reference: it is the roof against which the FP64 form's face-flux and sweep kernels are
+ * reported, since on this GPU they are bound by the FP64 pipe rather than by HBM. */
+int gb_fp64_rate(double *flop_per_s);
 
 /* Residual norm of gb_res_calculate (same arguments, same values in out and in the solve states)
  * computed with no allocation on success: its scratch is a static device array of fixed size
@@ -147,6 +154,8 @@ int gb_timer_stop(gb_solver *h, float *ms);
  * GB_NOALLOC_MAX_SOLVES slots (blocks of all solves) are rejected with GB_ERR_ARG. All calls on a device share the one
  * array, so calls that overlap in time race and must be serialised by the caller. The first call
  * on a device looks the array up and zeroes it: make that call before any stream capture begins.
+ * The looked-up address is kept for the life of the process, so do not call it again after a
+ * cudaDeviceReset of that device.
  * Call it with the handle's device current. */
 #define GB_NOALLOC_MAX_SOLVES 128
 int gb_res_calculate_noalloc(gb_solver *h, int level, double *out);

@@ -7,11 +7,20 @@
 # (GCC rejects its firstprivate loop variables). source/TimeStep.cpp is UTF-16 and is
 # converted into the output directory before compiling. Runs with NT=1 only.
 #
-#   oracle/build_ref.sh [REF_ROOT]     (default REF_ROOT=/root/reference)
+#   oracle/build_ref.sh [REF_ROOT]
+#
+# REF_ROOT is the reference checkout (the argument, else the REF_ROOT environment variable, else a
+# directory named "reference" beside this repository). FP32=1 builds the reference's default FP32
+# build (REAL = float) into oracle/_ref32 instead.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${REF_ROOT:-$HERE/../../reference}}"
 OUT="$HERE/_ref"
+PREC="-DSINGLE"
+if [ "${FP32:-0}" = "1" ]; then
+  OUT="$HERE/_ref32"
+  PREC=""
+fi
 if [ ! -d "$REF/source" ]; then
   echo "reference sources not found at $REF (the oracle/_ref build only runs where they exist)" >&2
   exit 3
@@ -19,7 +28,7 @@ fi
 mkdir -p "$OUT/obj"
 iconv -f UTF-16 -t UTF-8 "$REF/source/TimeStep.cpp" > "$OUT/TimeStep_utf8.cpp"
 CXX="${CXX:-g++}"
-FLAGS="-std=c++17 -O2 -fpermissive -w -DSINGLE -D_finite=finite -D_isnan=isnan -ffp-contract=off -I$REF/include"
+FLAGS="-std=c++17 -O2 -fpermissive -w $PREC -D_finite=finite -D_isnan=isnan -ffp-contract=off -I$REF/include"
 pids=()
 for src in "$REF"/source/*.cpp "$OUT/TimeStep_utf8.cpp"; do
   base="$(basename "$src" .cpp)"

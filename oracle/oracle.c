@@ -20,7 +20,16 @@
 #define NQ 5
 #define NP 6
 enum { PD = 0, PU, PV, PW, PP, PT };       /* TPrimVars order: dens uvel vvel wvel press temp */
+/* The reference's REAL is float unless SINGLE is defined (include/defs.h:28-54). The default build
+ * here is its FP64 build (the parity form); ORC_FP32 gives its default FP32 build, used only as the
+ * CPU timing beside the GPU's mixed form (not pinned bit for bit). */
+#ifdef ORC_FP32
+typedef float REAL;
+#define RSCAN "%f"
+#else
 typedef double REAL;
+#define RSCAN "%lf"
+#endif
 #define MAXV(a, b) (((a) > (b)) ? (a) : (b))
 #define MINV(a, b) (((a) < (b)) ? (a) : (b))
 #define PIF 3.1415926535897932f           /* include/defs.h:204 (float literal) */
@@ -239,7 +248,7 @@ static int read_config(orc_solver *s, const char *dir, char *grid, char *bcf, ch
     RL(); s->Len_ref = stof_(b);
     RL(); s->ev_ratio = stof_(b);
     RL(); s->inlet_dir.x = s->inlet_dir.y = s->inlet_dir.z = 0;
-    sscanf(b, "%lf %lf %lf", &s->inlet_dir.x, &s->inlet_dir.y, &s->inlet_dir.z);
+    sscanf(b, RSCAN " " RSCAN " " RSCAN, &s->inlet_dir.x, &s->inlet_dir.y, &s->inlet_dir.z);
     RL();                                                           /* outlet angle */
     RL();                                                           /* mass flow imposed */
     RL();
@@ -404,7 +413,7 @@ static int read_grid(orc_solver *s, const char *dir, const char *grid, int IMb, 
             for (int i = 1; i <= IM; i++) {
                 if (!read_line(&r, b, sizeof b)) { seterr(err, el, "grid file ended early"); fclose(r.f); return -1; }
                 size_t p = IX(L, i, j, k);
-                if (sscanf(b, "%lf %lf %lf", &L->x[p], &L->y[p], &L->z[p]) != 3) { seterr(err, el, "bad grid line"); fclose(r.f); return -1; }
+                if (sscanf(b, RSCAN " " RSCAN " " RSCAN, &L->x[p], &L->y[p], &L->z[p]) != 3) { seterr(err, el, "bad grid line"); fclose(r.f); return -1; }
             }
     fclose(r.f);
     return 0;

@@ -14,21 +14,22 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
-_lib: Optional[ctypes.CDLL] = None
+# the reference's default FP32 build of the path (REAL = float): CPU timing beside the mixed form
+LIB32_PATH = os.path.join(HERE, "_build", "liboracle32.so")
+_libs: Dict[bool, ctypes.CDLL] = {}
 
 
 def build(force: bool = False) -> str:
     src = os.path.join(HERE, "oracle.c")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+    if force or any(not os.path.exists(p) or os.path.getmtime(p) < os.path.getmtime(src) for p in (LIB_PATH, LIB32_PATH)):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 
 
-def lib() -> ctypes.CDLL:
-    global _lib
-    if _lib is None:
+def lib(fp32: bool = False) -> ctypes.CDLL:
+    if fp32 not in _libs:
         build()
-        L = ctypes.CDLL(LIB_PATH)
+        L = ctypes.CDLL(LIB32_PATH if fp32 else LIB_PATH)
         L.orc_open.restype = ctypes.c_void_p
         L.orc_open.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int]
         L.orc_close.argtypes = [ctypes.c_void_p]
@@ -43,8 +44,8 @@ def lib() -> ctypes.CDLL:
         L.orc_set_cv.restype = ctypes.c_int
         L.orc_cfl.argtypes = [ctypes.c_void_p]
         L.orc_cfl.restype = ctypes.c_double
-        _lib = L
-    return _lib
+        _libs[fp32] = L
+    return _libs[fp32]
 
 
 SHAPES = {
@@ -72,8 +73,8 @@ for _d, _f in (("I", lambda I, J, K: (2, J - 1, K - 1)), ("J", lambda I, J, K: (
 class Oracle:
     """One CPU solve of a case directory (config.dat + grid + BoundaryDefinition.dat)."""
 
-    def __init__(self, case_dir: str):
-        self._L = lib()
+    def __init__(self, case_dir: str, fp32: bool = False):
+        self._L = lib(fp32)
         err = ctypes.create_string_buffer(512)
         h = self._L.orc_open(case_dir.encode(), err, 512)
         if not h:

@@ -9,8 +9,9 @@ evaluation at that state (every intermediate array) in tests/golden/<name>.npz.
 Only runs where the reference sources and a C++ compiler exist; the fixtures it writes are
 committed so the tests need neither.
 
-    python tests/golden/make_golden.py [name ...]      (default: every short case, the restart case and
-                                                        the multi-block and stage cases; long cases by name)
+    python tests/golden/make_golden.py [name ...]      (default: every short case, the restart case,
+                                                        the multi-block and stage cases and the FP32-build
+                                                        histories; long cases by name)
 """
 from __future__ import annotations
 
@@ -87,6 +88,15 @@ STAGE = {
 RESTART = {
     "rotor_9x9x33_restart": ("rotor_passage", dict(IM=9, JM=9, KM=33), {}, 10, 10),
 }
+
+# the reference's default FP32 build (REAL = float; oracle/_ref32, FP32=1 oracle/build_ref.sh):
+# driver history only, on the case directory of an FP64 fixture. It pins the oracle's FP32 build,
+# which is the CPU timing beside the GPU's mixed form, to FP32 round-off (not bit for bit).
+FP32_RUNS = {
+    "duct_9x9x17_fp32": ("duct_9x9x17", 20),
+    "rotor_9x9x33_mg_fp32": ("rotor_9x9x33_mg", 14),
+}
+HARNESS32 = os.path.join(ROOT, "oracle", "_ref32", "ref_harness")
 
 KEEP_R = ["cv", "pv", "mut", "ev", "res_ev", "omega", "lamcI", "lamcJ", "lamcK", "lamvI", "lamvJ", "lamvK", "dt", "FcI", "FcJ",
           "FcK", "FvI", "FvJ", "FvK", "res", "dIS_pv", "dIP_pv", "dJS_pv", "dJP_pv", "dKS_pv", "dKP_pv", "dIS_cv",
@@ -169,7 +179,22 @@ def make_multi(name: str) -> None:
     print(name, "iterations:", int(data["history"].shape[0]))
 
 
+def make_fp32(name: str) -> None:
+    src, n_iter = FP32_RUNS[name]
+    with tempfile.TemporaryDirectory() as tmp:
+        for f in os.listdir(os.path.join(HERE, src)):
+            shutil.copy(os.path.join(HERE, src, f), tmp)
+        out = os.path.join(tmp, "out")
+        subprocess.run([HARNESS32, str(n_iter), out, "0"], cwd=tmp, check=True, stdout=subprocess.DEVNULL)
+        hist = np.load(os.path.join(out, "history.npy"))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), history=hist, case=np.array(src))
+    print(name, "iterations:", int(hist.shape[0]))
+
+
 def make(name: str) -> None:
+    if name in FP32_RUNS:
+        make_fp32(name)
+        return
     if name in MULTI or name in STAGE:
         make_multi(name)
         return
@@ -211,5 +236,5 @@ def make(name: str) -> None:
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: oracle/build_ref.sh")
-    for n in (sys.argv[1:] or list(CASES) + list(RESTART) + list(MULTI) + list(STAGE)):
+    for n in (sys.argv[1:] or list(CASES) + list(RESTART) + list(MULTI) + list(STAGE) + list(FP32_RUNS)):
         make(n)

@@ -12,7 +12,7 @@ from conftest import PKG, ROOT
 
 def declared():
     txt = open(os.path.join(ROOT, "include", "gbturbo.h")).read()
-    return sorted(set(re.findall(r"\b(gb_[a-z_]+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(gb_[a-z0-9_]+)\s*\(", txt)))
 
 
 def test_header_declares_expected_entry_points(gbturbo):

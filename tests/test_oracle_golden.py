@@ -41,3 +41,17 @@ def test_oracle_reports_bad_case(tmp_path, oracle_mod, meshgen):
     meshgen.write_case(case, str(tmp_path))
     with pytest.raises(RuntimeError, match="not on this path"):
         oracle_mod.Oracle(str(tmp_path))
+
+
+# The oracle's FP32 build (REAL = float) against the reference's own FP32 build: the same operations
+# in single precision, so the histories agree to FP32 round-off, not bit for bit (the oracle calls
+# the double libm functions where the reference's C++ picks the float overloads). It is the CPU
+# timing beside the GPU's mixed form; the tolerance is a few hundred FP32 ulps over the run.
+@pytest.mark.parametrize("name", ["duct_9x9x17_fp32", "rotor_9x9x33_mg_fp32"])
+def test_oracle_fp32_build_tracks_the_reference_fp32_build(name, oracle_mod):
+    g = np.load(golden_dir(name) + ".npz")
+    hist = g["history"]
+    mine = oracle_mod.Oracle(golden_dir(str(g["case"])), fp32=True).run(hist.shape[0])
+    cols = [1, 6, 7, 8]                         # Res.dens, m_in, m_out, PR
+    rel = np.abs(mine[:, cols] - hist[:, cols]) / np.abs(hist[:, cols])
+    assert rel.max() < 2e-5, rel.max(axis=0)

@@ -24,6 +24,11 @@ def _close(a, b):
     ("duct_9x9x17", "FP64", 1, 1),
     ("rotor_9x9x33_mg", "FP64", 2, 2),
     ("rotor_9x9x33_mg", "MIXED", 3, 1),
+    # multi-block cases: the blocks of a case count their arrivals on its first slot, and the last
+    # block to arrive folds the partials of every block of the case
+    ("rotor_9x9x33_3block", "FP64", 1, 1),
+    ("rotor_9x9x33_3block", "MIXED", 2, 1),
+    ("rotor_9x9x33_3block_mg", "FP64", 2, 2),
 ])
 def test_noalloc_norm_matches_res_calculate(gpu_lib, name, precision, dirs, level):
     with gpu_lib.Solver([golden_dir(name)] * dirs, getattr(gpu_lib, precision)) as s:
