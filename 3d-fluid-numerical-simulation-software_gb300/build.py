@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbturbo.so")
 SOURCES = ["geometry.cu", "bc.cu", "resflux_cell.cu", "resflux_face.cu", "lusgs.cu", "mg.cu", "solver.cu",
-           "capi.cu", "case_io.cpp", "noalloc.cu", "restart_io.cpp", "sa.cu", "warmstart.cu", "peak.cu"]
+           "capi.cu", "case_io.cpp", "noalloc.cu", "restart_io.cpp", "sa.cu", "warmstart.cu", "peak.cu", "face_tma.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

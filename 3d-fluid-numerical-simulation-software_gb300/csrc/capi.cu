@@ -261,6 +261,14 @@ int gb_sweep_tuning(gb_solver *h, int level, int out[2])
     return GB_OK;
 }
 
+int gb_face_staging(gb_solver *h, int level, int *tma)
+{
+    NEED(h); LEVEL(h, level);
+    if (!tma) { g_err = "null buffer"; return GB_ERR_ARG; }
+    *tma = h->s->face_staged(level) ? 1 : 0;
+    return GB_OK;
+}
+
 int gb_set_graphs(gb_solver *h, int enable) { NEED(h); h->s->use_graphs = enable != 0; return GB_OK; }
 
 int gb_timer_start(gb_solver *h)

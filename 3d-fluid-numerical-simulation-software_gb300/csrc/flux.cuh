@@ -48,8 +48,8 @@ __device__ __forceinline__ void recon1(int type, T eta, T FF, T F, T B, T BB, T 
         R = B - ((T)0.5 * f) * (B - F);
     } else if (type == 500) {               // MUSCL3 with the smooth (van Albada-type) limiter
         T a = F - FF, b = B - F, c = BB - B;
-        T SL = ((T)2 * a * b + eps) / (a * a + b * b + eps);
-        T SR = ((T)2 * c * b + eps) / (c * c + b * b + eps);
+        T SL = fdiv<T>((T)2 * a * b + eps, a * a + b * b + eps);
+        T SR = fdiv<T>((T)2 * c * b + eps, c * c + b * b + eps);
         // S/3 as a product with 1/3 (the FP64 divide is the costly instruction here; within rounding)
         const T third = (T)(1.0 / 3.0);
         const T sl3 = SL * third, sr3 = SR * third;
@@ -60,7 +60,7 @@ __device__ __forceinline__ void recon1(int type, T eta, T FF, T F, T B, T BB, T 
 
 // primitive reconstruction + positivity fallback + conversion to conserved variables
 template <typename T>
-__device__ __forceinline__ void recon_prim(int type, T gamma, const P6<T> &FF, const P6<T> &F, const P6<T> &B,
+__device__ __forceinline__ void recon_prim(int type, T rgm1, const P6<T> &FF, const P6<T> &F, const P6<T> &B,
                                            const P6<T> &BB, C5<T> &cl, C5<T> &cr)
 {
     const T eta = (T)(double)0.2f, lz = (T)(double)1E-20f;
@@ -72,7 +72,6 @@ __device__ __forceinline__ void recon_prim(int type, T gamma, const P6<T> &FF, c
     recon1(type, eta, FF.p, F.p, B.p, BB.p, l.p, r.p);
     if (l.d <= lz || l.p <= lz) l = F;
     if (r.d <= lz || r.p <= lz) r = B;
-    const T rgm1 = (T)1 / (gamma - (T)1);
     cl.d = l.d; cl.mx = l.d * l.u; cl.my = l.d * l.v; cl.mz = l.d * l.w;
     cl.e = l.p * rgm1 + l.d * (l.u * l.u + l.v * l.v + l.w * l.w) * (T)0.5;
     cr.d = r.d; cr.mx = r.d * r.u; cr.my = r.d * r.v; cr.mz = r.d * r.w;
@@ -106,26 +105,26 @@ __device__ __forceinline__ C5<T> roe(T gamma, const C5<T> &QL, const C5<T> &QR, 
 {
     const T g1 = gamma - (T)1;
     // divisions by the densities as products with their reciprocals (within rounding)
-    T dL = QL.d, rdL = (T)1 / dL, uL = QL.mx * rdL, vL = QL.my * rdL, wL = QL.mz * rdL, EL = QL.e * rdL;
+    T dL = QL.d, rdL = frcp<T>(dL), uL = QL.mx * rdL, vL = QL.my * rdL, wL = QL.mz * rdL, EL = QL.e * rdL;
     T pL = g1 * dL * (EL - (T)0.5 * (uL * uL + vL * vL + wL * wL));
     T HL = EL + pL * rdL;
-    T dR = QR.d, rdR = (T)1 / dR, uR = QR.mx * rdR, vR = QR.my * rdR, wR = QR.mz * rdR, ER = QR.e * rdR;
+    T dR = QR.d, rdR = frcp<T>(dR), uR = QR.mx * rdR, vR = QR.my * rdR, wR = QR.mz * rdR, ER = QR.e * rdR;
     T pR = g1 * dR * (ER - (T)0.5 * (uR * uR + vR * vR + wR * wR));
     T HR = ER + pR * rdR;
     T unL = uL - qe, unR = uR - qe;
-    T tmp = tsqrt(dR * rdL);
-    T inv = (T)1 / ((T)1 + tmp);
+    T tmp = fsqrt<T>(dR * rdL);
+    T inv = frcp<T>((T)1 + tmp);
     T ua = (uL + tmp * uR) * inv, va = (vL + tmp * vR) * inv, wa = (wL + tmp * wR) * inv, Ha = (HL + tmp * HR) * inv;
     T q2 = ua * ua + va * va + wa * wa;
-    T ca = tsqrt(g1 * (Ha - (T)0.5 * q2));
+    T ca = fsqrt<T>(g1 * (Ha - (T)0.5 * q2));
     T una = ua - qe;
     const T delta = (T)0.5;
     T l1 = entropy_corr(tabs(una - ca), delta), l2 = entropy_corr(tabs(una), delta), l5 = entropy_corr(tabs(una + ca), delta);
     T dd = dR - dL, dmx = QR.mx - QL.mx, dmy = QR.my - QL.my, dmz = QR.mz - QL.mz, de = QR.e - QL.e;
     T a2, a3;
     if constexpr (sizeof(T) == 8) {
-        a2 = dmy / (va + (T)(double)1E-8f) - dd;
-        a3 = dmz / (wa + (T)(double)1E-8f) - dd;
+        a2 = fdiv<T>(dmy, va + (T)(double)1E-8f) - dd;
+        a3 = fdiv<T>(dmz, wa + (T)(double)1E-8f) - dd;
     } else {
         // mixed form: the FP32 round-off of a near-zero tangential velocity (about 1e-8 of the
         // speed) is as large as the reference's 1e-8 regularisation, so v + 1e-8 can reach 0 and the
@@ -135,10 +134,10 @@ __device__ __forceinline__ C5<T> roe(T gamma, const C5<T> &QL, const C5<T> &QR, 
         T d2 = va + eps, d3 = wa + eps;
         if (tabs(d2) < h) d2 = d2 < (T)0 ? -h : h;
         if (tabs(d3) < h) d3 = d3 < (T)0 ? -h : h;
-        a2 = dmy / d2 - dd;
-        a3 = dmz / d3 - dd;
+        a2 = fdiv<T>(dmy, d2) - dd;
+        a3 = fdiv<T>(dmz, d3) - dd;
     }
-    const T rca = (T)1 / ca;
+    const T rca = frcp<T>(ca);
     T a4 = g1 * (dd * (Ha - ua * ua - va * va - wa * wa) + ua * dmx + va * dmy + wa * dmz - de) * (rca * rca);
     T a1 = ((ua + ca) * dd - dmx - ca * a4) * ((T)0.5 * rca);
     T a5 = dd - (a1 + a4);

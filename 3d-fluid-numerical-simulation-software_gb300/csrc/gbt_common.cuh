@@ -134,6 +134,9 @@ struct GeoW {
 template <typename T>
 struct PhysW {
     T gamma, gm1, rgas, pr_lam, pr_tur, c_timestep, relax, inv_re, suth_c1, suth_c2;
+    // formed once in FP64 on the host: 1 / (gamma - 1) and the conductivity factors
+    // gamma R / (gamma - 1) / Pr of the laminar and turbulent parts
+    T rgm1, cond_lam, cond_tur;
 };
 
 template <typename T>
@@ -150,6 +153,10 @@ inline PhysW<T> phys_working(const Phys &P)
     w.inv_re = (T)(1.0 / P.re_ref);
     w.suth_c1 = (T)P.suth_c1;
     w.suth_c2 = (T)P.suth_c2;
+    const double g1 = (double)w.gamma - 1.0, cp = (double)w.gamma * (double)w.rgas / g1;
+    w.rgm1 = (T)(1.0 / g1);
+    w.cond_lam = (T)(cp / (double)w.pr_lam);
+    w.cond_tur = (T)(cp / (double)w.pr_tur);
     return w;
 }
 
@@ -158,11 +165,66 @@ enum {
     GBT_STATUS_NAN = 1,          // a residual norm or an integral is not finite
     GBT_STATUS_LIMITER = 2,      // the positivity limiter replaced cells in the last step
     GBT_STATUS_LIMITER_OVF = 4,  // more limited cells than the list holds (processed by a full scan)
+    GBT_STATUS_WAIT_TIMEOUT = 8, // a kernel's bounded wait for its own asynchronous copies ran out
 };
 
 template <typename T> __device__ __forceinline__ T tsqrt(T x);
 template <> __device__ __forceinline__ double tsqrt<double>(double x) { return sqrt(x); }
 template <> __device__ __forceinline__ float tsqrt<float>(float x) { return sqrtf(x); }
+
+// Reciprocal, quotient and square root for the FP64 form's compute-bound kernels. GB300 runs FP64
+// at about 1/64 of its FP32 rate and every FP64 instruction (add, multiply, FMA) holds the pipe
+// equally long, so the IEEE-rounded division and root (a hardware approximation followed by a long
+// refinement and correction) are among the costliest steps of the face flux. These forms keep the
+// hardware approximation and refine it by Newton-Raphson iteration (the textbook method; see
+// e.g. P. Markstein, "Computation of elementary functions on the IBM RISC System/6000 processor",
+// IBM J. Res. Dev. 34(1), 1990), to within two units in the last place of the IEEE results
+// (checked against them by gb_fp64_arith_check):
+//   1/b: r0 from rcp.approx.ftz.f64, e = 1 - b r0, then the third-order step r1 = r0 + r0 (e + e^2),
+//        whose relative error is about e^3 -- three FMAs;
+//   sqrt(x): y0 from rsqrt.approx.ftz.f64, s0 = x y0, then two Heron steps s <- s + (x - s^2) y0 / 2
+//        with the approximate 1/(2 sqrt x) held fixed -- one multiply and four FMAs.
+// The FP32 (mixed) form, whose results are held to FP32-level tolerances against the FP64 solve,
+// takes the hardware approximations themselves (rcp.approx.ftz.f32, sqrt.approx.ftz.f32: a
+// relative error of a few units in the last place, one instruction each, where the IEEE forms take
+// a refinement sequence and a slow-path test). The arguments here are positive normal numbers
+// (densities, sums of squares plus a regularisation, speeds of sound, temperatures) or regularised
+// quotients; like the IEEE forms, 1/0 gives a non-finite value.
+__device__ __forceinline__ double rcp_nr(double b)
+{
+    double r0;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r0) : "d"(b));
+    const double e = fma(-b, r0, 1.0);
+    return fma(fma(e, e, e), r0, r0);
+}
+__device__ __forceinline__ double sqrt_nr(double x)
+{
+    double y0;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y0) : "d"(x));
+    const double h = 0.5 * y0;
+    double s = x * y0;
+    s = fma(fma(-s, s, x), h, s);
+    return fma(fma(-s, s, x), h, s);
+}
+template <typename T> __device__ __forceinline__ T frcp(T b);
+template <> __device__ __forceinline__ double frcp<double>(double b) { return rcp_nr(b); }
+template <> __device__ __forceinline__ float frcp<float>(float b)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
+    return r;
+}
+template <typename T> __device__ __forceinline__ T fdiv(T a, T b);
+template <> __device__ __forceinline__ double fdiv<double>(double a, double b) { return a * rcp_nr(b); }
+template <> __device__ __forceinline__ float fdiv<float>(float a, float b) { return a * frcp<float>(b); }
+template <typename T> __device__ __forceinline__ T fsqrt(T x);
+template <> __device__ __forceinline__ double fsqrt<double>(double x) { return sqrt_nr(x); }
+template <> __device__ __forceinline__ float fsqrt<float>(float x)
+{
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 
 // Sutherland law of the reference (include/FluidProps.h:107-112); T^1.5 as T*sqrt(T).
 // |(o - c) / o| for the residual norm: the reciprocal of o is seeded by an FP32 division and
@@ -192,6 +254,13 @@ template <typename T>
 __device__ __forceinline__ T sutherland(const PhysW<T> &P, T temp)
 {
     return P.inv_re * (temp * tsqrt(temp)) * P.suth_c1 / (temp + P.suth_c2);
+}
+
+// the face flux's evaluation, with the FP64 form's refined root and quotient
+template <typename T>
+__device__ __forceinline__ T sutherland_face(const PhysW<T> &P, T temp)
+{
+    return fdiv<T>(P.inv_re * (temp * fsqrt<T>(temp)) * P.suth_c1, temp + P.suth_c2);
 }
 
 template <typename T>

@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
                 // evaluation of the path is; the 2000-iteration efficiency is sensitive to how the
                 // compiler contracts these products, so the expressions stay where they were pinned
                 const T po = S.pp[nb];
-                const T oinv = (T)1 / od;
+                const T oinv = frcp<T>(od);
                 const T Vo = omx * oinv * nx + omy * oinv * ny + omz * oinv * nz;
                 const T dov = Vo - ve;
                 fo[0] = od * dov;
@@ -71,9 +71,9 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
         }
         if (d == 0) {
             if constexpr (sizeof(T) == 8) {
-                alpha = S.gvol[q] / S.dt[q] + P.relax * (S.lamc[0][q] + S.lamc[1][q] + S.lamc[2][q]) +
+                alpha = fdiv<T>(S.gvol[q], S.dt[q]) + P.relax * (S.lamc[0][q] + S.lamc[1][q] + S.lamc[2][q]) +
                         (T)2 * (S.lamv[0][q] + S.lamv[1][q] + S.lamv[2][q]);
-                inva = (T)1 / alpha;
+                inva = frcp<T>(alpha);
             } else {
                 inva = S.ainv[q];
                 alpha = S.alpha[q];
@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
         T pn, dn;
         if constexpr (sizeof(T) == 8) {
             // FP64 (parity) form: the reference's sequence, u = m_x / rho, ...
-            const T inv = (T)1 / nd;
+            const T inv = frcp<T>(nd);
             const T u = nmx * inv, v = nmy * inv, w = nmz * inv, E = ne * inv;
             pn = P.gm1 * nd * (E - (T)0.5 * (u * u + v * v + w * w));
             dn = (u * nx + v * ny + w * nz) - ve;
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
             // density is computed, so that only V_n = (m.n)/rho and p = (g-1)(rho E - |m|^2/(2 rho))
             // follow it on the plane-to-plane critical path (the same quantities, regrouped)
             const T mn = nmx * nx + nmy * ny + nmz * nz, m2 = nmx * nmx + nmy * nmy + nmz * nmz;
-            const T inv = (T)1 / nd;
+            const T inv = frcp<T>(nd);
             pn = P.gm1 * (ne - (T)0.5 * (m2 * inv));
             dn = mn * inv - ve;
         }

@@ -2,7 +2,10 @@
 // sweep kernels are bound by the FP64 pipe rather than by HBM. Each thread runs eight independent
 // chains of dependent FMAs (x = x * a + b, |a| < 1, so the values stay bounded); the grid covers
 // every SM several times over, so the FP64 pipe, not latency, sets the rate. Two FLOPs per FMA.
+// Also here: a device check of the FP64 form's Newton-refined reciprocal, quotient and square root
+// against the IEEE operations.
 #include "../../include/gbturbo.h"
+#include "gbt_common.cuh"
 #include <cuda_runtime.h>
 
 namespace {
@@ -62,5 +65,45 @@ extern "C" int gb_fp64_rate(double *flop_per_s)
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     if (out) cudaFree(out);
+    return rc;
+}
+
+// ---- the FP64 form's reciprocal, quotient and square root against the IEEE operations ----
+namespace {
+
+__global__ void k_arith(int op, const double *__restrict__ x, const double *__restrict__ y, long long n, double *out)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const double a = x[t], b = y[t];
+    double v;
+    switch (op) {
+    case 0: v = gbt::fdiv<double>(a, b); break;
+    case 1: v = gbt::fsqrt<double>(a); break;
+    case 2: v = gbt::frcp<double>(a); break;
+    case 3: v = a / b; break;
+    default: v = sqrt(a); break;
+    }
+    out[t] = v;
+}
+
+}  // namespace
+
+extern "C" int gb_fp64_arith_check(int op, const double *x, const double *y, long long n, double *out)
+{
+    if (op < 0 || op > 4 || !x || !out || n < 1 || ((op == 0 || op == 3) && !y)) return GB_ERR_ARG;
+    double *d = nullptr;
+    const size_t bytes = sizeof(double) * (size_t)n;
+    if (cudaMalloc(&d, 3 * bytes) != cudaSuccess) return GB_ERR_CUDA;
+    int rc = GB_OK;
+    if (cudaMemcpy(d, x, bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(d + n, y ? y : x, bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+        rc = GB_ERR_CUDA;
+    } else {
+        k_arith<<<(unsigned)((n + 255) / 256), 256>>>(op, d, d + n, n, d + 2 * n);
+        if (cudaGetLastError() != cudaSuccess || cudaMemcpy(out, d + 2 * n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = GB_ERR_CUDA;
+    }
+    cudaFree(d);
     return rc;
 }

@@ -61,6 +61,7 @@ struct Level {
     Geo G{};
     GeoW<T> GW{};                         // working-precision geometry (aliases in FP64, FP32 copies in mixed)
     DevBuf geow_mem;
+    DevBuf tma_mem;                       // tensor maps of the TMA-staged face stage (mixed form)
     DevBuf fd_mem;                        // JST face dissipation
     DevBuf sa_mem, sa_tab_mem;            // Spalart-Allmaras fields; its tables
     DevBuf wdist_mem;                     // Baldwin-Lomax wall distances (fine level)
@@ -81,6 +82,7 @@ struct Level {
         c.stream = s;
         c.maxIM = maxIM; c.maxJM = maxJM; c.maxKM = maxKM;
         c.pool_n = pool_n;
+        c.face_tma = tma_mem.p;
         return c;
     }
 };
@@ -784,6 +786,10 @@ public:
             for (int c = 0; c < 2; c++) W.cc[c] = take();
             for (int c = 0; c < 9; c++) W.cm[c] = take();
             launch_geometry_working(ctx(l), G, W);
+            if constexpr (sizeof(T) == 4) {
+                // the face stage's tiles staged by TMA where every box row is 16-byte aligned
+                if (face_tma_eligible(Lv.lv)) Lv.tma_mem.p = build_face_tma(Lv.lv, W, Lv.W, &Lv.tma_mem.bytes);
+            }
         }
     }
 
@@ -1146,6 +1152,10 @@ public:
     }
     void res_calculate(int l) override { launch_res_norm<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, norm_part, norm_blk); }
     void sweep_shape(int l, int out[2]) const override { out[0] = lev[l].planes.cpw; out[1] = lev[l].planes.wpb; }
+    bool face_staged(int l) const override
+    {
+        return lev[l].tma_mem.p != nullptr && P.recon_var == 200 && P.recon == 500 && P.scheme == 300;
+    }
     void res_calculate_static(int l, double *host_out) override
     {
         launch_res_norm_static<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, ncase, host_out);

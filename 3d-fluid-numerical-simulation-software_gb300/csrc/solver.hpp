@@ -80,6 +80,8 @@ public:
     virtual void set_use_force(int level, bool on) = 0;
     // block shape the sweep autotuner chose for a level: cells per warp, warps per block
     virtual void sweep_shape(int level, int out[2]) const = 0;
+    // whether a level's face stage runs on tiles staged in shared memory by TMA (mixed form)
+    virtual bool face_staged(int level) const = 0;
     // stage profiler: while on, iterations run eagerly and every stage is bracketed by events
     virtual void profile_begin() = 0;
     // "stage:milliseconds:launches;..." totals since profile_begin

@@ -82,11 +82,13 @@ def load() -> ctypes.CDLL:
         "gb_write_solution": ([vp, ip, ctypes.c_char_p], ip),
         "gb_set_graphs": ([vp, ip], ip),
         "gb_sweep_tuning": ([vp, ip, ctypes.POINTER(ip)], ip),
+        "gb_face_staging": ([vp, ip, ctypes.POINTER(ip)], ip),
         "gb_profile_begin": ([vp], ip),
         "gb_profile_end": ([vp, ctypes.c_char_p, ip], ip),
         "gb_timer_start": ([vp], ip),
         "gb_timer_stop": ([vp, ctypes.POINTER(ctypes.c_float)], ip),
         "gb_fp64_rate": ([dp], ip),
+        "gb_fp64_arith_check": ([ip, dp, dp, ctypes.c_longlong, dp], ip),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -106,7 +108,7 @@ EXPORTED = ["gb_solver_create", "gb_solver_destroy", "gb_last_error", "gb_dims",
             "gb_case_blocks", "gb_case_info", "gb_solver_create_levels", "gb_start_from_fine_state", "gb_ws_create", "gb_ws_destroy",
             "gb_ws_num_params", "gb_ws_add_solves", "gb_ws_samples", "gb_ws_train", "gb_ws_apply", "gb_ws_get_params",
             "gb_ws_set_params", "gb_ws_get_norm", "gb_ws_set_norm", "gb_ws_forward", "gb_ws_forward_backward",
-            "gb_ws_benchmark", "gb_fp64_rate"]
+            "gb_ws_benchmark", "gb_fp64_rate", "gb_fp64_arith_check", "gb_face_staging"]
 
 
 class GBError(RuntimeError):
@@ -147,6 +149,19 @@ def fp64_rate() -> float:
     if rc != 0:
         raise GBError(f"gb_fp64_rate failed ({rc})")
     return float(v.value)
+
+
+def fp64_arith_check(op: int, x: np.ndarray, y: Optional[np.ndarray] = None) -> np.ndarray:
+    """the device's FP64 arithmetic on host arrays: op 0 x / y, 1 sqrt(x), 2 1 / x as the FP64 form's
+    kernels compute them (Newton-refined), 3 and 4 the IEEE x / y and sqrt(x)"""
+    L = load()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    yy = None if y is None else np.ascontiguousarray(y, dtype=np.float64)
+    out = np.empty_like(x)
+    rc = L.gb_fp64_arith_check(op, _dp(x), None if yy is None else _dp(yy), x.size, _dp(out))
+    if rc != 0:
+        raise GBError(f"gb_fp64_arith_check failed ({rc})")
+    return out
 
 
 FIELD_SHAPES = {
@@ -340,6 +355,13 @@ class Solver:
         v = (ctypes.c_int * 2)()
         self._ck(self._L.gb_sweep_tuning(self.h, level, v))
         return int(v[0]), int(v[1])
+
+    def face_staging(self, level: int = 1) -> bool:
+        """True when the level's face stage runs on TMA-staged tiles (the mixed form's default scheme
+        on meshes with KM = 4n + 1 >= 33)"""
+        v = ctypes.c_int(0)
+        self._ck(self._L.gb_face_staging(self.h, level, ctypes.byref(v)))
+        return bool(v.value)
 
     def set_graphs(self, on: bool) -> None:
         self._ck(self._L.gb_set_graphs(self.h, int(on)))

@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--blocks", type=int, default=1, choices=[1, 3],
                     help="3: the passage as three blocks joined by interfaces (reference's rotor-67 layout)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-solves", action="store_true",
+                    help="skip the converged-solves-per-hour measurement of the default line (about a minute)")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the secondary measurements of the mixed-precision and batched forms")
     ap.add_argument("--study", choices=["precision", "solves", "multigrid", "warmstart", "network"],
@@ -130,17 +132,19 @@ def _write_sampled_case(job):
 
 
 # ---------------------------------------------------------------------------------------------
-# algorithmic bytes per kernel launch (each input/output element counted once; "geo" and "cv"
-# are FP64 in both forms, "w" is the working precision). unit: "cell" (fine cells), "face"
-# (faces of one family, about one per cell), "plane_cell" (cells of one hyperplane)
+# algorithmic bytes per kernel launch: each input/output element counted once, at the width the
+# kernel reads it ("w": the working precision, 8 B in FP64, 4 B in the mixed form, whose face and
+# sweep kernels read FP32 copies of the geometry; "int": 4 B). unit: "face" (faces of one family,
+# about one per cell), "plane_cell" (cells of one hyperplane)
 # ---------------------------------------------------------------------------------------------
 ALG = {
-    # S(3) s nrm(3) t1(3) t2(3) qe metrics(9) = 23 geo; prim 6 + mu_t 1 of one cell; 10 fluxes out
-    "face_flux": {"unit": "face", "geo": 23, "cv": 0, "w": 17, "int": 1},
-    # vol dt lamc(3) lamv(3) + res or dq (5) + neighbour cv(5) dq(5) p(1) + mean normal(3) area
-    # entrainment, per direction amortised to one cell: cn 9 cs 3 cve 3; dq out 5
-    "sweep_forward": {"unit": "plane_cell", "geo": 16, "cv": 5, "w": 24, "int": 0},
-    "sweep_backward": {"unit": "plane_cell", "geo": 16, "cv": 5, "w": 24, "int": 0},
+    # S(3) s nrm(3) t1(3) t2(3) qe metrics(9) = 23 geometry; prim 6 + mu_t 1 of one cell; 10 fluxes
+    # out; the wall flag
+    "face_flux": {"unit": "face", "w": 40, "int": 1},
+    # plane-order copies: vol dt lamc(3) lamv(3) + res or dq (5) + neighbour cv(5) dq(5) p(1) + mean
+    # normal(3) area entrainment, per direction amortised to one cell: cn 9 cs 3 cve 3; dq out 5
+    "sweep_forward": {"unit": "plane_cell", "w": 45, "int": 0},
+    "sweep_backward": {"unit": "plane_cell", "w": 45, "int": 0},
 }
 
 
@@ -177,7 +181,7 @@ def fp64_ops_per_unit():
 
 def alg_bytes_per_unit(stage, wsize):
     a = ALG[stage]
-    return 8 * a["geo"] + 8 * a["cv"] + wsize * a["w"] + 4 * a["int"]
+    return wsize * a["w"] + 4 * a["int"]
 
 
 class ClockSampler:
@@ -449,6 +453,103 @@ def study_solves(gbturbo, tmp, cycles, npoints):
                                           "batch's mean fine-cell count"}
     out["batched_mixed_over_plain_fp64_solves_per_hour"] = (out["mixed_batch_sampled"]["solves_per_hour"] /
                                                            out["fp64_single_sampled"]["solves_per_hour"])
+    return out
+
+
+def measure_solves(gbturbo, tmp, n_train=64, n_test=32, train_cycles=600, steps=3000, cap=2500, n_fp64=4,
+                   mesh=(25, 25, 65), seed=2024, batch=32768):
+    """Converged solves per hour, end to end through the public API, on a stand-in for the batched
+    configuration: the seeded operating-point sampler (back pressure U[1.05, 1.30] x p_t, speed
+    {0.8, 0.9, 1.0} x 16000 rpm, stagger offset N(0, 1 deg)) on one 25 x 25 x 65 mesh of the blade
+    family, where the uniform start converges (the full-size passages stall first). A point is
+    converged at the first cycle that meets the reference's rule (density residual <= 1e-6 and
+    |m_in - m_out| / m_in <= 0.003, source/Structured_FV3D.cpp:214), else it stops at the cap.
+      batched mixed, uniform start: the n_test held-out points as one batch until all converged or
+        the cap (case files read, geometry, cycles with the history read back every 100);
+      batched mixed, learned warm start: the same batch from the network's field (residual-gated
+        fallback to the uniform start), with the training data (n_train further points as one mixed
+        batch, train_cycles cycles) and the training (steps Adam steps) charged to its time;
+      plain FP64, one solve at a time from the uniform start, on n_fp64 held-out points (the
+        lowest, highest and evenly spaced back pressures between), each until its rule or the cap.
+    solves/hour = converged points / wall hours. For the subsample points the plain FP64 solve
+    converged, each batch form's integrals at its own convergence are compared with the FP64 solve's
+    (inlet mass flow within 0.1%, pressure ratio within 1e-4)."""
+    import meshgen as mg
+    import speedline
+    ops = mg.sample_operating_points(n_train + n_test, seed)
+    for op in ops:
+        op["IM"], op["JM"], op["KM"] = mesh
+    jobs = [(os.path.join(tmp, f"sv{q}"), op) for q, op in enumerate(ops)]
+    with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
+        cells = pool.map(_write_sampled_case, jobs)
+    dirs = [d for d, _ in jobs]
+    prm = [[op["pb"], op["rpm"] / 16000.0, op["stagger_offset"]] for op in ops]
+    tr, te = slice(0, n_train), slice(n_train, n_train + n_test)
+    tol = 1e-6
+    out = {"workload": "stand-in for the batched configuration: sampled operating points on one 25x25x65 mesh "
+                       "of the rotor blade family (36,864 cells)",
+           "held_out_points": n_test, "train_points": n_train, "train_cycles": train_cycles, "train_steps": steps,
+           "cycle_cap": cap, "tol": tol, "mass_ratio_limit": speedline.MASS_RATIO_LIMIT}
+
+    t0 = time.perf_counter()
+    table_u = speedline.run(dirs[te], gbturbo.MIXED, max_iter=cap, chunk=100, tol=tol)
+    t_u = time.perf_counter() - t0
+
+    t0 = time.perf_counter()
+    w = gbturbo.WarmStart(seed=7)
+    with gbturbo.Solver(dirs[tr], gbturbo.MIXED) as s:
+        s.init_uniform()
+        s.iterate(train_cycles, history=False)
+        w.add_solves(s, prm[tr])
+    for k in range(steps // 500):
+        w.train(500, batch=batch, lr=1e-3 if k < (steps // 500) * 3 // 4 else 3e-4)
+    t_train = time.perf_counter() - t0
+    kept = []
+
+    def warm(s):
+        used, _, _ = w.apply(s, prm[te])
+        kept.append(int(np.sum(used)))
+
+    t0 = time.perf_counter()
+    table_w = speedline.run(dirs[te], gbturbo.MIXED, max_iter=cap, chunk=100, tol=tol, start=warm)
+    t_w = time.perf_counter() - t0 + t_train
+    w.close()
+
+    order = sorted(range(n_test), key=lambda q: prm[n_train + q][0])
+    sub = sorted({order[round(i * (n_test - 1) / max(n_fp64 - 1, 1))] for i in range(n_fp64)})
+    t_f, rows_f = 0.0, {}
+    for q in sub:
+        t0 = time.perf_counter()
+        rows_f[q] = speedline.run([dirs[n_train + q]], gbturbo.FP64, max_iter=cap, chunk=100, tol=tol)[0]
+        t_f += time.perf_counter() - t0
+
+    def agree(table):
+        n = 0
+        for q, r in rows_f.items():
+            if r["converged"] and table[q]["converged"]:
+                n += (abs(table[q]["m_in"] - r["m_in"]) <= 1e-3 * abs(r["m_in"]) and
+                      abs(table[q]["pressure_ratio"] - r["pressure_ratio"]) <= 1e-4)
+        return int(n)
+
+    conv_f = sum(1 for r in rows_f.values() if r["converged"])
+    f_sph = 3600.0 * conv_f / t_f
+    for name, table, t in (("batched_mixed_uniform", table_u, t_u), ("batched_mixed_warm", table_w, t_w)):
+        conv = sum(1 for r in table if r["converged"])
+        out[name] = {"wall_s": round(t, 2), "converged": conv, "solves_per_hour": 3600.0 * conv / t,
+                     "median_cycles_converged": float(np.median([r["iteration"] for r in table if r["converged"]]))
+                     if conv else None,
+                     "agree_with_fp64_on_subsample": agree(table)}
+    out["batched_mixed_warm"]["train_s"] = round(t_train, 2)
+    out["batched_mixed_warm"]["network_field_kept"] = kept[0] if kept else 0
+    out["plain_fp64_one_at_a_time"] = {"subsample": [n_train + q for q in sub], "wall_s": round(t_f, 2),
+                                       "converged": conv_f, "solves_per_hour": f_sph,
+                                       "cycles": [rows_f[q]["iteration"] for q in sub],
+                                       "back_pressure_ratios": [round(prm[n_train + q][0], 4) for q in sub]}
+    out["fp64_subsample_converged"] = conv_f
+    for name in ("batched_mixed_uniform", "batched_mixed_warm"):
+        out[name]["ratio_vs_plain_fp64"] = out[name]["solves_per_hour"] / f_sph if f_sph > 0 else None
+    for d in dirs:
+        shutil.rmtree(d, ignore_errors=True)
     return out
 
 
@@ -777,6 +878,8 @@ def run_gpu(args, rank, world, dist):
                 and args.variant == "default" and args.levels == 2):
             n_ref = max(args.warmup, 3) + args.steps + nprof
             forms = measure_forms(gbturbo, dirs, cells, n_ref, s.integrals(1)[0], min(args.steps, 50), tmp)
+            if not args.no_solves:
+                forms["solves_per_hour"] = measure_solves(gbturbo, os.path.join(tmp, "solves"))
         s.close()
 
         # --- end to end through the C-ABI: case files on the host -> handle (upload + geometry)

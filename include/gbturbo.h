@@ -127,6 +127,12 @@ int gb_sync(gb_solver *h);
  * block, chosen at create by timing the plane chains of each candidate shape; the choice changes
  * timing only, not results */
 int gb_sweep_tuning(gb_solver *h, int level, int out[2]);
+/* whether a level's face stage runs on tiles of faces staged in shared memory by the tensor memory
+ * accelerator (*tma = 1; the mixed form's default scheme on meshes whose k extent KM is 4n + 1 and
+ * at least 33) or reads its stencils straight from HBM (*tma = 0); the choice changes timing only,
+ * the arithmetic is the same. The environment variable GBTURBO_FACE_TMA=0 at create disables the
+ * staged form. No counterpart in the reference. */
+int gb_face_staging(gb_solver *h, int level, int *tma);
 /* 0 disables graph replay in gb_iterate (eager launches) */
 int gb_set_graphs(gb_solver *h, int enable);
 /* stage profiler: between the two calls iterations run without graphs and every stage of the
@@ -145,6 +151,12 @@ int gb_timer_stop(gb_solver *h, float *ms);
  * reference: it is the roof against which the FP64 form's face-flux and sweep kernels are
  * reported, since on this GPU they are bound by the FP64 pipe rather than by HBM. */
 int gb_fp64_rate(double *flop_per_s);
+/* The FP64 form's Newton-refined reciprocal, quotient and square root (which replace the IEEE
+ * division and root in its compute-bound kernels) evaluated on the device for n inputs, so that
+ * they can be checked against the IEEE operations: op 0 x / y, 1 sqrt(x), 2 1 / x; op 3 and 4 are
+ * the device's IEEE x / y and sqrt(x). x, y (y only for ops 0 and 3) and out are host arrays.
+ * No counterpart in the reference. */
+int gb_fp64_arith_check(int op, const double *x, const double *y, long long n, double *out);
 
 /* Residual norm of gb_res_calculate (same arguments, same values in out and in the solve states)
  * computed with no allocation on success: its scratch is a static device array of fixed size

@@ -65,6 +65,11 @@ CASES = {
 # same generator call (its grid file is several MB)
 LONG = {
     "duct_33x33x65_2000": ("annular_duct", dict(IM=33, JM=33, KM=65), {}, 2000),
+    # the rotor blade family on a 25x25x65 mesh at 1.05 x p_t, two-level FAS: the reference's driver
+    # runs it until its convergence rule stops it (cycle 1371 of at most 6000)
+    "rotor_25x25x65_converged": ("rotor_passage", dict(IM=25, JM=25, KM=65),
+                                 {"Pout": "%.1f" % (1.05 * 101325.0), "multigrid": "Y", "coarse_iter": "2",
+                                  "Ma0": "0.45", "maxiter": "6000"}, 6000),
 }
 
 # multi-block: the rotor passage cut at the blade's leading- and trailing-edge planes into three
