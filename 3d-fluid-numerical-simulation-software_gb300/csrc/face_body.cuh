@@ -5,7 +5,8 @@
 // source/Spectral_curl_grad.cpp:85-493 and source/ViscousFlux.cpp:9-269), written once for the
 // two ways the face stage reads its inputs: straight from the padded boxes in HBM (k_face) and from
 // a tile staged in shared memory by the tensor memory accelerator (k_face_tma). Cells are addressed
-// as base index + offsets with the strides of whichever array holds them.
+// as base index + offsets with the strides of whichever array holds them. Indices are 32-bit: a
+// level's pool holds fewer than 2^31 cells of every field (the solver refuses larger batches).
 #pragma once
 #include "gbt_common.cuh"
 #include "flux.cuh"
@@ -17,7 +18,7 @@ namespace gbt {
 // needs each value
 template <typename T> struct FaceGeo {
     const T *S[3], *s, *nrm[3], *t1[3], *t2[3], *qe, *m[9];
-    long long q;
+    int q;
 };
 
 // cell fields the face stage reads: the six primitive variables and mu_t (or the conserved
@@ -28,7 +29,7 @@ template <typename T> struct CellSrc {
 };
 
 template <typename T>
-__device__ __forceinline__ P6<T> ld_p6(const CellSrc<T> &C, long long q)
+__device__ __forceinline__ P6<T> ld_p6(const CellSrc<T> &C, int q)
 {
     P6<T> v = {C.pv[PD][q], C.pv[PU][q], C.pv[PV][q], C.pv[PW][q], C.pv[PP][q], C.pv[PT][q]};
     return v;
@@ -40,7 +41,7 @@ __device__ __forceinline__ P6<T> ld_p6(const CellSrc<T> &C, long long q)
 // (source/Spectral_curl_grad.cpp:115-203 and the J/K counterparts, including the extra 0.25 of
 // :311-314 on J faces at j = JM, k = 1).
 template <typename T, int F, int DT>
-__device__ __forceinline__ T tan_diff(const T *__restrict__ c, long long p, long long sn, long long st, int a, int NN,
+__device__ __forceinline__ T tan_diff(const T *__restrict__ c, int p, int sn, int st, int a, int NN,
                                       int b, int TT)
 {
     // cells: (0,0)=p, (-1,0)=p-sn, (0,+1)=p+st, (-1,+1)=p-sn+st, (0,-1)=p-st, (-1,-1)=p-sn-st
@@ -74,11 +75,11 @@ __device__ __forceinline__ T tan_diff(const T *__restrict__ c, long long p, long
 // FP64 conserved variables, through the plain form's global indices).
 template <typename T, int F, int MODE>
 __device__ __forceinline__ void face_body(const Phys &P, const PhysW<T> &PC, const CellSrc<T> &C, const double *const *cv,
-                                          long long p, long long sI, long long sJ, long long sK, int i, int j, int k,
+                                          int p, int sI, int sJ, int sK, int i, int j, int k,
                                           int IM, int JM, int KM, const FaceGeo<T> &g, int wq, T rot, T cx, T cy, T out[10])
 {
     const int recon_var = MODE ? 200 : P.recon_var, recon = MODE ? 500 : P.recon, scheme = MODE ? 300 : P.scheme;
-    const long long sn = F == 0 ? sI : (F == 1 ? sJ : sK);
+    const int sn = F == 0 ? sI : (F == 1 ? sJ : sK);
     const int NN = F == 0 ? IM : (F == 1 ? JM : KM);
     const int a = F == 0 ? i : (F == 1 ? j : k);
     const T gamma = PC.gamma, g1 = PC.gm1;
@@ -88,7 +89,7 @@ __device__ __forceinline__ void face_body(const Phys &P, const PhysW<T> &PC, con
         // wall face: flux from the face average of ghost and interior, in the wall's frame
         // (source/WallFlux.cpp:70-175); the JST central flux has the same form in the block's
         // frame (source/JST_Convective.cpp:53-95)
-        const long long m = p - sn;
+        const int m = p - sn;
         const P6<T> A = ld_p6(C, p), Bq = ld_p6(C, m);
         const T d = (T)0.5 * (A.d + Bq.d), u = (T)0.5 * (A.u + Bq.u), v = (T)0.5 * (A.v + Bq.v),
                 w = (T)0.5 * (A.w + Bq.w), pr = (T)0.5 * (A.p + Bq.p);
@@ -101,12 +102,12 @@ __device__ __forceinline__ void face_body(const Phys &P, const PhysW<T> &PC, con
     } else {
         // stencil FF, F, B, BB along the face normal; the first ghost layer is skipped in favour of
         // the reconstruction layers
-        const long long p0 = p - (long long)a * sn;
+        const int p0 = p - a * sn;
         auto rm = [NN](int c) { return c <= 0 ? c - 1 : (c >= NN ? c + 1 : c); };
-        const long long q0 = p0 + rm(a - 2) * sn, q1 = p0 + rm(a - 1) * sn, q2 = p0 + rm(a) * sn, q3 = p0 + rm(a + 1) * sn;
+        const int q0 = p0 + rm(a - 2) * sn, q1 = p0 + rm(a - 1) * sn, q2 = p0 + rm(a) * sn, q3 = p0 + rm(a + 1) * sn;
         C5<T> cl, cr;
         if (!MODE && recon_var == 100) {
-            auto ldc = [cv](long long q) {
+            auto ldc = [cv](int q) {
                 C5<T> v = {(T)cv[0][q], (T)cv[1][q], (T)cv[2][q], (T)cv[3][q], (T)cv[4][q]};
                 return v;
             };
@@ -140,7 +141,7 @@ __device__ __forceinline__ void face_body(const Phys &P, const PhysW<T> &PC, con
 
     // ---- viscous flux ----
     const int iD1 = F == 0 ? 1 : 0, iD2 = F == 2 ? 1 : 2;   // tangential directions (kesi/yita/zita order)
-    const long long st1 = iD1 == 0 ? sI : sJ, st2 = iD2 == 1 ? sJ : sK;
+    const int st1 = iD1 == 0 ? sI : sJ, st2 = iD2 == 1 ? sJ : sK;
     const int b1 = iD1 == 0 ? i : j, T1 = iD1 == 0 ? IM : JM;
     const int b2 = iD2 == 1 ? j : k, T2 = iD2 == 1 ? JM : KM;
     T dn[4], d1[4], d2[4];
@@ -160,7 +161,7 @@ __device__ __forceinline__ void face_body(const Phys &P, const PhysW<T> &PC, con
         else if (F == 1) { dk[q] = d1[q]; de[q] = dn[q]; dz[q] = d2[q]; }
         else { dk[q] = d1[q]; de[q] = d2[q]; dz[q] = dn[q]; }
     }
-    const long long gq = g.q;
+    const int gq = g.q;
     const T m0 = g.m[0][gq], m1 = g.m[1][gq], m2 = g.m[2][gq], m3 = g.m[3][gq], m4 = g.m[4][gq], m5 = g.m[5][gq],
             m6 = g.m[6][gq], m7 = g.m[7][gq], m8 = g.m[8][gq];
     T gx[4], gy[4], gz[4];
@@ -170,7 +171,7 @@ __device__ __forceinline__ void face_body(const Phys &P, const PhysW<T> &PC, con
         gy[q] = dk[q] * m1 + de[q] * m4 + dz[q] * m7;
         gz[q] = dk[q] * m2 + de[q] * m5 + dz[q] * m8;
     }
-    const long long m = p - sn;
+    const int m = p - sn;
     const T h = (T)0.5;
     const T uf = h * (C.pv[PU][p] + C.pv[PU][m]), vf = h * (C.pv[PV][p] + C.pv[PV][m]);
     const T wf = h * (C.pv[PW][p] + C.pv[PW][m]), tf = h * (C.pv[PT][p] + C.pv[PT][m]);

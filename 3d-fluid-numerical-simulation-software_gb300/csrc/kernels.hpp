@@ -17,7 +17,8 @@ struct LaunchCtx {
     void (*hook)(void *user, const char *stage, int begin, int launches, int level) = nullptr;
     void *hook_user = nullptr;
     int level = 0;                            // grid level of these launches (1 = fine)
-    const void *face_tma = nullptr;           // tensor maps of the TMA-staged face stage (mixed form), or null
+    const void *face_tma = nullptr;           // tables of the TMA-staged face stage (mixed form), or null
+    const void *face_tma_host = nullptr;      // their header, on the host
     void mark(const char *stage, int begin, int launches = 1) const { if (hook) hook(hook_user, stage, begin, launches, level); }
     dim3 grid_n(long long n, int bs) const { return dim3((unsigned)((n + bs - 1) / bs), batch.nsolve); }
     dim3 grid_cells(int bs) const { return grid_n((long long)(maxIM - 1) * (maxJM - 1) * (maxKM - 1), bs); }
@@ -108,7 +109,8 @@ void launch_boundary(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> 
 // residual stages; level = 1 for the fine mesh (turbulence model only there)
 // the mixed form's face stage with tiles staged in shared memory by TMA (csrc/face_tma.cu)
 bool face_tma_eligible(const std::vector<Lvl> &lv);
-void *build_face_tma(const std::vector<Lvl> &lv, const GeoW<float> &G, const Flow<float> &W, size_t *bytes);
+void *build_face_tma(const std::vector<Lvl> &lv, const GeoW<float> &G, const Flow<float> &W, size_t *bytes,
+                     unsigned char host_header[64]);
 void launch_face_tma(const LaunchCtx &ctx, const Phys &P, const PhysW<float> &PC, const GeoW<float> &GW, Flow<float> W,
                      const DevWall *walls);
 

@@ -21,8 +21,8 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 4) k_face(Batch B, P
     int ni, nj, nk, i, j, k;
     face_extent(L, F, ni, nj, nk);
     if (!box_index(ni, nj, nk, i, j, k)) return;
-    const long long p = ix(L, i, j, k);
-    const long long sI = (long long)L.NJ * L.NK, sJ = L.NK, sK = 1;
+    const int p = (int)ix(L, i, j, k);
+    const int sI = L.NJ * L.NK, sJ = L.NK, sK = 1;
     FaceGeo<T> g;
 #pragma unroll
     for (int c = 0; c < 3; c++) { g.S[c] = G.S[F][c]; g.nrm[c] = G.nrm[F][c]; g.t1[c] = G.t1[F][c]; g.t2[c] = G.t2[F][c]; }

@@ -61,7 +61,8 @@ struct Level {
     Geo G{};
     GeoW<T> GW{};                         // working-precision geometry (aliases in FP64, FP32 copies in mixed)
     DevBuf geow_mem;
-    DevBuf tma_mem;                       // tensor maps of the TMA-staged face stage (mixed form)
+    DevBuf tma_mem;                       // tables of the TMA-staged face stage (mixed form)
+    unsigned char tma_host[64] = {};      // their header
     DevBuf fd_mem;                        // JST face dissipation
     DevBuf sa_mem, sa_tab_mem;            // Spalart-Allmaras fields; its tables
     DevBuf wdist_mem;                     // Baldwin-Lomax wall distances (fine level)
@@ -83,6 +84,7 @@ struct Level {
         c.maxIM = maxIM; c.maxJM = maxJM; c.maxKM = maxKM;
         c.pool_n = pool_n;
         c.face_tma = tma_mem.p;
+        c.face_tma_host = tma_host;
         return c;
     }
 };
@@ -549,6 +551,8 @@ public:
             Lv.max_plane = std::max(Lv.max_plane, c.IM + c.JM + c.KM - 3);
         }
         Lv.pool_n = base;
+        // the face kernels index a level's pools with 32-bit offsets
+        if (base >= (long long)INT32_MAX) throw std::runtime_error("batch too large: a level's pool exceeds 2^31 cells");
         const size_t N = (size_t)base;
         timer.mark("level boxes", nullptr);
         // device descriptors
@@ -788,7 +792,7 @@ public:
             launch_geometry_working(ctx(l), G, W);
             if constexpr (sizeof(T) == 4) {
                 // the face stage's tiles staged by TMA where every box row is 16-byte aligned
-                if (face_tma_eligible(Lv.lv)) Lv.tma_mem.p = build_face_tma(Lv.lv, W, Lv.W, &Lv.tma_mem.bytes);
+                if (face_tma_eligible(Lv.lv)) Lv.tma_mem.p = build_face_tma(Lv.lv, W, Lv.W, &Lv.tma_mem.bytes, Lv.tma_host);
             }
         }
     }

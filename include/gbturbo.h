@@ -130,8 +130,9 @@ int gb_sweep_tuning(gb_solver *h, int level, int out[2]);
 /* whether a level's face stage runs on tiles of faces staged in shared memory by the tensor memory
  * accelerator (*tma = 1; the mixed form's default scheme on meshes whose k extent KM is 4n + 1 and
  * at least 33) or reads its stencils straight from HBM (*tma = 0); the choice changes timing only,
- * the arithmetic is the same. The environment variable GBTURBO_FACE_TMA=0 at create disables the
- * staged form. No counterpart in the reference. */
+ * the arithmetic is the same. The staged form is chosen at create by the environment variable
+ * GBTURBO_FACE_TMA (1: the cell fields staged, the per-face geometry streamed; 2: both staged;
+ * unset or 0: the plain kernel). No counterpart in the reference. */
 int gb_face_staging(gb_solver *h, int level, int *tma);
 /* 0 disables graph replay in gb_iterate (eager launches) */
 int gb_set_graphs(gb_solver *h, int enable);
