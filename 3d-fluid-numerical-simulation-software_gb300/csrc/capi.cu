@@ -4,6 +4,8 @@
 #include "warmstart.hpp"
 #include <cstring>
 #include <string>
+#include <thread>
+#include <algorithm>
 
 struct gb_solver {
     std::unique_ptr<gbt::SolverBase> s;
@@ -42,7 +44,7 @@ int gb_case_info(const char *case_dir, long long info[9], double *nodes_out, lon
 {
     if (!case_dir || !info) { g_err = "bad arguments"; return GB_ERR_ARG; }
     return guard([&] {
-        std::vector<gbt::CaseSpec> b = gbt::read_case(case_dir);
+        std::vector<gbt::CaseSpec> b = gbt::read_case(case_dir, (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
         const gbt::CaseSpec &c = b[0];
         long long nodes = 0, nin = 0, nout = 0, nwall = 0;
         for (auto &s : b) {
@@ -377,11 +379,12 @@ int gb_ws_forward_backward(gb_warmstart *w, const float *feat, const float *targ
         if (loss) *loss = l;
     });
 }
-int gb_ws_benchmark(gb_warmstart *w, long long n, int iters, float *ms_forward, float *ms_step)
+int gb_ws_benchmark(gb_warmstart *w, long long n, int iters, float *ms_forward, float *ms_step, float *ms_infer,
+                    double *max_diff)
 {
     NEEDW(w);
-    if (!ms_forward || !ms_step) { g_err = "null buffer"; return GB_ERR_ARG; }
-    return guard([&] { w->w->benchmark(n, iters, ms_forward, ms_step); });
+    if (!ms_forward || !ms_step || !ms_infer) { g_err = "null buffer"; return GB_ERR_ARG; }
+    return guard([&] { w->w->benchmark(n, iters, ms_forward, ms_step, ms_infer, max_diff); });
 }
 
 }  // extern "C"

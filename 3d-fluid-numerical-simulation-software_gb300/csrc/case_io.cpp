@@ -8,6 +8,9 @@
 #include <charconv>
 #include <system_error>
 #include <algorithm>
+#include <atomic>
+#include <thread>
+#include <vector>
 
 namespace gbt {
 
@@ -322,8 +325,9 @@ inline bool parse3(const char *b, const char *e, double &x, double &y, double &z
 }
 
 // the grid file: block count, then per block its id line, "IM JM KM" and the nodes, i fastest
-// (source/UserInput.cpp:241-290)
-void read_grid(const CaseSpec &c, const std::vector<BlockRow> &rows, std::vector<CaseSpec> &out)
+// (source/UserInput.cpp:241-290). A block's node lines are split in one pass, then parsed by
+// `threads` host threads (each line is one node, so a line's index is its node's).
+void read_grid(const CaseSpec &c, const std::vector<BlockRow> &rows, std::vector<CaseSpec> &out, int threads)
 {
     std::string path = c.dir + "/" + c.grid_file;
     GridText r(path, c.grid_file);
@@ -351,12 +355,70 @@ void read_grid(const CaseSpec &c, const std::vector<BlockRow> &rows, std::vector
         bs.IM = IM; bs.JM = JM; bs.KM = KM; bs.nblade = br.nblade; bs.rpm = br.rpm;
         size_t n = (size_t)IM * JM * KM;
         bs.x.resize(n); bs.y.resize(n); bs.z.resize(n);
-        for (size_t q = 0; q < n; q++) {
-            const char *lb, *le;
-            r.next(lb, le);
-            if (!parse3(lb, le, bs.x[q], bs.y[q], bs.z[q]))
-                throw std::runtime_error(c.grid_file + ": bad node line " + std::to_string(r.lineno));
+        const int line0 = r.lineno;                       // the line before the block's first node
+        // The node lines [pos0, ...): line q starts at pos0 (q = 0) or right after the q-th newline.
+        // The buffer is cut into `nt` byte ranges; each thread counts the newlines of its range,
+        // and after a prefix sum parses the lines that start in its range (parse3 stops at a
+        // comment, a carriage return or the line end the way the one-line reader's trimming does).
+        const char *base = r.buf.data();
+        const size_t pos0 = r.pos, end = r.buf.size();
+        const size_t nt = (threads > 1 && n >= 65536) ? (size_t)threads : 1;
+        std::vector<size_t> cut(nt + 1), nl_count(nt + 1, 0);
+        for (size_t t = 0; t <= nt; t++) cut[t] = pos0 + (end - pos0) * t / nt;
+        std::atomic<size_t> bad{n};                       // first node line that does not parse
+        std::atomic<size_t> next_pos{end};                // start of the line after the block's nodes
+        auto note_bad = [&](size_t q) {
+            size_t cur = bad.load();
+            while (q < cur && !bad.compare_exchange_weak(cur, q)) {}
+        };
+        auto count_range = [&](size_t t) {
+            nl_count[t + 1] = (size_t)std::count(base + cut[t], base + cut[t + 1], '\n');
+        };
+        auto parse_range = [&](size_t t) {
+            size_t q = 0;
+            for (size_t u = 0; u <= t; u++) q += nl_count[u];  // newlines before this range
+            const char *p = base + cut[t], *e = base + cut[t + 1];
+            const char *ls;                               // start of the next line to parse
+            if (t == 0) ls = base + pos0;
+            else {
+                // the first line starting in this range follows the first newline at or after cut[t] - 1
+                const char *nl = (const char *)std::memchr(p - 1, '\n', (size_t)(e - (p - 1)));
+                if (!nl || nl + 1 >= e) return;
+                q += (nl >= p) ? 1 : 0;                   // a newline at cut[t] - 1 was counted by the range before
+                ls = nl + 1;
+            }
+            while (ls < e) {
+                if (q >= n) {
+                    if (q == n) next_pos.store((size_t)(ls - base));
+                    return;
+                }
+                const char *nl = (const char *)std::memchr(ls, '\n', (size_t)(base + end - ls));
+                const char *le = nl ? nl : base + end;
+                if (!parse3(ls, le, bs.x[q], bs.y[q], bs.z[q])) note_bad(q);
+                q++;
+                if (!nl) break;
+                ls = nl + 1;
+            }
+        };
+        if (nt == 1) {
+            count_range(0);
+            parse_range(0);
+        } else {
+            std::vector<std::thread> pool;
+            for (size_t t = 0; t < nt; t++) pool.emplace_back(count_range, t);
+            for (auto &th : pool) th.join();
+            pool.clear();
+            for (size_t t = 0; t < nt; t++) pool.emplace_back(parse_range, t);
+            for (auto &th : pool) th.join();
         }
+        size_t total_nl = 0;
+        for (size_t t = 1; t <= nt; t++) total_nl += nl_count[t];
+        const size_t lines = total_nl + ((end > pos0 && base[end - 1] != '\n') ? 1 : 0);
+        if (lines < n) throw std::runtime_error(c.grid_file + ": file ended at line " + std::to_string(line0 + (int)lines + 1));
+        if (bad.load() < n)
+            throw std::runtime_error(c.grid_file + ": bad node line " + std::to_string(line0 + 1 + (int)bad.load()));
+        r.pos = next_pos.load();
+        r.lineno = line0 + (int)n;
         out.push_back(std::move(bs));
     }
 }
@@ -397,7 +459,7 @@ void validate(const CaseSpec &c)
 
 }  // namespace
 
-std::vector<CaseSpec> read_case(const std::string &dir)
+std::vector<CaseSpec> read_case(const std::string &dir, int threads)
 {
     CaseSpec c;
     c.dir = dir;
@@ -408,7 +470,7 @@ std::vector<CaseSpec> read_case(const std::string &dir)
     c.first_inlet = c.inlets[0];
     c.first_outlet = c.outlets[0];
     std::vector<CaseSpec> blocks;
-    read_grid(c, rows, blocks);
+    read_grid(c, rows, blocks, threads);
     for (auto &b : blocks) validate_block(b);
     return blocks;
 }

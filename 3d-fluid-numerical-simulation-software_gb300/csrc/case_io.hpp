@@ -57,8 +57,9 @@ struct CaseSpec {
 };
 
 // Reads a case directory into one spec per block (block order of the files); throws
-// std::runtime_error with a message naming the problem.
-std::vector<CaseSpec> read_case(const std::string &dir);
+// std::runtime_error with a message naming the problem. `threads` host threads parse the node
+// lines of large grids.
+std::vector<CaseSpec> read_case(const std::string &dir, int threads = 1);
 
 // One line of a reference input file: comment from '#' removed, leading and trailing blanks
 // removed (tabs are kept, as the reference keeps them); a trailing carriage return is dropped.

@@ -326,6 +326,7 @@ public:
     const int norm_blk = 304;            // two blocks per SM: the FP64 divisions spread over all SMs
     T *dtmin = nullptr;
     cudaGraphExec_t graphs[3] = {nullptr, nullptr, nullptr};
+    int phase_runs[3] = {0, 0, 0};        // iterations run in each driver phase (graphs: see iterate)
 
     // ---- stage profiler
     struct ProfRec { std::string stage; cudaEvent_t a, b; int launches, level; };
@@ -424,12 +425,14 @@ public:
             std::vector<std::vector<CaseSpec>> per_case(ncase);
             std::vector<std::exception_ptr> errs(ncase);
             std::atomic<int> next{0};
-            const unsigned nt = std::min<unsigned>((unsigned)ncase, std::max(1u, std::thread::hardware_concurrency()));
+            const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+            const unsigned nt = std::min<unsigned>((unsigned)ncase, hw);
+            const int per = (int)std::max(1u, std::min(16u, hw / nt));     // parse threads of each case's grid
             std::vector<std::thread> pool;
             for (unsigned t = 0; t < nt; t++)
                 pool.emplace_back([&] {
                     for (int i = next++; i < ncase; i = next++) {
-                        try { per_case[i] = read_case(dirs[i]); } catch (...) { errs[i] = std::current_exception(); }
+                        try { per_case[i] = read_case(dirs[i], per); } catch (...) { errs[i] = std::current_exception(); }
                     }
                 });
             for (auto &t : pool) t.join();
@@ -1268,7 +1271,11 @@ public:
             // a phase graph fixes the reporting level it was captured with: a restarted multigrid
             // case reports the coarse level for its first iterations, which therefore run eagerly
             const bool level_moves = reuse && report_level() != 1;
-            if (use_graphs && ph >= 0 && !profiling && !level_moves) {
+            // a phase is captured at its second iteration: the first runs eagerly, so that a phase
+            // that runs once (the start-up of a two-iteration coarse start) costs no capture and
+            // instantiation (eager launches and graph replay give the same bits)
+            const bool capture_now = ph >= 0 && !graphs[ph] && phase_runs[ph]++ >= 1;
+            if (use_graphs && ph >= 0 && !profiling && !level_moves && (graphs[ph] || capture_now)) {
                 if (!graphs[ph]) {
                     cudaGraph_t g;
                     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));

@@ -291,6 +291,167 @@ __global__ void __launch_bounds__(32 * (kEpiWarps + 2), 1) k_mlp_gemm(const __gr
     if (warp == kEpiWarps) tmem_dealloc(tmem, 512);
 }
 
+// ---------------------------------------------------------------- inference, all layers fused
+// Y[rows x 16] = the whole network on X[rows x 64], per tile of 128 rows, the activations kept on
+// chip: the tile's activations live in one shared-memory buffer in the K-major core-matrix layout
+// (8-column groups 2 KB apart, rows 16 B apart), each layer's accumulator in TMEM. Roles as in
+// k_mlp_gemm, persistent over the tiles:
+//   warp 16: TMA producer. Loads the tile's features into the activation buffer once the previous
+//     tile's last layer has read it, and streams the weights, 64-column chunk by chunk, layer by
+//     layer, through a 3-stage ring (the same chunks for every tile; they stay in L2).
+//   warp 17: MMA issuer. Per layer: waits for the epilogue of the layer before (its outputs are this
+//     layer's inputs, and it has read the accumulator out), issues the layer's MMAs with A from the
+//     activation buffer, commits the accumulator; after the last layer it frees the buffer.
+//   warps 0-15: epilogue. Per layer: bias and SiLU of the accumulator, rounded to BF16 and written
+//     over the activation buffer (hidden layers), or bias and FP32 rows of Y (the output layer).
+// The arithmetic is the layer-by-layer forward's (same MMA order, same epilogue), so the outputs
+// are the same bits; nothing but X and Y crosses HBM.
+struct InferArgs {
+    long long M;
+    const float *bias[kWsLayers];
+    float *Y;
+    int *err;
+};
+constexpr int kInfStages = 3;
+constexpr int kInfH = 128 * kWsHidden * 2;                  // 64 KB of activations
+constexpr int kInfSmem = kInfH + kInfStages * kStageB + 256;
+__host__ __device__ constexpr int inf_n(int l) { return l == kWsLayers - 1 ? kWsOut : kWsHidden; }
+__host__ __device__ constexpr int inf_chunks(int l) { return l == 0 ? kWsIn / kChunk : kWsHidden / kChunk; }
+
+__global__ void __launch_bounds__(32 * (kEpiWarps + 2), 1) k_mlp_infer(
+    const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tw0, const __grid_constant__ CUtensorMap tw1,
+    const __grid_constant__ CUtensorMap tw2, const __grid_constant__ CUtensorMap tw3, const __grid_constant__ CUtensorMap tw4,
+    const __grid_constant__ CUtensorMap tw5, InferArgs g)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    unsigned char *hbuf = sm;                                           // activations
+    unsigned char *ring = sm + kInfH;                                   // weight chunks
+    uint64_t *bars = reinterpret_cast<uint64_t *>(ring + kInfStages * kStageB);
+    // bars: full[3], empty[3], x_full, h_free, acc_full, h_ready
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 2 * kInfStages + 4);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t bar0 = smem_u32(bars);
+    auto full = [&](int s) { return bar0 + 8u * (uint32_t)s; };
+    auto empty = [&](int s) { return bar0 + 8u * (uint32_t)(kInfStages + s); };
+    const uint32_t x_full = bar0 + 8u * (2 * kInfStages), h_free = x_full + 8u, acc_full = x_full + 16u,
+                   h_ready = x_full + 24u;
+    const uint32_t hb = smem_u32(hbuf);
+    if (warp == kEpiWarps) tmem_alloc(smem_u32(slot), 256);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kInfStages; s++) { mbar_init(full(s), 1); mbar_init(empty(s), 1); }
+        mbar_init(x_full, 1);
+        mbar_init(h_free, 1);
+        mbar_init(acc_full, 1);
+        mbar_init(h_ready, kEpiWarps);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *slot;
+    const long long tiles = (g.M + 127) / 128;
+    bool failed = false;
+    if (warp == kEpiWarps) {
+        if (lane == 0) {
+            long long it = 0, ti = 0;
+            for (long long t = blockIdx.x; t < tiles && !failed; t += gridDim.x, ti++) {
+                if (!mbar_wait_bounded(h_free, (uint32_t)((ti & 1) ^ 1))) { failed = true; break; }
+                mbar_expect_tx(x_full, (uint32_t)(kWsIn / 8) * 128u * 16u);
+                for (int k8 = 0; k8 < kWsIn / 8; k8++) tma_load_2d(hb + (uint32_t)k8 * 2048u, &tmX, k8 * 8, (int)(t * 128), x_full);
+                for (int l = 0; l < kWsLayers && !failed; l++) {
+                    const CUtensorMap *wm = l == 0 ? &tw0 : l == 1 ? &tw1 : l == 2 ? &tw2 : l == 3 ? &tw3 : l == 4 ? &tw4 : &tw5;
+                    const int n = inf_n(l);
+                    for (int kc = 0; kc < inf_chunks(l); kc++, it++) {
+                        const int s = (int)(it % kInfStages);
+                        if (!mbar_wait_bounded(empty(s), (uint32_t)(((it / kInfStages) & 1) ^ 1))) { failed = true; break; }
+                        mbar_expect_tx(full(s), 8u * (uint32_t)n * 16u);
+                        const uint32_t b_s = smem_u32(ring + (size_t)s * kStageB);
+                        for (int k8 = 0; k8 < 8; k8++) tma_load_2d(b_s + (uint32_t)k8 * (uint32_t)n * 16u, wm, kc * kChunk + k8 * 8, 0, full(s));
+                    }
+                }
+            }
+        }
+    } else if (warp == kEpiWarps + 1) {
+        if (lane == 0) {
+            long long it = 0, ti = 0, hu = 0;
+            for (long long t = blockIdx.x; t < tiles && !failed; t += gridDim.x, ti++) {
+                if (!mbar_wait_bounded(x_full, (uint32_t)(ti & 1))) { failed = true; break; }
+                for (int l = 0; l < kWsLayers && !failed; l++) {
+                    // the epilogue of the layer before has written this layer's inputs and read the accumulator
+                    if (ti > 0 || l > 0) {
+                        if (!mbar_wait_bounded(h_ready, (uint32_t)(hu & 1))) { failed = true; break; }
+                        hu++;
+                    }
+                    tc_fence_after();
+                    const int n = inf_n(l);
+                    const uint32_t idesc = idesc_bf16(128, n);
+                    for (int kc = 0; kc < inf_chunks(l); kc++, it++) {
+                        const int s = (int)(it % kInfStages);
+                        if (!mbar_wait_bounded(full(s), (uint32_t)((it / kInfStages) & 1))) { failed = true; break; }
+                        tc_fence_after();
+                        const uint32_t b_s = smem_u32(ring + (size_t)s * kStageB);
+                        for (int ks = 0; ks < kChunk / 16; ks++)
+                            mma_bf16(tmem, smem_desc(hb + (uint32_t)(kc * (kChunk / 16) + ks) * 2u * 2048u, 2048u, 128u),
+                                     smem_desc(b_s + (uint32_t)ks * 2u * (uint32_t)n * 16u, (uint32_t)n * 16u, 128u), idesc,
+                                     (kc > 0 || ks > 0) ? 1u : 0u);
+                        mma_commit(empty(s));
+                    }
+                    if (failed) break;
+                    mma_commit(acc_full);
+                    if (l == kWsLayers - 1) mma_commit(h_free);
+                }
+            }
+        }
+    } else {
+        long long au = 0;
+        const int quad = warp & 3;
+        const int r = quad * 32 + lane;                                // the TMEM lane = row of the tile
+        for (long long t = blockIdx.x; t < tiles && !failed; t += gridDim.x) {
+            const long long row = t * 128 + r;
+            for (int l = 0; l < kWsLayers; l++, au++) {
+                const bool ok = mbar_wait_bounded(acc_full, (uint32_t)(au & 1));
+                tc_fence_after();
+                if (!ok) { failed = true; break; }
+                const int n = inf_n(l);
+                const int cols = n >= 64 ? n / 4 : 16;
+                const int cbeg = (warp >> 2) * cols, cend = cbeg + cols < n ? cbeg + cols : n;
+                const float *bias = g.bias[l];
+                for (int c0 = cbeg; c0 < cend; c0 += 16) {
+                    float v[16];
+                    tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, v);
+                    if (l < kWsLayers - 1) {
+                        alignas(16) bf16 ho[16];
+#pragma unroll
+                        for (int i = 0; i < 16; i++) {
+                            const float z = v[i] + bias[c0 + i];
+                            ho[i] = __float2bfloat16_rn(z * sigmoidf_(z));
+                        }
+                        uint4 *h0 = reinterpret_cast<uint4 *>(hbuf + (size_t)(c0 / 8) * 2048 + (size_t)r * 16);
+                        uint4 *h1 = reinterpret_cast<uint4 *>(hbuf + (size_t)(c0 / 8 + 1) * 2048 + (size_t)r * 16);
+                        *h0 = reinterpret_cast<uint4 *>(ho)[0];
+                        *h1 = reinterpret_cast<uint4 *>(ho)[1];
+                    } else if (row < g.M) {
+                        float4 *yp = reinterpret_cast<float4 *>(g.Y + row * kWsOut + c0);
+#pragma unroll
+                        for (int i = 0; i < 4; i++)
+                            yp[i] = make_float4(v[4 * i] + bias[c0 + 4 * i], v[4 * i + 1] + bias[c0 + 4 * i + 1],
+                                                v[4 * i + 2] + bias[c0 + 4 * i + 2], v[4 * i + 3] + bias[c0 + 4 * i + 3]);
+                    }
+                }
+                fence_proxy_async();                                   // the activations, for the tensor cores
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(h_ready);
+            }
+        }
+    }
+    if (failed) atomicOr(g.err, 1);
+    __syncwarp();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == kEpiWarps) tmem_dealloc(tmem, 256);
+}
+
 // ---------------------------------------------------------------- the weight gradient
 // part[(ay * gridDim.x + bx)][a][b] = sum over the CTA's cells of Xa[cell][128 ay + a] Xb[cell][b]
 // (a < 128, b < Nb): the cells are the product's K. Both operands are MN-major: a TMA box of 8
@@ -770,7 +931,23 @@ struct WarmStart::Impl {
             k_ws_weights_bf16<<<(kN[l] * kK[l] + 255) / 256, 256, 0, st>>>(P + w_off(l), kN[l], kK[l], Wb[l], Wt[l]);
     }
 
-    // rows of X0 -> Y (and the hidden activations)
+    // rows of X0 -> Y with every layer fused in one kernel (inference: no activations kept)
+    void infer(long long M)
+    {
+        if (M <= 0) return;
+        InferArgs g{};
+        g.M = M; g.Y = Y; g.err = err;
+        for (int l = 0; l < kWsLayers; l++) g.bias[l] = P + b_off(l);
+        const CUtensorMap tx = tensor_map_rows(X0, M, kWsIn, kWsIn, 128);
+        CUtensorMap tw[kWsLayers];
+        for (int l = 0; l < kWsLayers; l++) tw[l] = tensor_map_rows(Wb[l], kN[l], kK[l], kK[l], kN[l]);
+        const long long tiles = (M + 127) / 128;
+        const int grid = (int)std::min<long long>(tiles, n_sm);
+        k_mlp_infer<<<grid, 32 * (kEpiWarps + 2), kInfSmem, st>>>(tx, tw[0], tw[1], tw[2], tw[3], tw[4], tw[5], g);
+        WCK(cudaGetLastError());
+    }
+
+    // rows of X0 -> Y (and the hidden activations, which training needs)
     void forward(long long M)
     {
         const bf16 *in = X0;
@@ -827,6 +1004,7 @@ WarmStart::WarmStart(unsigned seed) : d(new Impl)
     WCK(cudaFuncSetAttribute(k_mlp_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
     WCK(cudaFuncSetAttribute(k_mlp_gemm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
     WCK(cudaFuncSetAttribute(k_mlp_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
+    WCK(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, kInfSmem));
     const size_t np = n_params();
     WCK(cudaMalloc(&d->P, sizeof(float) * np));
     WCK(cudaMalloc(&d->G, sizeof(float) * np));
@@ -1015,7 +1193,7 @@ void WarmStart::apply(SolverBase &s, const float *params, int *used, double *res
     for (long long t0 = 0; t0 < t.total; t0 += chunk) {
         const long long n = std::min(chunk, t.total - t0);
         k_ws_cell_features<<<(unsigned)((n + 255) / 256), 256, 0, m.st>>>(a, t0, n, m.nrm_d, m.X0);
-        m.forward(n);
+        m.infer(n);
         k_ws_write_cv<<<(unsigned)((n + 255) / 256), 256, 0, m.st>>>(a, t0, n, m.nrm_d, m.Y);
     }
     WCK(cudaStreamSynchronize(m.st));
@@ -1076,7 +1254,7 @@ void WarmStart::forward(const float *feat, int M, float *y)
     WCK(cudaMalloc(&f.p, f.bytes));
     WCK(cudaMemcpy(f.p, feat, f.bytes, cudaMemcpyHostToDevice));
     k_f32_to_bf16<<<(unsigned)(((size_t)M * kWsIn + 255) / 256), 256, 0, m.st>>>((const float *)f.p, (long long)M * kWsIn, m.X0);
-    m.forward(M);
+    m.infer(M);
     WCK(cudaMemcpyAsync(y, m.Y, sizeof(float) * (size_t)M * kWsOut, cudaMemcpyDeviceToHost, m.st));
     WCK(cudaStreamSynchronize(m.st));
     if (error_flag()) throw std::runtime_error("a tensor-core wait of the warm-start network ran out");
@@ -1118,7 +1296,7 @@ __global__ void k_ws_random_rows(long long M, unsigned long long seed, bf16 *X0,
     }
 }
 
-void WarmStart::benchmark(long long M, int iters, float *ms_forward, float *ms_step)
+void WarmStart::benchmark(long long M, int iters, float *ms_forward, float *ms_step, float *ms_infer, double *max_diff)
 {
     if (M < 128 || iters < 1) throw std::invalid_argument("benchmark: at least 128 rows and one iteration");
     Impl &m = *d;
@@ -1135,6 +1313,24 @@ void WarmStart::benchmark(long long M, int iters, float *ms_forward, float *ms_s
     float t = 0.f;
     WCK(cudaEventElapsedTime(&t, e0, e1));
     *ms_forward = t / iters;
+    // the fused inference: timed, and its outputs against the layer-by-layer pass's (the same bits)
+    std::vector<float> y_layers((size_t)M * kWsOut), y_fused((size_t)M * kWsOut);
+    WCK(cudaMemcpyAsync(y_layers.data(), m.Y, sizeof(float) * y_layers.size(), cudaMemcpyDeviceToHost, m.st));
+    m.infer(M);                                          // warm-up
+    WCK(cudaEventRecord(e0, m.st));
+    for (int i = 0; i < iters; i++) m.infer(M);
+    WCK(cudaEventRecord(e1, m.st));
+    WCK(cudaEventSynchronize(e1));
+    WCK(cudaEventElapsedTime(&t, e0, e1));
+    if (ms_infer) *ms_infer = t / iters;
+    WCK(cudaMemcpyAsync(y_fused.data(), m.Y, sizeof(float) * y_fused.size(), cudaMemcpyDeviceToHost, m.st));
+    WCK(cudaStreamSynchronize(m.st));
+    double dmax = 0.0;
+    for (size_t q = 0; q < y_fused.size(); q++) {
+        const double dq = std::fabs((double)y_fused[q] - (double)y_layers[q]);
+        dmax = (dq > dmax || dq != dq) ? dq : dmax;
+    }
+    if (max_diff) *max_diff = dmax;
     const int nb = (int)((M + 255) / 256);
     WCK(cudaEventRecord(e0, m.st));
     for (int i = 0; i < iters; i++) {

@@ -48,9 +48,11 @@ public:
     // normalised), the loss and the gradient of every parameter (n_params values)
     void forward(const float *feat, int M, float *y);
     float forward_backward(const float *feat, const float *target, int M, float *grad);
-    // device time (CUDA events on the network's stream) per forward pass and per forward and
-    // backward pass over M rows of device-resident random features and targets, mean of iters
-    void benchmark(long long M, int iters, float *ms_forward, float *ms_step);
+    // device time (CUDA events on the network's stream) per layer-by-layer forward pass, per
+    // forward and backward pass and per fused inference pass over M rows of device-resident random
+    // features and targets, mean of iters; max_diff: the largest difference between the fused and
+    // the layer-by-layer outputs
+    void benchmark(long long M, int iters, float *ms_forward, float *ms_step, float *ms_infer, double *max_diff);
     int error_flag();
 
 private:

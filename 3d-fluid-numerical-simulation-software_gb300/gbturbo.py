@@ -56,7 +56,8 @@ def load() -> ctypes.CDLL:
         "gb_ws_forward": ([vp, ctypes.POINTER(ctypes.c_float), ip, ctypes.POINTER(ctypes.c_float)], ip),
         "gb_ws_forward_backward": ([vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), ip,
                                     ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)], ip),
-        "gb_ws_benchmark": ([vp, ctypes.c_longlong, ip, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)], ip),
+        "gb_ws_benchmark": ([vp, ctypes.c_longlong, ip, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                             ctypes.POINTER(ctypes.c_float), dp], ip),
         "gb_resflux": ([vp, ip], ip),
         "gb_time_marching": ([vp, ip], ip),
         "gb_res_calculate": ([vp, ip, dp], ip),
@@ -486,7 +487,10 @@ class WarmStart:
         return float(loss.value), g
 
     def benchmark(self, rows: int, iters: int = 20):
-        """device ms per forward pass and per forward-and-backward pass over rows random rows"""
-        f, b = ctypes.c_float(), ctypes.c_float()
-        self._check(self._L.gb_ws_benchmark(self.h, int(rows), int(iters), ctypes.byref(f), ctypes.byref(b)))
-        return float(f.value), float(b.value)
+        """device ms per layer-by-layer forward pass, per forward-and-backward pass and per fused
+        inference pass over rows random rows, and the largest difference between the two forward
+        passes' outputs"""
+        f, b, i, dmax = ctypes.c_float(), ctypes.c_float(), ctypes.c_float(), ctypes.c_double()
+        self._check(self._L.gb_ws_benchmark(self.h, int(rows), int(iters), ctypes.byref(f), ctypes.byref(b),
+                                            ctypes.byref(i), ctypes.byref(dmax)))
+        return float(f.value), float(b.value), float(i.value), float(dmax.value)

@@ -697,7 +697,8 @@ def study_warmstart(gbturbo, tmp, cycles, n_test, n_train=256, mesh=(25, 25, 65)
 
 def study_network(gbturbo):
     """the warm-start network's tensor-core kernels alone: device time per forward pass and per
-    training pass (forward, loss, backward) at several row counts, and the dense BF16 rate they
+    training pass (forward, loss, backward) at several row counts, the fused inference pass (every
+    layer in one kernel), and the dense BF16 rate they
     reach (FLOPs per row: 2 x (64x256 + 4 x 256x256 + 256x16) forward; backward the same again for
     the weight gradients and again less the first layer's 2 x 64x256 for the data gradients)"""
     fwd_flop = 2 * (64 * 256 + 4 * 256 * 256 + 256 * 16)
@@ -711,11 +712,15 @@ def study_network(gbturbo):
     peak = float(peaks.get("bf16_tflops", 1900.0))
     with gbturbo.WarmStart(seed=1) as w:
         for rows in (32768, 262144, 1048576):
-            ms_f, ms_s = w.benchmark(rows, iters=20)
+            ms_f, ms_s, ms_i, dmax = w.benchmark(rows, iters=20)
             tf_f = fwd_flop * rows / (ms_f / 1000.0) / 1e12
             tf_s = step_flop * rows / (ms_s / 1000.0) / 1e12
-            out["rows"][str(rows)] = {"ms_forward": ms_f, "ms_train_step": ms_s, "tflops_forward": tf_f,
-                                      "tflops_train_step": tf_s, "frac_of_bf16_peak_forward": tf_f / peak}
+            tf_i = fwd_flop * rows / (ms_i / 1000.0) / 1e12
+            out["rows"][str(rows)] = {"ms_forward": ms_f, "ms_train_step": ms_s, "ms_inference_fused": ms_i,
+                                      "tflops_forward": tf_f, "tflops_train_step": tf_s,
+                                      "tflops_inference_fused": tf_i, "frac_of_bf16_peak_forward": tf_f / peak,
+                                      "frac_of_bf16_peak_inference_fused": tf_i / peak,
+                                      "fused_vs_layer_by_layer_max_abs_diff": dmax}
     out["bf16_peak_tflops"] = peak
     return out
 

@@ -228,9 +228,13 @@ int gb_ws_get_norm(gb_warmstart *w, float *out);
 int gb_ws_set_norm(gb_warmstart *w, const float *in);
 int gb_ws_forward(gb_warmstart *w, const float *feat, int n, float *y);
 int gb_ws_forward_backward(gb_warmstart *w, const float *feat, const float *target, int n, float *loss, float *grad);
-/* device time per forward pass and per forward-and-backward pass (loss and every gradient) over
- * n rows of device-resident random inputs, mean of iters after one warm-up (CUDA events) */
-int gb_ws_benchmark(gb_warmstart *w, long long n, int iters, float *ms_forward, float *ms_step);
+/* device time per layer-by-layer forward pass, per forward-and-backward pass (loss and every
+ * gradient) and per fused inference pass (every layer in one kernel, the activations kept on
+ * chip; gb_ws_forward and gb_ws_apply use it) over n rows of device-resident random inputs, mean
+ * of iters after one warm-up (CUDA events); max_diff (may be NULL) receives the largest difference
+ * between the fused and the layer-by-layer outputs on those rows (the same arithmetic: 0) */
+int gb_ws_benchmark(gb_warmstart *w, long long n, int iters, float *ms_forward, float *ms_step, float *ms_infer,
+                    double *max_diff);
 
 #ifdef __cplusplus
 }

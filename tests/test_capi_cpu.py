@@ -61,7 +61,7 @@ def test_warm_start_entry_points_check_their_arguments_without_gpu(gbturbo):
     assert L.gb_ws_set_norm(None, None) == -1
     assert L.gb_ws_forward(None, None, 0, None) == -1
     assert L.gb_ws_forward_backward(None, None, None, 0, None, None) == -1
-    assert L.gb_ws_benchmark(None, 1024, 1, None, None) == -1
+    assert L.gb_ws_benchmark(None, 1024, 1, None, None, None, None) == -1
     assert L.gb_ws_samples(None) == -1
     assert L.gb_start_from_fine_state(None) == -1
     assert L.gb_ws_destroy(None) == 0

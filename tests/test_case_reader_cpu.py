@@ -89,3 +89,19 @@ def test_short_grid_is_reported(built, tmp_path):
     (tmp_path / "grid.dat").write_text("\n".join(g[:200]) + "\n")
     with pytest.raises(built.GBError, match="ended"):
         built.case_info(str(tmp_path))
+
+
+def test_large_grid_parsed_in_parallel_threads(built, meshgen, tmp_path):
+    """a grid of more than 65,536 nodes is parsed by several host threads: every coordinate as the
+    one-thread parse gives it, and a bad line reported by its own line number"""
+    meshgen.write_case(meshgen.rotor_passage(IM=25, JM=41, KM=97, options={}), str(tmp_path))
+    info, xyz = built.case_info(str(tmp_path), nodes=True)
+    ref = _grid_nodes(str(tmp_path))
+    assert info["nodes"] == ref.shape[0] == 25 * 41 * 97
+    assert np.array_equal(xyz, ref)
+    g = (tmp_path / "grid.dat").read_text().split("\n")
+    bad = 3 + 70000                                # 1-based line of node 70000 (count, id, size lines first)
+    g[bad - 1] = "0.1 x 0.3"
+    (tmp_path / "grid.dat").write_text("\n".join(g))
+    with pytest.raises(built.GBError, match=f"bad node line {bad}$"):
+        built.case_info(str(tmp_path))

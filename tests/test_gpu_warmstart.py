@@ -1,6 +1,7 @@
 """The learned warm start on the GPU (gb_ws_*): the tcgen05 products of the network against the
 CPU oracle (oracle/mlp_oracle.py, BF16 rounding at the kernels' storage points, float64
-accumulation): outputs at 1e-2 and every parameter gradient at 3e-2 relative (normwise per
+accumulation): outputs at 1e-2 (the fused inference kernel, which gb_ws_forward runs, and its
+bitwise equality with the layer-by-layer forward that training uses) and every parameter gradient at 3e-2 relative (normwise per
 tensor; the kernels accumulate in FP32 in another order, and one BF16 ulp of a stored
 intermediate is 4e-3); the fallback rule; and what a trained network gains over the uniform start
 on a family of small rotor passages."""
@@ -50,6 +51,17 @@ def test_forward_matches_oracle(gpu_lib, M):
     yo, _ = mo.forward(p, x)
     assert _rel(y[:, :mo.N_USED], yo[:, :mo.N_USED]) < 1e-2
     assert np.all(y[:, mo.N_USED:] == 0.0)
+
+
+@pytest.mark.parametrize("M", [4133, 65536])
+def test_fused_inference_equals_the_layer_by_layer_forward(gpu_lib, M):
+    """the fused inference kernel (every layer in one launch, activations in shared memory and TMEM)
+    runs the layer-by-layer forward's arithmetic in the same order: the same bits on random rows,
+    including a last tile with fewer than 128 rows"""
+    with gpu_lib.WarmStart(seed=9) as w:
+        ms_f, ms_s, ms_i, dmax = w.benchmark(M, iters=2)
+    assert ms_f > 0.0 and ms_s > 0.0 and ms_i > 0.0
+    assert dmax == 0.0, dmax
 
 
 @pytest.mark.parametrize("M", [256, 1777])
