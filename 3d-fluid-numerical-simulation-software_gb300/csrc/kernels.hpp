@@ -76,6 +76,7 @@ struct PlaneTables {
     int stride = 0, max_plane = 0;
     long long nq = 0;
     int cpw = 10, wpb = 1;                        // sweep block shape: cells per warp, warps per block (autotuned)
+    int df = 0;                                   // FP64 form: 1 = double-float sweep (k_sweep_df), dQ held as pairs
     std::vector<int> max_count;
 };
 

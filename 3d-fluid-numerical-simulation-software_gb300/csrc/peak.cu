@@ -6,6 +6,7 @@
 // against the IEEE operations.
 #include "../../include/gbturbo.h"
 #include "gbt_common.cuh"
+#include "dfloat.cuh"
 #include <cuda_runtime.h>
 
 namespace {
@@ -68,7 +69,8 @@ extern "C" int gb_fp64_rate(double *flop_per_s)
     return rc;
 }
 
-// ---- the FP64 form's reciprocal, quotient and square root against the IEEE operations ----
+// ---- the FP64 form's reciprocal, quotient and square root, and the double-float operations, ----
+// ---- against the IEEE FP64 operations                                                      ----
 namespace {
 
 __global__ void k_arith(int op, const double *__restrict__ x, const double *__restrict__ y, long long n, double *out)
@@ -82,7 +84,15 @@ __global__ void k_arith(int op, const double *__restrict__ x, const double *__re
     case 1: v = gbt::fsqrt<double>(a); break;
     case 2: v = gbt::frcp<double>(a); break;
     case 3: v = a / b; break;
-    default: v = sqrt(a); break;
+    case 4: v = sqrt(a); break;
+    // double-float operations, through the conversions from and to FP64
+    case 5: v = gbt::df_to_double(gbt::df_from(a) + gbt::df_from(b)); break;
+    case 6: v = gbt::df_to_double(gbt::df_from(a) - gbt::df_from(b)); break;
+    case 7: v = gbt::df_to_double(gbt::df_from(a) * gbt::df_from(b)); break;
+    case 8: v = gbt::df_to_double(gbt::df_from(a) / gbt::df_from(b)); break;
+    case 9: v = gbt::df_to_double(gbt::df_sqrt(gbt::df_from(a))); break;
+    case 10: v = gbt::df_to_double(gbt::df_rcp(gbt::df_from(a))); break;
+    default: v = gbt::df_to_double(gbt::df_from(a)); break;
     }
     out[t] = v;
 }
@@ -91,7 +101,8 @@ __global__ void k_arith(int op, const double *__restrict__ x, const double *__re
 
 extern "C" int gb_fp64_arith_check(int op, const double *x, const double *y, long long n, double *out)
 {
-    if (op < 0 || op > 4 || !x || !out || n < 1 || ((op == 0 || op == 3) && !y)) return GB_ERR_ARG;
+    const bool binary = op == 0 || op == 3 || (op >= 5 && op <= 8);
+    if (op < 0 || op > 11 || !x || !out || n < 1 || (binary && !y)) return GB_ERR_ARG;
     double *d = nullptr;
     const size_t bytes = sizeof(double) * (size_t)n;
     if (cudaMalloc(&d, 3 * bytes) != cudaSuccess) return GB_ERR_CUDA;
