@@ -198,6 +198,36 @@ __device__ __forceinline__ bool operator>(dfloat a, dfloat b) { return b < a; }
 __device__ __forceinline__ bool operator<=(dfloat a, dfloat b) { return !(b < a); }
 __device__ __forceinline__ bool operator>=(dfloat a, dfloat b) { return !(a < b); }
 
+// Conversions between FP32 and FP64 by integer operations, giving the same bits as the conversion
+// instructions (which run on the FP64 pipe): f32_to_f64 is exact; f64_to_f32_rn rounds to nearest,
+// ties to even. The rare operands outside the plain cases (FP32 subnormals, results in the FP32
+// subnormal range, infinities, NaN) take the conversion instruction.
+__device__ __forceinline__ double f32_to_f64(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    const unsigned long long frac = (unsigned long long)(u & 0x7fffffu) << 29;
+    if (e == 0 && (u & 0x7fffffu) == 0) return __longlong_as_double((long long)sign);   // +-0
+    if (e == 0 || e == 255) return (double)f;
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 896) << 52) | frac));
+}
+__device__ __forceinline__ float f64_to_f32_rn(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
+    const unsigned sign = hw & 0x80000000u;
+    const int e = (int)((hw >> 20) & 0x7ffu);
+    if (e >= 897 && e <= 1150) {                              // normal FP32 range (overflow rounds to inf)
+        unsigned f = sign | ((unsigned)(e - 896) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29);
+        const unsigned rest = lw & 0x1fffffffu, half = 0x10000000u;
+        if (rest > half || (rest == half && (f & 1u))) f += 1u;   // a carry moves into the exponent
+        return __uint_as_float(f);
+    }
+    if (e <= 872) return __uint_as_float(sign);               // |x| < 2^-150: rounds to +-0
+    return __double2float_rn(x);
+}
+
 // pairs stored in place of FP64 values (8 bytes each, same alignment)
 __device__ __forceinline__ dfloat df_load(const double *p)
 {

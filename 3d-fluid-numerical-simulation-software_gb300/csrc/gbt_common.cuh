@@ -10,6 +10,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include "dfloat.cuh"
 
 namespace gbt {
 
@@ -168,6 +169,19 @@ enum {
     GBT_STATUS_WAIT_TIMEOUT = 8, // a kernel's bounded wait for its own asynchronous copies ran out
 };
 
+// an FP64 value in the working precision, and a working-precision value in FP64, with the
+// conversion instructions' rounding but without the FP64 pipe (dfloat.cuh)
+template <typename T> __device__ __forceinline__ T to_work(double x)
+{
+    if constexpr (sizeof(T) == 8) return x;
+    else return f64_to_f32_rn(x);
+}
+template <typename T> __device__ __forceinline__ double to_f64(T x)
+{
+    if constexpr (sizeof(T) == 8) return x;
+    else return f32_to_f64(x);
+}
+
 template <typename T> __device__ __forceinline__ T tsqrt(T x);
 template <> __device__ __forceinline__ double tsqrt<double>(double x) { return sqrt(x); }
 template <> __device__ __forceinline__ float tsqrt<float>(float x) { return sqrtf(x); }
@@ -237,11 +251,18 @@ __device__ __forceinline__ double rel_change(double o, double c)
     const double r1 = r0 * fma(-o, r0, 2.0);
     return fabs((o - c) * r1);
 }
-// the mixed form's term: the exact FP64 difference over o to FP32 accuracy (relative error of the
-// term, and so of the norm, below 2e-7), four FP64-pipe instructions in place of seven
+// the mixed form's term, |o - c| / |o| to FP32 accuracy without FP64 instructions: o and c split
+// into double-float pairs by integer operations (dfloat.cuh), their difference formed in FP32
+// (o.hi - c.hi is exact where the two are within a factor of two, so the difference keeps about
+// 2^-47 |o| absolute accuracy), times the approximate reciprocal of o.hi, widened to FP64 exactly
+// for the FP64 accumulation. Relative error of the term about 2^-22 wherever |o - c| > 2^-24 |o|.
 __device__ __forceinline__ double rel_change_mixed(double o, double c)
 {
-    return (double)fabsf((float)(o - c) * (1.0f / (float)o));
+    const dfloat a = df_from(o), b = df_from(c);
+    const float diff = __fadd_rn(__fsub_rn(a.hi, b.hi), __fsub_rn(a.lo, b.lo));
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a.hi));
+    return f32_to_f64(fabsf(__fmul_rn(diff, r)));
 }
 template <typename T>
 __device__ __forceinline__ double rel_change_t(double o, double c)

@@ -26,11 +26,12 @@ __device__ __forceinline__ void release_next_plane() { asm volatile("griddepcont
 // loads are dense. The neighbour's old flux F_n(Q) and the diagonal do not depend on dQ and are
 // formed before the wait, so only the new flux F_n(Q + dQ) and the combination sit on the
 // plane-to-plane critical path. Each lane's term is formed as
-//   u = (|S|/2) (F_n(Q+dQ) - F_n(Q)) +- (relax lambda_c / 2 + lambda_v) dQ_n
+//   u = ((|S|/2) (F_n(Q+dQ) - F_n(Q)) +- (relax lambda_c / 2 + lambda_v) dQ_n) / alpha
 // (+ forward, - backward): the reference's A and V terms of the same neighbour, grouped per lane
-// (source/LU_SGS_Marching.cpp:95-150, 293-419), so that the first lane forms
-//   forward:  dQ = (-R + (u_I + u_J + u_K)) / alpha
-//   backward: dQ = (alpha dQ* - (u_I + u_J + u_K)) / alpha.
+// and divided by the cell's diagonal (source/LU_SGS_Marching.cpp:95-150, 293-419), so that the first
+// lane forms
+//   forward:  dQ = -R / alpha + (u_I + u_J + u_K)
+//   backward: dQ = dQ* - (u_I + u_J + u_K).
 // In the FP64 form the terms before the wait are formed here in the reference's sequence; in the
 // mixed form the gather forms them for all cells at once. (k_sweep_df below is the FP64 form's
 // optional double-float variant.)
@@ -48,7 +49,7 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
     int nb = -1;
     T nx = 0, ny = 0, nz = 0, ve = 0, od = 0, omx = 0, omy = 0, omz = 0, oe = 0, sd = 0, rl = 0, lv = 0;
     T fo[5] = {(T)0, (T)0, (T)0, (T)0, (T)0}, rhs[5] = {(T)0, (T)0, (T)0, (T)0, (T)0};
-    T alpha = (T)1, inva = (T)1;
+    T inva = (T)1;
     if (active) {
         nb = S.nb[DIR > 0 ? 0 : 1][d][q];
         if (nb >= 0) {
@@ -74,22 +75,21 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
             sd = S.gs[d][nb];
             lv = S.lamv[d][nb];
         }
-        if (d == 0) {
-            if constexpr (sizeof(T) == 8) {
-                alpha = fdiv<T>(S.gvol[q], S.dt[q]) + P.relax * (S.lamc[0][q] + S.lamc[1][q] + S.lamc[2][q]) +
-                        (T)2 * (S.lamv[0][q] + S.lamv[1][q] + S.lamv[2][q]);
-                inva = frcp<T>(alpha);
-            } else {
-                inva = S.ainv[q];
-                alpha = S.alpha[q];
-            }
-            if (DIR > 0) {
+        // the cell's 1 / alpha on all three lanes (the warp executes these instructions once)
+        if constexpr (sizeof(T) == 8) {
+            const T alpha = fdiv<T>(S.gvol[q], S.dt[q]) + P.relax * (S.lamc[0][q] + S.lamc[1][q] + S.lamc[2][q]) +
+                            (T)2 * (S.lamv[0][q] + S.lamv[1][q] + S.lamv[2][q]);
+            inva = frcp<T>(alpha);
+        } else {
+            inva = S.ainv[q];
+        }
+        if (DIR > 0 && d == 0) {
 #pragma unroll
-                for (int c = 0; c < 5; c++) rhs[c] = -S.res[c][q];
-            }
+            for (int c = 0; c < 5; c++) rhs[c] = -S.res[c][q] * inva;
         }
     }
-    const T hs = (T)0.5 * sd, cq = (T)0.5 * rl + lv;
+    // the lane's coefficients, divided by alpha here so that the combination is three additions
+    const T hs = ((T)0.5 * sd) * inva, cq = ((T)0.5 * rl + lv) * inva;
     wait_previous_plane();
     T dqp[5];                            // backward sweep: this cell's forward-sweep dQ
     if (DIR < 0 && active && d == 0) {
@@ -103,7 +103,8 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
         for (int c = 0; c < 5; c++) dqn[c] = S.dq[c][nb];
         // flux difference F_n(Q+dQ) - F_n(Q) of the neighbour across its mean normal; the momentum
         // projection and |m|^2 are formed while the reciprocal of the density is computed, so that
-        // only V_n = (m.n)/rho and p = (g-1)(rho E - |m|^2/(2 rho)) follow it
+        // only V_n = (m.n)/rho and p = (g-1)(rho E - |m|^2/(2 rho)) follow it, and the old flux is
+        // taken off the pressure term, which does not wait for V_n
         const T nd = od + dqn[0], nmx = omx + dqn[1], nmy = omy + dqn[2], nmz = omz + dqn[3], ne = oe + dqn[4];
         const T mn = nmx * nx + nmy * ny + nmz * nz, m2 = nmx * nmx + nmy * nmy + nmz * nmz;
         const T inv = frcp<T>(nd);
@@ -111,10 +112,10 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
         const T dn = mn * inv - ve;
         T dF[5];
         dF[0] = nd * dn - fo[0];
-        dF[1] = (nmx * dn + pn * nx) - fo[1];
-        dF[2] = (nmy * dn + pn * ny) - fo[2];
-        dF[3] = (nmz * dn + pn * nz) - fo[3];
-        dF[4] = ((ne + pn) * dn + pn * ve) - fo[4];
+        dF[1] = nmx * dn + (pn * nx - fo[1]);
+        dF[2] = nmy * dn + (pn * ny - fo[2]);
+        dF[3] = nmz * dn + (pn * nz - fo[3]);
+        dF[4] = (ne + pn) * dn + (pn * ve - fo[4]);
 #pragma unroll
         for (int c = 0; c < 5; c++) u[c] = DIR > 0 ? hs * dF[c] + cq * dqn[c] : hs * dF[c] - cq * dqn[c];
     }
@@ -128,8 +129,7 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
 #pragma unroll
     for (int c = 0; c < 5; c++) {
         const T sum = (u[c] + u1[c]) + u2[c];
-        const T r = DIR > 0 ? rhs[c] + sum : alpha * dqp[c] - sum;
-        S.dq[c][q] = r * inva;
+        S.dq[c][q] = DIR > 0 ? rhs[c] + sum : dqp[c] - sum;
     }
 }
 
@@ -242,8 +242,8 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep_df(PhysW<double> P, SweepDat
 // flow inputs of the sweeps into plane order (before every forward sweep)
 // and, in the mixed form, the parts of the sweeps that do not depend on dQ, for all cells at once:
 // every cell's old flux F_n(Q) as the neighbour in each direction (across its mean normal, in the
-// rotating frame), its diagonal alpha = Vol/dt + relax sum lambda_c + 2 sum lambda_v and 1/alpha,
-// relax * lambda_c (the FP64 form forms them in the sweep kernel, where its parity was pinned)
+// rotating frame), 1/alpha of its diagonal alpha = Vol/dt + relax sum lambda_c + 2 sum lambda_v,
+// relax * lambda_c (the FP64 form forms them in the sweep kernel, in the reference's sequence)
 template <typename T>
 __global__ void __launch_bounds__(256) k_sweep_gather(PhysW<T> P, Flow<T> W, SweepData<T> S, long long nq)
 {
@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(256) k_sweep_gather(PhysW<T> P, Flow<T> W, Swe
     const long long p = S.cell[q];
     T cv[5], lc[3], lv[3];
 #pragma unroll
-    for (int c = 0; c < 5; c++) { cv[c] = (T)W.cv[c][p]; S.cv[c][q] = cv[c]; S.res[c][q] = W.res[c][p]; }
+    for (int c = 0; c < 5; c++) { cv[c] = to_work<T>(W.cv[c][p]); S.cv[c][q] = cv[c]; S.res[c][q] = W.res[c][p]; }
 #pragma unroll
     for (int d = 0; d < 3; d++) {
         lc[d] = W.lamc[d][p]; lv[d] = W.lamv[d][p];
@@ -265,7 +265,6 @@ __global__ void __launch_bounds__(256) k_sweep_gather(PhysW<T> P, Flow<T> W, Swe
     S.dt[q] = dt;
     if constexpr (sizeof(T) == 8) return;
     const T alpha = S.gvol[q] / dt + P.relax * (lc[0] + lc[1] + lc[2]) + (T)2 * (lv[0] + lv[1] + lv[2]);
-    S.alpha[q] = alpha;
     S.ainv[q] = (T)1 / alpha;
     const T od = cv[0], omx = cv[1], omy = cv[2], omz = cv[3], oe = cv[4];
     const T oinv = (T)1 / od;
@@ -375,10 +374,10 @@ __global__ void __launch_bounds__(256) k_sweep_fill(SweepData<T> S, long long nq
     for (int d = 0; d < 3; d++) { S.lamc[d][q] = (T)1; S.lamv[d][q] = (T)0.1; }
     S.dt[q] = (T)1;
     for (int c = 0; c < NQ; c++) { S.res[c][q] = (T)1e-3; S.dq[c][q] = (T)0; }
-    if (S.alpha) {
+    if (S.ainv) {
         for (int d = 0; d < 3; d++)
             for (int c = 0; c < NQ; c++) S.fo[d][c][q] = (T)0;
-        S.alpha[q] = (T)2; S.ainv[q] = (T)0.5;
+        S.ainv[q] = (T)0.5;
     }
 }
 
@@ -459,10 +458,11 @@ __device__ __forceinline__ void prim_from_cons(const Phys &P, const double c[5],
 {
     if constexpr (sizeof(T) == 4) {
         // mixed form: primitives are stored in FP32, so they are formed in FP32 from the FP64 Q
-        const float d = (float)c[0], rd = 1.0f / d;
-        const float u = (float)c[1] * rd, v = (float)c[2] * rd, w = (float)c[3] * rd;
+        // (conversions by integer operations: the same roundings as the conversion instructions)
+        const float d = f64_to_f32_rn(c[0]), rd = 1.0f / d;
+        const float u = f64_to_f32_rn(c[1]) * rd, v = f64_to_f32_rn(c[2]) * rd, w = f64_to_f32_rn(c[3]) * rd;
         const float V2 = u * u + v * v + w * w;
-        const float pr = ((float)P.gamma - 1.0f) * ((float)c[4] - d * V2 * 0.5f);
+        const float pr = ((float)P.gamma - 1.0f) * (f64_to_f32_rn(c[4]) - d * V2 * 0.5f);
         q[PD] = d; q[PU] = u; q[PV] = v; q[PW] = w; q[PP] = pr; q[PT] = pr * rd / (float)P.rgas;
     } else {
         // one FP64 division by the density, products with its reciprocal (within rounding)
@@ -494,7 +494,7 @@ __global__ void __launch_bounds__(256) k_update(Batch B, Phys P, Flow<T> W, int 
     for (int n = 0; n < 5; n++) {
         const double o = W.cv[n][p];
         W.cvold[n][p] = o;
-        c[n] = o + (double)W.dq[n][p];
+        c[n] = o + to_f64<T>(W.dq[n][p]);
         W.cv[n][p] = c[n];
     }
     T q[6];

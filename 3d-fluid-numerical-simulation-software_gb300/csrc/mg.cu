@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(256) k_delta(Batch B, Flow<T> W)
     if (!box_index(L.IM - 1, L.JM - 1, L.KM - 1, i, j, k)) return;
     const long long p = ix(L, i, j, k);
 #pragma unroll
-    for (int c = 0; c < NQ; c++) W.dq2h[c][p] = (T)(W.cv[c][p] - W.cv2h[c][p]);
+    for (int c = 0; c < NQ; c++) W.dq2h[c][p] = to_work<T>(W.cv[c][p] - W.cv2h[c][p]);
 }
 
 // 12 edges then 8 corners of the ghost layer, for Q and for the coarse correction

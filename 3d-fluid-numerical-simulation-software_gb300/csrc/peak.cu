@@ -92,7 +92,10 @@ __global__ void k_arith(int op, const double *__restrict__ x, const double *__re
     case 8: v = gbt::df_to_double(gbt::df_from(a) / gbt::df_from(b)); break;
     case 9: v = gbt::df_to_double(gbt::df_sqrt(gbt::df_from(a))); break;
     case 10: v = gbt::df_to_double(gbt::df_rcp(gbt::df_from(a))); break;
-    default: v = gbt::df_to_double(gbt::df_from(a)); break;
+    case 11: v = gbt::df_to_double(gbt::df_from(a)); break;
+    // FP32 <-> FP64 conversions by integer operations against the conversion instructions
+    case 12: v = gbt::f32_to_f64(gbt::f64_to_f32_rn(a)); break;
+    default: v = (double)__double2float_rn(a); break;
     }
     out[t] = v;
 }
@@ -102,7 +105,7 @@ __global__ void k_arith(int op, const double *__restrict__ x, const double *__re
 extern "C" int gb_fp64_arith_check(int op, const double *x, const double *y, long long n, double *out)
 {
     const bool binary = op == 0 || op == 3 || (op >= 5 && op <= 8);
-    if (op < 0 || op > 11 || !x || !out || n < 1 || (binary && !y)) return GB_ERR_ARG;
+    if (op < 0 || op > 13 || !x || !out || n < 1 || (binary && !y)) return GB_ERR_ARG;
     double *d = nullptr;
     const size_t bytes = sizeof(double) * (size_t)n;
     if (cudaMalloc(&d, 3 * bytes) != cudaSuccess) return GB_ERR_CUDA;

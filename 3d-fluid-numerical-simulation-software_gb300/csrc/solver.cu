@@ -854,7 +854,7 @@ public:
         pt.nq = (long long)nq;
         auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
         const bool sa = P.turb_sa && l == 1;
-        const size_t n_pre = sizeof(T) == 4 ? 17 : 0;      // mixed form: old fluxes and diagonal from the gather
+        const size_t n_pre = sizeof(T) == 4 ? 16 : 0;      // mixed form: old fluxes and 1 / diagonal from the gather
         const size_t n_t = 16 + 18 + NQ + n_pre + (sa ? 19 : 0);   // geometry, flow inputs, dQ (and the SA sweep's)
         Lv.plane_mem.bytes = al(sizeof(int) * start.size()) + al(sizeof(long long) * nq) + 6 * al(sizeof(int) * nq) +
                              n_t * al(sizeof(T) * nq) + 256;
@@ -890,7 +890,7 @@ public:
         if (n_pre) {
             for (int d = 0; d < 3; d++)
                 for (int c = 0; c < NQ; c++) S.fo[d][c] = arr();
-            S.alpha = arr(); S.ainv = arr();
+            S.ainv = arr();
         }
         if (sa) {
             for (int d = 0; d < 3; d++) { S.sa_vn[d] = arr(); S.sa_eb[d] = arr(); S.sa_s[d] = arr(); S.sa_rl[d] = arr(); S.sa_lv[d] = arr(); }

@@ -156,7 +156,9 @@ def fp64_rate() -> float:
 def fp64_arith_check(op: int, x: np.ndarray, y: Optional[np.ndarray] = None) -> np.ndarray:
     """the device's FP64 arithmetic on host arrays: op 0 x / y, 1 sqrt(x), 2 1 / x as the FP64 form's
     kernels compute them (Newton-refined), 3 and 4 the IEEE x / y and sqrt(x); 5-10 x + y, x - y,
-    x * y, x / y, sqrt(x), 1 / x in double-float (FP32 pairs), 11 x converted to a pair and back"""
+    x * y, x / y, sqrt(x), 1 / x in double-float (FP32 pairs), 11 x converted to a pair and back,
+    12 and 13 x rounded to FP32 and widened back by integer operations / by the conversion
+    instructions"""
     L = load()
     x = np.ascontiguousarray(x, dtype=np.float64)
     yy = None if y is None else np.ascontiguousarray(y, dtype=np.float64)

@@ -169,7 +169,8 @@ int gb_fp64_rate(double *flop_per_s);
  * inputs, so that they can be checked against the IEEE operations: op 0 x / y, 1 sqrt(x), 2 1 / x;
  * op 3 and 4 are the device's IEEE x / y and sqrt(x); ops 5-10 are x + y, x - y, x * y, x / y,
  * sqrt(x) and 1 / x in double-float and op 11 the conversion of x to a double-float pair and back,
- * each from FP64 inputs to an FP64 result. x, y (y only for ops 0, 3 and 5-8) and out are host
+ * each from FP64 inputs to an FP64 result; op 12 rounds x to FP32 and widens it back by integer
+ * operations (the mixed form's conversions), op 13 by the conversion instructions. x, y (y only for ops 0, 3 and 5-8) and out are host
  * arrays. No counterpart in the reference. */
 int gb_fp64_arith_check(int op, const double *x, const double *y, long long n, double *out);
 

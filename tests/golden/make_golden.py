@@ -70,6 +70,12 @@ LONG = {
     "rotor_25x25x65_converged": ("rotor_passage", dict(IM=25, JM=25, KM=65),
                                  {"Pout": "%.1f" % (1.05 * 101325.0), "multigrid": "Y", "coarse_iter": "2",
                                   "Ma0": "0.45", "maxiter": "6000"}, 6000),
+    # the benchmark's passage (129x49x49 nodes, 1.20 x p_t, two-level FAS) run for 2000 cycles: the
+    # reference's own solution leaves the converging branch (mass flow falls from about 28.6 to 10
+    # between cycles 800 and 1800 and the outlet flow reverses); single-threaded about 80 minutes
+    "rotor_129x49x49_2000": ("rotor_passage", dict(IM=49, JM=49, KM=129),
+                             {"Pout": "%.1f" % (1.20 * 101325.0), "multigrid": "Y", "coarse_iter": "2",
+                              "Ma0": "0.45"}, 2000),
 }
 
 # multi-block: the rotor passage cut at the blade's leading- and trailing-edge planes into three

@@ -85,3 +85,22 @@ def test_double_float_operations(gpu_lib):
     want = x - z
     ok = want != 0
     assert np.max(np.abs(got[ok] - want[ok]) / np.abs(want[ok])) <= DF_REL[6]
+
+
+def test_integer_conversions_equal_the_conversion_instructions(gpu_lib):
+    # FP64 -> FP32 (round to nearest, ties to even) -> FP64 by integer operations against the
+    # conversion instructions and numpy, bit for bit: random values over the whole FP32 range,
+    # halfway cases (ties), the largest finite FP32 and just above, FP32 subnormal results, zeros
+    rng = np.random.default_rng(17)
+    x = 10.0 ** rng.uniform(-44.0, 38.5, 1 << 17) * rng.choice([-1.0, 1.0], 1 << 17)
+    f = rng.uniform(1.0, 2.0, 1 << 14).astype(np.float32).astype(np.float64)
+    ulp = np.spacing(f.astype(np.float32)).astype(np.float64)
+    ties = np.concatenate([f + 0.5 * ulp, f - 0.25 * ulp, f + 0.5 * ulp * (1 + 2.0 ** -28)])
+    edge = np.array([0.0, -0.0, float(np.finfo(np.float32).max), 3.4028235677973366e38, 1e39, -1e39,
+                     2.0 ** -149, 2.0 ** -150, 1.5 * 2.0 ** -150, 2.0 ** -126, 2.0 ** -127, 1e-300, np.inf, -np.inf])
+    for v in (x, ties, edge):
+        got = gpu_lib.fp64_arith_check(12, v)
+        want = gpu_lib.fp64_arith_check(13, v)
+        assert np.array_equal(got.view(np.int64), want.view(np.int64))
+        with np.errstate(over="ignore"):
+            assert np.array_equal(got.view(np.int64), v.astype(np.float32).astype(np.float64).view(np.int64))

@@ -11,7 +11,14 @@ generator call).
    relative (5e-8 at most measured); along the whole run they stay within 1e-5 (the start-up transient amplifies the
    last bits, by up to 3e-6 measured). The mixed form converges within ten cycles of it, to its
    integrals within 0.1% in mass flow and 1e-4 in pressure ratio.
-2. The 65x33x33 annular duct, single grid, 2000 iterations (no rotation, no blade): mass flows
+2. The benchmark's own passage, 129x49x49 nodes at 1.20 x p_t, two-level FAS, 2000 cycles
+   against the reference's run of the same case (fixture rotor_129x49x49_2000): the reference's
+   solution does not converge; it leaves the converging branch near cycle 800 (inlet mass flow
+   28.6 at cycle 500, 24.1 at 1000, 11.1 at 1500) and the outlet flow reverses before cycle 2000.
+   The FP64 GPU path follows it: mass flows and pressure ratio within 1e-6 up to cycle 800
+   (5.3e-7 measured) and 1e-5 up to cycle 1150 (5.8e-6), the same breakdown afterwards; the mixed
+   form within 1e-5 up to cycle 800 (1.3e-6) and the same breakdown.
+3. The 65x33x33 annular duct, single grid, 2000 iterations (no rotation, no blade): mass flows
    and total-pressure ratio to 1e-6. The duct does no work, so its efficiency
    eta = (PR^((g-1)/g) - 1) / (Tt_out / Tt_in - 1) is a ratio of two numbers near zero; it is held
    to 1e-6 times its condition number (the relative change of eta per relative change of its two
@@ -100,6 +107,39 @@ def test_rotor_mixed_converges_to_the_fp64_integrals(rotor_case, rotor_fp64, gpu
     for col in (INTEGRALS["m_in"], INTEGRALS["m_out"]):
         assert abs(h[c - 1, col] - f[col]) / abs(f[col]) < 1e-3
     assert abs(h[c - 1, INTEGRALS["PR"]] - f[INTEGRALS["PR"]]) < 1e-4
+
+
+PASSAGE = "rotor_129x49x49_2000"
+PASSAGE_OPTS = {"Pout": "%.1f" % (1.20 * 101325.0), "multigrid": "Y", "coarse_iter": "2", "Ma0": "0.45"}
+
+
+@pytest.fixture(scope="module")
+def passage_case(tmp_path_factory, meshgen):
+    ref = np.load(f"{GOLDEN}/{PASSAGE}.npz")["history"]
+    d = str(tmp_path_factory.mktemp("long") / PASSAGE)
+    meshgen.write_case(meshgen.rotor_passage(IM=49, JM=49, KM=129, options=dict(PASSAGE_OPTS), name=PASSAGE), d)
+    return d, ref
+
+
+def _breaks_down(h):
+    # inlet mass flow below 0.45 of its cycle-500 value somewhere in cycles 1300-2000, and reversed
+    # flow at the outlet (negative outlet mass flow) before cycle 2000
+    return float(np.min(h[1299:, 6])) < 0.45 * float(h[499, 6]) and float(np.min(h[1299:, 7])) < 0.0
+
+
+@pytest.mark.parametrize("form", ["fp64", "mixed"])
+def test_benchmark_passage_follows_the_reference_into_its_breakdown(passage_case, gpu_lib, form):
+    d, ref = passage_case
+    with gpu_lib.Solver(d, gpu_lib.FP64 if form == "fp64" else gpu_lib.MIXED) as s:
+        s.init_uniform()
+        h = s.iterate(ref.shape[0])[:, 0, :]
+    assert _breaks_down(ref)
+    assert _breaks_down(h)
+    cols = [INTEGRALS["m_in"], INTEGRALS["m_out"], INTEGRALS["PR"]]
+    windows = [(800, 1e-6), (1150, 1e-5)] if form == "fp64" else [(800, 1e-5)]
+    for n, bar in windows:
+        err = float(np.max(np.abs(h[:n][:, cols] - ref[:n][:, cols]) / np.abs(ref[:n][:, cols])))
+        assert err < bar, (form, n, err)
 
 
 @pytest.fixture(scope="module")
