@@ -95,8 +95,10 @@ __device__ __forceinline__ void recon_cons(int type, T gamma, const C5<T> &FF, c
     if (cr.d <= lz || pR <= lz) cr = B;
 }
 
+// Harten's entropy fix z > d ? z : 0.5 (z^2 + d^2) / d at the Roe flux's d = 0.5, where it is
+// z^2 + 0.25 bit for bit (the halving and the division by one half are exact)
 template <typename T>
-__device__ __forceinline__ T entropy_corr(T z, T d) { return z > d ? z : (T)0.5 * (z * z + d * d) / d; }
+__device__ __forceinline__ T entropy_corr_half(T z) { return z > (T)0.5 ? z : z * z + (T)0.25; }
 
 // Roe flux in the face frame with Harten's fix (delta fixed at 0.5) and the reference's wave
 // strengths arr[2], arr[3] divided by (v+1e-8), (w+1e-8)
@@ -118,8 +120,7 @@ __device__ __forceinline__ C5<T> roe(T gamma, const C5<T> &QL, const C5<T> &QR, 
     T q2 = ua * ua + va * va + wa * wa;
     T ca = fsqrt<T>(g1 * (Ha - (T)0.5 * q2));
     T una = ua - qe;
-    const T delta = (T)0.5;
-    T l1 = entropy_corr(tabs(una - ca), delta), l2 = entropy_corr(tabs(una), delta), l5 = entropy_corr(tabs(una + ca), delta);
+    T l1 = entropy_corr_half(tabs(una - ca)), l2 = entropy_corr_half(tabs(una)), l5 = entropy_corr_half(tabs(una + ca));
     T dd = dR - dL, dmx = QR.mx - QL.mx, dmy = QR.my - QL.my, dmz = QR.mz - QL.mz, de = QR.e - QL.e;
     T a2, a3;
     if constexpr (sizeof(T) == 8) {

@@ -239,6 +239,44 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep_df(PhysW<double> P, SweepDat
     }
 }
 
+// dQ from plane order back into the box (after the backward sweep), through shared-memory tiles.
+// A hyperplane's cells are never neighbours in the k-contiguous box (consecutive plane cells
+// (i, j, k), (i, j+1, k-1) lie NK - 1 apart), so a per-cell copy writes one DRAM sector per value.
+// A block here takes a 32 x 32 (j, k) tile of one i-row of one solve and one component (grid.z):
+// it reads the tile's j + k = const diagonals, which are runs of consecutive plane-order indices
+// (the plane order enumerates i, then j), and writes k-rows of the box, so both sides move whole
+// sectors. (The same tiling for the gather, box to plane order before the forward sweep, was
+// slower than the per-cell gather: the mixed form's derived terms then need a second pass.)
+template <typename T>
+__global__ void __launch_bounds__(256) k_sweep_scatter_tiled(Batch B, const int *__restrict__ rq,
+                                                             const long long *__restrict__ rq_off, SweepData<T> S, Flow<T> W,
+                                                             int tj, int tk)
+{
+    const int s = blockIdx.y, c = blockIdx.z;             // solve, component
+    const Lvl L = B.lv[s];
+    const int nI = L.IM - 1, nJ = L.JM - 1, nK = L.KM - 1;
+    const int kb = (int)(blockIdx.x % (unsigned)tk), jb = (int)((blockIdx.x / (unsigned)tk) % (unsigned)tj);
+    const int i = (int)(blockIdx.x / ((unsigned)tk * (unsigned)tj)) + 1;
+    const int j0 = jb * 32 + 1, k0 = kb * 32 + 1;
+    if (i > nI || j0 > nJ || k0 > nK) return;
+    // row stride 34: the diagonals (word offset 33 jj + dd) and the k-rows both hit 32 banks
+    __shared__ T tile[32][34];
+    const int lane = threadIdx.x & 31, w = (int)(threadIdx.x >> 5);
+    const int *rqi = rq + rq_off[s] + (i - 1);          // row start of plane pl: rqi[pl * nI]
+    const T *src = S.dq[c];
+    for (int dd = w; dd < 63; dd += 8) {
+        const int kk = dd - lane, j = j0 + lane, k = k0 + kk;
+        if (kk >= 0 && kk < 32 && j <= nJ && k <= nK) tile[lane][kk] = src[rqi[(long long)(i + j + k) * nI] + j];
+    }
+    __syncthreads();
+    T *dst = W.dq[c];
+#pragma unroll
+    for (int r = w; r < 32; r += 8) {
+        const int j = j0 + r, k = k0 + lane;
+        if (j <= nJ && k <= nK) dst[ix(L, i, j, k)] = tile[r][lane];
+    }
+}
+
 // flow inputs of the sweeps into plane order (before every forward sweep)
 // and, in the mixed form, the parts of the sweeps that do not depend on dQ, for all cells at once:
 // every cell's old flux F_n(Q) as the neighbour in each direction (across its mean normal, in the
@@ -442,7 +480,13 @@ void launch_lusgs_sweeps(const LaunchCtx &ctx, const PhysW<T> &P, const Geo &G, 
         ctx.mark("sa_sweeps", 0, np - 2);
     }
     ctx.mark("sweep_scatter", 1, 1);
-    k_sweep_scatter<T><<<gq, 256, 0, ctx.stream>>>(W, S, pt.nq, pt.df != 0);
+    if (pt.df) {
+        k_sweep_scatter<T><<<gq, 256, 0, ctx.stream>>>(W, S, pt.nq, true);
+    } else {
+        const int tj = (ctx.maxJM - 1 + 31) / 32, tk = (ctx.maxKM - 1 + 31) / 32;
+        const unsigned gx = (unsigned)((ctx.maxIM - 1) * tj * tk);
+        k_sweep_scatter_tiled<T><<<dim3(gx, ctx.batch.nsolve, NQ), 256, 0, ctx.stream>>>(ctx.batch, pt.rq, pt.rq_off, S, W, tj, tk);
+    }
     ctx.mark("sweep_scatter", 0, 1);
 }
 

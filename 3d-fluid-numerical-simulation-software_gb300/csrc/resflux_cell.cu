@@ -146,17 +146,35 @@ __global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, PhysW<T> PC, Flow
     // line order n0 = 1..N-1 (n0 = 1 next to the wall); warp wp takes n0 = 1 + wp, 1 + wp + BL_WARPS, ...
 #define CELL(n0) (p0 + (long long)(lo ? (n0) : N - (n0)) * sn)
     // pass 1: wall shear, taken as the largest |omega * mu_l| along the line
+    // Each pass takes a thread's points in chunks of four whose loads are issued together (indices
+    // clamped to the line, so that the loads need no guard) and then processed in line order; the
+    // first BL_CACHE points in unrolled chunks, so that pass 2 keeps their damping in registers.
     T tmax = (T)0;
     bool any = false;
     if (live) {
-        for (int n0 = 1 + wp; n0 < N; n0 += BL_WARPS) {
-            const long long p = CELL(n0);
-            const T ml = sutherland(PC, W.pv[PT][p]);
-            const T tw = tabs(W.omega[p] * ml);
-            if (n0 == 1) { sh_d1[lane] = W.pv[PD][p]; sh_m1[lane] = ml; }     // first cell: density, mu_l
+        auto p1 = [&](int n0, T tp, T om) {
+            const T ml = sutherland(PC, tp);
+            const T tw = tabs(om * ml);
+            if (n0 == 1) { sh_d1[lane] = W.pv[PD][CELL(1)]; sh_m1[lane] = ml; }   // first cell: density, mu_l
             if (!any || tw > tmax) tmax = tw;
             any = true;
+        };
+#pragma unroll
+        for (int ch = 0; ch < BL_CACHE / 4; ch++) {
+            const int nb = 1 + wp + ch * 4 * BL_WARPS;
+            if (nb < N) {
+                T tv[4], ov[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const long long p = CELL(min(nb + u * BL_WARPS, N - 1));
+                    tv[u] = W.pv[PT][p]; ov[u] = W.omega[p];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (nb + u * BL_WARPS < N) p1(nb + u * BL_WARPS, tv[u], ov[u]);
+            }
         }
+        for (int n0 = 1 + wp + BL_CACHE * BL_WARPS; n0 < N; n0 += BL_WARPS) p1(n0, W.pv[PT][CELL(n0)], W.omega[CELL(n0)]);
     }
     sh_a[wp][lane] = tmax;
     sh_n[wp][lane] = any;
@@ -178,17 +196,33 @@ __global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, PhysW<T> PC, Flow
     // van Driest damping of this thread's first BL_CACHE points, reused by pass 3
     T c_damp[BL_CACHE];
     if (live) {
-        int ci = 0;
-        for (int n0 = 1 + wp; n0 < N; n0 += BL_WARPS, ci++) {
-            const long long p = CELL(n0);
-            const T dis = DIST(n0);
-            const T u = W.pv[PU][p], v = W.pv[PV][p], w = W.pv[PW][p];
+        auto p2 = [&](int n0, T dis, T u, T v, T w, T om) -> T {
             const T V = tsqrt(u * u + v * v + w * w);
             if (V > Udif) Udif = V;
             const T damp = (T)1 - exp(-(dis * Ret) / Aplus);
-            if (ci < BL_CACHE) c_damp[ci] = damp;
-            const T F = dis * tabs(W.omega[p]) * damp;
+            const T F = dis * tabs(om) * damp;
             if (F > Fmax) { Fmax = F; ymax = dis; nmax = n0; }
+            return damp;
+        };
+#pragma unroll
+        for (int ch = 0; ch < BL_CACHE / 4; ch++) {
+            const int nb = 1 + wp + ch * 4 * BL_WARPS;
+            if (nb < N) {
+                T dv[4], uv[4], vv[4], wv[4], ov[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int m = min(nb + u * BL_WARPS, N - 1);
+                    const long long p = CELL(m);
+                    dv[u] = DIST(m); uv[u] = W.pv[PU][p]; vv[u] = W.pv[PV][p]; wv[u] = W.pv[PW][p]; ov[u] = W.omega[p];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (nb + u * BL_WARPS < N) c_damp[ch * 4 + u] = p2(nb + u * BL_WARPS, dv[u], uv[u], vv[u], wv[u], ov[u]);
+            }
+        }
+        for (int n0 = 1 + wp + BL_CACHE * BL_WARPS; n0 < N; n0 += BL_WARPS) {
+            const long long p = CELL(n0);
+            p2(n0, DIST(n0), W.pv[PU][p], W.pv[PV][p], W.pv[PW][p], W.omega[p]);
         }
     }
     __syncthreads();
@@ -215,13 +249,9 @@ __global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, PhysW<T> PC, Flow
     const T ym = sh_ymax[lane], Fwake = sh_fwake[lane];
     // (Ret * dis) equals (dis * Ret) exactly, so the cached damping is the value pass 3 would form
     // pass 3: inner and outer viscosity, the smaller one merged into mu_t
-    int ci = 0;
-    for (int n0 = 1 + wp; n0 < N; n0 += BL_WARPS, ci++) {
+    auto p3 = [&](int n0, T dis, T damp, T om, T rho) {
         const long long p = CELL(n0);
-        const T dis = DIST(n0);
-        const T damp = ci < BL_CACHE ? c_damp[ci] : (T)1 - exp(-(Ret * dis) / Aplus);
         const T bL = kap * dis * damp;
-        const T om = W.omega[p], rho = W.pv[PD][p];
         const T m_in = rho * bL * bL * om;
         const T r = Ckleb * dis / ym;
         const T r2 = r * r;
@@ -231,12 +261,33 @@ __global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, PhysW<T> PC, Flow
         if (n0 == 1) {
             atomicMin(&W.blmin[p], 0ull);                      // wall-adjacent cell: mu_t = 0
             W.mut[p0 + (long long)(lo ? 0 : N) * sn] = (T)0;   // its ghost
-            continue;
+            return;
         }
         // the smallest mu_t over the walls whose lines reach the cell (the reference's merge,
         // BL_Model.cpp:88-96,163-171,239-247: the first wall sets it, later walls keep the minimum; mu_t >= 0, so
         // the minimum of the bit patterns is the minimum of the values and the walls' order is moot)
         atomicMin(&W.blmin[p], bl_bits(mt));
+    };
+#pragma unroll
+    for (int ch = 0; ch < BL_CACHE / 4; ch++) {
+        const int nb = 1 + wp + ch * 4 * BL_WARPS;
+        if (nb < N) {
+            T dv[4], ov[4], rv[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int m = min(nb + u * BL_WARPS, N - 1);
+                const long long p = CELL(m);
+                dv[u] = DIST(m); ov[u] = W.omega[p]; rv[u] = W.pv[PD][p];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (nb + u * BL_WARPS < N) p3(nb + u * BL_WARPS, dv[u], c_damp[ch * 4 + u], ov[u], rv[u]);
+        }
+    }
+    for (int n0 = 1 + wp + BL_CACHE * BL_WARPS; n0 < N; n0 += BL_WARPS) {
+        const long long p = CELL(n0);
+        const T dis = DIST(n0);
+        p3(n0, dis, (T)1 - exp(-(Ret * dis) / Aplus), W.omega[p], W.pv[PD][p]);
     }
 #undef CELL
 #undef DIST

@@ -812,9 +812,13 @@ public:
         std::vector<long long> cell;
         std::vector<int> start((size_t)nsolve * pt.stride + 1, 0);
         std::vector<int> nbq[2][3];
+        std::vector<int> rq;                       // row starts of the transpositions (PlaneTables::rq)
+        std::vector<long long> rq_off(nsolve);
         for (int s = 0; s < nsolve; s++) {
             const Lvl &v = Lv.lv[s];
             const int nI = v.IM - 1, nJ = v.JM - 1, nK = v.KM - 1;
+            rq_off[s] = (long long)rq.size();
+            rq.resize(rq.size() + (size_t)pt.stride * nI, 0);
             // q of interior cell (i,j,k) of this solve
             std::vector<int> qof((size_t)nI * nJ * nK, -1);
             auto at = [&](int i, int j, int k) -> int & { return qof[((size_t)(i - 1) * nJ + (j - 1)) * nK + (k - 1)]; };
@@ -822,14 +826,17 @@ public:
                 start[(size_t)s * pt.stride + pl] = (int)cell.size();
                 int c = 0;
                 if (pl >= 3)
-                    for (int i = 1; i <= nI; i++)
+                    for (int i = 1; i <= nI; i++) {
+                        bool first = true;
                         for (int j = 1; j <= nJ; j++) {
                             const int k = pl - i - j;
                             if (k < 1 || k > nK) continue;
+                            if (first) { rq[(size_t)rq_off[s] + (size_t)pl * nI + (i - 1)] = (int)cell.size() - j; first = false; }
                             at(i, j, k) = (int)cell.size();
                             cell.push_back(ix(v, i, j, k));
                             c++;
                         }
+                    }
                 pt.max_count[pl] = std::max(pt.max_count[pl], c);
             }
             if (cell.size() > (size_t)0x7fffffff) throw std::runtime_error("batch too large for the plane tables");
@@ -857,13 +864,19 @@ public:
         const size_t n_pre = sizeof(T) == 4 ? 16 : 0;      // mixed form: old fluxes and 1 / diagonal from the gather
         const size_t n_t = 16 + 18 + NQ + n_pre + (sa ? 19 : 0);   // geometry, flow inputs, dQ (and the SA sweep's)
         Lv.plane_mem.bytes = al(sizeof(int) * start.size()) + al(sizeof(long long) * nq) + 6 * al(sizeof(int) * nq) +
-                             n_t * al(sizeof(T) * nq) + 256;
+                             al(sizeof(int) * rq.size()) + al(sizeof(long long) * rq_off.size()) + n_t * al(sizeof(T) * nq) + 256;
         CK(cudaMalloc(&Lv.plane_mem.p, Lv.plane_mem.bytes));
         char *q = (char *)Lv.plane_mem.p;
         auto take = [&](size_t b) { char *r = q; q += al(b); return r; };
         int *dstart = (int *)take(sizeof(int) * start.size());
         CK(cudaMemcpy(dstart, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
         pt.start = dstart;
+        int *drq = (int *)take(sizeof(int) * rq.size());
+        CK(cudaMemcpy(drq, rq.data(), sizeof(int) * rq.size(), cudaMemcpyHostToDevice));
+        long long *drq_off = (long long *)take(sizeof(long long) * rq_off.size());
+        CK(cudaMemcpy(drq_off, rq_off.data(), sizeof(long long) * rq_off.size(), cudaMemcpyHostToDevice));
+        pt.rq = drq;
+        pt.rq_off = drq_off;
         SweepData<T> &S = Lv.sweep;
         long long *dcell = (long long *)take(sizeof(long long) * nq);
         CK(cudaMemcpy(dcell, cell.data(), sizeof(long long) * nq, cudaMemcpyHostToDevice));
