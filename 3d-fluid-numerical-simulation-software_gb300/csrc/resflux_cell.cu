@@ -9,8 +9,8 @@
 namespace gbt {
 
 // lambda_c per direction and |curl V| (needs ghosts of the velocity)
-template <typename T>
-__global__ void __launch_bounds__(256) k_cell_a(Batch B, Phys P, PhysW<T> PC, GeoW<T> G, Flow<T> W)
+template <typename T, bool NS>   // NS: Navier-Stokes (the curl is needed), else Euler
+__global__ void __launch_bounds__(256) k_cell_a(Batch B, PhysW<T> PC, GeoW<T> G, Flow<T> W)
 {
     const int s = blockIdx.y;
     const Lvl L = B.lv[s];
@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(256) k_cell_a(Batch B, Phys P, PhysW<T> PC, Ge
         T sx = G.sb[d][0][p], sy = G.sb[d][1][p], sz = G.sb[d][2][p];
         lam[d] = tabs(ur * sx + vr * sy + w * sz) + cs * tsqrt(sx * sx + sy * sy + sz * sz);
     }
-    if (!P.equation_ns) {
+    if constexpr (!NS) {
 #pragma unroll
         for (int d = 0; d < 3; d++) W.lamc[d][p] = lam[d];
         return;
@@ -321,8 +321,8 @@ __global__ void k_wall_mut(Batch B, Flow<T> W, const DevWall *walls)
 }
 
 // viscous spectral radii and the local time step
-template <typename T>
-__global__ void __launch_bounds__(256) k_cell_b(Batch B, Phys P, PhysW<T> PC, GeoW<T> G, Flow<T> W, int level)
+template <typename T, bool NS>   // NS: Navier-Stokes (viscous radii), else Euler
+__global__ void __launch_bounds__(256) k_cell_b(Batch B, PhysW<T> PC, GeoW<T> G, Flow<T> W, int level)
 {
     const int s = blockIdx.y;
     const Lvl L = B.lv[s];
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(256) k_cell_b(Batch B, Phys P, PhysW<T> PC, Ge
     const T vol = G.vol[p];
     T lc = W.lamc[0][p] + W.lamc[1][p] + W.lamc[2][p];
     T lv = (T)0;
-    if (P.equation_ns) {
+    if constexpr (NS) {
         const T ml = sutherland(PC, W.pv[PT][p]);
         const T mt = W.mut[p];
         const T rho = W.pv[PD][p];
@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(256) k_cell_b(Batch B, Phys P, PhysW<T> PC, Ge
         for (int d = 0; d < 3; d++) W.lamv[d][p] = l[d];
         lv = l[0] + l[1] + l[2];
     }
-    W.dt[p] = (T)(dtf * cfl) * vol / (lc + PC.c_timestep * lv);
+    W.dt[p] = to_work<T>(dtf * cfl) * vol / (lc + PC.c_timestep * lv);
 }
 
 // global time stepping: minimum over the solve, then broadcast (source/TimeStep.cpp:64-87)
@@ -401,7 +401,8 @@ void launch_cell_stages(const LaunchCtx &ctx, const Phys &P, const PhysW<T> &PC,
 {
     const Batch &B = ctx.batch;
     ctx.mark("spectral_curl", 1);
-    k_cell_a<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, PC, GW, W);
+    if (P.equation_ns) k_cell_a<T, true><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, PC, GW, W);
+    else k_cell_a<T, false><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, PC, GW, W);
     ctx.mark("spectral_curl", 0);
     ctx.mark("baldwin_lomax", 1, 4);
     if (level == 1 && P.turb_bl && bc.n_wall > 0) {
@@ -419,7 +420,8 @@ void launch_cell_stages(const LaunchCtx &ctx, const Phys &P, const PhysW<T> &PC,
     }
     ctx.mark("baldwin_lomax", 0, 4);
     ctx.mark("time_step", 1, 2);
-    k_cell_b<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, PC, GW, W, level);
+    if (P.equation_ns) k_cell_b<T, true><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, PC, GW, W, level);
+    else k_cell_b<T, false><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, PC, GW, W, level);
     if (P.global_dt) {
         k_dt_min<T><<<dim3(1, B.nsolve), 1024, 0, ctx.stream>>>(B, W, scratch);
         k_dt_set<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, W, scratch);

@@ -136,9 +136,11 @@ __global__ void __launch_bounds__(128) k_jst_dissip(Batch B, Phys P, Flow<T> W)
     for (int c = 0; c < NQ; c++) W.Fd[F][c][p] = d[c];
 }
 
-// face sums, rotation source, residual R = Fc - Fv (- Fd with JST)
-template <typename T>
-__global__ void __launch_bounds__(256) k_cell_sum(Batch B, Phys P, GeoW<T> G, Flow<T> W)
+// face sums, rotation source, residual R = Fc - Fv (- Fd with JST). The viscous and dissipation
+// terms are compile-time switches (NS, JST), so that every load of a cell is issued before the
+// first sum instead of behind a branch.
+template <typename T, bool NS, bool JST>
+__global__ void __launch_bounds__(256) k_cell_sum(Batch B, GeoW<T> G, Flow<T> W)
 {
     const int s = blockIdx.y;
     const Lvl L = B.lv[s];
@@ -154,10 +156,10 @@ __global__ void __launch_bounds__(256) k_cell_sum(Batch B, Phys P, GeoW<T> G, Fl
     for (int c = 0; c < NQ; c++) {
         T fc = W.Ff[0][c][pI] - W.Ff[0][c][p] + W.Ff[1][c][pJ] - W.Ff[1][c][p] + W.Ff[2][c][pK] - W.Ff[2][c][p] - src[c];
         T fv = (T)0;
-        if (P.equation_ns)
+        if constexpr (NS)
             fv = W.Vf[0][c][pI] - W.Vf[0][c][p] + W.Vf[1][c][pJ] - W.Vf[1][c][p] + W.Vf[2][c][pK] - W.Vf[2][c][p];
         r[c] = fc - fv;
-        if (W.Fd[0][0])
+        if constexpr (JST)
             r[c] = r[c] - (W.Fd[0][c][pI] - W.Fd[0][c][p] + W.Fd[1][c][pJ] - W.Fd[1][c][p] + W.Fd[2][c][pK] - W.Fd[2][c][p]);
     }
 #pragma unroll
@@ -212,7 +214,11 @@ void launch_resflux(const LaunchCtx &ctx, const Phys &P, const PhysW<T> &PC, con
         ctx.mark("jst_dissipation", 0, 7);
     }
     ctx.mark("cell_sum", 1);
-    k_cell_sum<T><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, P, GW, W);
+    const bool jst = W.Fd[0][0] != nullptr;
+    if (P.equation_ns && !jst) k_cell_sum<T, true, false><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, GW, W);
+    else if (P.equation_ns) k_cell_sum<T, true, true><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, GW, W);
+    else if (!jst) k_cell_sum<T, false, false><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, GW, W);
+    else k_cell_sum<T, false, true><<<ctx.grid_cells(256), 256, 0, ctx.stream>>>(B, GW, W);
     ctx.mark("cell_sum", 0);
 }
 
