@@ -83,18 +83,29 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
         } else {
             inva = S.ainv[q];
         }
-        if (DIR > 0 && d == 0) {
+        if (DIR > 0) {
+            if constexpr (sizeof(T) == 8) {
+                // lane d combines components d and d + 3 (below)
+                rhs[0] = -S.res[d][q] * inva;
+                if (d < 2) rhs[1] = -S.res[d + 3][q] * inva;
+            } else if (d == 0) {
 #pragma unroll
-            for (int c = 0; c < 5; c++) rhs[c] = -S.res[c][q] * inva;
+                for (int c = 0; c < 5; c++) rhs[c] = -S.res[c][q] * inva;
+            }
         }
     }
     // the lane's coefficients, divided by alpha here so that the combination is three additions
     const T hs = ((T)0.5 * sd) * inva, cq = ((T)0.5 * rl + lv) * inva;
     wait_previous_plane();
     T dqp[5];                            // backward sweep: this cell's forward-sweep dQ
-    if (DIR < 0 && active && d == 0) {
+    if (DIR < 0 && active) {
+        if constexpr (sizeof(T) == 8) {
+            dqp[0] = S.dq[d][q];
+            if (d < 2) dqp[1] = S.dq[d + 3][q];
+        } else if (d == 0) {
 #pragma unroll
-        for (int c = 0; c < 5; c++) dqp[c] = S.dq[c][q];
+            for (int c = 0; c < 5; c++) dqp[c] = S.dq[c][q];
+        }
     }
     T u[5] = {(T)0, (T)0, (T)0, (T)0, (T)0};
     if (nb >= 0) {
@@ -119,17 +130,55 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
 #pragma unroll
         for (int c = 0; c < 5; c++) u[c] = DIR > 0 ? hs * dF[c] + cq * dqn[c] : hs * dF[c] - cq * dqn[c];
     }
-    T u1[5], u2[5];
+    if constexpr (sizeof(T) == 8) {
+        // FP64: the three lanes of a cell share the combination, lane d taking components d and
+        // d + 3, so that the warp runs two rounds of three FP64 additions instead of five (each FP64
+        // instruction holds the sub-partition for about 70 cycles whatever the active lanes). In
+        // sub-round r, lane d reads from lane (d + r) mod 3 of its cell the term of component d + 3t,
+        // which that lane selects from its own terms; the sums keep the order (u_I + u_J) + u_K.
+        const int base = lane - d;
 #pragma unroll
-    for (int c = 0; c < 5; c++) {
-        u1[c] = __shfl_down_sync(0xffffffffu, u[c], 1);
-        u2[c] = __shfl_down_sync(0xffffffffu, u[c], 2);
-    }
-    if (!active || d != 0) return;
+        for (int t = 0; t < 2; t++) {
+            T part[3] = {(T)0, (T)0, (T)0};
 #pragma unroll
-    for (int c = 0; c < 5; c++) {
-        const T sum = (u[c] + u1[c]) + u2[c];
-        S.dq[c][q] = DIR > 0 ? rhs[c] + sum : dqp[c] - sum;
+            for (int r = 1; r <= 2; r++) {
+                const int src = d + r < 3 ? d + r : d + r - 3;        // the lane read from (its d)
+                const int cs = (d >= r ? d - r : d - r + 3) + 3 * t;  // the component this lane sends
+                T send = (T)0;
+#pragma unroll
+                for (int m = 0; m < 5; m++)
+                    if (cs == m) send = u[m];
+                const T got = __shfl_sync(0xffffffffu, send, base + src);
+                if (src == 0) part[0] = got;
+                else if (src == 1) part[1] = got;
+                else part[2] = got;
+            }
+            const int c = d + 3 * t;
+            T own = (T)0;
+#pragma unroll
+            for (int m = 0; m < 5; m++)
+                if (c == m) own = u[m];
+            if (d == 0) part[0] = own;
+            else if (d == 1) part[1] = own;
+            else part[2] = own;
+            if (active && c < 5) {
+                const T sum = (part[0] + part[1]) + part[2];
+                S.dq[c][q] = DIR > 0 ? rhs[t] + sum : dqp[t] - sum;
+            }
+        }
+    } else {
+        T u1[5], u2[5];
+#pragma unroll
+        for (int c = 0; c < 5; c++) {
+            u1[c] = __shfl_down_sync(0xffffffffu, u[c], 1);
+            u2[c] = __shfl_down_sync(0xffffffffu, u[c], 2);
+        }
+        if (!active || d != 0) return;
+#pragma unroll
+        for (int c = 0; c < 5; c++) {
+            const T sum = (u[c] + u1[c]) + u2[c];
+            S.dq[c][q] = DIR > 0 ? rhs[c] + sum : dqp[c] - sum;
+        }
     }
 }
 
