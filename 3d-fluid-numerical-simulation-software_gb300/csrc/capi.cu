@@ -273,17 +273,6 @@ int gb_face_staging(gb_solver *h, int level, int *tma)
 
 int gb_set_graphs(gb_solver *h, int enable) { NEED(h); h->s->use_graphs = enable != 0; return GB_OK; }
 
-int gb_set_sweep_arith(gb_solver *h, int double_float)
-{
-    NEED(h);
-    if (double_float != 0 && double_float != 1) return GB_ERR_ARG;
-    int rc = GB_OK;
-    const int g = guard([&] {
-        if (!h->s->set_sweep_arith(double_float)) rc = GB_ERR_ARG;
-    });
-    return g != GB_OK ? g : rc;
-}
-
 int gb_timer_start(gb_solver *h)
 {
     NEED(h);

@@ -76,7 +76,6 @@ struct PlaneTables {
     int stride = 0, max_plane = 0;
     long long nq = 0;
     int cpw = 10, wpb = 1;                        // sweep block shape: cells per warp, warps per block (autotuned)
-    int df = 0;                                   // FP64 form: 1 = double-float sweep (k_sweep_df), dQ held as pairs
     // row starts for the tiled scatter of dQ: the plane-order index of interior cell
     // (i, j, k) of solve s is rq[rq_off[s] + (i + j + k) * (IM - 1) + i - 1] + j
     const int *rq = nullptr;

@@ -8,7 +8,6 @@
 #include "gbt_common.cuh"
 #include "kernels.hpp"
 #include "flux.cuh"
-#include "dfloat.cuh"
 
 namespace gbt {
 
@@ -33,8 +32,7 @@ __device__ __forceinline__ void release_next_plane() { asm volatile("griddepcont
 //   forward:  dQ = -R / alpha + (u_I + u_J + u_K)
 //   backward: dQ = dQ* - (u_I + u_J + u_K).
 // In the FP64 form the terms before the wait are formed here in the reference's sequence; in the
-// mixed form the gather forms them for all cells at once. (k_sweep_df below is the FP64 form's
-// optional double-float variant.)
+// mixed form the gather forms them for all cells at once.
 template <typename T, int DIR, int CPW, int WPB>   // DIR = +1 forward, -1 backward; CPW cells per warp, WPB warps per block
 __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, const int *__restrict__ pstart,
                                                     int pstride, int plane)
@@ -182,112 +180,6 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
     }
 }
 
-// The FP64 form's optional double-float sweep (gb_set_sweep_arith): the same plane chain, with
-// everything before the wait on the FP64
-// pipe (the neighbour's old state and normal velocity V = m.n / rho - v_e, and the diagonal
-// alpha = Vol/dt + relax sum lambda_c + 2 sum lambda_v, in the reference's sequence) and the
-// dQ-dependent half in double-float arithmetic (dfloat.cuh, about 47 significant bits): on GB300
-// each FP64 instruction holds a sub-partition for about 70 cycles, and that half is a chain of some
-// 60 of them per plane on one warp per sub-partition. The flux difference is formed in delta form,
-// from dQ and the old state,
-//   dV   = (rho (dm.n) - drho (m.n)) / (rho rho'),   rho' = rho + drho,
-//   dp   = (g-1) (de - (rho dm.(2m + dm) - drho |m|^2) / (2 rho rho')),
-//   dF   = (rho' dV + drho V,  m dV + dm V' + dp n,  (e + p) dV + (de + dp) V' + dp v_e),  V' = V + dV,
-// which is F_n(Q + dQ) - F_n(Q) in exact arithmetic without the cancellation of the two fluxes:
-// its error is a few units of 2^-47 of dF itself, below the FP64 rounding of the reference's
-// difference of fluxes (2^-53 of F) wherever |dF| < |F| / 128. The plane-order dQ holds
-// double-float pairs in its FP64 slots (k_sweep_scatter converts them back); Q, the residual and
-// every other stage stay FP64. The result is not the reference's FP64 rounding: it converges to
-// the same solution (integrals within 1e-7 of the reference's converged run), but trajectories
-// that pass through the discrete switches of the method (Baldwin-Lomax maxima, the positivity
-// limiter) part from the reference's wherever a switch falls the other way.
-template <int DIR, int CPW, int WPB>
-__global__ void __launch_bounds__(32 * WPB) k_sweep_df(PhysW<double> P, SweepData<double> S, const int *__restrict__ pstart,
-                                                       int pstride, int plane)
-{
-    release_next_plane();
-    const int lane = threadIdx.x & 31, slot = lane / 3, d = lane - 3 * slot;
-    const int s = blockIdx.y;
-    const int base = pstart[s * pstride + plane], cnt = pstart[s * pstride + plane + 1] - base;
-    const int idx = (blockIdx.x * WPB + (int)(threadIdx.x >> 5)) * CPW + slot;
-    const bool active = lane < 3 * CPW && idx < cnt;
-    const int q = base + idx;
-    int nb = -1;
-    const dfloat z = df_make(0.f, 0.f);
-    // the neighbour's old state: rho, m, e + p, p, its normal and entrainment speed, V, m.n, |m|^2
-    dfloat rho = z, mx = z, my = z, mz = z, ep = z, nx = z, ny = z, nz = z, ve = z, V = z, mn = z, m2 = z;
-    dfloat hs = z, cq = z, rhs[5] = {z, z, z, z, z}, alpha = z, inva = z;
-    const dfloat gm1 = df_from(P.gm1);
-    if (active) {
-        nb = S.nb[DIR > 0 ? 0 : 1][d][q];
-        if (nb >= 0) {
-            const double nxd = S.gn[d][0][nb], nyd = S.gn[d][1][nb], nzd = S.gn[d][2][nb], ved = S.gve[d][nb];
-            const double od = S.cv[0][nb], omx = S.cv[1][nb], omy = S.cv[2][nb], omz = S.cv[3][nb], oe = S.cv[4][nb];
-            const double po = S.pp[nb];
-            const double oinv = frcp<double>(od);
-            const double Vo = omx * oinv * nxd + omy * oinv * nyd + omz * oinv * nzd;
-            V = df_from(Vo - ved);
-            mn = df_from(omx * nxd + omy * nyd + omz * nzd);
-            m2 = df_from(omx * omx + omy * omy + omz * omz);
-            ep = df_from(oe + po);
-            rho = df_from(od); mx = df_from(omx); my = df_from(omy); mz = df_from(omz);
-            nx = df_from(nxd); ny = df_from(nyd); nz = df_from(nzd); ve = df_from(ved);
-            hs = df_scale(df_from(S.gs[d][nb]), 0.5f);
-            cq = df_from(fma(0.5 * P.relax, S.lamc[d][nb], S.lamv[d][nb]));
-        }
-        if (d == 0) {
-            const double a = fdiv<double>(S.gvol[q], S.dt[q]) + P.relax * (S.lamc[0][q] + S.lamc[1][q] + S.lamc[2][q]) +
-                             2.0 * (S.lamv[0][q] + S.lamv[1][q] + S.lamv[2][q]);
-            alpha = df_from(a);
-            inva = df_rcp(alpha);
-            if (DIR > 0) {
-#pragma unroll
-                for (int c = 0; c < 5; c++) rhs[c] = df_from(-S.res[c][q]);
-            }
-        }
-    }
-    wait_previous_plane();
-    dfloat dqp[5];                       // backward sweep: this cell's forward-sweep dQ
-    if (DIR < 0 && active && d == 0) {
-#pragma unroll
-        for (int c = 0; c < 5; c++) dqp[c] = df_load(S.dq[c] + q);
-    }
-    dfloat u[5] = {z, z, z, z, z};
-    if (nb >= 0) {
-        dfloat dq[5];
-#pragma unroll
-        for (int c = 0; c < 5; c++) dq[c] = df_load(S.dq[c] + nb);
-        const dfloat irr = df_rcp(rho * (rho + dq[0]));
-        const dfloat dmn = dq[1] * nx + dq[2] * ny + dq[3] * nz;
-        const dfloat dV = (rho * dmn - dq[0] * mn) * irr;
-        const dfloat dmm = dq[1] * (df_scale(mx, 2.f) + dq[1]) + dq[2] * (df_scale(my, 2.f) + dq[2]) +
-                           dq[3] * (df_scale(mz, 2.f) + dq[3]);
-        const dfloat dp = gm1 * (dq[4] - df_scale((rho * dmm - dq[0] * m2) * irr, 0.5f));
-        const dfloat Vn = V + dV;
-        dfloat dF[5];
-        dF[0] = (rho + dq[0]) * dV + dq[0] * V;
-        dF[1] = (mx * dV + dq[1] * Vn) + dp * nx;
-        dF[2] = (my * dV + dq[2] * Vn) + dp * ny;
-        dF[3] = (mz * dV + dq[3] * Vn) + dp * nz;
-        dF[4] = (ep * dV + (dq[4] + dp) * Vn) + dp * ve;
-#pragma unroll
-        for (int c = 0; c < 5; c++) u[c] = DIR > 0 ? hs * dF[c] + cq * dq[c] : hs * dF[c] - cq * dq[c];
-    }
-    dfloat u1[5], u2[5];
-#pragma unroll
-    for (int c = 0; c < 5; c++) {
-        u1[c] = df_make(__shfl_down_sync(0xffffffffu, u[c].hi, 1), __shfl_down_sync(0xffffffffu, u[c].lo, 1));
-        u2[c] = df_make(__shfl_down_sync(0xffffffffu, u[c].hi, 2), __shfl_down_sync(0xffffffffu, u[c].lo, 2));
-    }
-    if (!active || d != 0) return;
-#pragma unroll
-    for (int c = 0; c < 5; c++) {
-        const dfloat sum = (u[c] + u1[c]) + u2[c];
-        const dfloat r = DIR > 0 ? rhs[c] + sum : alpha * dqp[c] - sum;
-        df_store(S.dq[c] + q, r * inva);
-    }
-}
-
 // dQ from plane order back into the box (after the backward sweep), through shared-memory tiles.
 // A hyperplane's cells are never neighbours in the k-contiguous box (consecutive plane cells
 // (i, j, k), (i, j+1, k-1) lie NK - 1 apart), so a per-cell copy writes one DRAM sector per value.
@@ -368,21 +260,6 @@ __global__ void __launch_bounds__(256) k_sweep_gather(PhysW<T> P, Flow<T> W, Swe
     }
 }
 
-// dQ back into the box (after the backward sweep; with the double-float sweep the plane-order dQ
-// holds double-float pairs)
-template <typename T>
-__global__ void __launch_bounds__(256) k_sweep_scatter(Flow<T> W, SweepData<T> S, long long nq, bool pairs)
-{
-    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nq) return;
-    const long long p = S.cell[q];
-#pragma unroll
-    for (int c = 0; c < 5; c++) {
-        if constexpr (sizeof(T) == 8) W.dq[c][p] = pairs ? df_to_double(df_load(S.dq[c] + q)) : S.dq[c][q];
-        else W.dq[c][p] = S.dq[c][q];
-    }
-}
-
 // geometry of the sweeps into plane order, in the working precision (once per level)
 template <typename T>
 __global__ void __launch_bounds__(256) k_sweep_geometry(Geo G, SweepData<T> S, long long nq)
@@ -414,12 +291,6 @@ static void launch_plane_v(const LaunchCtx &ctx, const PhysW<T> &P, const PlaneT
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = first ? 0 : 1;     // the first plane of a sweep waits for everything before it
-    if constexpr (sizeof(T) == 8) {
-        if (pt.df) {
-            cudaLaunchKernelEx(&cfg, k_sweep_df<DIR, CPW, WPB>, P, S, pt.start, pt.stride, pl);
-            return;
-        }
-    }
     cudaLaunchKernelEx(&cfg, k_sweep<T, DIR, CPW, WPB>, P, S, pt.start, pt.stride, pl);
 }
 
@@ -529,13 +400,9 @@ void launch_lusgs_sweeps(const LaunchCtx &ctx, const PhysW<T> &P, const Geo &G, 
         ctx.mark("sa_sweeps", 0, np - 2);
     }
     ctx.mark("sweep_scatter", 1, 1);
-    if (pt.df) {
-        k_sweep_scatter<T><<<gq, 256, 0, ctx.stream>>>(W, S, pt.nq, true);
-    } else {
-        const int tj = (ctx.maxJM - 1 + 31) / 32, tk = (ctx.maxKM - 1 + 31) / 32;
-        const unsigned gx = (unsigned)((ctx.maxIM - 1) * tj * tk);
-        k_sweep_scatter_tiled<T><<<dim3(gx, ctx.batch.nsolve, NQ), 256, 0, ctx.stream>>>(ctx.batch, pt.rq, pt.rq_off, S, W, tj, tk);
-    }
+    const int tj = (ctx.maxJM - 1 + 31) / 32, tk = (ctx.maxKM - 1 + 31) / 32;
+    const unsigned gx = (unsigned)((ctx.maxIM - 1) * tj * tk);
+    k_sweep_scatter_tiled<T><<<dim3(gx, ctx.batch.nsolve, NQ), 256, 0, ctx.stream>>>(ctx.batch, pt.rq, pt.rq_off, S, W, tj, tk);
     ctx.mark("sweep_scatter", 0, 1);
 }
 

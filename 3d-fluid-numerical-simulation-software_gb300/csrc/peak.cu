@@ -69,8 +69,8 @@ extern "C" int gb_fp64_rate(double *flop_per_s)
     return rc;
 }
 
-// ---- the FP64 form's reciprocal, quotient and square root, and the double-float operations, ----
-// ---- against the IEEE FP64 operations                                                      ----
+// ---- the FP64 form's reciprocal, quotient and square root against the IEEE FP64 operations, and ----
+// ---- the integer splits and conversions of dfloat.cuh                                            ----
 namespace {
 
 __global__ void k_arith(int op, const double *__restrict__ x, const double *__restrict__ y, long long n, double *out)
@@ -85,16 +85,10 @@ __global__ void k_arith(int op, const double *__restrict__ x, const double *__re
     case 2: v = gbt::frcp<double>(a); break;
     case 3: v = a / b; break;
     case 4: v = sqrt(a); break;
-    // double-float operations, through the conversions from and to FP64
-    case 5: v = gbt::df_to_double(gbt::df_from(a) + gbt::df_from(b)); break;
-    case 6: v = gbt::df_to_double(gbt::df_from(a) - gbt::df_from(b)); break;
-    case 7: v = gbt::df_to_double(gbt::df_from(a) * gbt::df_from(b)); break;
-    case 8: v = gbt::df_to_double(gbt::df_from(a) / gbt::df_from(b)); break;
-    case 9: v = gbt::df_to_double(gbt::df_sqrt(gbt::df_from(a))); break;
-    case 10: v = gbt::df_to_double(gbt::df_rcp(gbt::df_from(a))); break;
-    case 11: v = gbt::df_to_double(gbt::df_from(a)); break;
-    // FP32 <-> FP64 conversions by integer operations against the conversion instructions
-    case 12: v = gbt::f32_to_f64(gbt::f64_to_f32_rn(a)); break;
+    // the split of an FP64 value into an FP32 pair (its value summed back in FP64), and FP32 <->
+    // FP64 conversions by integer operations against the conversion instructions
+    case 5: { const gbt::dfloat d = gbt::df_from(a); v = (double)d.hi + (double)d.lo; } break;
+    case 6: v = gbt::f32_to_f64(gbt::f64_to_f32_rn(a)); break;
     default: v = (double)__double2float_rn(a); break;
     }
     out[t] = v;
@@ -104,8 +98,8 @@ __global__ void k_arith(int op, const double *__restrict__ x, const double *__re
 
 extern "C" int gb_fp64_arith_check(int op, const double *x, const double *y, long long n, double *out)
 {
-    const bool binary = op == 0 || op == 3 || (op >= 5 && op <= 8);
-    if (op < 0 || op > 13 || !x || !out || n < 1 || (binary && !y)) return GB_ERR_ARG;
+    const bool binary = op == 0 || op == 3;
+    if (op < 0 || op > 7 || !x || !out || n < 1 || (binary && !y)) return GB_ERR_ARG;
     double *d = nullptr;
     const size_t bytes = sizeof(double) * (size_t)n;
     if (cudaMalloc(&d, 3 * bytes) != cudaSuccess) return GB_ERR_CUDA;

@@ -19,7 +19,6 @@
 // source/SA_Model.cpp:19-29).
 #include "gbt_common.cuh"
 #include "kernels.hpp"
-#include "dfloat.cuh"
 
 namespace gbt {
 
@@ -371,21 +370,14 @@ __device__ __forceinline__ void sa_wait_previous() { asm volatile("griddepcontro
 __device__ __forceinline__ void sa_release_next() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 template <typename T, int DIR>
-__global__ void __launch_bounds__(256) k_sa_sweep_prep(PhysW<T> PC, Geo G, Flow<T> W, SweepData<T> S, long long nq,
-                                                       bool pairs)
+__global__ void __launch_bounds__(256) k_sa_sweep_prep(PhysW<T> PC, Geo G, Flow<T> W, SweepData<T> S, long long nq)
 {
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nq) return;
     const long long p = S.cell[q];
     const double o0 = W.cv[0][p], o1 = W.cv[1][p], o2 = W.cv[2][p], o3 = W.cv[3][p];
-    // the mean flow's dQ in plane order (double-float pairs with the FP64 form's double-float sweep)
-    auto dqv = [&](int c) -> double {
-        if constexpr (sizeof(T) == 8) {
-            if (pairs) return df_to_double(df_load(S.dq[c] + q));
-        }
-        return (double)S.dq[c][q];
-    };
-    const T dn0 = (T)(o0 + dqv(0)), dn1 = (T)(o1 + dqv(1)), dn2 = (T)(o2 + dqv(2)), dn3 = (T)(o3 + dqv(3));
+    const T dn0 = (T)(o0 + (double)S.dq[0][q]), dn1 = (T)(o1 + (double)S.dq[1][q]), dn2 = (T)(o2 + (double)S.dq[2][q]),
+            dn3 = (T)(o3 + (double)S.dq[3][q]);
     const T evo = (T)W.ev[p];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
@@ -472,10 +464,10 @@ void launch_sa_sweep(const LaunchCtx &ctx, const PhysW<T> &PC, const Geo &G, Flo
     const int np = pt.max_plane;
     const unsigned gq = (unsigned)((pt.nq + 255) / 256);
     if (dir > 0) {
-        k_sa_sweep_prep<T, 1><<<gq, 256, 0, ctx.stream>>>(PC, G, W, S, pt.nq, pt.df != 0);
+        k_sa_sweep_prep<T, 1><<<gq, 256, 0, ctx.stream>>>(PC, G, W, S, pt.nq);
         for (int pl = 3; pl <= np; pl++) launch_sa_plane<T, 1>(ctx, S, pt, pl, pl == 3);
     } else {
-        k_sa_sweep_prep<T, -1><<<gq, 256, 0, ctx.stream>>>(PC, G, W, S, pt.nq, pt.df != 0);
+        k_sa_sweep_prep<T, -1><<<gq, 256, 0, ctx.stream>>>(PC, G, W, S, pt.nq);
         for (int pl = np; pl >= 3; pl--) launch_sa_plane<T, -1>(ctx, S, pt, pl, pl == np);
         k_sa_sweep_scatter<T><<<gq, 256, 0, ctx.stream>>>(W, S, pt.nq);
     }

@@ -1172,17 +1172,6 @@ public:
     }
     void res_calculate(int l) override { launch_res_norm<T>(ctx(l), lev[l].G, lev[l].W, lev[l].totalvol, norm_part, norm_blk); }
     void sweep_shape(int l, int out[2]) const override { out[0] = lev[l].planes.cpw; out[1] = lev[l].planes.wpb; }
-    bool set_sweep_arith(int df) override
-    {
-        if (sizeof(T) != 8) return df == 0;            // the mixed form's sweep is FP32 throughout
-        CK(cudaStreamSynchronize(stream));
-        for (int l = 1; l <= ng; l++) lev[l].planes.df = df ? 1 : 0;
-        // captured phases hold the other kernels: capture again
-        for (auto &g : graphs)
-            if (g) { CK(cudaGraphExecDestroy(g)); g = nullptr; }
-        for (int &r : phase_runs) r = 0;
-        return true;
-    }
     bool face_staged(int l) const override
     {
         return lev[l].tma_mem.p != nullptr && P.recon_var == 200 && P.recon == 500 && P.scheme == 300;

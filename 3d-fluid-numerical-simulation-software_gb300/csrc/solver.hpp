@@ -80,9 +80,6 @@ public:
     virtual void set_use_force(int level, bool on) = 0;
     // block shape the sweep autotuner chose for a level: cells per warp, warps per block
     virtual void sweep_shape(int level, int out[2]) const = 0;
-    // FP64 form: 1 runs the LU-SGS sweeps' dQ-dependent half in double-float arithmetic
-    // (k_sweep_df), 0 in FP64 (the default); false where the form has no such choice
-    virtual bool set_sweep_arith(int df) = 0;
     // whether a level's face stage runs on tiles staged in shared memory by TMA (mixed form)
     virtual bool face_staged(int level) const = 0;
     // stage profiler: while on, iterations run eagerly and every stage is bracketed by events

@@ -90,7 +90,6 @@ def load() -> ctypes.CDLL:
         "gb_timer_stop": ([vp, ctypes.POINTER(ctypes.c_float)], ip),
         "gb_fp64_rate": ([dp], ip),
         "gb_fp64_arith_check": ([ip, dp, dp, ctypes.c_longlong, dp], ip),
-        "gb_set_sweep_arith": ([vp, ip], ip),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -110,7 +109,7 @@ EXPORTED = ["gb_solver_create", "gb_solver_destroy", "gb_last_error", "gb_dims",
             "gb_case_blocks", "gb_case_info", "gb_solver_create_levels", "gb_start_from_fine_state", "gb_ws_create", "gb_ws_destroy",
             "gb_ws_num_params", "gb_ws_add_solves", "gb_ws_samples", "gb_ws_train", "gb_ws_apply", "gb_ws_get_params",
             "gb_ws_set_params", "gb_ws_get_norm", "gb_ws_set_norm", "gb_ws_forward", "gb_ws_forward_backward",
-            "gb_ws_benchmark", "gb_fp64_rate", "gb_fp64_arith_check", "gb_face_staging", "gb_set_sweep_arith"]
+            "gb_ws_benchmark", "gb_fp64_rate", "gb_fp64_arith_check", "gb_face_staging"]
 
 
 class GBError(RuntimeError):
@@ -155,10 +154,9 @@ def fp64_rate() -> float:
 
 def fp64_arith_check(op: int, x: np.ndarray, y: Optional[np.ndarray] = None) -> np.ndarray:
     """the device's FP64 arithmetic on host arrays: op 0 x / y, 1 sqrt(x), 2 1 / x as the FP64 form's
-    kernels compute them (Newton-refined), 3 and 4 the IEEE x / y and sqrt(x); 5-10 x + y, x - y,
-    x * y, x / y, sqrt(x), 1 / x in double-float (FP32 pairs), 11 x converted to a pair and back,
-    12 and 13 x rounded to FP32 and widened back by integer operations / by the conversion
-    instructions"""
+    kernels compute them (Newton-refined), 3 and 4 the IEEE x / y and sqrt(x); 5 x split into a
+    pair of FP32 numbers and summed back, 6 and 7 x rounded to FP32 and widened back by integer
+    operations / by the conversion instructions"""
     L = load()
     x = np.ascontiguousarray(x, dtype=np.float64)
     yy = None if y is None else np.ascontiguousarray(y, dtype=np.float64)
@@ -370,11 +368,6 @@ class Solver:
 
     def set_graphs(self, on: bool) -> None:
         self._ck(self._L.gb_set_graphs(self.h, int(on)))
-
-    def set_sweep_arith(self, double_float: bool) -> None:
-        """FP64 handles: True runs the dQ-dependent half of the LU-SGS sweeps in double-float
-        arithmetic (about 47 bits, FP32 pipe), False (the default) in FP64"""
-        self._ck(self._L.gb_set_sweep_arith(self.h, int(double_float)))
 
     def profile_begin(self) -> None:
         self._ck(self._L.gb_profile_begin(self.h))

@@ -49,9 +49,6 @@ def parse():
                     help="3: the three-level V-cycle extension (the reference stops at two levels)")
     ap.add_argument("--variant", default="default", choices=["default", "jst", "sa", "stage"],
                     help="numerical variant of the passage: JST, Spalart-Allmaras (single grid), rotor-stator stage")
-    ap.add_argument("--sweep", default="fp64", choices=["fp64", "double-float"],
-                    help="FP64 form: arithmetic of the LU-SGS sweeps' dQ-dependent half (double-float: pairs of "
-                         "FP32 numbers, about 47 bits, on the FP32 pipe; not the reference's rounding)")
     ap.add_argument("--blocks", type=int, default=1, choices=[1, 3],
                     help="3: the passage as three blocks joined by interfaces (reference's rotor-67 layout)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -317,10 +314,9 @@ def run_reference(args, rank, world, dist):
 
 
 def measure_forms(gbturbo, dirs, cells, n_ref, ref_int, steps, tmp):
-    """secondary numbers beside the FP64 headline: the FP64 form with the double-float sweep and
-    the mixed-precision form on the same passage (device-timed cycles, and their integrals after the
-    same number of cycles as the FP64 run, relative to the FP64 values), and batches of 8 and 64
-    operating points in the mixed form"""
+    """secondary numbers beside the FP64 headline: the mixed-precision form on the same passage
+    (device-timed cycles, and its integrals after the same number of cycles as the FP64 run,
+    relative to the FP64 values), and batches of 8 and 64 operating points in the mixed form"""
     out = {}
     m = gbturbo.Solver(dirs, gbturbo.MIXED)
     m.init_uniform()
@@ -332,29 +328,6 @@ def measure_forms(gbturbo, dirs, cells, n_ref, ref_int, steps, tmp):
     got = m.integrals(1)[0]
     m.close()
     names = ["m_in", "m_out", "PR", "eta"]
-    mixed_int, mixed_ms = got, ms
-    # the FP64 form with the double-float sweep: the same cycles, the sweeps' device time from the
-    # stage profiler, and the integrals after as many cycles as the FP64 run relative to its values
-    f = gbturbo.Solver(dirs, gbturbo.FP64)
-    f.set_sweep_arith(True)
-    f.init_uniform()
-    f.iterate(3, history=False)
-    f.timer_start()
-    f.iterate(steps, history=False)
-    fms = f.timer_stop()
-    f.profile_begin()
-    f.iterate(5, history=False)
-    fprof = f.profile_end()
-    f.iterate(n_ref - 3 - steps - 5, history=False)
-    fgot = f.integrals(1)[0]
-    f.close()
-    out["fp64_double_float_sweep"] = {
-        "value": cells * steps / (fms / 1000.0), "unit": "cell-updates/s", "ms_per_step": fms / steps, "steps": steps,
-        "sweeps_ms_per_step": round((fprof.get("sweep_forward", (0,))[0] + fprof.get("sweep_backward", (0,))[0]) / 5, 4),
-        "cycles_compared": n_ref,
-        "rel_err_vs_fp64": {n: abs(float(fgot[q] - ref_int[q]) / float(ref_int[q])) for q, n in enumerate(names)},
-        "note": "FP64 everywhere except the LU-SGS sweeps' dQ-dependent half (double-float pairs, ~47 bits, delta form)"}
-    got, ms = mixed_int, mixed_ms
     out["mixed"] = {"value": cells * steps / (ms / 1000.0), "unit": "cell-updates/s", "ms_per_step": ms / steps,
                     "steps": steps, "cycles_compared": n_ref,
                     "rel_err_vs_fp64": {n: abs(float(got[q] - ref_int[q]) / float(ref_int[q])) for q, n in enumerate(names)}}
@@ -817,7 +790,6 @@ def config_block(args, cells, nsolve):
                        "sa": "Roe + MUSCL3 (primitive), Spalart-Allmaras, LU-SGS, single grid",
                        "stage": "Roe + MUSCL3 (primitive), Baldwin-Lomax, LU-SGS, 2-level FAS, mixing plane"}[
                            getattr(args, "variant", "default")],
-            "sweep_arith": getattr(args, "sweep", "fp64") if args.precision == "fp64" else "fp32",
             "l2": "inputs larger than L2 (FP64 working set well above 129 MB), no flush",
             "parallelism": "replicas"}
 
@@ -842,10 +814,7 @@ def run_gpu(args, rank, world, dist):
         grid_bytes = sum(os.path.getsize(os.path.join(d, "grid.dat")) for d in dirs)
 
         # --- device-resident throughput (value)
-        dfs = prec == gbturbo.FP64 and args.sweep == "double-float"
         s = gbturbo.Solver(dirs, prec, levels=args.levels)
-        if dfs:
-            s.set_sweep_arith(True)
         s.init_uniform()
         s.iterate(max(args.warmup, 3), history=False)
         s.sync()
@@ -911,7 +880,7 @@ def run_gpu(args, rank, world, dist):
                                 "alg_bytes_per_launch": bytes_per_launch}}
         forms = None
         if (rank == 0 and world == 1 and not args.no_forms and prec == gbturbo.FP64 and nsolve == 1 and args.blocks == 1
-                and args.variant == "default" and args.levels == 2 and not dfs):
+                and args.variant == "default" and args.levels == 2):
             n_ref = max(args.warmup, 3) + args.steps + nprof
             forms = measure_forms(gbturbo, dirs, cells, n_ref, s.integrals(1)[0], min(args.steps, 50), tmp)
             if not args.no_solves:
@@ -923,8 +892,6 @@ def run_gpu(args, rank, world, dist):
         barrier(dist)
         t0 = time.perf_counter()
         e = gbturbo.Solver(dirs, prec, levels=args.levels)
-        if dfs:
-            e.set_sweep_arith(True)
         e.init_uniform()
         e.iterate(max(args.warmup, 3), history=True)
         for _ in range(args.steps):

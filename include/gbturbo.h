@@ -136,17 +136,6 @@ int gb_sweep_tuning(gb_solver *h, int level, int out[2]);
 int gb_face_staging(gb_solver *h, int level, int *tma);
 /* 0 disables graph replay in gb_iterate (eager launches) */
 int gb_set_graphs(gb_solver *h, int enable);
-/* FP64 handles: 1 runs the dQ-dependent half of each LU-SGS hyperplane (the flux difference
- * F(Q+dQ) - F(Q) in delta form, the combination and the division by the diagonal) in double-float
- * arithmetic, pairs of FP32 numbers with about 47 significant bits, on the FP32 pipe; 0 (the
- * default) keeps the FP64 arithmetic of source/LU_SGS_Marching.cpp:95-150, 293-419. Everything
- * else stays FP64. The double-float sweep converges to the same solution (integrals within about
- * 1e-7 of the FP64 run) but is not the reference's rounding, so runs that cross a discrete
- * switch of the method (Baldwin-Lomax maxima, the positivity limiter) differently part from the
- * reference's trajectory. Takes effect from the next iteration (captured graphs are dropped).
- * GB_ERR_ARG for 1 on a mixed-precision handle or a value other than 0 and 1. No counterpart in
- * the reference. */
-int gb_set_sweep_arith(gb_solver *h, int double_float);
 /* stage profiler: between the two calls iterations run without graphs and every stage of the
  * path is bracketed by CUDA events on the handle's stream; gb_profile_end writes
  * "stage:milliseconds:kernel launches:evaluations on level 1,2,3;..." totals into buf (an
@@ -164,14 +153,12 @@ int gb_timer_stop(gb_solver *h, float *ms);
  * reported, since on this GPU they are bound by the FP64 pipe rather than by HBM. */
 int gb_fp64_rate(double *flop_per_s);
 /* The FP64 form's Newton-refined reciprocal, quotient and square root (which replace the IEEE
- * division and root in its compute-bound kernels) and its double-float operations (pairs of FP32
- * numbers, about 47 significant bits, used by the LU-SGS sweep) evaluated on the device for n
- * inputs, so that they can be checked against the IEEE operations: op 0 x / y, 1 sqrt(x), 2 1 / x;
- * op 3 and 4 are the device's IEEE x / y and sqrt(x); ops 5-10 are x + y, x - y, x * y, x / y,
- * sqrt(x) and 1 / x in double-float and op 11 the conversion of x to a double-float pair and back,
- * each from FP64 inputs to an FP64 result; op 12 rounds x to FP32 and widens it back by integer
- * operations (the mixed form's conversions), op 13 by the conversion instructions. x, y (y only for ops 0, 3 and 5-8) and out are host
- * arrays. No counterpart in the reference. */
+ * division and root in its compute-bound kernels) evaluated on the device for n inputs, so that
+ * they can be checked against the IEEE operations: op 0 x / y, 1 sqrt(x), 2 1 / x; op 3 and 4 are
+ * the device's IEEE x / y and sqrt(x). Also the mixed form's integer operations: op 5 splits x into
+ * a pair of FP32 numbers (returned as their FP64 sum), op 6 rounds x to FP32 and widens it back by
+ * integer operations, op 7 does the same by the conversion instructions. x, y (y only for ops 0
+ * and 3) and out are host arrays. No counterpart in the reference. */
 int gb_fp64_arith_check(int op, const double *x, const double *y, long long n, double *out);
 
 /* Residual norm of gb_res_calculate (same arguments, same values in out and in the solve states)

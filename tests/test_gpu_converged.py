@@ -76,25 +76,6 @@ def test_rotor_fp64_converges_with_the_reference(rotor_case, rotor_fp64):
         assert along < 1e-5, (name, along)
 
 
-def test_rotor_double_float_sweep_converges_with_the_reference(rotor_case, gpu_lib):
-    # the FP64 form with the LU-SGS sweeps' dQ-dependent half in double-float (gb_set_sweep_arith):
-    # the same bars as the FP64 sweep (measured along the run: 2.1e-6 in m_out, 3.1e-6 in eta)
-    d, ref = rotor_case
-    n = ref.shape[0]
-    with gpu_lib.Solver(d, gpu_lib.FP64) as s:
-        s.set_sweep_arith(True)
-        s.init_uniform()
-        h = s.iterate(n + 20)[:, 0, :]
-    c = first_converged(h)
-    assert c is not None and abs(c - n) <= 5, c
-    h = h[:n]
-    for name, col in INTEGRALS.items():
-        err = abs(h[-1, col] - ref[-1, col]) / abs(ref[-1, col])
-        assert err < 1e-6, (name, h[-1, col], ref[-1, col], err)
-        along = float(np.max(np.abs(h[:, col] - ref[:, col]) / np.abs(ref[:, col])))
-        assert along < 1e-5, (name, along)
-
-
 def test_rotor_mixed_converges_to_the_fp64_integrals(rotor_case, rotor_fp64, gpu_lib):
     d, ref = rotor_case
     n = ref.shape[0]
