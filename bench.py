@@ -166,14 +166,14 @@ def alg_units_per_step(stage, slot_dims, evals, nprof):
 
 
 def fp64_ops_per_unit():
-    """FP64 operations (2 x DFMA + DMUL + DADD thread instructions, counted by ncu) per unit of a
-    stage of the FP64 form, from profiles/fp64_ops_per_unit.txt"""
+    """per unit of a stage of the FP64 form, from profiles/fp64_ops_per_unit.txt (ncu counts):
+    (FP64 operations = 2 x DFMA + DMUL + DADD thread instructions, FP64-pipe thread instructions)"""
     out = {}
     try:
         for line in open(os.path.join(ROOT, "profiles", "fp64_ops_per_unit.txt")):
             f = line.split()
-            if len(f) >= 3 and not line.startswith("#"):
-                out[f[0]] = float(f[2])
+            if len(f) >= 4 and not line.startswith("#"):
+                out[f[0]] = (float(f[2]), float(f[3]))
     except FileNotFoundError:
         pass
     return out
@@ -864,16 +864,24 @@ def run_gpu(args, rank, world, dist):
         roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                     "frac": achieved / peak, "traffic": traffic, "alg_bytes_per_launch": bytes_per_launch,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800 GB/s"}
-        flops_unit = fp64_ops_per_unit().get(dom) if prec == gbturbo.FP64 else None
-        if flops_unit is not None:
+        counts = fp64_ops_per_unit().get(dom) if prec == gbturbo.FP64 else None
+        if counts is not None:
             # the FP64 form is bound by the FP64 pipe: counted FP64 operations of the stage (ncu, per
-            # face or plane cell) over its device time, against the FP64 rate measured in this run
+            # face or plane cell) over its device time, against the FP64 rate measured in this run.
+            # DADD and DMUL hold the pipe as long as an FMA, so beside the FLOP fraction the line
+            # gives the pipe's occupancy: FP64 instructions issued per second against the FMA-chain
+            # loop's instructions per second (half its FLOP rate).
+            flops_unit, inst_unit = counts
             rate = gbturbo.fp64_rate() / 1e12
+            sec = dom_ms / nprof / 1000.0
             flop_step = units_step * flops_unit
-            tf = flop_step / (dom_ms / nprof / 1000.0) / 1e12
+            tf = flop_step / sec / 1e12
+            ti = units_step * inst_unit / sec / 1e12
             roofline = {"bound": "fp64", "kernel": dom, "achieved": tf, "peak": rate, "unit": "TFLOP/s",
                         "frac": tf / rate, "traffic": traffic, "flop_per_launch": flop_step / (dom_launches / nprof),
                         "flop_per_unit": flops_unit,
+                        "fp64_pipe": {"achieved": ti, "peak": rate / 2.0, "unit": "T FP64 instructions/s",
+                                      "frac": ti / (rate / 2.0), "inst_per_unit": inst_unit},
                         "peak_source": "FP64 FMA-chain loop timed in this run (gb_fp64_rate); "
                                        "MEASURED_PEAKS.json holds no FP64 figure",
                         "hbm": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
