@@ -94,10 +94,6 @@ struct SweepData {
     T *gn[3][3] = {}, *gs[3] = {}, *gve[3] = {}, *gvol = nullptr;   // per direction: mean normal, |S|, entrainment
     T *cv[NQ] = {}, *pp = nullptr, *lamc[3] = {}, *lamv[3] = {}, *dt = nullptr, *res[NQ] = {};
     T *dq[NQ] = {};
-    // formed by the gather (they do not depend on dQ): per cell as the neighbour in direction d, its
-    // old flux F_n(Q) across its mean normal; per cell, 1 / alpha of the diagonal. lamc holds
-    // relax * lambda_c after the gather
-    T *fo[3][NQ] = {}, *ainv = nullptr;
     // Spalart-Allmaras sweep (null without it), per cell as a neighbour in direction d: normal
     // velocity with the mean flow's dQ added, old variable times old normal velocity, mean |S|,
     // relax * lambda_c, lambda_v; per cell: old variable, diagonal, residual, update

@@ -31,8 +31,8 @@ __device__ __forceinline__ void release_next_plane() { asm volatile("griddepcont
 // lane forms
 //   forward:  dQ = -R / alpha + (u_I + u_J + u_K)
 //   backward: dQ = dQ* - (u_I + u_J + u_K).
-// In the FP64 form the terms before the wait are formed here in the reference's sequence; in the
-// mixed form the gather forms them for all cells at once.
+// The terms that do not depend on dQ (the neighbour's old flux, the diagonal) are formed before the
+// wait, in the reference's sequence.
 template <typename T, int DIR, int CPW, int WPB>   // DIR = +1 forward, -1 backward; CPW cells per warp, WPB warps per block
 __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, const int *__restrict__ pstart,
                                                     int pstride, int plane)
@@ -54,22 +54,17 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
             nx = S.gn[d][0][nb]; ny = S.gn[d][1][nb]; nz = S.gn[d][2][nb];
             ve = S.gve[d][nb];
             od = S.cv[0][nb]; omx = S.cv[1][nb]; omy = S.cv[2][nb]; omz = S.cv[3][nb]; oe = S.cv[4][nb];
-            if constexpr (sizeof(T) == 8) {
-                const T po = S.pp[nb];
-                const T oinv = frcp<T>(od);
-                const T Vo = omx * oinv * nx + omy * oinv * ny + omz * oinv * nz;
-                const T dov = Vo - ve;
-                fo[0] = od * dov;
-                fo[1] = omx * dov + po * nx;
-                fo[2] = omy * dov + po * ny;
-                fo[3] = omz * dov + po * nz;
-                fo[4] = (oe + po) * dov + po * ve;
-                rl = P.relax * S.lamc[d][nb];
-            } else {
-#pragma unroll
-                for (int c = 0; c < 5; c++) fo[c] = S.fo[d][c][nb];
-                rl = S.lamc[d][nb];                    // relax * lambda_c, formed by the gather
-            }
+            const T po = S.pp[nb];
+            // (the FP64 form's quotients Newton-refined, as in its other kernels; the mixed form's IEEE)
+            const T oinv = sizeof(T) == 8 ? frcp<T>(od) : (T)1 / od;
+            const T Vo = omx * oinv * nx + omy * oinv * ny + omz * oinv * nz;
+            const T dov = Vo - ve;
+            fo[0] = od * dov;
+            fo[1] = omx * dov + po * nx;
+            fo[2] = omy * dov + po * ny;
+            fo[3] = omz * dov + po * nz;
+            fo[4] = (oe + po) * dov + po * ve;
+            rl = P.relax * S.lamc[d][nb];
             sd = S.gs[d][nb];
             lv = S.lamv[d][nb];
         }
@@ -79,7 +74,9 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
                             (T)2 * (S.lamv[0][q] + S.lamv[1][q] + S.lamv[2][q]);
             inva = frcp<T>(alpha);
         } else {
-            inva = S.ainv[q];
+            const T alpha = S.gvol[q] / S.dt[q] + P.relax * (S.lamc[0][q] + S.lamc[1][q] + S.lamc[2][q]) +
+                            (T)2 * (S.lamv[0][q] + S.lamv[1][q] + S.lamv[2][q]);
+            inva = (T)1 / alpha;
         }
         if (DIR > 0) {
             if constexpr (sizeof(T) == 8) {
@@ -180,20 +177,32 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
     }
 }
 
-// dQ from plane order back into the box (after the backward sweep), through shared-memory tiles.
-// A hyperplane's cells are never neighbours in the k-contiguous box (consecutive plane cells
-// (i, j, k), (i, j+1, k-1) lie NK - 1 apart), so a per-cell copy writes one DRAM sector per value.
-// A block here takes a 32 x 32 (j, k) tile of one i-row of one solve and one component (grid.z):
-// it reads the tile's j + k = const diagonals, which are runs of consecutive plane-order indices
-// (the plane order enumerates i, then j), and writes k-rows of the box, so both sides move whole
-// sectors. (The same tiling for the gather, box to plane order before the forward sweep, was
-// slower than the per-cell gather: the mixed form's derived terms then need a second pass.)
-template <typename T>
-__global__ void __launch_bounds__(256) k_sweep_scatter_tiled(Batch B, const int *__restrict__ rq,
-                                                             const long long *__restrict__ rq_off, SweepData<T> S, Flow<T> W,
-                                                             int tj, int tk)
+// Box <-> plane order through shared-memory tiles: the sweeps' flow inputs into plane order before
+// the forward sweep, dQ back into the box after the backward sweep. A hyperplane's cells are never
+// neighbours in the k-contiguous box (consecutive plane cells (i, j, k), (i, j+1, k-1) lie NK - 1
+// apart), so a per-cell copy moves one DRAM sector per value on one side. A block here takes a
+// 32 x 32 (j, k) tile of one i-row of one solve and one array (grid.z): it moves the box's k-rows
+// and the tile's j + k = const diagonals, which are runs of consecutive plane-order indices (the
+// plane order enumerates i, then j), so both sides move whole sectors. The diagonals' starts are
+// read once per block and a warp's eight diagonals are unrolled, so that their loads are in flight
+// together. Values are converted on the way from the source to the destination type (FP64 Q to
+// the working type with the conversion instructions' rounding).
+constexpr int kTileArrays = 13;
+template <typename Src, typename Dst> struct TileList {
+    const Src *src[kTileArrays];
+    Dst *dst[kTileArrays];
+};
+template <typename Dst, typename Src> __device__ __forceinline__ Dst tile_conv(Src v)
 {
-    const int s = blockIdx.y, c = blockIdx.z;             // solve, component
+    if constexpr (sizeof(Src) == 8 && sizeof(Dst) == 4) return f64_to_f32_rn(v);
+    else return (Dst)v;
+}
+
+template <typename Src, typename Dst, bool TO_PLANE>
+__global__ void __launch_bounds__(256) k_plane_tile(Batch B, const int *__restrict__ rq, const long long *__restrict__ rq_off,
+                                                    TileList<Src, Dst> A, int tj, int tk)
+{
+    const int s = blockIdx.y, a = blockIdx.z;             // solve, array
     const Lvl L = B.lv[s];
     const int nI = L.IM - 1, nJ = L.JM - 1, nK = L.KM - 1;
     const int kb = (int)(blockIdx.x % (unsigned)tk), jb = (int)((blockIdx.x / (unsigned)tk) % (unsigned)tj);
@@ -201,63 +210,66 @@ __global__ void __launch_bounds__(256) k_sweep_scatter_tiled(Batch B, const int 
     const int j0 = jb * 32 + 1, k0 = kb * 32 + 1;
     if (i > nI || j0 > nJ || k0 > nK) return;
     // row stride 34: the diagonals (word offset 33 jj + dd) and the k-rows both hit 32 banks
-    __shared__ T tile[32][34];
+    __shared__ Dst tile[32][34];
+    __shared__ int qd[63];                               // plane-order index of (i, j0, k0 + dd) minus j0
     const int lane = threadIdx.x & 31, w = (int)(threadIdx.x >> 5);
-    const int *rqi = rq + rq_off[s] + (i - 1);          // row start of plane pl: rqi[pl * nI]
-    const T *src = S.dq[c];
-    for (int dd = w; dd < 63; dd += 8) {
-        const int kk = dd - lane, j = j0 + lane, k = k0 + kk;
-        if (kk >= 0 && kk < 32 && j <= nJ && k <= nK) tile[lane][kk] = src[rqi[(long long)(i + j + k) * nI] + j];
-    }
-    __syncthreads();
-    T *dst = W.dq[c];
+    // (a diagonal beyond the solve's last plane holds no cell of the solve: its entry is clamped to
+    // the table and never used)
+    if (threadIdx.x < 63) qd[threadIdx.x] = rq[rq_off[s] + (long long)min(i + j0 + k0 + (int)threadIdx.x, nI + nJ + nK) * nI + (i - 1)];
+    const Src *src = A.src[a];
+    Dst *dst = A.dst[a];
+    if (TO_PLANE) {
 #pragma unroll
-    for (int r = w; r < 32; r += 8) {
-        const int j = j0 + r, k = k0 + lane;
-        if (j <= nJ && k <= nK) dst[ix(L, i, j, k)] = tile[r][lane];
+        for (int r = w; r < 32; r += 8) {
+            const int j = j0 + r, k = k0 + lane;
+            if (j <= nJ && k <= nK) tile[r][lane] = tile_conv<Dst>(src[ix(L, i, j, k)]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            const int dd = w + 8 * e, kk = dd - lane, j = j0 + lane, k = k0 + kk;
+            if (dd < 63 && kk >= 0 && kk < 32 && j <= nJ && k <= nK) dst[qd[dd] + j] = tile[lane][kk];
+        }
+    } else {
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            const int dd = w + 8 * e, kk = dd - lane, j = j0 + lane, k = k0 + kk;
+            if (dd < 63 && kk >= 0 && kk < 32 && j <= nJ && k <= nK) tile[lane][kk] = tile_conv<Dst>(src[qd[dd] + j]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = w; r < 32; r += 8) {
+            const int j = j0 + r, k = k0 + lane;
+            if (j <= nJ && k <= nK) dst[ix(L, i, j, k)] = tile[r][lane];
+        }
     }
 }
 
-// flow inputs of the sweeps into plane order (before every forward sweep)
-// and, in the mixed form, the parts of the sweeps that do not depend on dQ, for all cells at once:
-// every cell's old flux F_n(Q) as the neighbour in each direction (across its mean normal, in the
-// rotating frame), 1/alpha of its diagonal alpha = Vol/dt + relax sum lambda_c + 2 sum lambda_v,
-// relax * lambda_c (the FP64 form forms them in the sweep kernel, in the reference's sequence)
-template <typename T>
-__global__ void __launch_bounds__(256) k_sweep_gather(PhysW<T> P, Flow<T> W, SweepData<T> S, long long nq)
+template <typename Src, typename Dst, bool TO_PLANE>
+static void launch_plane_tile(const LaunchCtx &ctx, const PlaneTables &pt, const TileList<Src, Dst> &A, int n)
 {
-    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nq) return;
-    const long long p = S.cell[q];
-    T cv[5], lc[3], lv[3];
-#pragma unroll
-    for (int c = 0; c < 5; c++) { cv[c] = to_work<T>(W.cv[c][p]); S.cv[c][q] = cv[c]; S.res[c][q] = W.res[c][p]; }
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        lc[d] = W.lamc[d][p]; lv[d] = W.lamv[d][p];
-        // the FP64 form keeps lambda_c and forms relax * lambda_c and the diagonal in the sweep
-        S.lamc[d][q] = sizeof(T) == 8 ? lc[d] : P.relax * lc[d];
-        S.lamv[d][q] = lv[d];
-    }
-    const T po = W.pv[PP][p], dt = W.dt[p];
-    S.pp[q] = po;
-    S.dt[q] = dt;
-    if constexpr (sizeof(T) == 8) return;
-    const T alpha = S.gvol[q] / dt + P.relax * (lc[0] + lc[1] + lc[2]) + (T)2 * (lv[0] + lv[1] + lv[2]);
-    S.ainv[q] = (T)1 / alpha;
-    const T od = cv[0], omx = cv[1], omy = cv[2], omz = cv[3], oe = cv[4];
-    const T oinv = (T)1 / od;
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        const T nx = S.gn[d][0][q], ny = S.gn[d][1][q], nz = S.gn[d][2][q], ve = S.gve[d][q];
-        const T Vo = omx * oinv * nx + omy * oinv * ny + omz * oinv * nz;
-        const T dov = Vo - ve;
-        S.fo[d][0][q] = od * dov;
-        S.fo[d][1][q] = omx * dov + po * nx;
-        S.fo[d][2][q] = omy * dov + po * ny;
-        S.fo[d][3][q] = omz * dov + po * nz;
-        S.fo[d][4][q] = (oe + po) * dov + po * ve;
-    }
+    const int tj = (ctx.maxJM - 1 + 31) / 32, tk = (ctx.maxKM - 1 + 31) / 32;
+    const unsigned gx = (unsigned)((ctx.maxIM - 1) * tj * tk);
+    k_plane_tile<Src, Dst, TO_PLANE><<<dim3(gx, ctx.batch.nsolve, n), 256, 0, ctx.stream>>>(ctx.batch, pt.rq, pt.rq_off, A, tj, tk);
+}
+
+// the sweeps' flow inputs into plane order (before every forward sweep): Q in the working type,
+// the residual, lambda_c, lambda_v, p and dt (two launches)
+template <typename T>
+static void launch_sweep_gather(const LaunchCtx &ctx, const PlaneTables &pt, const Flow<T> &W, const SweepData<T> &S)
+{
+    TileList<double, T> q = {};
+    for (int c = 0; c < NQ; c++) { q.src[c] = W.cv[c]; q.dst[c] = S.cv[c]; }
+    launch_plane_tile<double, T, true>(ctx, pt, q, NQ);
+    TileList<T, T> f = {};
+    int n = 0;
+    for (int c = 0; c < NQ; c++) { f.src[n] = W.res[c]; f.dst[n++] = S.res[c]; }
+    for (int d = 0; d < 3; d++) { f.src[n] = W.lamc[d]; f.dst[n++] = S.lamc[d]; }
+    for (int d = 0; d < 3; d++) { f.src[n] = W.lamv[d]; f.dst[n++] = S.lamv[d]; }
+    f.src[n] = W.pv[PP]; f.dst[n++] = S.pp;
+    f.src[n] = W.dt; f.dst[n++] = S.dt;
+    launch_plane_tile<T, T, true>(ctx, pt, f, n);
 }
 
 // geometry of the sweeps into plane order, in the working precision (once per level)
@@ -332,11 +344,6 @@ __global__ void __launch_bounds__(256) k_sweep_fill(SweepData<T> S, long long nq
     for (int d = 0; d < 3; d++) { S.lamc[d][q] = (T)1; S.lamv[d][q] = (T)0.1; }
     S.dt[q] = (T)1;
     for (int c = 0; c < NQ; c++) { S.res[c][q] = (T)1e-3; S.dq[c][q] = (T)0; }
-    if (S.ainv) {
-        for (int d = 0; d < 3; d++)
-            for (int c = 0; c < NQ; c++) S.fo[d][c][q] = (T)0;
-        S.ainv[q] = (T)0.5;
-    }
 }
 
 // Autotuner of the sweep's block shape (cells per warp, warps per block): times the forward and
@@ -381,11 +388,10 @@ void launch_lusgs_sweeps(const LaunchCtx &ctx, const PhysW<T> &P, const Geo &G, 
                          const SweepData<T> &S)
 {
     const int np = pt.max_plane;
-    const unsigned gq = (unsigned)((pt.nq + 255) / 256);
-    ctx.mark("sweep_forward", 1, np - 1);
-    k_sweep_gather<T><<<gq, 256, 0, ctx.stream>>>(P, W, S, pt.nq);
+    ctx.mark("sweep_forward", 1, np);                 // two gather launches and the planes
+    launch_sweep_gather<T>(ctx, pt, W, S);
     for (int pl = 3; pl <= np; pl++) launch_plane<T, 1>(ctx, P, pt, S, pl, pl == 3);
-    ctx.mark("sweep_forward", 0, np - 1);
+    ctx.mark("sweep_forward", 0, np);
     if (W.ev) {
         ctx.mark("sa_sweeps", 1, np - 2);
         launch_sa_sweep<T>(ctx, P, G, W, pt, S, 1);
@@ -400,9 +406,9 @@ void launch_lusgs_sweeps(const LaunchCtx &ctx, const PhysW<T> &P, const Geo &G, 
         ctx.mark("sa_sweeps", 0, np - 2);
     }
     ctx.mark("sweep_scatter", 1, 1);
-    const int tj = (ctx.maxJM - 1 + 31) / 32, tk = (ctx.maxKM - 1 + 31) / 32;
-    const unsigned gx = (unsigned)((ctx.maxIM - 1) * tj * tk);
-    k_sweep_scatter_tiled<T><<<dim3(gx, ctx.batch.nsolve, NQ), 256, 0, ctx.stream>>>(ctx.batch, pt.rq, pt.rq_off, S, W, tj, tk);
+    TileList<T, T> dq = {};
+    for (int c = 0; c < NQ; c++) { dq.src[c] = S.dq[c]; dq.dst[c] = W.dq[c]; }
+    launch_plane_tile<T, T, false>(ctx, pt, dq, NQ);
     ctx.mark("sweep_scatter", 0, 1);
 }
 

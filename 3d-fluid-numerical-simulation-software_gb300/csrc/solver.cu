@@ -861,8 +861,7 @@ public:
         pt.nq = (long long)nq;
         auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
         const bool sa = P.turb_sa && l == 1;
-        const size_t n_pre = sizeof(T) == 4 ? 16 : 0;      // mixed form: old fluxes and 1 / diagonal from the gather
-        const size_t n_t = 16 + 18 + NQ + n_pre + (sa ? 19 : 0);   // geometry, flow inputs, dQ (and the SA sweep's)
+        const size_t n_t = 16 + 18 + NQ + (sa ? 19 : 0);   // geometry, flow inputs, dQ (and the SA sweep's)
         Lv.plane_mem.bytes = al(sizeof(int) * start.size()) + al(sizeof(long long) * nq) + 6 * al(sizeof(int) * nq) +
                              al(sizeof(int) * rq.size()) + al(sizeof(long long) * rq_off.size()) + n_t * al(sizeof(T) * nq) + 256;
         CK(cudaMalloc(&Lv.plane_mem.p, Lv.plane_mem.bytes));
@@ -900,11 +899,6 @@ public:
         S.dt = arr();
         for (int c = 0; c < NQ; c++) S.res[c] = arr();
         for (int c = 0; c < NQ; c++) S.dq[c] = arr();
-        if (n_pre) {
-            for (int d = 0; d < 3; d++)
-                for (int c = 0; c < NQ; c++) S.fo[d][c] = arr();
-            S.ainv = arr();
-        }
         if (sa) {
             for (int d = 0; d < 3; d++) { S.sa_vn[d] = arr(); S.sa_eb[d] = arr(); S.sa_s[d] = arr(); S.sa_rl[d] = arr(); S.sa_lv[d] = arr(); }
             S.sa_ev0 = arr(); S.sa_alpha = arr(); S.sa_res = arr(); S.sa_dq = arr();
