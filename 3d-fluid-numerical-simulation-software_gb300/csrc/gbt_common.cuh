@@ -56,6 +56,8 @@ struct Flow {
     double *cvold[NQ];
     T *pv[NPV];
     T *mut, *omega, *dt;
+    T *mul;                                          // FP64 form: laminar viscosity (Sutherland) per cell, formed
+                                                     // with the spectral radii for Baldwin-Lomax and the viscous radii
     T *lamc[3], *lamv[3];
     T *Ff[3][NQ], *Vf[3][NQ];                        // face convective / viscous fluxes
     T *Fd[3][NQ];                                    // face artificial dissipation (JST only, else null)

@@ -47,6 +47,10 @@ __global__ void __launch_bounds__(256) k_cell_a(Batch B, PhysW<T> PC, GeoW<T> G,
 #pragma unroll
     for (int d = 0; d < 3; d++) W.lamc[d][p] = lam[d];
     W.omega[p] = om;
+    // FP64 form: the cell's laminar viscosity, once for the Baldwin-Lomax lines that cross it (up to
+    // four) and the viscous spectral radii (the same function of the same temperature, so the same
+    // value; on the FP64 pipe it costs about 25 instructions). The mixed form forms it where it is used.
+    if constexpr (sizeof(T) == 8) W.mul[p] = sutherland(PC, W.pv[PT][p]);
 }
 
 // Baldwin-Lomax inner/outer viscosity (source/BL_Model.cpp:283-329) along the wall-normal lines
@@ -152,8 +156,7 @@ __global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, PhysW<T> PC, Flow
     T tmax = (T)0;
     bool any = false;
     if (live) {
-        auto p1 = [&](int n0, T tp, T om) {
-            const T ml = sutherland(PC, tp);
+        auto p1 = [&](int n0, T ml, T om) {
             const T tw = tabs(om * ml);
             if (n0 == 1) { sh_d1[lane] = W.pv[PD][CELL(1)]; sh_m1[lane] = ml; }   // first cell: density, mu_l
             if (!any || tw > tmax) tmax = tw;
@@ -167,14 +170,15 @@ __global__ void __launch_bounds__(32 * BL_WARPS) k_bl(Batch B, PhysW<T> PC, Flow
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
                     const long long p = CELL(min(nb + u * BL_WARPS, N - 1));
-                    tv[u] = W.pv[PT][p]; ov[u] = W.omega[p];
+                    tv[u] = sizeof(T) == 8 ? W.mul[p] : sutherland(PC, W.pv[PT][p]); ov[u] = W.omega[p];
                 }
 #pragma unroll
                 for (int u = 0; u < 4; u++)
                     if (nb + u * BL_WARPS < N) p1(nb + u * BL_WARPS, tv[u], ov[u]);
             }
         }
-        for (int n0 = 1 + wp + BL_CACHE * BL_WARPS; n0 < N; n0 += BL_WARPS) p1(n0, W.pv[PT][CELL(n0)], W.omega[CELL(n0)]);
+        for (int n0 = 1 + wp + BL_CACHE * BL_WARPS; n0 < N; n0 += BL_WARPS)
+            p1(n0, sizeof(T) == 8 ? W.mul[CELL(n0)] : sutherland(PC, W.pv[PT][CELL(n0)]), W.omega[CELL(n0)]);
     }
     sh_a[wp][lane] = tmax;
     sh_n[wp][lane] = any;
@@ -336,7 +340,7 @@ __global__ void __launch_bounds__(256) k_cell_b(Batch B, PhysW<T> PC, GeoW<T> G,
     T lc = W.lamc[0][p] + W.lamc[1][p] + W.lamc[2][p];
     T lv = (T)0;
     if constexpr (NS) {
-        const T ml = sutherland(PC, W.pv[PT][p]);
+        const T ml = sizeof(T) == 8 ? W.mul[p] : sutherland(PC, W.pv[PT][p]);   // FP64: formed by k_cell_a
         const T mt = W.mut[p];
         const T rho = W.pv[PD][p];
         const T a = (T)(double)(4.0f / 3.0f) / rho, b = PC.gamma / rho;

@@ -598,7 +598,7 @@ public:
         T *t = (T *)Lv.flow_t_mem.p;
         auto tk = [&]() { T *r = t; t += N; return r; };
         for (int c = 0; c < NPV; c++) W.pv[c] = tk();
-        W.mut = tk(); W.omega = tk(); W.dt = tk();
+        W.mut = tk(); W.omega = tk(); W.dt = tk(); W.mul = tk();
         for (int f = 0; f < 3; f++) { W.lamc[f] = tk(); W.lamv[f] = tk(); for (int c = 0; c < NQ; c++) { W.Ff[f][c] = tk(); W.Vf[f][c] = tk(); } }
         for (int c = 0; c < NQ; c++) { W.res[c] = tk(); W.dq[c] = tk(); W.res2h[c] = tk(); W.dq2h[c] = tk(); }
         if (P.turb_sa && l == 1) {
