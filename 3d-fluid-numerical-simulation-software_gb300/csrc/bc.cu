@@ -205,7 +205,7 @@ __global__ void k_bc_wall(Batch B, Phys P, Geo G, Flow<T> W, const DevWall *wall
 // rotated about z by +-delta_th
 template <typename T>
 __global__ void k_bc_periodic(Batch B, Flow<T> W, const long long *dst, const long long *src, const int *meta,
-                              long long n)
+                              const double *trig, long long n)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -220,7 +220,9 @@ __global__ void k_bc_periodic(Batch B, Flow<T> W, const long long *dst, const lo
 #pragma unroll
     for (int m = 0; m < 6; m++) q[m] = W.pv[m][a];
     if (dr != 0.0) {
-        const double cs = cos(dr), sn = sin(dr);
+        // cos(dr) and sin(dr), formed once per solve by k_periodic_trig with the same functions
+        const double *tr = trig + 4 * s + (sg > 0 ? 0 : 2);
+        const double cs = tr[0], sn = tr[1];
         const double mx = c[1], my = c[2];
         c[1] = mx * cs - my * sn;
         c[2] = my * cs + mx * sn;
@@ -229,6 +231,25 @@ __global__ void k_bc_periodic(Batch B, Flow<T> W, const long long *dst, const lo
         q[PV] = (T)(v * cs + u * sn);
     }
     st_state(W, b, c, q);
+}
+
+// cosine and sine of the periodic rotation +-delta_th of every solve (the entries of the gather
+// list read them instead of evaluating FP64 trigonometric functions per ghost cell)
+__global__ void k_periodic_trig(Batch B, double *trig)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= B.nsolve) return;
+    const double x = B.sc[s].delta_th;
+    const double p = 1.0 * x, m = -1.0 * x;
+    trig[4 * s + 0] = cos(p);
+    trig[4 * s + 1] = sin(p);
+    trig[4 * s + 2] = cos(m);
+    trig[4 * s + 3] = sin(m);
+}
+
+void launch_periodic_trig(const LaunchCtx &ctx, double *trig)
+{
+    k_periodic_trig<<<(ctx.batch.nsolve + 127) / 128, 128, 0, ctx.stream>>>(ctx.batch, trig);
 }
 
 // mixing plane (CMesh::BndCondMixingPlane, source/BndCondMixingPlane.cpp:287-520), one warp per
@@ -349,7 +370,8 @@ void launch_boundary(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> 
     }
     if (bc.n_wall) k_bc_wall<T><<<dim3((bc.max_wall + 127) / 128, bc.n_wall), 128, 0, ctx.stream>>>(B, P, G, W, bc.wall);
     if (bc.n_per)
-        k_bc_periodic<T><<<(unsigned)((bc.n_per + 255) / 256), 256, 0, ctx.stream>>>(B, W, bc.per_dst, bc.per_src, bc.per_meta, bc.n_per);
+        k_bc_periodic<T><<<(unsigned)((bc.n_per + 255) / 256), 256, 0, ctx.stream>>>(B, W, bc.per_dst, bc.per_src, bc.per_meta,
+                                                                                   bc.per_trig, bc.n_per);
     if (W.ev) launch_sa_boundary<T>(ctx, P, W, bc);
     if (bc.n_mix) {
         k_mix_average<T><<<dim3(bc.max_mix_rows, bc.n_mix, 2), 32, 0, ctx.stream>>>(B, P, G, W, bc.mix, bc.max_mix_rows, bc.mix_avg);

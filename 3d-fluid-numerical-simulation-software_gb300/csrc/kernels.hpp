@@ -46,6 +46,7 @@ struct BcTables {
     // periodic exchange as a gather list: dst <- rotate(src, sign * delta_th of the solve)
     const long long *per_dst = nullptr, *per_src = nullptr;
     const int *per_meta = nullptr;                // solve * 4 + (sign + 1)
+    const double *per_trig = nullptr;             // per solve: cos, sin of +delta_th, then of -delta_th
     long long n_per = 0;
     int max_outlet_im = 0, max_outlet_jm = 0;
     double *outlet_cu = nullptr;                  // per outlet patch: mass-weighted swirl of each radial row
@@ -102,6 +103,8 @@ struct SweepData {
 };
 
 void launch_geometry(const LaunchCtx &ctx, const Geo &G, double *totalvol);
+// the periodic rotation's cosines and sines per solve (BcTables::per_trig), once at create
+void launch_periodic_trig(const LaunchCtx &ctx, double *trig);
 
 template <typename T>
 void launch_boundary(const LaunchCtx &ctx, const Phys &P, const Geo &G, Flow<T> F, const BcTables &bc);

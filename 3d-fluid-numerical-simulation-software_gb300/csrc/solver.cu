@@ -1062,7 +1062,8 @@ public:
                      bytes(outl1.size(), sizeof(DevInOut)) + bytes(walls.size(), sizeof(DevWall)) + bytes(pdst.size(), 8) * 2 +
                      bytes(pmeta.size(), 4) + bytes(outl.size() * (size_t)(bc.max_outlet_im + 1), 8) +
                      bytes((size_t)nsolve * 2 * kIntegralBlocks * 3, 8) + bytes(sa_dst_h.size(), 8) * 2 +
-                     bytes(mixes.size(), sizeof(DevMix)) + bytes(mixes.size() * (size_t)bc.max_mix_rows * kMixVals, 8) + 256;
+                     bytes(mixes.size(), sizeof(DevMix)) + bytes(mixes.size() * (size_t)bc.max_mix_rows * kMixVals, 8) +
+                     bytes((size_t)nsolve * 4, 8) + 256;
         CK(cudaMalloc(&Lv.tab_mem.p, tot));
         char *q = (char *)Lv.tab_mem.p;
         auto up = [&](const void *h, size_t n, size_t sz) {
@@ -1088,6 +1089,9 @@ public:
         bc.mix_avg = (double *)up(nullptr, 0, 8); q += bytes(mixes.size() * (size_t)bc.max_mix_rows * kMixVals, 8);
         bc.outlet_cu = (double *)up(nullptr, 0, 8); q += bytes(outl.size() * (size_t)(bc.max_outlet_im + 1), 8);
         bc.integ_part = (double *)up(nullptr, 0, 8); q += bytes((size_t)nsolve * 2 * kIntegralBlocks * 3, 8);
+        double *trig = (double *)up(nullptr, 0, 8); q += bytes((size_t)nsolve * 4, 8);
+        bc.per_trig = trig;
+        launch_periodic_trig(ctx(l), trig);
         for (int f = 0; f < 3; f++)
             CK(cudaMemcpy((void *)Lv.W.wallf[f], wallf[f].data(), sizeof(int) * (size_t)Lv.pool_n, cudaMemcpyHostToDevice));
         Lv.walls_h = walls;
