@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(32 * WPB) k_sweep(PhysW<T> P, SweepData<T> S, 
 // indices (the plane order enumerates i, then j), so both sides move whole sectors. The diagonals'
 // starts are read once per block; the loads of all arrays of the group are issued before the first
 // store. Batches take groups of five arrays, so that a block keeps some twenty loads per thread in
-// flight (the 64-point batch's gather and scatter 1.12 ms faster per cycle than with one array per
+// flight (the 64-point batch's gather and scatter 0.68 ms faster per cycle than with one array per
 // block); single solves keep one array per block, where the grid then has enough blocks to fill
 // the GPU (five-array groups made the single FP64 solve's scatter 13 us slower). Values are converted on the
 // way from the source to the destination type (FP64 Q to the working type with the conversion
